@@ -1,0 +1,84 @@
+/* CPU restatement of the reference regular-grid reconstruction path (test infrastructure only).
+ *
+ * This library is the oracle the CUDA path is checked against and the CPU baseline that the
+ * benchmark times.  It is never linked into the product library.  Every function restates one
+ * step of the reference (file:line cited at its definition in epr_oracle.cpp).
+ *
+ * Conventions shared with the CUDA path:
+ *   - node (function) index: axis 0 most significant, (r+1)^Dim nodes per level (r = 2^depth);
+ *   - element index: axis 0 most significant, r^Dim elements;
+ *   - packed skew matrices: p[i(i-1)/2 + j] for i > j (Dim(Dim-1)/2 values);
+ *   - column stencils: 3^Dim values per node i, entry o holds M(i + off(o), i), where
+ *     o = sum_d (off[d]+1) 3^(Dim-1-d).
+ */
+#ifndef EPR_ORACLE_H
+#define EPR_ORACLE_H
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct epr_oracle epr_oracle;
+
+typedef struct epr_oracle_params {
+    double s_weight;      /* --sWeight (screening) */
+    double d_weight;      /* --dWeight (Dirichlet) */
+    double n_sigma;       /* --nSigma */
+    double i_mult;        /* --iMult */
+    int t_radius;         /* --tRadius */
+    int d_radius;         /* --dRadius */
+    int gs_iters;         /* --gsIters */
+    int min_solve_depth;  /* --minSolveDepth */
+    int max_solve_depth;  /* --maxSolveDepth (-1 = depth) */
+    unsigned int seed;    /* --seed */
+    int threads;          /* OpenMP threads (0 = all) */
+} epr_oracle_params;
+
+void epr_oracle_default_params(epr_oracle_params *p);
+
+/* world -> unit cube map (ExteriorPoisson.h:100-123); xform is (Dim+1)x(Dim+1) with the same
+ * (column, row) element order as the reference SquareMatrix; positions are mapped in place. */
+int epr_oracle_unit_cube(int dim, size_t n, double scale, double *pos, double *xform);
+
+epr_oracle *epr_oracle_create(int dim, int depth, const epr_oracle_params *p);
+void epr_oracle_destroy(epr_oracle *o);
+
+/* unit-cube positions (n x Dim) and packed skew frames (n x Dim(Dim-1)/2) */
+int epr_oracle_set_samples(epr_oracle *o, size_t n, const double *pos, const double *skew);
+
+/* Runs ordered sampling, density estimation, skew splatting, S(E), R, B and the Galerkin
+ * hierarchy (ExteriorPoisson.h:126-313). */
+int epr_oracle_build(epr_oracle *o);
+
+/* Replaces the system of one level: A = R + dWeight K (column stencil), B (column stencil), c. */
+int epr_oracle_set_level_system(epr_oracle *o, int level, const double *R, const double *B, double c);
+
+/* Named arrays: "cells","measure","noise","depth","S","leaf_depth","R","B","A","density","skew",
+ * "exists". Returns the number of doubles written (out may be NULL to query the size). */
+long epr_oracle_get(epr_oracle *o, const char *name, int level, double *out);
+
+size_t epr_oracle_num_nodes(int dim, int level);
+
+/* energies(): out[0] = fit, out[1] = regularisation, out[2] = wedge square norm
+ * (SystemEnergy.h:486-497). */
+int epr_oracle_energy(epr_oracle *o, int level, const double *x, const double *y, double *out);
+/* quadraticFit at every node: out is N x 5 (Q20, Q02, Q11, Q10, Q01), SystemEnergy.h:542-643 */
+int epr_oracle_quadfit(epr_oracle *o, int level, const double *x, const double *y, double *out);
+/* gradient of the energy: gx, gy (N each) */
+int epr_oracle_gradient(epr_oracle *o, int level, const double *x, const double *y, double *gx, double *gy);
+/* paired Gauss-Seidel, iters full sweeps over the 2^Dim parity colours (ExteriorPoissonSolvers.h:156-196) */
+int epr_oracle_gs(epr_oracle *o, int level, double *x, double *y, int iters);
+/* prolongation of a level-`level` vector to level+1 (Hat.scalars.inl:1747-1779) */
+int epr_oracle_prolong(epr_oracle *o, int level, const double *coarse, double *fine);
+/* Gauss-Newton matvec of the energy's quadratic model at (x,y) applied to (dx,dy) */
+int epr_oracle_gn_matvec(epr_oracle *o, int level, const double *x, const double *y,
+                         const double *dx, const double *dy, double *ox, double *oy);
+
+/* cascadic solve (ExteriorPoisson.h:315-409); x_out,y_out receive the hierarchical coefficients of
+ * every level concatenated (level 0 first); energies_out = (E0, fit, reg). */
+int epr_oracle_solve(epr_oracle *o, double *x_out, double *y_out, double *energies_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,189 @@
+"""ctypes front end of the CPU restatement (oracle/epr_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as the checker and by
+bench.py's CPU-baseline leg.  The product package never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libepr_oracle.so")
+_lib = None
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("s_weight", ctypes.c_double),
+        ("d_weight", ctypes.c_double),
+        ("n_sigma", ctypes.c_double),
+        ("i_mult", ctypes.c_double),
+        ("t_radius", ctypes.c_int),
+        ("d_radius", ctypes.c_int),
+        ("gs_iters", ctypes.c_int),
+        ("min_solve_depth", ctypes.c_int),
+        ("max_solve_depth", ctypes.c_int),
+        ("seed", ctypes.c_uint),
+        ("threads", ctypes.c_int),
+    ]
+
+
+def build() -> str:
+    """Compiles the restatement (make -C oracle port)."""
+    subprocess.run(["make", "-s", "-C", _HERE, "port"], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
+                os.path.join(_HERE, "epr_oracle.cpp")):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.POINTER(ctypes.c_double)
+        L.epr_oracle_create.restype = ctypes.c_void_p
+        L.epr_oracle_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(Params)]
+        L.epr_oracle_destroy.argtypes = [ctypes.c_void_p]
+        L.epr_oracle_default_params.argtypes = [ctypes.POINTER(Params)]
+        L.epr_oracle_unit_cube.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.c_double, P, P]
+        L.epr_oracle_set_samples.argtypes = [ctypes.c_void_p, ctypes.c_size_t, P, P]
+        L.epr_oracle_build.argtypes = [ctypes.c_void_p]
+        L.epr_oracle_set_level_system.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, ctypes.c_double]
+        L.epr_oracle_get.restype = ctypes.c_long
+        L.epr_oracle_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, P]
+        L.epr_oracle_num_nodes.restype = ctypes.c_size_t
+        L.epr_oracle_num_nodes.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.epr_oracle_energy.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P]
+        L.epr_oracle_quadfit.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P]
+        L.epr_oracle_gradient.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, P]
+        L.epr_oracle_gs.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, ctypes.c_int]
+        L.epr_oracle_prolong.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P]
+        L.epr_oracle_gn_matvec.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, P, P, P]
+        L.epr_oracle_solve.argtypes = [ctypes.c_void_p, P, P, P]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().epr_oracle_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def num_nodes(dim: int, level: int) -> int:
+    return (2 ** level + 1) ** dim
+
+
+def unit_cube(pos: np.ndarray, scale: float = 1.1):
+    pos = np.ascontiguousarray(pos, dtype=np.float64).copy()
+    n, dim = pos.shape
+    xf = np.zeros((dim + 1) * (dim + 1))
+    rc = lib().epr_oracle_unit_cube(dim, n, scale, _p(pos), _p(xf))
+    if rc:
+        raise ValueError(f"unit_cube failed ({rc})")
+    return pos, xf.reshape(dim + 1, dim + 1)
+
+
+class Oracle:
+    """One reconstruction problem (dimension, depth, parameters) on the CPU."""
+
+    def __init__(self, dim: int, depth: int, **params):
+        self.dim, self.depth = dim, depth
+        self.params = default_params(**params)
+        self._h = lib().epr_oracle_create(dim, depth, ctypes.byref(self.params))
+        if not self._h:
+            raise ValueError("invalid oracle configuration")
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().epr_oracle_destroy(self._h)
+            self._h = None
+
+    def set_samples(self, pos_unit: np.ndarray, skew_packed: np.ndarray):
+        pos = np.ascontiguousarray(pos_unit, dtype=np.float64)
+        sk = np.ascontiguousarray(skew_packed, dtype=np.float64)
+        if lib().epr_oracle_set_samples(self._h, pos.shape[0], _p(pos), _p(sk)):
+            raise ValueError("set_samples failed")
+
+    def build(self):
+        if lib().epr_oracle_build(self._h):
+            raise RuntimeError("build failed")
+
+    def set_level_system(self, level, R, B, c):
+        R = np.ascontiguousarray(R, dtype=np.float64)
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        lib().epr_oracle_set_level_system(self._h, level, _p(R), _p(B), float(c))
+
+    def get(self, name: str, level: int = 0) -> np.ndarray:
+        n = lib().epr_oracle_get(self._h, name.encode(), level, None)
+        if n < 0:
+            raise KeyError(name)
+        out = np.zeros(n)
+        lib().epr_oracle_get(self._h, name.encode(), level, _p(out))
+        return out
+
+    def nodes(self, level):
+        return num_nodes(self.dim, level)
+
+    def energy(self, level, x, y):
+        out = np.zeros(3)
+        lib().epr_oracle_energy(self._h, level, _p(np.ascontiguousarray(x, np.float64)),
+                                _p(np.ascontiguousarray(y, np.float64)), _p(out))
+        return out
+
+    def quadfit(self, level, x, y):
+        out = np.zeros((self.nodes(level), 5))
+        lib().epr_oracle_quadfit(self._h, level, _p(np.ascontiguousarray(x, np.float64)),
+                                 _p(np.ascontiguousarray(y, np.float64)), _p(out))
+        return out
+
+    def gradient(self, level, x, y):
+        gx = np.zeros(self.nodes(level))
+        gy = np.zeros(self.nodes(level))
+        lib().epr_oracle_gradient(self._h, level, _p(np.ascontiguousarray(x, np.float64)),
+                                  _p(np.ascontiguousarray(y, np.float64)), _p(gx), _p(gy))
+        return gx, gy
+
+    def gs(self, level, x, y, iters=1):
+        x = np.array(x, dtype=np.float64)
+        y = np.array(y, dtype=np.float64)
+        lib().epr_oracle_gs(self._h, level, _p(x), _p(y), iters)
+        return x, y
+
+    def prolong(self, level, xc):
+        out = np.zeros(self.nodes(level + 1))
+        lib().epr_oracle_prolong(self._h, level, _p(np.ascontiguousarray(xc, np.float64)), _p(out))
+        return out
+
+    def gn_matvec(self, level, x, y, dx, dy):
+        ox = np.zeros(self.nodes(level))
+        oy = np.zeros(self.nodes(level))
+        a = [np.ascontiguousarray(v, np.float64) for v in (x, y, dx, dy)]
+        lib().epr_oracle_gn_matvec(self._h, level, *[_p(v) for v in a], _p(ox), _p(oy))
+        return ox, oy
+
+    def solve(self):
+        tot = sum(self.nodes(l) for l in range(self.depth + 1))
+        x = np.zeros(tot)
+        y = np.zeros(tot)
+        e = np.zeros(3)
+        lib().epr_oracle_solve(self._h, _p(x), _p(y), _p(e))
+        xs, ys, off = [], [], 0
+        for l in range(self.depth + 1):
+            n = self.nodes(l)
+            xs.append(x[off:off + n])
+            ys.append(y[off:off + n])
+            off += n
+        return xs, ys, e

@@ -1,0 +1,96 @@
+"""Writes the golden fixtures of tests/golden/*.npz from the reference implementation itself.
+
+Run in a checkout that has the reference sources (the fixtures are committed, so the tests never
+need them):
+
+    make -C oracle ref              # builds oracle/_ref/ref_harness from the reference headers
+    python tests/golden/make_golden.py
+
+Each fixture stores the exact inputs (world positions and packed skew frames as the reference's
+PLY reader returns them) and the reference's outputs for them: unit-cube positions, ordered
+cells, estimator measure / noise / depth per sample, the splatted frame field S(E), leaf depths,
+the system matrices of selected levels as column stencils, energies / quadratic fits / one paired
+Gauss-Seidel sweep for seeded random coefficients, and the cascadic solve result.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from exteriorpoissonrecon_gb300 import samples  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+# name, workload, sample count, seed, depth, levels whose full stencils are stored
+CASES = [
+    ("knot3_d4", "knot", 4096, 0, 4, [2, 4]),
+    ("link3_d4", "link", 6000, 3, 4, [1, 4]),
+    ("cliff4_d3", "clifford", 4000, 5, 3, [1, 2]),
+]
+
+
+def make(name, workload, n, seed, depth, stencil_levels):
+    pos, frames = samples.make_workload(workload, n, seed=seed)
+    with tempfile.TemporaryDirectory() as td:
+        ply = os.path.join(td, "in.ply")
+        samples.write_ply(ply, pos, frames)
+        out = os.path.join(td, "dump")
+        subprocess.run([HARNESS, ply, str(depth), out], check=True)
+        L = lambda k: np.load(os.path.join(out, k + ".npy"))  # noqa: E731
+        fx = {
+            "depth": np.array(depth),
+            "world_pos": L("world_pos"),
+            "skew": L("skew"),
+            "pos": L("pos"),
+            "world_to_unit": L("world_to_unit"),
+            "cells": L("cells"),
+            "cell_counts": L("cell_counts"),
+            "est_measure": L("est_measure"),
+            "est_noise": L("est_noise"),
+            "est_depth": L("est_depth"),
+            "S": L("S"),
+            "leaf_depth": L("leaf_depth"),
+            "c": L("c"),
+            "sol_energies": L("sol_energies"),
+            "solX": L("solX"),
+            "solY": L("solY"),
+            "indexer_hash": L("indexer_hash"),
+            "stencil_levels": np.array(stencil_levels),
+        }
+        for l in range(depth + 1):
+            fx[f"energies_d{l}"] = L(f"energies_d{l}")
+            fx[f"xr_d{l}"] = L(f"xr_d{l}")
+            fx[f"yr_d{l}"] = L(f"yr_d{l}")
+            fx[f"solx_d{l}"] = L(f"solx_d{l}")
+            fx[f"soly_d{l}"] = L(f"soly_d{l}")
+            if l < depth:
+                fx[f"prolong_d{l}"] = L(f"prolong_d{l}")
+        for l in stencil_levels:
+            fx[f"R_d{l}"] = L(f"R_d{l}")
+            fx[f"B_d{l}"] = L(f"B_d{l}")
+        # quadratic fits and one GS sweep at the finest level and one coarse level
+        for l in sorted({depth, max(depth - 2, 0)}):
+            fx[f"quadfit_d{l}"] = L(f"quadfit_d{l}")
+            fx[f"gsx_d{l}"] = L(f"gsx_d{l}")
+            fx[f"gsy_d{l}"] = L(f"gsy_d{l}")
+        for l in range(depth + 1):
+            fx[f"density_l{l}"] = L(f"density_l{l}")
+            fx[f"skew_l{l}"] = L(f"skew_l{l}")
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **fx)
+    print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB")
+
+
+if __name__ == "__main__":
+    if not os.path.exists(HARNESS):
+        sys.exit("build the reference harness first: make -C oracle ref")
+    for case in CASES:
+        make(*case)
