@@ -1,0 +1,298 @@
+"""GB300-native implementation of ExteriorPoissonRecon's regular-grid solve path.
+
+The compute path is libepr_cuda.so (CUDA, sm_103a) behind the C ABI of include/epr.h.  This
+module is the Python host side: a ctypes binding of that ABI and a `Reconstructor` that mirrors
+the reference's interface (ExteriorPoissonRecon/ExteriorPoisson.h:56-94):
+
+    r = Reconstructor(dim, depth, positions_unit_cube, skew_packed, sWeight=..., ...)
+    r.solve()                 # Reconstructor::solve
+    r.x(level), r.y(level)    # Reconstructor::x / y (hierarchical coefficients)
+
+There is no CPU fallback: if the library is missing or no GPU is present the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+from . import samples  # noqa: F401  (re-exported helper module)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libepr_cuda.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "epr.h")
+
+EPR_OK = 0
+EPR_FP64, EPR_FP32 = 0, 1
+EPR_SOLVER_CASCADIC, EPR_SOLVER_MULTIGRID = 0, 1
+
+_lib = None
+
+
+class EprError(RuntimeError):
+    pass
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("s_weight", ctypes.c_double),
+        ("d_weight", ctypes.c_double),
+        ("n_sigma", ctypes.c_double),
+        ("i_mult", ctypes.c_double),
+        ("t_radius", ctypes.c_int),
+        ("d_radius", ctypes.c_int),
+        ("gs_iters", ctypes.c_int),
+        ("min_solve_depth", ctypes.c_int),
+        ("max_solve_depth", ctypes.c_int),
+        ("seed", ctypes.c_uint),
+        ("precision", ctypes.c_int),
+        ("solver", ctypes.c_int),
+        ("tolerance", ctypes.c_double),
+        ("max_cycles", ctypes.c_int),
+        ("verbose", ctypes.c_int),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("initial_energy", ctypes.c_double),
+        ("fit_energy", ctypes.c_double),
+        ("reg_energy", ctypes.c_double),
+        ("solve_ms", ctypes.c_double),
+        ("build_ms", ctypes.c_double),
+        ("grad_norm0", ctypes.c_double),
+        ("grad_norm", ctypes.c_double),
+        ("cycles", ctypes.c_int),
+        ("node_updates", ctypes.c_int64),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# reference flag names -> epr_params fields
+_FLAG_NAMES = {
+    "sWeight": "s_weight", "dWeight": "d_weight", "nSigma": "n_sigma", "iMult": "i_mult",
+    "tRadius": "t_radius", "dRadius": "d_radius", "gsIters": "gs_iters",
+    "minSolveDepth": "min_solve_depth", "maxSolveDepth": "max_solve_depth", "seed": "seed",
+}
+
+
+def header_symbols() -> list[str]:
+    """Names of the functions include/epr.h declares."""
+    with open(HEADER) as f:
+        txt = f.read()
+    return sorted(set(re.findall(r"\b(epr_[a-z_0-9]+)\s*\(", txt)))
+
+
+def load():
+    """Loads libepr_cuda.so (building it first if only the sources are present)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from .build import build
+        build()
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER(ctypes.c_double)
+    vp = ctypes.c_void_p
+    L.epr_default_params.argtypes = [ctypes.POINTER(Params)]
+    L.epr_create.restype = vp
+    L.epr_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(Params)]
+    L.epr_destroy.argtypes = [vp]
+    L.epr_last_error.restype = ctypes.c_char_p
+    L.epr_last_error.argtypes = [vp]
+    L.epr_global_error.restype = ctypes.c_char_p
+    L.epr_set_samples.argtypes = [vp, ctypes.c_size_t, P, P]
+    L.epr_build.argtypes = [vp]
+    L.epr_set_level_system.argtypes = [vp, ctypes.c_int, P, P, ctypes.c_double]
+    L.epr_set_coefficients.argtypes = [vp, ctypes.c_int, P, P]
+    L.epr_get_coefficients.argtypes = [vp, ctypes.c_int, P, P]
+    L.epr_energy.argtypes = [vp, ctypes.c_int, P]
+    L.epr_quadfit.argtypes = [vp, ctypes.c_int, P]
+    L.epr_gradient.argtypes = [vp, ctypes.c_int, P, P]
+    L.epr_gs.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.epr_prolong.argtypes = [vp, ctypes.c_int]
+    L.epr_gn_matvec.argtypes = [vp, ctypes.c_int, P, P, P, P]
+    L.epr_solve.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.epr_get_solution.argtypes = [vp, ctypes.c_int, P, P]
+    L.epr_get_array.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, P, ctypes.c_size_t,
+                                ctypes.POINTER(ctypes.c_size_t)]
+    L.epr_synchronize.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    load().epr_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        k = _FLAG_NAMES.get(k, k)
+        if k == "precision" and isinstance(v, str):
+            v = {"fp64": EPR_FP64, "fp32": EPR_FP32}[v.lower()]
+        if k == "solver" and isinstance(v, str):
+            v = {"cascadic": EPR_SOLVER_CASCADIC, "multigrid": EPR_SOLVER_MULTIGRID}[v.lower()]
+        setattr(p, k, v)
+    return p
+
+
+def unit_cube(pos_world: np.ndarray, scale: float = 1.1):
+    """ExteriorPoisson::ToUnitCube (ExteriorPoisson.h:100-123): centre the bounding box, scale by
+    1/(max extent * scale), shift by 1/2.  Returns (mapped positions, (Dim+1)^2 matrix in the
+    reference's (column, row) layout)."""
+    pos = np.asarray(pos_world, dtype=np.float64)
+    if pos.shape[0] == 0:
+        raise ValueError("Expected some samples: 0")
+    dim = pos.shape[1]
+    lo, hi = pos.min(axis=0), pos.max(axis=0)
+    ext = float((hi - lo).max())
+    k = 1.0 / (ext * scale)
+    t = (-(lo + hi) / 2.0) * k + 0.5
+    xf = np.zeros((dim + 1, dim + 1))
+    for d in range(dim):
+        xf[d, d] = k
+        xf[dim, d] = t[d]
+    xf[dim, dim] = 1.0
+    return pos * k + t, xf
+
+
+def pack_skew(frames: np.ndarray) -> np.ndarray:
+    return samples.pack_skew(frames)
+
+
+class Reconstructor:
+    """One reconstruction problem on the GPU (mirrors ExteriorPoisson::Reconstructor)."""
+
+    def __init__(self, dim: int, depth: int, pos_unit=None, skew_packed=None, build: bool = True, **params):
+        L = load()
+        self.dim, self.depth = int(dim), int(depth)
+        self.params = default_params(**params)
+        self._h = L.epr_create(self.dim, self.depth, ctypes.byref(self.params))
+        if not self._h:
+            raise EprError(L.epr_global_error().decode())
+        self.stats = Stats()
+        if pos_unit is not None:
+            self.set_samples(pos_unit, skew_packed)
+            if build:
+                self.build()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().epr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc != EPR_OK:
+            raise EprError(f"[{rc}] " + load().epr_last_error(self._h).decode())
+
+    def nodes(self, level: int) -> int:
+        return (2 ** level + 1) ** self.dim
+
+    # ---------------------------------------------------------------- setup
+    def set_samples(self, pos_unit, skew_packed):
+        pos = np.ascontiguousarray(pos_unit, dtype=np.float64)
+        sk = np.ascontiguousarray(skew_packed, dtype=np.float64)
+        if pos.ndim != 2 or pos.shape[1] != self.dim or sk.shape != (pos.shape[0], self.dim * (self.dim - 1) // 2):
+            raise ValueError("positions must be n x dim and frames n x dim(dim-1)/2")
+        self._check(load().epr_set_samples(self._h, pos.shape[0], _p(pos), _p(sk)))
+
+    def build(self):
+        self._check(load().epr_build(self._h))
+
+    def set_level_system(self, level, R, B, c):
+        R = np.ascontiguousarray(R, dtype=np.float64)
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        self._check(load().epr_set_level_system(self._h, level, _p(R), _p(B), float(c)))
+
+    def get(self, name: str, level: int = 0) -> np.ndarray:
+        n = ctypes.c_size_t(0)
+        self._check(load().epr_get_array(self._h, name.encode(), level, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value)
+        self._check(load().epr_get_array(self._h, name.encode(), level, _p(out), n.value, ctypes.byref(n)))
+        return out
+
+    # ---------------------------------------------------------------- per-level operators
+    def set_coefficients(self, level, x, y):
+        self._check(load().epr_set_coefficients(self._h, level, _p(np.ascontiguousarray(x, np.float64)),
+                                                 _p(np.ascontiguousarray(y, np.float64))))
+
+    def coefficients(self, level):
+        x = np.zeros(self.nodes(level))
+        y = np.zeros(self.nodes(level))
+        self._check(load().epr_get_coefficients(self._h, level, _p(x), _p(y)))
+        return x, y
+
+    def energy(self, level, x=None, y=None):
+        if x is not None:
+            self.set_coefficients(level, x, y)
+        out = np.zeros(3)
+        self._check(load().epr_energy(self._h, level, _p(out)))
+        return out
+
+    def quadfit(self, level, x=None, y=None):
+        if x is not None:
+            self.set_coefficients(level, x, y)
+        out = np.zeros((self.nodes(level), 5))
+        self._check(load().epr_quadfit(self._h, level, _p(out)))
+        return out
+
+    def gradient(self, level, x=None, y=None):
+        if x is not None:
+            self.set_coefficients(level, x, y)
+        gx = np.zeros(self.nodes(level))
+        gy = np.zeros(self.nodes(level))
+        self._check(load().epr_gradient(self._h, level, _p(gx), _p(gy)))
+        return gx, gy
+
+    def gs(self, level, x=None, y=None, iters=1):
+        if x is not None:
+            self.set_coefficients(level, x, y)
+        self._check(load().epr_gs(self._h, level, iters))
+        return self.coefficients(level)
+
+    def prolong(self, level):
+        self._check(load().epr_prolong(self._h, level))
+
+    def gn_matvec(self, level, dx, dy):
+        ox = np.zeros(self.nodes(level))
+        oy = np.zeros(self.nodes(level))
+        self._check(load().epr_gn_matvec(self._h, level, _p(np.ascontiguousarray(dx, np.float64)),
+                                         _p(np.ascontiguousarray(dy, np.float64)), _p(ox), _p(oy)))
+        return ox, oy
+
+    # ---------------------------------------------------------------- solve
+    def solve(self):
+        self._check(load().epr_solve(self._h, ctypes.byref(self.stats)))
+        return self.stats.as_dict()
+
+    def x(self, level):
+        x = np.zeros(self.nodes(level))
+        y = np.zeros(self.nodes(level))
+        self._check(load().epr_get_solution(self._h, level, _p(x), _p(y)))
+        return x
+
+    def y(self, level):
+        x = np.zeros(self.nodes(level))
+        y = np.zeros(self.nodes(level))
+        self._check(load().epr_get_solution(self._h, level, _p(x), _p(y)))
+        return y
+
+    def solution(self):
+        xs, ys = [], []
+        for l in range(self.depth + 1):
+            x = np.zeros(self.nodes(l))
+            y = np.zeros(self.nodes(l))
+            self._check(load().epr_get_solution(self._h, l, _p(x), _p(y)))
+            xs.append(x)
+            ys.append(y)
+        return xs, ys

@@ -1,0 +1,625 @@
+// The C ABI of libepr_cuda (declared in include/epr.h): context management, host <-> device
+// transfers and the solver drivers.  All arithmetic runs in the kernels of epr_solve.cu and
+// epr_setup.cu; this file only sequences them on the context's stream.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/epr.h"
+#include "epr_common.cuh"
+#include "epr_context.h"
+#include "epr_kernels.h"
+#include "epr_setup.h"
+
+namespace {
+
+thread_local std::string g_error;
+
+}  // namespace
+
+namespace epr {
+
+void Context::fail(int code, const char *fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    err = buf;
+    status = code;
+}
+
+bool Context::cuda_ok(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return true;
+    fail(e == cudaErrorMemoryAllocation ? EPR_ERR_NOMEM : EPR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    cudaGetLastError();
+    return false;
+}
+
+bool Context::launch_ok(const char *what) { return cuda_ok(cudaGetLastError(), what); }
+
+bool Context::alloc(void **p, size_t bytes, const char *what)
+{
+    *p = nullptr;
+    if (bytes == 0) return true;
+    return cuda_ok(cudaMallocAsync(p, bytes, stream), what);
+}
+
+void Context::release(void *p)
+{
+    if (p) cudaFreeAsync(p, stream);
+}
+
+int64_t Context::nodes(int level) const
+{
+    int64_t n = 1;
+    for (int d = 0; d < dim; d++) n *= (int64_t)((1 << level) + 1);
+    return n;
+}
+int Context::stencil() const { return dim == 3 ? 27 : 81; }
+
+bool Context::ensure_level(int l)
+{
+    Level &L = levels[l];
+    if (L.N) return true;
+    L.N = nodes(l);
+    size_t S = (size_t)stencil();
+    if (!alloc((void **)&L.xy64, sizeof(double) * 2 * L.N, "alloc xy")) return false;
+    if (!alloc((void **)&L.A64, sizeof(double) * S * L.N, "alloc A")) return false;
+    if (!alloc((void **)&L.B64, sizeof(double) * S * L.N, "alloc B")) return false;
+    if (!cuda_ok(cudaMemsetAsync(L.xy64, 0, sizeof(double) * 2 * L.N, stream), "memset xy")) return false;
+    if (!cuda_ok(cudaMemsetAsync(L.A64, 0, sizeof(double) * S * L.N, stream), "memset A")) return false;
+    if (!cuda_ok(cudaMemsetAsync(L.B64, 0, sizeof(double) * S * L.N, stream), "memset B")) return false;
+    if (P.precision == EPR_FP32)
+    {
+        if (!alloc((void **)&L.xy32, sizeof(float) * 2 * L.N, "alloc xy32")) return false;
+        if (!alloc((void **)&L.A32, sizeof(float) * S * L.N, "alloc A32")) return false;
+        if (!alloc((void **)&L.B32, sizeof(float) * S * L.N, "alloc B32")) return false;
+        if (!cuda_ok(cudaMemsetAsync(L.xy32, 0, sizeof(float) * 2 * L.N, stream), "memset xy32")) return false;
+    }
+    return true;
+}
+
+bool Context::sync_system32(int l)
+{
+    if (P.precision != EPR_FP32) return true;
+    Level &L = levels[l];
+    size_t S = (size_t)stencil();
+    launch_convert_d2f(L.A64, L.A32, (int64_t)S * L.N, stream);
+    launch_convert_d2f(L.B64, L.B32, (int64_t)S * L.N, stream);
+    return launch_ok("convert system");
+}
+
+// device coefficients <-> the precision the solve works in
+bool Context::push_xy(int l)
+{
+    if (P.precision != EPR_FP32) return true;
+    launch_convert_d2f(levels[l].xy64, levels[l].xy32, 2 * levels[l].N, stream);
+    return launch_ok("convert xy");
+}
+bool Context::pull_xy(int l)
+{
+    if (P.precision != EPR_FP32) return true;
+    launch_convert_f2d(levels[l].xy32, levels[l].xy64, 2 * levels[l].N, stream);
+    return launch_ok("convert xy");
+}
+
+Context::~Context()
+{
+    if (stream)
+    {
+        for (Level &L : levels)
+        {
+            release(L.xy64); release(L.xy32); release(L.A64); release(L.B64); release(L.A32); release(L.B32);
+            release(L.tmp64); release(L.tmp32);
+        }
+        release(red.partial); release(red.out); release(d_err); release(d_fit);
+        setup.release(*this);
+        cudaStreamSynchronize(stream);
+        cudaStreamDestroy(stream);
+    }
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+}
+
+// ---------------------------------------------------------------------------------------------
+// typed dispatch helpers
+// ---------------------------------------------------------------------------------------------
+template <typename F>
+int with_dim(Context *c, F &&f)
+{
+    if (c->dim == 3) return f(std::integral_constant<int, 3>{});
+    return f(std::integral_constant<int, 4>{});
+}
+
+template <typename Real>
+LevelPtrs<Real> level_ptrs(Context *c, int l)
+{
+    Level &L = c->levels[l];
+    LevelPtrs<Real> p;
+    p.level = l;
+    p.N = L.N;
+    if constexpr (std::is_same<Real, double>::value) { p.xy = L.xy64; p.A = L.A64; p.B = L.B64; }
+    else { p.xy = L.xy32; p.A = L.A32; p.B = L.B32; }
+    return p;
+}
+
+bool Context::energy(int l, double *out3)
+{
+    bool fp32 = P.precision == EPR_FP32;
+    with_dim(this, [&](auto dd) {
+        constexpr int D = decltype(dd)::value;
+        if (fp32) launch_energy<D, float>(level_ptrs<float>(this, l), levels[l].xy32, red, stream);
+        else launch_energy<D, double>(level_ptrs<double>(this, l), levels[l].xy64, red, stream);
+        return 0;
+    });
+    if (!launch_ok("energy")) return false;
+    double h[3];
+    if (!cuda_ok(cudaMemcpyAsync(h, red.out, sizeof(h), cudaMemcpyDeviceToHost, stream), "energy copy")) return false;
+    if (!cuda_ok(cudaStreamSynchronize(stream), "energy sync")) return false;
+    out3[0] = h[0] - 2. * h[1] + c;
+    out3[1] = h[2];
+    out3[2] = h[0];
+    return true;
+}
+
+bool Context::gs(int l, int iters)
+{
+    bool fp32 = P.precision == EPR_FP32;
+    for (int it = 0; it < iters; it++)
+        for (int col = 0; col < (1 << dim); col++)
+        {
+            with_dim(this, [&](auto dd) {
+                constexpr int D = decltype(dd)::value;
+                if (fp32) launch_gs_colour<D, float>(level_ptrs<float>(this, l), col, d_err, stream);
+                else launch_gs_colour<D, double>(level_ptrs<double>(this, l), col, d_err, stream);
+                return 0;
+            });
+        }
+    stats.node_updates += (int64_t)iters * levels[l].N;
+    return launch_ok("gs");
+}
+
+bool Context::check_errors()
+{
+    unsigned int h = 0;
+    if (!cuda_ok(cudaMemcpyAsync(&h, d_err, sizeof(h), cudaMemcpyDeviceToHost, stream), "error flag")) return false;
+    if (!cuda_ok(cudaStreamSynchronize(stream), "sync")) return false;
+    if (h & ERR_NONFINITE) { fail(EPR_ERR_NUMERIC, "a Gauss-Seidel update produced a non-finite value"); return false; }
+    return true;
+}
+
+bool Context::prolong_add(int l)
+{
+    bool fp32 = P.precision == EPR_FP32;
+    with_dim(this, [&](auto dd) {
+        constexpr int D = decltype(dd)::value;
+        if (fp32) launch_prolong<D, float>(l, levels[l].xy32, levels[l + 1].xy32, 1, stream);
+        else launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 1, stream);
+        return 0;
+    });
+    return launch_ok("prolong");
+}
+
+// Random<double> (Misha/Geometry.inl:430-438) on the C library generator
+static double RandomDouble()
+{
+    const unsigned long long ULL_RAND_MAX = (unsigned long long)(RAND_MAX) + 1;
+    const double RAND_MAX_SQUARED = double(ULL_RAND_MAX * ULL_RAND_MAX - 1);
+    unsigned long long r1 = rand();
+    unsigned long long r2 = rand();
+    long long v = (long long)(r1 * ULL_RAND_MAX + r2);
+    return double(v) / RAND_MAX_SQUARED;
+}
+
+bool Context::upload_xy(int l, const double *x, const double *y)
+{
+    std::vector<double> h(2 * levels[l].N);
+    for (int64_t i = 0; i < levels[l].N; i++) { h[2 * i] = x[i]; h[2 * i + 1] = y[i]; }
+    if (!cuda_ok(cudaMemcpyAsync(levels[l].xy64, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, stream), "upload xy")) return false;
+    if (!push_xy(l)) return false;
+    return cuda_ok(cudaStreamSynchronize(stream), "upload sync");
+}
+
+bool Context::download_xy(int l, double *x, double *y, bool fromSolution)
+{
+    std::vector<double> h(2 * levels[l].N);
+    double *src = fromSolution ? levels[l].tmp64 : levels[l].xy64;
+    if (!fromSolution && !pull_xy(l)) return false;
+    if (!cuda_ok(cudaMemcpyAsync(h.data(), src, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream), "download xy")) return false;
+    if (!cuda_ok(cudaStreamSynchronize(stream), "download sync")) return false;
+    for (int64_t i = 0; i < levels[l].N; i++) { x[i] = h[2 * i]; y[i] = h[2 * i + 1]; }
+    return true;
+}
+
+// The reference's cascadic schedule (ExteriorPoisson.h:315-409)
+bool Context::solve_cascadic()
+{
+    const int minD = std::min(P.min_solve_depth, depth);
+    const int maxD = P.max_solve_depth < 0 ? depth : std::min(P.max_solve_depth, depth);
+    bool fp32 = P.precision == EPR_FP32;
+    for (int l = 0; l <= depth; l++)
+    {
+        if (!cuda_ok(cudaMemsetAsync(levels[l].xy64, 0, sizeof(double) * 2 * levels[l].N, stream), "clear")) return false;
+        if (fp32 && !cuda_ok(cudaMemsetAsync(levels[l].xy32, 0, sizeof(float) * 2 * levels[l].N, stream), "clear")) return false;
+    }
+    // random initial guess at the coarsest solve level, scaled to the target's magnitude
+    {
+        srand(P.seed);
+        int64_t N = levels[minD].N;
+        std::vector<double> x(N), y(N);
+        for (int64_t i = 0; i < N; i++) { x[i] = RandomDouble(); y[i] = RandomDouble(); }
+        if (!upload_xy(minD, x.data(), y.data())) return false;
+        double e[3];
+        if (!energy(minD, e)) return false;
+        double s = std::sqrt(std::sqrt(c / e[2]));
+        for (int64_t i = 0; i < N; i++) { x[i] *= s; y[i] *= s; }
+        if (!upload_xy(minD, x.data(), y.data())) return false;
+    }
+    cudaEventRecord(ev0, stream);
+    for (int l = minD; l <= maxD; l++)
+    {
+        int iters = (int)std::ceil(std::pow(P.i_mult, depth - l) * P.gs_iters);
+        double e0[3] = {0, 0, 0};
+        if (P.verbose && !energy(l, e0)) return false;
+        if (!gs(l, iters)) return false;
+        if (P.verbose)
+        {
+            double e1[3];
+            if (!energy(l, e1)) return false;
+            printf("Error[%2d]: %9.5f -> %.5f = %.5f + %.5f\n", 1 << l, e0[0] + e0[1], e1[0] + e1[1], e1[0], e1[1]);
+        }
+        if (l < maxD && !prolong_add(l)) return false;
+    }
+    cudaEventRecord(ev1, stream);
+    if (!check_errors()) return false;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    stats.solve_ms = ms;
+    double e[3];
+    if (!energy(maxD, e)) return false;
+    stats.initial_energy = c;
+    stats.fit_energy = e[0];
+    stats.reg_energy = e[1];
+    if (P.verbose)
+        printf("Error: %g -> %g = %g + %g => %g\n", c, e[0] + e[1], e[0], e[1], std::sqrt((e[0] + e[1]) / c));
+    // regular coefficients of every level in xy64, then hierarchical residuals into tmp64
+    for (int l = 0; l <= depth; l++)
+        if (!pull_xy(l)) return false;
+    for (int l = maxD; l < depth; l++)
+    {
+        with_dim(this, [&](auto dd) {
+            constexpr int D = decltype(dd)::value;
+            launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 0, stream);
+            return 0;
+        });
+    }
+    for (int l = 0; l <= depth; l++)
+    {
+        if (!levels[l].tmp64 && !alloc((void **)&levels[l].tmp64, sizeof(double) * 2 * levels[l].N, "alloc sol")) return false;
+        if (!cuda_ok(cudaMemcpyAsync(levels[l].tmp64, levels[l].xy64, sizeof(double) * 2 * levels[l].N, cudaMemcpyDeviceToDevice, stream), "copy")) return false;
+    }
+    for (int l = depth; l > 0; l--)
+    {
+        // tmp64[l] -= P xy64[l-1]: prolong into a scratch then subtract
+        double *scratch = nullptr;
+        if (!alloc((void **)&scratch, sizeof(double) * 2 * levels[l].N, "alloc scratch")) return false;
+        with_dim(this, [&](auto dd) {
+            constexpr int D = decltype(dd)::value;
+            launch_prolong<D, double>(l - 1, levels[l - 1].xy64, scratch, 0, stream);
+            return 0;
+        });
+        launch_axpy<double>(levels[l].tmp64, scratch, 2 * levels[l].N, -1.0, stream);
+        release(scratch);
+        if (!launch_ok("hierarchical")) return false;
+    }
+    solved = true;
+    return cuda_ok(cudaStreamSynchronize(stream), "solve sync");
+}
+
+}  // namespace epr
+
+using epr::Context;
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+extern "C" {
+
+void epr_default_params(epr_params *p)
+{
+    if (!p) return;
+    p->s_weight = 100.;
+    p->d_weight = 0.00625;
+    p->n_sigma = 0.25;
+    p->i_mult = 2.;
+    p->t_radius = 1;
+    p->d_radius = 1;
+    p->gs_iters = 10;
+    p->min_solve_depth = 0;
+    p->max_solve_depth = -1;
+    p->seed = 0;
+    p->precision = EPR_FP64;
+    p->solver = EPR_SOLVER_CASCADIC;
+    p->tolerance = 1e-6;
+    p->max_cycles = 200;
+    p->verbose = 0;
+}
+
+const char *epr_global_error(void) { return g_error.c_str(); }
+
+struct epr_ctx : public epr::Context {};
+
+epr_ctx *epr_create(int dim, int depth, const epr_params *params)
+{
+    if (dim != 3 && dim != 4) { g_error = "dim must be 3 or 4"; return nullptr; }
+    int maxDepth = dim == 3 ? 10 : 7;
+    if (depth < 1 || depth > maxDepth) { g_error = "depth out of range (1.." + std::to_string(maxDepth) + ")"; return nullptr; }
+    epr_params p;
+    if (params) p = *params; else epr_default_params(&p);
+    if (p.t_radius < 0 || p.t_radius > 4 || p.d_radius < 0 || p.d_radius > 4) { g_error = "kernel radius must be in [0,4]"; return nullptr; }
+    if (p.precision != EPR_FP64 && p.precision != EPR_FP32) { g_error = "unknown precision"; return nullptr; }
+    epr_ctx *c = new epr_ctx;
+    c->dim = dim;
+    c->depth = depth;
+    c->P = p;
+    c->levels.resize(depth + 1);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess)
+    {
+        g_error = std::string("CUDA initialisation failed: ") + cudaGetErrorString(cudaGetLastError());
+        delete c;
+        return nullptr;
+    }
+    bool ok = c->alloc((void **)&c->red.partial, sizeof(double) * 4 * epr::Reduce::kMaxBlocks, "alloc reduce") &&
+              c->alloc((void **)&c->red.out, sizeof(double) * 4, "alloc reduce") &&
+              c->alloc((void **)&c->d_err, sizeof(unsigned int), "alloc flag") &&
+              c->cuda_ok(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream), "memset flag");
+    for (int l = 0; ok && l <= depth; l++) ok = c->ensure_level(l);
+    if (!ok)
+    {
+        g_error = c->err;
+        delete c;
+        return nullptr;
+    }
+    return c;
+}
+
+void epr_destroy(epr_ctx *ctx) { delete ctx; }
+
+const char *epr_last_error(const epr_ctx *ctx) { return ctx ? ctx->err.c_str() : g_error.c_str(); }
+
+#define EPR_CHECK_CTX(ctx) \
+    do { if (!(ctx)) { g_error = "null context"; return EPR_ERR_ARG; } (ctx)->status = EPR_OK; } while (0)
+#define EPR_CHECK_LEVEL(ctx, l) \
+    do { if ((l) < 0 || (l) > (ctx)->depth) { (ctx)->fail(EPR_ERR_ARG, "level %d out of range", (int)(l)); return EPR_ERR_ARG; } } while (0)
+#define EPR_RETURN(ctx, ok) return (ok) ? EPR_OK : ((ctx)->status ? (ctx)->status : EPR_ERR_CUDA)
+
+int epr_set_samples(epr_ctx *ctx, size_t n, const double *pos, const double *skew)
+{
+    EPR_CHECK_CTX(ctx);
+    if (!n || !pos || !skew) { ctx->fail(EPR_ERR_ARG, "expected some samples: %zu", n); return EPR_ERR_ARG; }
+    for (size_t i = 0; i < n * (size_t)ctx->dim; i++)
+        if (!std::isfinite(pos[i])) { ctx->fail(EPR_ERR_ARG, "sample %zu has a non-finite coordinate", i / ctx->dim); return EPR_ERR_ARG; }
+    size_t K = (size_t)(ctx->dim * (ctx->dim - 1) / 2);
+    for (size_t i = 0; i < n * K; i++)
+        if (!std::isfinite(skew[i])) { ctx->fail(EPR_ERR_ARG, "sample %zu has a non-finite frame", i / K); return EPR_ERR_ARG; }
+    EPR_RETURN(ctx, ctx->setup.set_samples(*ctx, n, pos, skew));
+}
+
+int epr_build(epr_ctx *ctx)
+{
+    EPR_CHECK_CTX(ctx);
+    if (!ctx->setup.n) { ctx->fail(EPR_ERR_STATE, "epr_build called before epr_set_samples"); return EPR_ERR_STATE; }
+    EPR_RETURN(ctx, ctx->setup.build(*ctx));
+}
+
+int epr_set_level_system(epr_ctx *ctx, int level, const double *R, const double *B, double c)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!R || !B) { ctx->fail(EPR_ERR_ARG, "null stencil"); return EPR_ERR_ARG; }
+    epr::Level &L = ctx->levels[level];
+    size_t S = (size_t)ctx->stencil();
+    // host column stencils (node-major) -> device offset-major
+    std::vector<double> a(S * L.N), b(S * L.N);
+    for (int64_t i = 0; i < L.N; i++)
+        for (size_t o = 0; o < S; o++) { a[o * L.N + i] = R[i * S + o]; b[o * L.N + i] = B[i * S + o]; }
+    bool ok = ctx->cuda_ok(cudaMemcpyAsync(L.A64, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice, ctx->stream), "upload R") &&
+              ctx->cuda_ok(cudaMemcpyAsync(L.B64, b.data(), sizeof(double) * b.size(), cudaMemcpyHostToDevice, ctx->stream), "upload B") &&
+              epr::add_dirichlet(*ctx, level) && ctx->sync_system32(level) &&
+              ctx->cuda_ok(cudaStreamSynchronize(ctx->stream), "sync");
+    ctx->c = c;
+    ctx->have_system = true;
+    EPR_RETURN(ctx, ok);
+}
+
+int epr_set_coefficients(epr_ctx *ctx, int level, const double *x, const double *y)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!x || !y) { ctx->fail(EPR_ERR_ARG, "null coefficients"); return EPR_ERR_ARG; }
+    EPR_RETURN(ctx, ctx->upload_xy(level, x, y));
+}
+
+int epr_get_coefficients(epr_ctx *ctx, int level, double *x, double *y)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!x || !y) { ctx->fail(EPR_ERR_ARG, "null output"); return EPR_ERR_ARG; }
+    EPR_RETURN(ctx, ctx->download_xy(level, x, y, false));
+}
+
+int epr_energy(epr_ctx *ctx, int level, double *out3)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!out3) { ctx->fail(EPR_ERR_ARG, "null output"); return EPR_ERR_ARG; }
+    EPR_RETURN(ctx, ctx->energy(level, out3));
+}
+
+int epr_quadfit(epr_ctx *ctx, int level, double *out)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!out) { ctx->fail(EPR_ERR_ARG, "null output"); return EPR_ERR_ARG; }
+    epr::Level &L = ctx->levels[level];
+    double *d = nullptr;
+    bool ok = ctx->alloc((void **)&d, sizeof(double) * 5 * L.N, "alloc fit");
+    if (ok)
+    {
+        bool fp32 = ctx->P.precision == EPR_FP32;
+        epr::with_dim(ctx, [&](auto dd) {
+            constexpr int D = decltype(dd)::value;
+            if (fp32) epr::launch_quadfit<D, float>(epr::level_ptrs<float>(ctx, level), L.xy32, d, ctx->stream);
+            else epr::launch_quadfit<D, double>(epr::level_ptrs<double>(ctx, level), L.xy64, d, ctx->stream);
+            return 0;
+        });
+        ok = ctx->launch_ok("quadfit") &&
+             ctx->cuda_ok(cudaMemcpyAsync(out, d, sizeof(double) * 5 * L.N, cudaMemcpyDeviceToHost, ctx->stream), "copy fit") &&
+             ctx->cuda_ok(cudaStreamSynchronize(ctx->stream), "sync");
+        ctx->release(d);
+    }
+    EPR_RETURN(ctx, ok);
+}
+
+int epr_gradient(epr_ctx *ctx, int level, double *gx, double *gy)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!gx || !gy) { ctx->fail(EPR_ERR_ARG, "null output"); return EPR_ERR_ARG; }
+    std::vector<double> q(5 * ctx->levels[level].N);
+    int rc = epr_quadfit(ctx, level, q.data());
+    if (rc) return rc;
+    for (int64_t i = 0; i < ctx->levels[level].N; i++) { gx[i] = q[5 * i + 3]; gy[i] = q[5 * i + 4]; }
+    return EPR_OK;
+}
+
+int epr_gs(epr_ctx *ctx, int level, int iters)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (iters < 0) { ctx->fail(EPR_ERR_ARG, "negative iteration count"); return EPR_ERR_ARG; }
+    EPR_RETURN(ctx, ctx->gs(level, iters) && ctx->check_errors());
+}
+
+int epr_prolong(epr_ctx *ctx, int level)
+{
+    EPR_CHECK_CTX(ctx);
+    if (level < 0 || level >= ctx->depth) { ctx->fail(EPR_ERR_ARG, "level %d has no finer level", level); return EPR_ERR_ARG; }
+    EPR_RETURN(ctx, ctx->prolong_add(level) && ctx->cuda_ok(cudaStreamSynchronize(ctx->stream), "sync"));
+}
+
+int epr_gn_matvec(epr_ctx *ctx, int level, const double *dx, const double *dy, double *ox, double *oy)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!dx || !dy || !ox || !oy) { ctx->fail(EPR_ERR_ARG, "null vector"); return EPR_ERR_ARG; }
+    epr::Level &L = ctx->levels[level];
+    std::vector<double> h(2 * L.N);
+    for (int64_t i = 0; i < L.N; i++) { h[2 * i] = dx[i]; h[2 * i + 1] = dy[i]; }
+    double *d64 = nullptr, *o64 = nullptr;
+    float *d32 = nullptr, *o32 = nullptr;
+    bool fp32 = ctx->P.precision == EPR_FP32;
+    bool ok = ctx->alloc((void **)&d64, sizeof(double) * 2 * L.N, "alloc") && ctx->alloc((void **)&o64, sizeof(double) * 2 * L.N, "alloc") &&
+              ctx->cuda_ok(cudaMemcpyAsync(d64, h.data(), sizeof(double) * 2 * L.N, cudaMemcpyHostToDevice, ctx->stream), "upload");
+    if (ok && fp32)
+    {
+        ok = ctx->alloc((void **)&d32, sizeof(float) * 2 * L.N, "alloc") && ctx->alloc((void **)&o32, sizeof(float) * 2 * L.N, "alloc");
+        if (ok) epr::launch_convert_d2f(d64, d32, 2 * L.N, ctx->stream);
+    }
+    if (ok)
+    {
+        epr::with_dim(ctx, [&](auto dd) {
+            constexpr int D = decltype(dd)::value;
+            if (fp32) epr::launch_gn_matvec<D, float>(epr::level_ptrs<float>(ctx, level), L.xy32, d32, o32, ctx->stream);
+            else epr::launch_gn_matvec<D, double>(epr::level_ptrs<double>(ctx, level), L.xy64, d64, o64, ctx->stream);
+            return 0;
+        });
+        if (fp32) epr::launch_convert_f2d(o32, o64, 2 * L.N, ctx->stream);
+        ok = ctx->launch_ok("gn matvec") &&
+             ctx->cuda_ok(cudaMemcpyAsync(h.data(), o64, sizeof(double) * 2 * L.N, cudaMemcpyDeviceToHost, ctx->stream), "download") &&
+             ctx->cuda_ok(cudaStreamSynchronize(ctx->stream), "sync");
+        if (ok)
+            for (int64_t i = 0; i < L.N; i++) { ox[i] = h[2 * i]; oy[i] = h[2 * i + 1]; }
+    }
+    ctx->release(d64); ctx->release(o64); ctx->release(d32); ctx->release(o32);
+    EPR_RETURN(ctx, ok);
+}
+
+int epr_solve(epr_ctx *ctx, epr_stats *stats)
+{
+    EPR_CHECK_CTX(ctx);
+    if (!ctx->have_system) { ctx->fail(EPR_ERR_STATE, "epr_solve called before epr_build"); return EPR_ERR_STATE; }
+    ctx->stats.node_updates = 0;
+    bool ok;
+    if (ctx->P.solver == EPR_SOLVER_MULTIGRID) ok = epr::solve_multigrid(*ctx);
+    else ok = ctx->solve_cascadic();
+    if (ok && stats) *stats = ctx->stats;
+    EPR_RETURN(ctx, ok);
+}
+
+int epr_get_solution(epr_ctx *ctx, int level, double *x, double *y)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!ctx->solved) { ctx->fail(EPR_ERR_STATE, "no solution yet"); return EPR_ERR_STATE; }
+    if (!x || !y) { ctx->fail(EPR_ERR_ARG, "null output"); return EPR_ERR_ARG; }
+    EPR_RETURN(ctx, ctx->download_xy(level, x, y, true));
+}
+
+int epr_get_array(epr_ctx *ctx, const char *name, int level, double *out, size_t cap, size_t *count)
+{
+    EPR_CHECK_CTX(ctx);
+    if (!name) { ctx->fail(EPR_ERR_ARG, "null name"); return EPR_ERR_ARG; }
+    std::string nm(name);
+    if (nm == "R" || nm == "B" || nm == "A")
+    {
+        EPR_CHECK_LEVEL(ctx, level);
+        epr::Level &L = ctx->levels[level];
+        size_t S = (size_t)ctx->stencil(), n = S * (size_t)L.N;
+        if (count) *count = n;
+        if (!out) return EPR_OK;
+        if (cap < n) { ctx->fail(EPR_ERR_ARG, "output too small (%zu < %zu)", cap, n); return EPR_ERR_ARG; }
+        std::vector<double> a(n), r(n);
+        bool ok = ctx->cuda_ok(cudaMemcpyAsync(a.data(), nm == "B" ? L.B64 : L.A64, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+        if (ok && nm == "R")
+        {
+            // R = A - dWeight K
+            double *k = nullptr;
+            ok = ctx->alloc((void **)&k, sizeof(double) * n, "alloc") &&
+                 ctx->cuda_ok(cudaMemsetAsync(k, 0, sizeof(double) * n, ctx->stream), "memset") &&
+                 epr::add_dirichlet_to(*ctx, level, k, 1.0) &&
+                 ctx->cuda_ok(cudaMemcpyAsync(r.data(), k, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+            ctx->release(k);
+        }
+        ok = ok && ctx->cuda_ok(cudaStreamSynchronize(ctx->stream), "sync");
+        if (!ok) EPR_RETURN(ctx, false);
+        for (int64_t i = 0; i < L.N; i++)
+            for (size_t o = 0; o < S; o++)
+                out[i * S + o] = a[o * L.N + i] - (nm == "R" ? ctx->P.d_weight * r[o * L.N + i] : 0.);
+        return EPR_OK;
+    }
+    if (nm == "c")
+    {
+        if (count) *count = 1;
+        if (out && cap >= 1) out[0] = ctx->c;
+        return EPR_OK;
+    }
+    EPR_RETURN(ctx, ctx->setup.get(*ctx, nm, out, cap, count));
+}
+
+int epr_synchronize(epr_ctx *ctx)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_RETURN(ctx, ctx->cuda_ok(cudaStreamSynchronize(ctx->stream), "sync"));
+}
+
+}  // extern "C"

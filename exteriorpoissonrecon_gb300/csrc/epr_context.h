@@ -1,0 +1,99 @@
+// Internal state of one epr_ctx (see include/epr.h).  Host code only.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/epr.h"
+#include "epr_kernels.h"
+
+namespace epr {
+
+struct Context;
+
+// Device storage of one level of the hierarchy.
+struct Level
+{
+    int64_t N = 0;
+    double *xy64 = nullptr;   // interleaved (x, y), regular coefficients
+    double *A64 = nullptr;    // R + dWeight K, column stencil, offset-major
+    double *B64 = nullptr;    // frame constraint, column stencil, offset-major
+    double *tmp64 = nullptr;  // hierarchical solution after a solve
+    float *xy32 = nullptr;    // float copies used when precision == EPR_FP32
+    float *A32 = nullptr;
+    float *B32 = nullptr;
+    float *tmp32 = nullptr;
+};
+
+// Sample-side state of the build (ordered sampling, estimator, splats).  Defined in epr_setup.cu.
+struct Setup
+{
+    size_t n = 0;               // samples
+    int64_t ncells = 0;         // occupied finest cells
+    double *pos = nullptr;      // n x dim, unit cube
+    double *skew = nullptr;     // n x K packed frames
+    int *order = nullptr;       // samples sorted by cell (Morton order of the cell, stable)
+    int64_t *cellKey = nullptr; // Morton key of each occupied cell
+    int *cellStart = nullptr;   // ncells + 1
+    int *cellOfFinest = nullptr;// dense map finest cell -> occupied index or -1
+    double *measure = nullptr, *noise = nullptr, *sdepth = nullptr;  // per sample
+    double *S = nullptr;        // finest elements x K
+    int *leaf = nullptr;        // leaf tree depth per finest element
+    std::vector<double *> density, skewGrid;  // per tree level
+    std::vector<uint8_t *> refinedD, refinedS; // per tree depth
+
+    bool set_samples(Context &c, size_t n, const double *pos, const double *skew);
+    bool build(Context &c);
+    bool get(Context &c, const std::string &name, double *out, size_t cap, size_t *count);
+    void release(Context &c);
+};
+
+struct Context
+{
+    int dim = 0, depth = 0;
+    epr_params P{};
+    std::string err;
+    int status = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<Level> levels;
+    Reduce red;
+    unsigned int *d_err = nullptr;
+    double *d_fit = nullptr;
+    double c = 0;
+    bool have_system = false;
+    bool solved = false;
+    epr_stats stats{};
+    Setup setup;
+
+    virtual ~Context();
+    void fail(int code, const char *fmt, ...);
+    bool cuda_ok(cudaError_t e, const char *what);
+    bool launch_ok(const char *what);
+    bool alloc(void **p, size_t bytes, const char *what);
+    void release(void *p);
+    int64_t nodes(int level) const;
+    int stencil() const;
+    bool ensure_level(int l);
+    bool sync_system32(int l);
+    bool push_xy(int l);
+    bool pull_xy(int l);
+    bool energy(int l, double *out3);
+    bool gs(int l, int iters);
+    bool check_errors();
+    bool prolong_add(int l);
+    bool upload_xy(int l, const double *x, const double *y);
+    bool download_xy(int l, double *x, double *y, bool fromSolution);
+    bool solve_cascadic();
+};
+
+// A64[level] += dWeight K (the Dirichlet stiffness of the level, with the reference's
+// resolution-1 stencil table, see epr_setup.cu)
+bool add_dirichlet(Context &c, int level);
+bool add_dirichlet_to(Context &c, int level, double *dst, double w);
+// Nonlinear multigrid driver (epr_mg.cu)
+bool solve_multigrid(Context &c);
+
+}  // namespace epr

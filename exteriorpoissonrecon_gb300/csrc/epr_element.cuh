@@ -1,0 +1,281 @@
+// Exact element integrals of the quartic "wedge" term of the energy.
+//
+// On one element the fields x, y are multilinear; the 2-form
+//     W(x,y)_{PQ} = (d_P y d_Q x - d_P x d_Q y) / 2         (P > Q)
+// is the reference's alternating product grad x ^ grad y (Include/Hat.inl:32-37, 243-248:
+// packed entry (i,j), i > j, of (v1 v2^T - v2 v1^T)/2 with v1 = grad x, v2 = grad y), and the
+// fitting energy integrates its Frobenius norm (Hat.inl:358-370: the packed inner product counts
+// every off-diagonal entry twice).  The reference evaluates these integrals through precomputed
+// per-node stencils of 1,358 (3D) / 22,952 (4D) coefficients (Hat.products.inl:32-107).  Here
+// they are integrated per element and per component:
+//   component (P,Q) of W is linear in xi_P and xi_Q and quadratic in the other coordinates, so the
+//   product of two such components is integrated exactly by a 2 x 2 x 3^(D-2) Gauss rule
+//   (12 points in 3D, 36 in 4D).  Gradients at the Gauss points come from sum factorisation:
+//   corner differences along one axis, then 1-D interpolation axis by axis.
+//
+// All routines work in reference-element units; integrals over the physical element (side 1/r)
+// are the returned sums times r^(4-D)/2, which the callers apply (a power of two: exact).
+#pragma once
+#include "epr_common.cuh"
+
+namespace epr {
+
+template <int D>
+__host__ __device__ constexpr int cbit(int c, int d) { return (c >> (D - 1 - d)) & 1; }
+
+// The two axes (P > Q) of packed component k, in the reference's packing order
+// (k = P(P-1)/2 + Q, Hat.inl:32-37), and the remaining axes in increasing order.
+template <int D, int K>
+struct Component
+{
+    static constexpr int P = (K == 0) ? 1 : (K <= 2) ? 2 : (K <= 5) ? 3 : -1;
+    static constexpr int Q = K - P * (P - 1) / 2;
+    static constexpr int M = D - 2;
+    static constexpr int other(int m)
+    {
+        int c = 0;
+        for (int d = 0; d < D; d++)
+        {
+            if (d == P || d == Q) continue;
+            if (c == m) return d;
+            c++;
+        }
+        return -1;
+    }
+    // corner index with the given bits on P, Q and the others (others: bit (M-1-m) of bo <-> axis other(m))
+    static constexpr int corner(int bP, int bQ, int bo)
+    {
+        int c = bP << (D - 1 - P) | bQ << (D - 1 - Q);
+        for (int m = 0; m < M; m++) c |= ((bo >> (M - 1 - m)) & 1) << (D - 1 - other(m));
+        return c;
+    }
+};
+
+// 1-D hat pieces at Gauss points
+template <typename Real>
+__device__ __forceinline__ Real hat2(int b, int g) { return b ? (Real)Gauss::X2(g) : (Real)(1.0 - Gauss::X2(g)); }
+template <typename Real>
+__device__ __forceinline__ Real hat3(int b, int g) { return b ? (Real)Gauss::X3(g) : (Real)(1.0 - Gauss::X3(g)); }
+
+// Derivative of a multilinear corner field along axis A (the "derived" axis), tabulated at
+// 2 Gauss points of axis B (the partner axis of the component) and 3 Gauss points of each other
+// axis.  out[g * 3^M + go] with go enumerating the others (first other slowest).
+template <int D, int K, bool AisP, typename Real>
+__device__ __forceinline__ void derivative_table(const Real *f, Real *out)
+{
+    using Cp = Component<D, K>;
+    constexpr int M = Cp::M;
+    constexpr int NO = 1 << M;      // other-axis corners
+    constexpr int NG = ipow(3, M);  // other-axis Gauss points
+    // difference along A, indexed [bB][bo]
+    Real dif[2][NO];
+#pragma unroll
+    for (int bB = 0; bB < 2; bB++)
+#pragma unroll
+        for (int bo = 0; bo < NO; bo++)
+        {
+            int c1 = AisP ? Cp::corner(1, bB, bo) : Cp::corner(bB, 1, bo);
+            int c0 = AisP ? Cp::corner(0, bB, bo) : Cp::corner(bB, 0, bo);
+            dif[bB][bo] = f[c1] - f[c0];
+        }
+    // interpolate along B at the 2-point rule
+    Real t[2][NO];
+#pragma unroll
+    for (int g = 0; g < 2; g++)
+#pragma unroll
+        for (int bo = 0; bo < NO; bo++) t[g][bo] = hat2<Real>(0, g) * dif[0][bo] + hat2<Real>(1, g) * dif[1][bo];
+    // interpolate along the others at the 3-point rule
+    if constexpr (M == 1)
+    {
+#pragma unroll
+        for (int g = 0; g < 2; g++)
+#pragma unroll
+            for (int go = 0; go < 3; go++) out[g * NG + go] = hat3<Real>(0, go) * t[g][0] + hat3<Real>(1, go) * t[g][1];
+    }
+    else
+    {
+#pragma unroll
+        for (int g = 0; g < 2; g++)
+#pragma unroll
+            for (int g0 = 0; g0 < 3; g0++)
+            {
+                Real u0 = hat3<Real>(0, g0) * t[g][0] + hat3<Real>(1, g0) * t[g][2];  // bo = b0*2 + b1
+                Real u1 = hat3<Real>(0, g0) * t[g][1] + hat3<Real>(1, g0) * t[g][3];
+#pragma unroll
+                for (int g1 = 0; g1 < 3; g1++) out[g * NG + g0 * 3 + g1] = hat3<Real>(0, g1) * u0 + hat3<Real>(1, g1) * u1;
+            }
+    }
+}
+
+template <int M>
+__device__ __forceinline__ double other_weight(int go)
+{
+    if constexpr (M == 1) return Gauss::W3(go);
+    else return Gauss::W3(go / 3) * Gauss::W3(go % 3);
+}
+
+// ---------------------------------------------------------------------------------------------
+// sum over the Gauss points of |W|^2 (reference units), one component
+// ---------------------------------------------------------------------------------------------
+template <int D, int K, typename Real>
+__device__ __forceinline__ Real component_wedge(const Real *x, const Real *y)
+{
+    constexpr int NG = ipow(3, D - 2);
+    Real xP[2 * NG], xQ[2 * NG], yP[2 * NG], yQ[2 * NG];
+    derivative_table<D, K, true>(x, xP);
+    derivative_table<D, K, false>(x, xQ);
+    derivative_table<D, K, true>(y, yP);
+    derivative_table<D, K, false>(y, yQ);
+    Real s = 0;
+#pragma unroll
+    for (int gp = 0; gp < 2; gp++)
+#pragma unroll
+        for (int gq = 0; gq < 2; gq++)
+#pragma unroll
+            for (int go = 0; go < NG; go++)
+            {
+                Real w = (Real)(Gauss::W2(gp) * Gauss::W2(gq) * other_weight<D - 2>(go));
+                Real W = yP[gq * NG + go] * xQ[gp * NG + go] - xP[gq * NG + go] * yQ[gp * NG + go];
+                s += w * W * W;
+            }
+    return s;
+}
+
+template <int D, typename Real>
+__device__ __forceinline__ Real element_wedge(const Real *x, const Real *y)
+{
+    Real s = component_wedge<D, 0>(x, y) + component_wedge<D, 1>(x, y) + component_wedge<D, 2>(x, y);
+    if constexpr (D == 4) s += component_wedge<D, 3>(x, y) + component_wedge<D, 4>(x, y) + component_wedge<D, 5>(x, y);
+    return s;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Quadratic-fit integrals of corner A of the element, one component (reference units):
+//   h0 = sum |U|^2, h1 = sum |V|^2, h2 = sum <U,V>, h3 = sum <W,U>, h4 = sum <W,V>
+// with U = W(phi_A, y), V = W(x, phi_A) (the derivatives of W along x_A and y_A).
+// ---------------------------------------------------------------------------------------------
+template <int D, int K, typename Real>
+__device__ __forceinline__ void component_fit(const Real *x, const Real *y, int A, Real *h)
+{
+    using Cp = Component<D, K>;
+    constexpr int M = Cp::M;
+    constexpr int NG = ipow(3, M);
+    Real xP[2 * NG], xQ[2 * NG], yP[2 * NG], yQ[2 * NG];
+    derivative_table<D, K, true>(x, xP);
+    derivative_table<D, K, false>(x, xQ);
+    derivative_table<D, K, true>(y, yP);
+    derivative_table<D, K, false>(y, yQ);
+    const int aP = cbit<D>(A, Cp::P), aQ = cbit<D>(A, Cp::Q);
+    const Real sP = aP ? (Real)1 : (Real)-1, sQ = aQ ? (Real)1 : (Real)-1;
+    int ao[M > 0 ? M : 1];
+#pragma unroll
+    for (int m = 0; m < M; m++) ao[m] = cbit<D>(A, Cp::other(m));
+#pragma unroll
+    for (int go = 0; go < NG; go++)
+    {
+        Real lo;
+        if constexpr (M == 1) lo = hat3<Real>(ao[0], go);
+        else lo = hat3<Real>(ao[0], go / 3) * hat3<Real>(ao[1], go % 3);
+        Real wo = (Real)other_weight<M>(go);
+#pragma unroll
+        for (int gp = 0; gp < 2; gp++)
+#pragma unroll
+            for (int gq = 0; gq < 2; gq++)
+            {
+                Real w = (Real)(Gauss::W2(gp) * Gauss::W2(gq)) * wo;
+                Real phP = sP * hat2<Real>(aQ, gq) * lo;
+                Real phQ = sQ * hat2<Real>(aP, gp) * lo;
+                Real xp = xP[gq * NG + go], xq = xQ[gp * NG + go];
+                Real yp = yP[gq * NG + go], yq = yQ[gp * NG + go];
+                Real W = yp * xq - xp * yq;
+                Real U = yp * phQ - phP * yq;
+                Real V = phP * xq - xp * phQ;
+                Real wU = w * U, wV = w * V;
+                h[0] += wU * U;
+                h[1] += wV * V;
+                h[2] += wU * V;
+                h[3] += wU * W;
+                h[4] += wV * W;
+            }
+    }
+}
+
+template <int D, typename Real>
+__device__ __forceinline__ void element_fit(const Real *x, const Real *y, int A, Real *h)
+{
+    component_fit<D, 0>(x, y, A, h);
+    component_fit<D, 1>(x, y, A, h);
+    component_fit<D, 2>(x, y, A, h);
+    if constexpr (D == 4)
+    {
+        component_fit<D, 3>(x, y, A, h);
+        component_fit<D, 4>(x, y, A, h);
+        component_fit<D, 5>(x, y, A, h);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Gauss-Newton products for corner A: J(d) = W(dx, y) + W(x, dy);
+//   s[0] = sum <J(d), U>,  s[1] = sum <J(d), V>   (reference units)
+// ---------------------------------------------------------------------------------------------
+template <int D, int K, typename Real>
+__device__ __forceinline__ void component_gn(const Real *x, const Real *y, const Real *dx, const Real *dy, int A, Real *s)
+{
+    using Cp = Component<D, K>;
+    constexpr int M = Cp::M;
+    constexpr int NG = ipow(3, M);
+    Real xP[2 * NG], xQ[2 * NG], yP[2 * NG], yQ[2 * NG];
+    Real dxP[2 * NG], dxQ[2 * NG], dyP[2 * NG], dyQ[2 * NG];
+    derivative_table<D, K, true>(x, xP);
+    derivative_table<D, K, false>(x, xQ);
+    derivative_table<D, K, true>(y, yP);
+    derivative_table<D, K, false>(y, yQ);
+    derivative_table<D, K, true>(dx, dxP);
+    derivative_table<D, K, false>(dx, dxQ);
+    derivative_table<D, K, true>(dy, dyP);
+    derivative_table<D, K, false>(dy, dyQ);
+    const int aP = cbit<D>(A, Cp::P), aQ = cbit<D>(A, Cp::Q);
+    const Real sP = aP ? (Real)1 : (Real)-1, sQ = aQ ? (Real)1 : (Real)-1;
+    int ao[M > 0 ? M : 1];
+#pragma unroll
+    for (int m = 0; m < M; m++) ao[m] = cbit<D>(A, Cp::other(m));
+#pragma unroll
+    for (int go = 0; go < NG; go++)
+    {
+        Real lo;
+        if constexpr (M == 1) lo = hat3<Real>(ao[0], go);
+        else lo = hat3<Real>(ao[0], go / 3) * hat3<Real>(ao[1], go % 3);
+        Real wo = (Real)other_weight<M>(go);
+#pragma unroll
+        for (int gp = 0; gp < 2; gp++)
+#pragma unroll
+            for (int gq = 0; gq < 2; gq++)
+            {
+                Real w = (Real)(Gauss::W2(gp) * Gauss::W2(gq)) * wo;
+                Real phP = sP * hat2<Real>(aQ, gq) * lo;
+                Real phQ = sQ * hat2<Real>(aP, gp) * lo;
+                int ip = gq * NG + go, iq = gp * NG + go;
+                Real J = (yP[ip] * dxQ[iq] - dxP[ip] * yQ[iq]) + (dyP[ip] * xQ[iq] - xP[ip] * dyQ[iq]);
+                Real U = yP[ip] * phQ - phP * yQ[iq];
+                Real V = phP * xQ[iq] - xP[ip] * phQ;
+                s[0] += w * J * U;
+                s[1] += w * J * V;
+            }
+    }
+}
+
+template <int D, typename Real>
+__device__ __forceinline__ void element_gn(const Real *x, const Real *y, const Real *dx, const Real *dy, int A, Real *s)
+{
+    component_gn<D, 0>(x, y, dx, dy, A, s);
+    component_gn<D, 1>(x, y, dx, dy, A, s);
+    component_gn<D, 2>(x, y, dx, dy, A, s);
+    if constexpr (D == 4)
+    {
+        component_gn<D, 3>(x, y, dx, dy, A, s);
+        component_gn<D, 4>(x, y, dx, dy, A, s);
+        component_gn<D, 5>(x, y, dx, dy, A, s);
+    }
+}
+
+}  // namespace epr

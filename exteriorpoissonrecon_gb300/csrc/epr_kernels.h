@@ -1,0 +1,53 @@
+// Host-side declarations of the CUDA launchers (instantiated for Dim 3/4 and double/float in
+// epr_solve.cu and epr_setup.cu).  Only plain pointers and sizes cross this header.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace epr {
+
+// One level of the hierarchy as the solve kernels see it.
+template <typename Real>
+struct LevelPtrs
+{
+    int level = 0;
+    int64_t N = 0;            // nodes
+    Real *xy = nullptr;       // 2N interleaved (x, y)
+    const Real *A = nullptr;  // 3^Dim * N column stencil of R + dWeight K (offset-major)
+    const Real *B = nullptr;  // 3^Dim * N column stencil of the frame constraint
+};
+
+// Scratch for deterministic two-pass reductions
+struct Reduce
+{
+    double *partial = nullptr;  // >= kMaxBlocks * 4 doubles
+    double *out = nullptr;      // >= 4 doubles
+    static constexpr int kMaxBlocks = 4096;
+};
+
+template <int D, typename Real>
+void launch_energy(const LevelPtrs<Real> &L, const Real *xy, const Reduce &red, cudaStream_t s);
+// writes N x 5 doubles (Q20, Q02, Q11, Q10, Q01)
+template <int D, typename Real>
+void launch_quadfit(const LevelPtrs<Real> &L, const Real *xy, double *out, cudaStream_t s);
+template <int D, typename Real>
+void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, cudaStream_t s);
+template <int D, typename Real>
+void launch_gn_matvec(const LevelPtrs<Real> &L, const Real *xy, const Real *dxy, Real *out, cudaStream_t s);
+// fine (2 N_f) = P coarse (2 N_c), pairs; add != 0 accumulates
+template <int D, typename Real>
+void launch_prolong(int coarseLevel, const Real *coarse, Real *fine, int add, cudaStream_t s);
+// coarse = P^T fine, pairs
+template <int D, typename Real>
+void launch_restrict(int coarseLevel, const Real *fine, Real *coarse, cudaStream_t s);
+
+// elementwise helpers
+template <typename Real>
+void launch_scale(Real *v, int64_t n, double s, cudaStream_t st);
+template <typename Real>
+void launch_axpy(Real *y, const Real *x, int64_t n, double a, cudaStream_t st);
+void launch_convert_d2f(const double *in, float *out, int64_t n, cudaStream_t st);
+void launch_convert_f2d(const float *in, double *out, int64_t n, cudaStream_t st);
+
+}  // namespace epr

@@ -1,0 +1,1114 @@
+// Build phase on the device: ordered sampling, the density estimator, the frame splat, S(E), and
+// the screening (R), constraint (B) and Dirichlet (K) stencils with their Galerkin hierarchy.
+//
+// Reference correspondence (paths relative to the reference checkout):
+//   sort by cell             OrderedSampler                      Include/OrderedSamples.inl:32-85
+//   density splat            TreeEstimator ctor / addSamples     Include/GridSamples.inl:361-391,436-491,740-771
+//   estimator queries        TreeEstimator::operator()/depth     Include/GridSamples.inl:774-896
+//   frame splat              Reconstructor ctor                  ExteriorPoissonRecon/ExteriorPoisson.h:181-264
+//   S(E)                     TreeSplatter::operator()(p)         Include/GridSamples.inl:600-651
+//   R                        ScalarFunctions::deltaMass          Include/Hat.scalars.inl:977-1063
+//   B, c                     ScalarFunctions::stiffness, ctor    Include/Hat.scalars.inl:1585-1690, SystemEnergy.h:447-462
+//   K                        StiffnessStencil / FullIntegrationStencil  Include/Hat.scalars.inl:261-293,528-545
+//   Galerkin                 SingleCycleCascadicSystemEnergy::restrict  Include/SystemEnergy.h:464-477
+//
+// The reference's trees (RegularTreeNode) are stored here as dense per-depth vertex grids: a node
+// that the reference never creates never receives data, so its dense value is zero.  The only
+// structural information the reference uses is which cells have children (the depth of the leaf
+// containing a point); it is kept as one byte per cell and depth.
+//
+// Splats are deterministic gathers: samples are sorted by the Morton key of their cell, so the
+// samples of any coarser cell are one contiguous range; every output vertex is reduced by one
+// warp in a fixed order.
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include <cub/cub.cuh>
+
+#include "epr_common.cuh"
+#include "epr_setup.h"
+
+namespace epr {
+
+namespace {
+
+constexpr int kMaxDeg = 9;  // 2 * 4 + 1
+
+// ---------------------------------------------------------------------------------------------
+// small device helpers
+// ---------------------------------------------------------------------------------------------
+__device__ inline void bspline_eval(int deg, double x, double *v)
+{
+    // iterative form of the recursive evaluation of GridSamples.inl:50-65
+    v[deg] = 1.;
+    for (int k = 1; k <= deg; k++)
+    {
+        const double scale = 1. / k;
+        int b = deg - k;
+        v[b] = v[b + 1] * (1. - x) * scale;
+        for (int i = 1; i < k; i++)
+        {
+            double x1 = (x - i + k), x2 = (-x + i + 1);
+            v[b + i] = (v[b + i] * x1 + v[b + i + 1] * x2) * scale;
+        }
+        v[b + k] *= x * scale;
+    }
+}
+
+template <int D>
+__host__ __device__ inline int64_t morton(const int *E, int bits)
+{
+    int64_t k = 0;
+    for (int b = bits - 1; b >= 0; b--)
+        for (int d = 0; d < D; d++) k = (k << 1) | ((E[d] >> b) & 1);
+    return k;
+}
+
+template <int D>
+__host__ __device__ inline void demorton(int64_t k, int bits, int *E)
+{
+    for (int d = 0; d < D; d++) E[d] = 0;
+    for (int b = 0; b < bits; b++)
+        for (int d = D - 1; d >= 0; d--) { E[d] |= (int)(k & 1) << b; k >>= 1; }
+}
+
+// first index in sorted keys[0..n) with key >= v
+__device__ inline int64_t lower_bound(const int64_t *keys, int64_t n, int64_t v)
+{
+    int64_t lo = 0, hi = n;
+    while (lo < hi)
+    {
+        int64_t mid = (lo + hi) >> 1;
+        if (keys[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// cell of p at resolution res as the reference's tree descent finds it (strict ">" at splits,
+// Misha/RegularTree.inl:538-543): points on a face belong to the lower cell
+__device__ inline int tree_cell(double p, int res)
+{
+    double s = p * res;
+    int o = (int)floor(s);
+    if ((double)o == s && o > 0) o--;
+    return o;
+}
+
+__device__ inline double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+inline unsigned int nblocks(int64_t n, int t) { return (unsigned int)((n + t - 1) / t); }
+
+// ---------------------------------------------------------------------------------------------
+// ordered sampling
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__global__ void cell_keys_kernel(const double *pos, int64_t n, int depth, int64_t *keys, int *vals)
+{
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int r = 1 << depth;
+    int E[D];
+    for (int d = 0; d < D; d++)
+    {
+        int e = (int)floor(pos[i * D + d] * r);
+        E[d] = e < 0 ? 0 : (e > r - 1 ? r - 1 : e);
+    }
+    keys[i] = morton<D>(E, depth);
+    vals[i] = (int)i;
+}
+
+__global__ void cell_flags_kernel(const int64_t *keys, int64_t n, int *flags)
+{
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    flags[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+__global__ void cell_start_kernel(const int64_t *keys, const int *flags, const int *ids, int64_t n, int *cellStart,
+                                  int64_t *cellKey)
+{
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (flags[i]) { cellStart[ids[i]] = (int)i; cellKey[ids[i]] = keys[i]; }
+    if (i == n - 1) cellStart[ids[i] + 1] = (int)n;
+}
+
+template <int D>
+__global__ void finest_map_kernel(const int64_t *cellKey, int64_t ncells, int depth, int *map)
+{
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= ncells) return;
+    int E[D];
+    demorton<D>(cellKey[k], depth, E);
+    int r = 1 << depth;
+    int64_t e = 0;
+    for (int d = 0; d < D; d++) e = e * r + E[d];
+    map[e] = (int)k;
+}
+
+// merged sample of each occupied cell: mean position and (count, sum p, sum p p^T)
+// (GridSamples.inl:381-388 with DensityAndNoiseInfo(p, 1), :74)
+template <int D>
+__global__ void merge_cells_kernel(const double *pos, const int *order, const int *cellStart, int64_t ncells,
+                                   double *mean, double *datum)
+{
+    constexpr int W = 1 + D + D * D;
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= ncells) return;
+    double p[D], dat[W];
+    for (int d = 0; d < D; d++) p[d] = 0;
+    for (int w = 0; w < W; w++) dat[w] = 0;
+    for (int j = cellStart[k]; j < cellStart[k + 1]; j++)
+    {
+        const double *q = pos + (int64_t)order[j] * D;
+        for (int d = 0; d < D; d++) p[d] += q[d];
+        dat[0] += 1.;
+        for (int d = 0; d < D; d++) dat[1 + d] += q[d];
+        for (int a = 0; a < D; a++)
+            for (int b = 0; b < D; b++) dat[1 + D + a * D + b] += q[a] * q[b];
+    }
+    double cnt = (double)(cellStart[k + 1] - cellStart[k]);
+    for (int d = 0; d < D; d++) mean[k * D + d] = p[d] / cnt;
+    for (int w = 0; w < W; w++) datum[k * W + w] = dat[w];
+}
+
+// ---------------------------------------------------------------------------------------------
+// tree structure: refined[t][cell] = 1 when the depth-t cell has children (RegularTree.inl:728-845)
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__global__ void refine_kernel(const int64_t *cellKey, int64_t ncells, int depth, int t, int KR, const uint8_t *prevRefined,
+                              uint8_t *refined)
+{
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= ncells) return;
+    int E[D];
+    demorton<D>(cellKey[k], depth, E);
+    int lo[D], hi[D], I[D];
+    int side = 1 << t, pside = 1 << (t - 1);
+    for (int d = 0; d < D; d++)
+    {
+        int ct = E[d] >> (depth - t);  // ancestor at tree depth t+1
+        lo[d] = (ct - KR) >> 1;
+        hi[d] = (ct + KR + 1) >> 1;
+        I[d] = lo[d];
+    }
+    while (true)
+    {
+        bool ok = true;
+        int64_t li = 0, pi = 0;
+        for (int d = 0; d < D; d++)
+        {
+            if (I[d] < 0 || I[d] >= side) ok = false;
+            li = li * side + I[d];
+            pi = pi * pside + (I[d] >> 1);
+        }
+        if (ok && (t == 1 || prevRefined[pi])) refined[li] = 1;
+        int d = D - 1;
+        for (; d >= 0; d--) { if (++I[d] <= hi[d]) break; I[d] = lo[d]; }
+        if (d < 0) break;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// splat gathers: one warp per vertex of tree depth t (resolution 2^(t-1))
+// ---------------------------------------------------------------------------------------------
+struct SplatArgs
+{
+    const int64_t *cellKey;
+    const int *cellStart;
+    int64_t ncells;
+    int depth;  // finest depth
+    int t;      // tree depth of the grid
+    int KR;     // kernel radius (B-spline degree 2 KR + 1)
+};
+
+// range of occupied cells inside the depth-t cell C
+template <int D>
+__device__ inline void cell_range(const SplatArgs &a, const int *C, int64_t &lo, int64_t &hi)
+{
+    int s = a.depth + 1 - a.t;  // levels between depth-t cells and finest cells
+    int64_t m = morton<D>(C, a.t - 1);
+    lo = lower_bound(a.cellKey, a.ncells, m << (D * s));
+    hi = lower_bound(a.cellKey, a.ncells, (m + 1) << (D * s));
+}
+
+// Density splat of the merged cells (TreeSplatter::_addSample, GridSamples.inl:458-491 with the
+// depth weight of TreeEstimator, GridSamples.inl:749-760).
+template <int D>
+__global__ void density_gather_kernel(SplatArgs a, const double *mean, const double *datum, double depthWeight, double *grid)
+{
+    constexpr int W = 1 + D + D * D;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    int res = 1 << (a.t - 1), nv = res + 1;
+    int64_t NV = 1;
+    for (int d = 0; d < D; d++) NV *= nv;
+    if (warp >= NV) return;
+    int v[D];
+    {
+        int64_t t = warp;
+        for (int d = D - 1; d >= 0; d--) { v[d] = (int)(t % nv); t /= nv; }
+    }
+    const int deg = 2 * a.KR + 1;
+    int clo[D], chi[D], C[D];
+    for (int d = 0; d < D; d++)
+    {
+        clo[d] = max(0, v[d] - a.KR - 1);
+        chi[d] = min(res - 1, v[d] + a.KR);
+        C[d] = clo[d];
+    }
+    double acc[W];
+    for (int w = 0; w < W; w++) acc[w] = 0;
+    while (true)
+    {
+        int64_t lo, hi;
+        cell_range<D>(a, C, lo, hi);
+        for (int64_t k = lo + lane; k < hi; k += 32)
+        {
+            double wt = depthWeight;
+            for (int d = 0; d < D; d++)
+            {
+                double bs[kMaxDeg + 1];
+                double pr = mean[k * D + d] * res;
+                int e = (int)floor(pr);
+                bspline_eval(deg, pr - e, bs);
+                int i = v[d] - (C[d] - a.KR);
+                wt *= bs[i];
+            }
+            for (int w = 0; w < W; w++) acc[w] += wt * datum[k * W + w];
+        }
+        int d = D - 1;
+        for (; d >= 0; d--) { if (++C[d] <= chi[d]) break; C[d] = clo[d]; }
+        if (d < 0) break;
+    }
+    for (int w = 0; w < W; w++)
+    {
+        double s = warp_sum(acc[w]);
+        if (lane == 0) grid[warp * W + w] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// estimator queries (GridSamples.inl:774-896)
+// ---------------------------------------------------------------------------------------------
+template <int D>
+struct DensityGrids
+{
+    const double *g[12];
+    int depth;
+};
+
+template <int D>
+__device__ void density_interp(const DensityGrids<D> &G, int t, const double *p, double *out)
+{
+    constexpr int W = 1 + D + D * D;
+    for (int w = 0; w < W; w++) out[w] = 0;
+    if (t < 1) return;  // the root carries no data
+    int res = 1 << (t - 1), nv = res + 1;
+    int e[D];
+    double lv[D][2];
+    for (int d = 0; d < D; d++)
+    {
+        double s = p[d] * res;
+        int f = (int)floor(s);
+        double x = s - f;
+        lv[d][0] = 1. - x;
+        lv[d][1] = x;
+        e[d] = tree_cell(p[d], res);
+    }
+    const double *g = G.g[t - 1];
+    for (int c = 0; c < (1 << D); c++)
+    {
+        double s = 1.;
+        int64_t vi = 0;
+        bool in = true;
+        for (int d = 0; d < D; d++)
+        {
+            int b = (c >> (D - 1 - d)) & 1;
+            int o = e[d] + b;
+            if (o < 0 || o > res) in = false;
+            s *= lv[d][b];
+            vi = vi * nv + o;
+        }
+        if (!in) continue;
+        for (int w = 0; w < W; w++) out[w] += g[vi * W + w] * s;
+    }
+}
+
+template <int D>
+__device__ double samples_per_cell(const DensityGrids<D> &G, int t, const double *p)
+{
+    constexpr int W = 1 + D + D * D;
+    double info[W];
+    density_interp<D>(G, t, p, info);
+    return info[0] / (double)(1u << ((t - 1) * (D - 2)));
+}
+
+template <int D>
+__device__ double est_depth_raw(const DensityGrids<D> &G, int maxT, const double *p)
+{
+    const double tg = (double)(1 << (D - 2));
+    int d1 = maxT, d2 = maxT + 1;
+    while (d2 > 1 && samples_per_cell<D>(G, d1, p) < tg) d1--, d2--;
+    if (d2 == 1 || d2 == maxT + 1)
+    {
+        int d = (d2 == 1) ? 1 : maxT;
+        double spc = samples_per_cell<D>(G, d, p);
+        return d + log(spc / tg) / log(2.);
+    }
+    double s1 = samples_per_cell<D>(G, d1, p), s2 = samples_per_cell<D>(G, d2, p);
+    if (!s2) return d1;
+    return d1 + log(tg / s1) / log(s2 / s1);
+}
+
+// ascending eigenvalues of a symmetric D x D matrix (cyclic Jacobi)
+template <int D>
+__device__ void sym_eigenvalues(double a[D][D], double *ev)
+{
+    for (int sweep = 0; sweep < 64; sweep++)
+    {
+        double off = 0;
+        for (int i = 0; i < D; i++)
+            for (int j = i + 1; j < D; j++) off += a[i][j] * a[i][j];
+        if (off == 0) break;
+        for (int p = 0; p < D; p++)
+            for (int q = p + 1; q < D; q++)
+            {
+                if (a[p][q] == 0) continue;
+                double theta = (a[q][q] - a[p][p]) / (2 * a[p][q]);
+                double t = (theta >= 0 ? 1. : -1.) / (fabs(theta) + sqrt(theta * theta + 1));
+                double c = 1 / sqrt(t * t + 1), s = t * c;
+                for (int k = 0; k < D; k++)
+                {
+                    double akp = a[k][p], akq = a[k][q];
+                    a[k][p] = c * akp - s * akq;
+                    a[k][q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < D; k++)
+                {
+                    double apk = a[p][k], aqk = a[q][k];
+                    a[p][k] = c * apk - s * aqk;
+                    a[q][k] = s * apk + c * aqk;
+                }
+            }
+    }
+    for (int i = 0; i < D; i++) ev[i] = a[i][i];
+    for (int i = 1; i < D; i++)
+        for (int j = i; j > 0 && ev[j - 1] > ev[j]; j--) { double t = ev[j]; ev[j] = ev[j - 1]; ev[j - 1] = t; }
+}
+
+template <int D>
+__global__ void estimator_kernel(DensityGrids<D> G, const double *pos, int64_t n, double *measure, double *noise, double *sdepth)
+{
+    constexpr int W = 1 + D + D * D;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double p[D];
+    for (int d = 0; d < D; d++) p[d] = pos[i * D + d];
+    int maxT = G.depth + 1;
+    double dd = est_depth_raw<D>(G, maxT, p);
+    double info[W];
+    if (dd >= maxT) density_interp<D>(G, maxT, p, info);
+    else if (dd < 0) density_interp<D>(G, 1, p, info);
+    else
+    {
+        int d1 = (int)floor(dd), d2 = d1 + 1;
+        double f = dd - d1, b[W];
+        density_interp<D>(G, d1, p, info);
+        density_interp<D>(G, d2, p, b);
+        for (int w = 0; w < W; w++) info[w] = info[w] * (1. - f) + b[w] * f;
+    }
+    double wsum = info[0];
+    measure[i] = 1. / wsum;
+    double C[D][D];
+    for (int a = 0; a < D; a++)
+        for (int b = 0; b < D; b++) C[a][b] = info[1 + D + a * D + b] / wsum - info[1 + a] / wsum * info[1 + b] / wsum;
+    double ev[D];
+    sym_eigenvalues<D>(C, ev);
+    double sum = 0, low = 0;
+    for (int d = 0; d < D; d++) { sum += ev[d]; if (d < 2) low += ev[d]; }
+    noise[i] = (low * D) / (sum * 2);
+    sdepth[i] = dd - 1.;  // depth(p) of the estimator: leaf of a sample is at the finest depth
+}
+
+// ---------------------------------------------------------------------------------------------
+// frame splat gather (ExteriorPoisson.h:181-228 -> GridSamples.inl:393-456)
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__global__ void skew_gather_kernel(SplatArgs a, const double *pos, const double *skew, const int *order, const double *measure,
+                                   const double *sdepth, double *grid)
+{
+    constexpr int K = D * (D - 1) / 2;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    int res = 1 << (a.t - 1), nv = res + 1;
+    int64_t NV = 1;
+    for (int d = 0; d < D; d++) NV *= nv;
+    if (warp >= NV) return;
+    int v[D];
+    {
+        int64_t t = warp;
+        for (int d = D - 1; d >= 0; d--) { v[d] = (int)(t % nv); t /= nv; }
+    }
+    const int deg = 2 * a.KR + 1;
+    const double sampleScale = (double)(1ull << (a.depth * 2));
+    int clo[D], chi[D], C[D];
+    for (int d = 0; d < D; d++)
+    {
+        clo[d] = max(0, v[d] - a.KR - 1);
+        chi[d] = min(res - 1, v[d] + a.KR);
+        C[d] = clo[d];
+    }
+    double acc[K];
+    for (int k = 0; k < K; k++) acc[k] = 0;
+    const int maxT = a.depth + 1;
+    while (true)
+    {
+        int64_t lo, hi;
+        cell_range<D>(a, C, lo, hi);
+        if (lo < hi)
+        {
+            int j0 = a.cellStart[lo], j1 = a.cellStart[hi];
+            for (int j = j0 + lane; j < j1; j += 32)
+            {
+                int s = order[j];
+                // level weight of this sample at tree depth t
+                double dd = sdepth[s] + 1.;
+                double lw = 0;
+                if (dd >= maxT) lw = (a.t == maxT) ? (double)(1ull << (a.depth * D)) : 0.;
+                else if (dd <= 1) lw = (a.t == 1) ? 1. : 0.;
+                else
+                {
+                    int d1 = (int)floor(dd), d2 = d1 + 1;
+                    double f = dd - d1;
+                    if (a.t == d1) lw = (1. - f) * (double)(1ull << ((d1 - 1) * D));
+                    else if (a.t == d2) lw = f * (double)(1ull << ((d2 - 1) * D));
+                }
+                if (lw == 0) continue;
+                const double *q = pos + (int64_t)s * D;
+                double wt = lw;
+                for (int d = 0; d < D; d++)
+                {
+                    double bs[kMaxDeg + 1];
+                    double pr = q[d] * res;
+                    int e = (int)floor(pr);
+                    bspline_eval(deg, pr - e, bs);
+                    wt *= bs[v[d] - (C[d] - a.KR)];
+                }
+                const double *sk = skew + (int64_t)s * K;
+                double nrm = 0;
+                for (int k = 0; k < K; k++) nrm += 2 * sk[k] * sk[k];
+                nrm = sqrt(nrm);
+                double m = measure[s];
+                for (int k = 0; k < K; k++) acc[k] += wt * (sk[k] / nrm * m * sampleScale);
+            }
+        }
+        int d = D - 1;
+        for (; d >= 0; d--) { if (++C[d] <= chi[d]) break; C[d] = clo[d]; }
+        if (d < 0) break;
+    }
+    const double finalScale = pow(pow(0.5, a.depth), 1.5 * 2);
+    for (int k = 0; k < K; k++)
+    {
+        double s = warp_sum(acc[k]);
+        if (lane == 0) grid[warp * K + k] = s * finalScale;
+    }
+}
+
+// S(E) at element centres, summed over tree depths down to the leaf containing the centre
+template <int D>
+struct SkewGrids
+{
+    const double *g[12];
+    const uint8_t *refined[12];
+    int depth;
+};
+
+template <int D>
+__global__ void element_frame_kernel(SkewGrids<D> G, double *S, int *leaf)
+{
+    constexpr int K = D * (D - 1) / 2;
+    int r = 1 << G.depth;
+    int64_t NE = 1;
+    for (int d = 0; d < D; d++) NE *= r;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= NE) return;
+    int E[D];
+    {
+        int64_t t = e;
+        for (int d = D - 1; d >= 0; d--) { E[d] = (int)(t % r); t /= r; }
+    }
+    double p[D];
+    for (int d = 0; d < D; d++) p[d] = (E[d] + 0.5) / r;
+    int L = 1;
+    while (L <= G.depth)
+    {
+        int side = 1 << L, res = 1 << (L - 1);
+        int64_t li = 0;
+        for (int d = 0; d < D; d++) li = li * side + tree_cell(p[d], res);
+        if (!G.refined[L][li]) break;
+        L++;
+    }
+    double acc[K];
+    for (int k = 0; k < K; k++) acc[k] = 0;
+    for (int t = 1; t <= L; t++)
+    {
+        int res = 1 << (t - 1), nv = res + 1;
+        int c[D];
+        double lv[D][2];
+        for (int d = 0; d < D; d++)
+        {
+            double s = p[d] * res;
+            int f = (int)floor(s);
+            double x = s - f;
+            lv[d][0] = 1. - x;
+            lv[d][1] = x;
+            c[d] = tree_cell(p[d], res);
+        }
+        const double *g = G.g[t - 1];
+        for (int cc = 0; cc < (1 << D); cc++)
+        {
+            double w = 1.;
+            int64_t vi = 0;
+            for (int d = 0; d < D; d++)
+            {
+                int b = (cc >> (D - 1 - d)) & 1;
+                w *= lv[d][b];
+                vi = vi * nv + (c[d] + b);
+            }
+            for (int k = 0; k < K; k++) acc[k] += g[vi * K + k] * w;
+        }
+    }
+    for (int k = 0; k < K; k++) S[e * K + k] = acc[k];
+    leaf[e] = L;
+}
+
+// ---------------------------------------------------------------------------------------------
+// deterministic sums
+// ---------------------------------------------------------------------------------------------
+__global__ void sum_kernel(const double *v, int64_t n, int stride, int comps, double *partial)
+{
+    __shared__ double sh[32];
+    double acc = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        for (int k = 0; k < comps; k++) { double x = v[i * stride + k]; acc += (comps == 1) ? x : 2 * x * x; }
+    acc = warp_sum(acc);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sh[w] = acc;
+    __syncthreads();
+    if (w == 0)
+    {
+        double t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.;
+        t = warp_sum(t);
+        if (lane == 0) partial[blockIdx.x] = t;
+    }
+}
+__global__ void sum_finish_kernel(const double *partial, int nb, double *out)
+{
+    double s = 0;
+    for (int b = threadIdx.x; b < nb; b += 32) s += partial[b];
+    s = warp_sum(s);
+    if (threadIdx.x == 0) out[0] = s;
+}
+
+// ---------------------------------------------------------------------------------------------
+// stencils
+// ---------------------------------------------------------------------------------------------
+__host__ __device__ inline double mass1(int a, int b) { return a == b ? 1. / 3. : 1. / 6.; }
+__host__ __device__ inline double stiff1(int a, int b) { return a == b ? 1. : -1.; }
+__host__ __device__ inline double mixed1(int a) { return (a ? 1. : -1.) * 0.5; }
+
+// R = sWeight * mean(measure) * sum_samples w phi_a phi_b, gathered per column node a
+template <int D>
+__global__ void screening_kernel(const double *pos, const double *noise, const int *order, const int *cellStart,
+                                 const int *cellOfFinest, int depth, double nSigma, const double *scaleDev, double *A)
+{
+    constexpr int S = Dims<D>::S;
+    Grid<D> g(depth);
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    int I[D];
+    g.node(i, I);
+    double acc[S];
+    for (int o = 0; o < S; o++) acc[o] = 0;
+    bool any = false;
+    for (int a = 0; a < (1 << D); a++)
+    {
+        int E[D];
+        bool ok = true;
+        for (int d = 0; d < D; d++) { E[d] = I[d] - ((a >> (D - 1 - d)) & 1); if (E[d] < 0 || E[d] >= g.r) ok = false; }
+        if (!ok) continue;
+        int k = cellOfFinest[g.elem(E)];
+        if (k < 0) continue;
+        any = true;
+        for (int j = cellStart[k]; j < cellStart[k + 1]; j++)
+        {
+            int s = order[j];
+            double nz = noise[s];
+            double w = exp(-nz * nz / (2. * nSigma * nSigma));
+            double lv[D][2];
+            for (int d = 0; d < D; d++) { double x = pos[(int64_t)s * D + d] * g.r - E[d]; lv[d][0] = 1. - x; lv[d][1] = x; }
+            double pa = 1.;
+            for (int d = 0; d < D; d++) pa *= lv[d][(a >> (D - 1 - d)) & 1];
+            for (int b = 0; b < (1 << D); b++)
+            {
+                double pb = 1.;
+                int o = 0;
+                for (int d = 0; d < D; d++)
+                {
+                    int cb = (b >> (D - 1 - d)) & 1, ca = (a >> (D - 1 - d)) & 1;
+                    pb *= lv[d][cb];
+                    o = o * 3 + (cb - ca + 1);
+                }
+                acc[o] += pa * pb * w;
+            }
+        }
+    }
+    if (!any) return;
+    double sc = *scaleDev;
+    for (int o = 0; o < S; o++) A[(int64_t)o * g.N + i] = acc[o] * sc;
+}
+
+// B(f2, f1) = sum_E sum_{a != b} S_E(b, a) int_E d_a phi_f1 d_b phi_f2 (column f1)
+template <int D>
+__global__ void constraint_kernel(const double *Sel, int depth, double *B)
+{
+    constexpr int S = Dims<D>::S;
+    Grid<D> g(depth);
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    int I[D];
+    g.node(i, I);
+    double acc[S];
+    for (int o = 0; o < S; o++) acc[o] = 0;
+    const double invr = 1. / g.r;
+    for (int a = 0; a < (1 << D); a++)
+    {
+        int E[D];
+        bool ok = true;
+        for (int d = 0; d < D; d++) { E[d] = I[d] - ((a >> (D - 1 - d)) & 1); if (E[d] < 0 || E[d] >= g.r) ok = false; }
+        if (!ok) continue;
+        const double *s = Sel + g.elem(E) * Dims<D>::K;
+        for (int b = 0; b < (1 << D); b++)
+        {
+            int o = 0;
+            for (int d = 0; d < D; d++) o = o * 3 + (((b >> (D - 1 - d)) & 1) - ((a >> (D - 1 - d)) & 1) + 1);
+            double sum = 0;
+            for (int x = 0; x < D; x++)
+                for (int y = 0; y < D; y++)
+                {
+                    if (x == y) continue;
+                    // S_E(y, x): full matrix entry (column y, row x) from the packed lower triangle
+                    double syx = y > x ? s[y * (y - 1) / 2 + x] : -s[x * (x - 1) / 2 + y];
+                    if (syx == 0) continue;
+                    double v = 1.;
+                    for (int d = 0; d < D; d++)
+                    {
+                        int ca = (a >> (D - 1 - d)) & 1, cb = (b >> (D - 1 - d)) & 1;
+                        if (d == x) v *= mixed1(ca);
+                        else if (d == y) v *= mixed1(cb);
+                        else v *= mass1(ca, cb) * invr;
+                    }
+                    sum += syx * v;
+                }
+            acc[o] += sum;
+        }
+    }
+    for (int o = 0; o < S; o++) B[(int64_t)o * g.N + i] = acc[o];
+}
+
+// dst += w K with K the Dirichlet stiffness of the level.  At resolution 1 the reference's
+// full-integration stencil table holds only node 0's row (Hat.scalars.inl:261-293: the interior
+// case maps to index res/2 = 0 and the upper boundary case is never filled).
+template <int D>
+__global__ void dirichlet_kernel(int level, double w, double *dst)
+{
+    constexpr int S = Dims<D>::S;
+    Grid<D> g(level);
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    if (g.r == 1 && i != 0) return;
+    int I[D];
+    g.node(i, I);
+    const double h = 1. / g.r;
+    for (int o = 0; o < S; o++)
+    {
+        int off[D], J[D];
+        stencil_offset<D>(o, off);
+        bool ok = true;
+        int lo[D], hi[D];
+        for (int d = 0; d < D; d++)
+        {
+            J[d] = I[d] + off[d];
+            if (J[d] < 0 || J[d] > g.r) ok = false;
+            lo[d] = max(max(I[d], J[d]) - 1, 0);
+            hi[d] = min(min(I[d], J[d]), g.r - 1);
+            if (lo[d] > hi[d]) ok = false;
+        }
+        if (!ok) continue;
+        double sum = 0;
+        int E[D];
+        for (int d = 0; d < D; d++) E[d] = lo[d];
+        while (true)
+        {
+            for (int k = 0; k < D; k++)
+            {
+                double v = 1.;
+                for (int d = 0; d < D; d++)
+                {
+                    int a = I[d] - E[d], b = J[d] - E[d];
+                    v *= (d == k) ? stiff1(a, b) / h : mass1(a, b) * h;
+                }
+                sum += v;
+            }
+            int d = D - 1;
+            for (; d >= 0; d--) { if (++E[d] <= hi[d]) break; E[d] = lo[d]; }
+            if (d < 0) break;
+        }
+        dst[(int64_t)o * g.N + i] += w * sum;
+    }
+}
+
+// Galerkin P^T M P of a column stencil, one coarse column per thread
+template <int D>
+__global__ void galerkin_kernel(int fineLevel, const double *Mf, double *Mc)
+{
+    constexpr int S = Dims<D>::S;
+    Grid<D> gf(fineLevel), gc(fineLevel - 1);
+    int64_t J = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (J >= gc.N) return;
+    int Jc[D];
+    gc.node(J, Jc);
+    double acc[S];
+    for (int o = 0; o < S; o++) acc[o] = 0;
+    for (int go = 0; go < S; go++)
+    {
+        int goff[D], G[D];
+        stencil_offset<D>(go, goff);
+        bool ok = true;
+        double wg = 1.;
+        for (int d = 0; d < D; d++) { G[d] = 2 * Jc[d] + goff[d]; if (G[d] < 0 || G[d] > gf.r) ok = false; if (goff[d]) wg *= 0.5; }
+        if (!ok) continue;
+        int64_t gi = gf.node(G);
+        for (int fo = 0; fo < S; fo++)
+        {
+            double v = Mf[(int64_t)fo * gf.N + gi];
+            if (v == 0) continue;
+            int foff[D], F[D];
+            stencil_offset<D>(fo, foff);
+            for (int d = 0; d < D; d++) F[d] = G[d] + foff[d];
+            int n1 = 0;
+            for (int d = 0; d < D; d++) n1 += F[d] & 1;
+            for (int c = 0; c < (1 << n1); c++)
+            {
+                double w = wg * v;
+                int o = 0, bit = 0;
+                for (int d = 0; d < D; d++)
+                {
+                    int Ic;
+                    if (F[d] & 1) { Ic = ((F[d] - 1) >> 1) + ((c >> bit) & 1); bit++; w *= 0.5; }
+                    else Ic = F[d] >> 1;
+                    o = o * 3 + (Ic - Jc[d] + 1);
+                }
+                acc[o] += w;
+            }
+        }
+    }
+    for (int o = 0; o < S; o++) Mc[(int64_t)o * gc.N + J] = acc[o];
+}
+
+__global__ void scale_by_kernel(double *v, const double *num, double mult, int64_t den)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) v[0] = num[0] * mult / (double)den;
+}
+
+template <typename T>
+bool dalloc(Context &c, T **p, size_t count, const char *what)
+{
+    return c.alloc((void **)p, sizeof(T) * count, what);
+}
+
+// deterministic device sum of n values (comps==1) or of the Frobenius norms 2 sum v^2 of
+// n packed K-vectors (comps==K); result left in *out (device)
+bool device_sum(Context &c, const double *v, int64_t n, int comps, double *out)
+{
+    const int nb = 1024;
+    double *partial = nullptr;
+    if (!dalloc(c, &partial, nb, "alloc partial")) return false;
+    sum_kernel<<<nb, 256, 0, c.stream>>>(v, n, comps, comps, partial);
+    sum_finish_kernel<<<1, 32, 0, c.stream>>>(partial, nb, out);
+    c.release(partial);
+    return c.launch_ok("sum");
+}
+
+template <int D>
+bool build_impl(Context &c, Setup &st)
+{
+    constexpr int K = Dims<D>::K;
+    constexpr int W = 1 + D + D * D;
+    const int depth = c.depth;
+    const int64_t n = (int64_t)st.n;
+    cudaStream_t s = c.stream;
+    cudaEventRecord(c.ev0, s);
+
+    // ---- ordered sampling: Morton keys of the finest cells, stable radix sort ----
+    int64_t *keys = nullptr, *keysSorted = nullptr;
+    int *vals = nullptr, *flags = nullptr, *ids = nullptr;
+    if (!dalloc(c, &keys, n, "keys") || !dalloc(c, &keysSorted, n, "keys") || !dalloc(c, &vals, n, "vals") ||
+        !dalloc(c, &st.order, n, "order") || !dalloc(c, &flags, n, "flags") || !dalloc(c, &ids, n, "ids"))
+        return false;
+    cell_keys_kernel<D><<<nblocks(n, 256), 256, 0, s>>>(st.pos, n, depth, keys, vals);
+    {
+        size_t tmpBytes = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, tmpBytes, keys, keysSorted, vals, st.order, (int)n, 0, D * depth, s);
+        void *tmp = nullptr;
+        if (!c.alloc(&tmp, tmpBytes, "sort tmp")) return false;
+        cub::DeviceRadixSort::SortPairs(tmp, tmpBytes, keys, keysSorted, vals, st.order, (int)n, 0, D * depth, s);
+        c.release(tmp);
+    }
+    cell_flags_kernel<<<nblocks(n, 256), 256, 0, s>>>(keysSorted, n, flags);
+    {
+        size_t tmpBytes = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tmpBytes, flags, ids, (int)n, s);
+        void *tmp = nullptr;
+        if (!c.alloc(&tmp, tmpBytes, "scan tmp")) return false;
+        cub::DeviceScan::ExclusiveSum(tmp, tmpBytes, flags, ids, (int)n, s);
+        c.release(tmp);
+    }
+    int lastId = 0, lastFlag = 0;
+    if (!c.cuda_ok(cudaMemcpyAsync(&lastId, ids + n - 1, sizeof(int), cudaMemcpyDeviceToHost, s), "copy") ||
+        !c.cuda_ok(cudaMemcpyAsync(&lastFlag, flags + n - 1, sizeof(int), cudaMemcpyDeviceToHost, s), "copy") ||
+        !c.cuda_ok(cudaStreamSynchronize(s), "sync"))
+        return false;
+    st.ncells = lastId + lastFlag;
+    const int64_t nc = st.ncells;
+    if (!dalloc(c, &st.cellStart, nc + 1, "cellStart") || !dalloc(c, &st.cellKey, nc, "cellKey")) return false;
+    cell_start_kernel<<<nblocks(n, 256), 256, 0, s>>>(keysSorted, flags, ids, n, st.cellStart, st.cellKey);
+    c.release(keys); c.release(keysSorted); c.release(vals); c.release(flags); c.release(ids);
+    Grid<D> gfine(depth);
+    if (!dalloc(c, &st.cellOfFinest, gfine.NE, "cell map")) return false;
+    cudaMemsetAsync(st.cellOfFinest, 0xff, sizeof(int) * gfine.NE, s);
+    finest_map_kernel<D><<<nblocks(nc, 256), 256, 0, s>>>(st.cellKey, nc, depth, st.cellOfFinest);
+    if (!c.launch_ok("ordered sampling")) return false;
+
+    // ---- tree structure of both trees ----
+    auto buildRefined = [&](std::vector<uint8_t *> &ref, int KR) -> bool {
+        ref.assign(depth + 2, nullptr);
+        for (int t = 1; t <= depth; t++)
+        {
+            int64_t cells = 1;
+            for (int d = 0; d < D; d++) cells *= (int64_t)1 << t;
+            if (!dalloc(c, &ref[t], cells, "refined")) return false;
+            cudaMemsetAsync(ref[t], 0, cells, s);
+            refine_kernel<D><<<nblocks(nc, 256), 256, 0, s>>>(st.cellKey, nc, depth, t, KR, t > 1 ? ref[t - 1] : nullptr, ref[t]);
+        }
+        return c.launch_ok("refine");
+    };
+    if (!buildRefined(st.refinedD, c.P.d_radius)) return false;
+    if (!buildRefined(st.refinedS, c.P.t_radius)) return false;
+
+    // ---- density splat of the merged cells ----
+    double *mean = nullptr, *datum = nullptr;
+    if (!dalloc(c, &mean, nc * D, "mean") || !dalloc(c, &datum, nc * W, "datum")) return false;
+    merge_cells_kernel<D><<<nblocks(nc, 128), 128, 0, s>>>(st.pos, st.order, st.cellStart, nc, mean, datum);
+    st.density.assign(depth + 1, nullptr);
+    {
+        int KR = c.P.d_radius;
+        std::vector<double> bsv(2 * KR + 2);
+        {
+            // B-spline value at 1/2 of the centre piece (GridSamples.inl:753-756), on the host
+            int deg = 2 * KR + 1;
+            std::vector<double> v(deg + 1);
+            v[deg] = 1.;
+            for (int k = 1; k <= deg; k++)
+            {
+                const double scale = 1. / k;
+                int b = deg - k;
+                v[b] = v[b + 1] * (1. - 0.5) * scale;
+                for (int i = 1; i < k; i++) v[b + i] = (v[b + i] * (0.5 - i + k) + v[b + i + 1] * (-0.5 + i + 1)) * scale;
+                v[b + k] *= 0.5 * scale;
+            }
+            bsv = v;
+        }
+        double scale = std::pow(1. / bsv[KR + 1], 2);
+        for (int t = 1; t <= depth + 1; t++)
+        {
+            Grid<D> gl(t - 1);
+            if (!dalloc(c, &st.density[t - 1], gl.N * W, "density")) return false;
+            SplatArgs a{st.cellKey, st.cellStart, nc, depth, t, KR};
+            double dw = scale / std::pow(std::pow(0.5, t - 1), D - 2);
+            density_gather_kernel<D><<<nblocks(gl.N * 32, 256), 256, 0, s>>>(a, mean, datum, dw, st.density[t - 1]);
+        }
+    }
+    c.release(mean); c.release(datum);
+    if (!c.launch_ok("density splat")) return false;
+
+    // ---- estimator queries per sample ----
+    if (!dalloc(c, &st.measure, n, "measure") || !dalloc(c, &st.noise, n, "noise") || !dalloc(c, &st.sdepth, n, "depth")) return false;
+    {
+        DensityGrids<D> G;
+        for (int l = 0; l <= depth; l++) G.g[l] = st.density[l];
+        G.depth = depth;
+        estimator_kernel<D><<<nblocks(n, 128), 128, 0, s>>>(G, st.pos, n, st.measure, st.noise, st.sdepth);
+    }
+    if (!c.launch_ok("estimator")) return false;
+
+    // ---- frame splat ----
+    st.skewGrid.assign(depth + 1, nullptr);
+    for (int t = 1; t <= depth + 1; t++)
+    {
+        Grid<D> gl(t - 1);
+        if (!dalloc(c, &st.skewGrid[t - 1], gl.N * K, "skew grid")) return false;
+        SplatArgs a{st.cellKey, st.cellStart, nc, depth, t, c.P.t_radius};
+        skew_gather_kernel<D><<<nblocks(gl.N * 32, 256), 256, 0, s>>>(a, st.pos, st.skew, st.order, st.measure, st.sdepth, st.skewGrid[t - 1]);
+    }
+    if (!c.launch_ok("frame splat")) return false;
+
+    // ---- S(E), leaf depths, c ----
+    if (!dalloc(c, &st.S, gfine.NE * K, "S") || !dalloc(c, &st.leaf, gfine.NE, "leaf")) return false;
+    {
+        SkewGrids<D> G;
+        for (int l = 0; l <= depth; l++) G.g[l] = st.skewGrid[l];
+        for (int t = 0; t <= depth + 1 && t < 12; t++) G.refined[t] = st.refinedS[t];
+        G.depth = depth;
+        element_frame_kernel<D><<<nblocks(gfine.NE, 128), 128, 0, s>>>(G, st.S, st.leaf);
+    }
+    double *dsum = nullptr;
+    if (!dalloc(c, &dsum, 4, "sums")) return false;
+    if (!device_sum(c, st.S, gfine.NE, K, dsum)) return false;
+    double csum = 0;
+    if (!c.cuda_ok(cudaMemcpyAsync(&csum, dsum, sizeof(double), cudaMemcpyDeviceToHost, s), "copy") ||
+        !c.cuda_ok(cudaStreamSynchronize(s), "sync"))
+        return false;
+    c.c = csum / (double)gfine.NE;
+
+    // ---- finest stencils: R (into A64), B ----
+    Level &Lf = c.levels[depth];
+    const int S = Dims<D>::S;
+    cudaMemsetAsync(Lf.A64, 0, sizeof(double) * S * Lf.N, s);
+    if (c.P.s_weight > 0)
+    {
+        if (!device_sum(c, st.measure, n, 1, dsum + 1)) return false;
+        scale_by_kernel<<<1, 32, 0, s>>>(dsum + 2, dsum + 1, c.P.s_weight, n);
+        screening_kernel<D><<<nblocks(Lf.N, 128), 128, 0, s>>>(st.pos, st.noise, st.order, st.cellStart, st.cellOfFinest, depth,
+                                                               c.P.n_sigma, dsum + 2, Lf.A64);
+    }
+    constraint_kernel<D><<<nblocks(Lf.N, 128), 128, 0, s>>>(st.S, depth, Lf.B64);
+    if (!c.launch_ok("finest stencils")) return false;
+
+    // ---- Galerkin hierarchy of R and B, then A = R + dWeight K on every level ----
+    for (int l = depth; l > 0; l--)
+    {
+        Grid<D> gc(l - 1);
+        galerkin_kernel<D><<<nblocks(gc.N, 64), 64, 0, s>>>(l, c.levels[l].A64, c.levels[l - 1].A64);
+        galerkin_kernel<D><<<nblocks(gc.N, 64), 64, 0, s>>>(l, c.levels[l].B64, c.levels[l - 1].B64);
+    }
+    if (!c.launch_ok("galerkin")) return false;
+    for (int l = 0; l <= depth; l++)
+    {
+        if (!add_dirichlet(c, l)) return false;
+        if (!c.sync_system32(l)) return false;
+    }
+    c.release(dsum);
+    cudaEventRecord(c.ev1, s);
+    if (!c.cuda_ok(cudaStreamSynchronize(s), "build sync")) return false;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    c.stats.build_ms = ms;
+    c.have_system = true;
+    return true;
+}
+
+}  // namespace
+
+bool add_dirichlet_to(Context &c, int level, double *dst, double w)
+{
+    int64_t N = c.levels[level].N;
+    if (c.dim == 3) dirichlet_kernel<3><<<nblocks(N, 128), 128, 0, c.stream>>>(level, w, dst);
+    else dirichlet_kernel<4><<<nblocks(N, 128), 128, 0, c.stream>>>(level, w, dst);
+    return c.launch_ok("dirichlet");
+}
+
+bool add_dirichlet(Context &c, int level) { return add_dirichlet_to(c, level, c.levels[level].A64, c.P.d_weight); }
+
+bool Setup::set_samples(Context &c, size_t n_, const double *pos_, const double *skew_)
+{
+    release(c);
+    n = n_;
+    size_t K = (size_t)(c.dim * (c.dim - 1) / 2);
+    if (!dalloc(c, &pos, n * c.dim, "pos") || !dalloc(c, &skew, n * K, "skew")) return false;
+    return c.cuda_ok(cudaMemcpyAsync(pos, pos_, sizeof(double) * n * c.dim, cudaMemcpyHostToDevice, c.stream), "upload pos") &&
+           c.cuda_ok(cudaMemcpyAsync(skew, skew_, sizeof(double) * n * K, cudaMemcpyHostToDevice, c.stream), "upload skew") &&
+           c.cuda_ok(cudaStreamSynchronize(c.stream), "sync");
+}
+
+bool Setup::build(Context &c)
+{
+    if (c.dim == 3) return build_impl<3>(c, *this);
+    return build_impl<4>(c, *this);
+}
+
+bool Setup::get(Context &c, const std::string &name, double *out, size_t cap, size_t *count)
+{
+    auto copy_d = [&](const double *src, size_t num) -> bool {
+        if (count) *count = num;
+        if (!out) return true;
+        if (!src) { c.fail(EPR_ERR_STATE, "'%s' is not available before epr_build", name.c_str()); return false; }
+        if (cap < num) { c.fail(EPR_ERR_ARG, "output too small (%zu < %zu)", cap, num); return false; }
+        return c.cuda_ok(cudaMemcpyAsync(out, src, sizeof(double) * num, cudaMemcpyDeviceToHost, c.stream), "copy") &&
+               c.cuda_ok(cudaStreamSynchronize(c.stream), "sync");
+    };
+    size_t K = (size_t)(c.dim * (c.dim - 1) / 2);
+    int64_t NE = 1;
+    for (int d = 0; d < c.dim; d++) NE *= (int64_t)1 << c.depth;
+    if (name == "measure") return copy_d(measure, n);
+    if (name == "noise") return copy_d(noise, n);
+    if (name == "depth") return copy_d(sdepth, n);
+    if (name == "S") return copy_d(S, (size_t)NE * K);
+    if (name == "leaf_depth")
+    {
+        if (count) *count = (size_t)NE;
+        if (!out) return true;
+        if (!leaf) { c.fail(EPR_ERR_STATE, "not built"); return false; }
+        if (cap < (size_t)NE) { c.fail(EPR_ERR_ARG, "output too small"); return false; }
+        std::vector<int> h(NE);
+        if (!c.cuda_ok(cudaMemcpyAsync(h.data(), leaf, sizeof(int) * NE, cudaMemcpyDeviceToHost, c.stream), "copy") ||
+            !c.cuda_ok(cudaStreamSynchronize(c.stream), "sync"))
+            return false;
+        for (int64_t e = 0; e < NE; e++) out[e] = h[e];
+        return true;
+    }
+    if (name == "ncells")
+    {
+        if (count) *count = 1;
+        if (out && cap >= 1) out[0] = (double)ncells;
+        return true;
+    }
+    c.fail(EPR_ERR_ARG, "unknown array '%s'", name.c_str());
+    return false;
+}
+
+void Setup::release(Context &c)
+{
+    c.release(pos); c.release(skew); c.release(order); c.release(cellKey); c.release(cellStart); c.release(cellOfFinest);
+    c.release(measure); c.release(noise); c.release(sdepth); c.release(S); c.release(leaf);
+    for (double *p : density) c.release(p);
+    for (double *p : skewGrid) c.release(p);
+    for (uint8_t *p : refinedD) c.release(p);
+    for (uint8_t *p : refinedS) c.release(p);
+    density.clear(); skewGrid.clear(); refinedD.clear(); refinedS.clear();
+    pos = skew = measure = noise = sdepth = S = nullptr;
+    order = cellStart = cellOfFinest = leaf = nullptr;
+    cellKey = nullptr;
+    n = 0;
+    ncells = 0;
+}
+
+}  // namespace epr

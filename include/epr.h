@@ -1,0 +1,147 @@
+/* libepr_cuda: the GB300 (sm_103a) implementation of ExteriorPoissonRecon's regular-grid solve path.
+ *
+ * C ABI: plain pointers and sizes only, every call returns an int status (EPR_OK = 0), no
+ * exception crosses the boundary, and epr_last_error() describes the last failure of a context.
+ * One context = one reconstruction problem = one CUDA stream on the current device; a context is
+ * not thread-safe.  Host arrays are ordinary (pageable or pinned) host memory unless a function
+ * says "device".
+ *
+ * Reference interfaces replaced (paths relative to the reference checkout):
+ *   epr_create / epr_set_samples / epr_build
+ *       ExteriorPoisson::Reconstructor::Reconstructor      ExteriorPoissonRecon/ExteriorPoisson.h:59-72,126-313
+ *       (OrderedSampler OrderedSamples.h, TreeEstimator GridSamples.h:232-277 and the
+ *        SingleCycleCascadicSystemEnergy constructor / restrict SystemEnergy.h:135-141,447-477)
+ *   epr_solve
+ *       ExteriorPoisson::Reconstructor::solve              ExteriorPoisson.h:74-81,315-409
+ *   epr_get_solution
+ *       Reconstructor::x() / y()                            ExteriorPoisson.h:83-86
+ *   epr_energy
+ *       SystemEnergy::energies / operator()                 Include/SystemEnergy.h:63,91,486-497
+ *   epr_quadfit
+ *       SystemEnergy::quadraticFit                          Include/SystemEnergy.h:75,542-643
+ *   epr_gradient
+ *       SystemEnergy::d                                     Include/SystemEnergy.h:72,248-254
+ *   epr_gs
+ *       ExteriorPoissonSolvers::PairedGaussSeidelSolve      ExteriorPoissonRecon/ExteriorPoissonSolvers.h:74-76,156-196
+ *   epr_prolong
+ *       SystemEnergy::prolongation                          Include/SystemEnergy.h:99-100,162
+ *   epr_gn_matvec
+ *       the matrix of SystemEnergy::quadraticApproximation1/2 applied to a vector
+ *                                                           Include/SystemEnergy.h:80-84 (q.q * x, MG.h:120)
+ *   epr_get_array
+ *       read-only views of the reference's internal state (TreeEstimator::measure/noise/depth
+ *       GridSamples.inl:838-862, S(E) ExteriorPoisson.h:290-307, _R/_B SystemEnergy.h:172-175)
+ */
+#ifndef EPR_H
+#define EPR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EPR_OK 0
+#define EPR_ERR_ARG (-1)      /* invalid argument (sizes, level, null pointer) */
+#define EPR_ERR_CUDA (-2)     /* a CUDA runtime call failed */
+#define EPR_ERR_STATE (-3)    /* call out of order (e.g. solve before build) */
+#define EPR_ERR_NUMERIC (-4)  /* a kernel produced a non-finite value */
+#define EPR_ERR_NOMEM (-5)    /* device allocation failed */
+
+#define EPR_FP64 0  /* all arithmetic in double (parity with the reference to 1e-12) */
+#define EPR_FP32 1  /* smoothing / matvecs in float; energies, norms and the coarse solve in double */
+
+#define EPR_SOLVER_CASCADIC 0   /* the reference schedule: coarse-to-fine paired Gauss-Seidel */
+#define EPR_SOLVER_MULTIGRID 1  /* nonlinear multigrid V-cycles to a gradient tolerance */
+
+typedef struct epr_ctx epr_ctx;
+
+typedef struct epr_params {
+    double s_weight;      /* --sWeight   screening weight (code default 100) */
+    double d_weight;      /* --dWeight   Dirichlet weight (0.00625) */
+    double n_sigma;       /* --nSigma    noise-to-weight sigma (0.25) */
+    double i_mult;        /* --iMult     iteration multiplier per level (2) */
+    int t_radius;         /* --tRadius   frame splat kernel radius, 0..4 (1) */
+    int d_radius;         /* --dRadius   density kernel radius, 0..4 (1) */
+    int gs_iters;         /* --gsIters   Gauss-Seidel iterations at the finest level (10) */
+    int min_solve_depth;  /* --minSolveDepth (0) */
+    int max_solve_depth;  /* --maxSolveDepth (-1 = depth) */
+    unsigned int seed;    /* --seed      initial-guess seed (0) */
+    int precision;        /* EPR_FP64 or EPR_FP32 */
+    int solver;           /* EPR_SOLVER_CASCADIC or EPR_SOLVER_MULTIGRID */
+    double tolerance;     /* multigrid: stop when |grad E| / |grad E(x0)| <= tolerance (1e-6) */
+    int max_cycles;       /* multigrid: cycle cap (200) */
+    int verbose;          /* print the reference's per-level "Error[...]" lines */
+} epr_params;
+
+typedef struct epr_stats {
+    double initial_energy;   /* E0 = squareNorm of the target (the reference's "_err") */
+    double fit_energy;       /* final fitting term */
+    double reg_energy;       /* final regularisation term */
+    double solve_ms;         /* device time of the solve (CUDA events) */
+    double build_ms;         /* device time of epr_build */
+    double grad_norm0;       /* multigrid: |grad E| at the start of the finest level */
+    double grad_norm;        /* multigrid: |grad E| at exit */
+    int cycles;              /* multigrid cycles run */
+    int64_t node_updates;    /* paired Gauss-Seidel node updates performed */
+} epr_stats;
+
+void epr_default_params(epr_params *p);
+
+/* Context for a dim (3 or 4) reconstruction at the given depth (1..10 in 3D, 1..7 in 4D).
+ * Returns NULL on error; epr_global_error() then describes it. */
+epr_ctx *epr_create(int dim, int depth, const epr_params *params);
+void epr_destroy(epr_ctx *ctx);
+const char *epr_last_error(const epr_ctx *ctx);
+const char *epr_global_error(void);
+
+/* Samples in the unit cube (n x dim doubles) with their packed skew frames
+ * (n x dim(dim-1)/2 doubles, entry i(i-1)/2 + j holds (m(i,j) - m(j,i))/2 for i > j). */
+int epr_set_samples(epr_ctx *ctx, size_t n, const double *pos, const double *skew);
+
+/* Ordered sampling, density estimation, frame splatting, S(E), screening / constraint /
+ * Dirichlet stencils and the Galerkin hierarchy, all on the device. */
+int epr_build(epr_ctx *ctx);
+
+/* Replaces the system of one level with host column stencils: R (screening) and B (constraint)
+ * with 3^dim entries per node (entry o of node i holds M(i+off(o), i)), plus the constant c. */
+int epr_set_level_system(epr_ctx *ctx, int level, const double *R, const double *B, double c);
+
+/* Coefficients of one level (regular, not hierarchical), host arrays of (2^level+1)^dim doubles. */
+int epr_set_coefficients(epr_ctx *ctx, int level, const double *x, const double *y);
+int epr_get_coefficients(epr_ctx *ctx, int level, double *x, double *y);
+
+/* out[0] = fitting energy, out[1] = regularisation energy, out[2] = wedge square norm, for the
+ * level's current coefficients. */
+int epr_energy(epr_ctx *ctx, int level, double *out3);
+/* Quadratic fit of every node (N x 5: Q20, Q02, Q11, Q10, Q01). */
+int epr_quadfit(epr_ctx *ctx, int level, double *out);
+/* Energy gradient (dE/dx, dE/dy). */
+int epr_gradient(epr_ctx *ctx, int level, double *gx, double *gy);
+/* iters paired Gauss-Seidel sweeps over the 2^dim parity colours, in place. */
+int epr_gs(epr_ctx *ctx, int level, int iters);
+/* coefficients[level+1] += P coefficients[level] */
+int epr_prolong(epr_ctx *ctx, int level);
+/* (J^T J + A)(dx, dy) at the level's current coefficients: J is the linearised wedge residual,
+ * A = R + dWeight K.  This is half the Gauss-Newton Hessian of the energy. */
+int epr_gn_matvec(epr_ctx *ctx, int level, const double *dx, const double *dy, double *ox, double *oy);
+
+/* Runs the configured solver; stats may be NULL. */
+int epr_solve(epr_ctx *ctx, epr_stats *stats);
+/* Hierarchical solution coefficients of one level after epr_solve (what the reference writes to
+ * its .tree file: level 0 regular, level d > 0 the residual x[d] - P x[d-1]). */
+int epr_get_solution(epr_ctx *ctx, int level, double *x, double *y);
+
+/* Named internal arrays copied to host memory: "measure", "noise", "depth" (per sample),
+ * "S" (per finest element, packed), "leaf_depth", "R", "B" (per level, column stencils), "c".
+ * count receives the number of doubles; out may be NULL to query it. */
+int epr_get_array(epr_ctx *ctx, const char *name, int level, double *out, size_t cap, size_t *count);
+
+/* Waits for all work of the context. */
+int epr_synchronize(epr_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,28 @@
+"""CPU-side checks of the C ABI: the library builds for sm_103a, loads, and exports every function
+that include/epr.h declares (no CUDA calls are made)."""
+import ctypes
+
+import exteriorpoissonrecon_gb300 as epr
+
+
+def test_header_declares_the_boundary():
+    names = epr.header_symbols()
+    for required in ["epr_create", "epr_set_samples", "epr_build", "epr_solve", "epr_energy", "epr_quadfit",
+                     "epr_gradient", "epr_gs", "epr_gn_matvec", "epr_get_solution", "epr_destroy", "epr_last_error"]:
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = epr.load()
+    missing = [n for n in epr.header_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_params_struct_matches_defaults():
+    p = epr.default_params()
+    assert p.s_weight == 100.0 and p.d_weight == 0.00625 and p.n_sigma == 0.25 and p.i_mult == 2.0
+    assert p.t_radius == 1 and p.d_radius == 1 and p.gs_iters == 10 and p.seed == 0
+    assert p.max_solve_depth == -1 and p.precision == epr.EPR_FP64
+    q = epr.default_params(sWeight=50, gsIters=20, precision="fp32")
+    assert q.s_weight == 50 and q.gs_iters == 20 and q.precision == epr.EPR_FP32
+    assert ctypes.sizeof(epr.Params) == 80

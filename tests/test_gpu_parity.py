@@ -1,0 +1,143 @@
+"""Parity of the CUDA path (through the C ABI) against the reference's own outputs (golden
+fixtures) and against the CPU oracle at larger sizes.
+
+Tolerances: FP64 path 1e-12 relative for energies and stencils (1e-9 for the eigenvalue-based
+noise and for quantities accumulated over whole solves); FP32 path 1e-5 relative."""
+import numpy as np
+import pytest
+
+import exteriorpoissonrecon_gb300 as epr
+from conftest import GOLDEN_CASES, load_golden
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    assert a.shape == b.shape, (a.shape, b.shape)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module", params=GOLDEN_CASES)
+def built(request):
+    g = load_golden(request.param)
+    dim = g["pos"].shape[1]
+    depth = int(g["depth"])
+    r = epr.Reconstructor(dim, depth, g["pos"], g["skew"])
+    return g, r, dim, depth
+
+
+def test_estimator(built):
+    g, r, dim, depth = built
+    assert rel(r.get("measure"), g["est_measure"]) < 1e-12
+    assert rel(r.get("depth"), g["est_depth"]) < 1e-12
+    assert rel(r.get("noise"), g["est_noise"]) < 1e-9
+
+
+def test_frame_field(built):
+    g, r, dim, depth = built
+    assert np.array_equal(r.get("leaf_depth"), g["leaf_depth"])
+    assert rel(r.get("S"), g["S"]) < 1e-12
+    assert abs(r.get("c")[0] - g["c"][0]) < 1e-12 * g["c"][0]
+
+
+def test_stencils(built):
+    g, r, dim, depth = built
+    for l in g["stencil_levels"]:
+        assert rel(r.get("R", int(l)), g[f"R_d{l}"]) < 1e-10
+        assert rel(r.get("B", int(l)), g[f"B_d{l}"]) < 1e-12
+
+
+def test_energy_every_level(built):
+    g, r, dim, depth = built
+    for l in range(depth + 1):
+        e = r.energy(l, g[f"xr_d{l}"], g[f"yr_d{l}"])
+        ref = g[f"energies_d{l}"]
+        for k in range(3):
+            assert abs(e[k] - ref[k]) <= 1e-12 * abs(ref[k]) + 1e-14, (l, k, e, ref)
+
+
+def test_quadfit_and_gs(built):
+    g, r, dim, depth = built
+    for key in g:
+        if not key.startswith("quadfit_d"):
+            continue
+        l = int(key[len("quadfit_d"):])
+        x, y = g[f"xr_d{l}"], g[f"yr_d{l}"]
+        assert rel(r.quadfit(l, x, y), g[key]) < 1e-11
+        gx, gy = r.gs(l, x, y, 1)
+        assert rel(gx, g[f"gsx_d{l}"]) < 1e-11
+        assert rel(gy, g[f"gsy_d{l}"]) < 1e-11
+
+
+def test_cascadic_solve_matches_reference(built):
+    g, r, dim, depth = built
+    st = r.solve()
+    ref = g["sol_energies"]
+    assert abs(st["fit_energy"] - ref[0]) < 1e-10 * ref[0]
+    assert abs(st["reg_energy"] - ref[1]) < 1e-10 * ref[1]
+    xs, ys = r.solution()
+    for l in range(depth + 1):
+        assert rel(xs[l], g[f"solx_d{l}"]) < 1e-9
+        assert rel(ys[l], g[f"soly_d{l}"]) < 1e-9
+
+
+def test_fp32_operators(built):
+    """FP32 smoothing path: energy and quadratic fits within 1e-5 of the reference."""
+    g, _, dim, depth = built
+    r = epr.Reconstructor(dim, depth, g["pos"], g["skew"], precision="fp32")
+    l = depth
+    x, y = g[f"xr_d{l}"], g[f"yr_d{l}"]
+    e = r.energy(l, x, y)
+    ref = g[f"energies_d{l}"]
+    assert abs(e[2] - ref[2]) < 1e-5 * abs(ref[2])
+    assert abs(e[0] + e[1] - ref[0] - ref[1]) < 1e-5 * abs(ref[0] + ref[1])
+    assert rel(r.quadfit(l, x, y), g[f"quadfit_d{l}"]) < 1e-5
+
+
+def test_system_upload_path():
+    """epr_set_level_system + operators on an uploaded system (isolates the solve kernels)."""
+    g = load_golden("knot3_d4")
+    depth = int(g["depth"])
+    r = epr.Reconstructor(3, depth)
+    l = depth
+    r.set_level_system(l, g[f"R_d{l}"], g[f"B_d{l}"], g["c"][0])
+    e = r.energy(l, g[f"xr_d{l}"], g[f"yr_d{l}"])
+    ref = g[f"energies_d{l}"]
+    assert abs(e[0] - ref[0]) < 1e-12 * abs(ref[0])
+    assert abs(e[1] - ref[1]) < 1e-12 * abs(ref[1])
+
+
+@pytest.mark.parametrize("dim,depth,workload,n", [(3, 6, "link", 60000), (4, 4, "clifford", 60000)])
+def test_against_oracle_larger(dim, depth, workload, n):
+    pos, frames = epr.samples.make_workload(workload, n, seed=11)
+    pu, _ = epr.unit_cube(pos)
+    sk = epr.pack_skew(frames)
+    o = O.Oracle(dim, depth)
+    o.set_samples(pu, sk)
+    o.build()
+    r = epr.Reconstructor(dim, depth, pu, sk)
+    assert rel(r.get("measure"), o.get("measure")) < 1e-12
+    assert rel(r.get("S"), o.get("S")) < 1e-11
+    for l in (depth, depth - 1, 0):
+        assert rel(r.get("B", l), o.get("B", l)) < 1e-11
+        assert rel(r.get("R", l), o.get("R", l)) < 1e-10
+    rng = np.random.default_rng(1)
+    x = rng.uniform(-1, 1, o.nodes(depth))
+    y = rng.uniform(-1, 1, o.nodes(depth))
+    e = r.energy(depth, x, y)
+    eo = o.energy(depth, x, y)
+    assert rel(e, eo) < 1e-12
+    q = r.quadfit(depth, x, y)
+    assert rel(q, o.quadfit(depth, x, y)) < 1e-11
+    gx, gy = r.gs(depth, x, y, 2)
+    ox, oy = o.gs(depth, x, y, 2)
+    assert rel(gx, ox) < 1e-10 and rel(gy, oy) < 1e-10
+    dx = rng.uniform(-1, 1, o.nodes(depth))
+    dy = rng.uniform(-1, 1, o.nodes(depth))
+    r.set_coefficients(depth, x, y)
+    mx, my = r.gn_matvec(depth, dx, dy)
+    omx, omy = o.gn_matvec(depth, x, y, dx, dy)
+    assert rel(mx, omx) < 1e-11 and rel(my, omy) < 1e-11
