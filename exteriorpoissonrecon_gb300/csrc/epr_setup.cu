@@ -137,7 +137,8 @@ __global__ void cell_start_kernel(const int64_t *keys, const int *flags, const i
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (flags[i]) { cellStart[ids[i]] = (int)i; cellKey[ids[i]] = keys[i]; }
-    if (i == n - 1) cellStart[ids[i] + 1] = (int)n;
+    // ids is the exclusive scan of the flags: the last sample's cell is ids + flags - 1
+    if (i == n - 1) cellStart[ids[i] + flags[i]] = (int)n;
 }
 
 template <int D>
@@ -892,6 +893,18 @@ bool build_impl(Context &c, Setup &st)
     if (!dalloc(c, &st.cellStart, nc + 1, "cellStart") || !dalloc(c, &st.cellKey, nc, "cellKey")) return false;
     cell_start_kernel<<<nblocks(n, 256), 256, 0, s>>>(keysSorted, flags, ids, n, st.cellStart, st.cellKey);
     c.release(keys); c.release(keysSorted); c.release(vals); c.release(flags); c.release(ids);
+    {
+        int first = -1, last = -1;
+        if (!c.cuda_ok(cudaMemcpyAsync(&first, st.cellStart, sizeof(int), cudaMemcpyDeviceToHost, s), "copy") ||
+            !c.cuda_ok(cudaMemcpyAsync(&last, st.cellStart + nc, sizeof(int), cudaMemcpyDeviceToHost, s), "copy") ||
+            !c.cuda_ok(cudaStreamSynchronize(s), "sync"))
+            return false;
+        if (first != 0 || last != (int)n)
+        {
+            c.fail(EPR_ERR_STATE, "ordered sampling produced inconsistent cell ranges (%d, %d, %lld)", first, last, (long long)n);
+            return false;
+        }
+    }
     Grid<D> gfine(depth);
     if (!dalloc(c, &st.cellOfFinest, gfine.NE, "cell map")) return false;
     cudaMemsetAsync(st.cellOfFinest, 0xff, sizeof(int) * gfine.NE, s);

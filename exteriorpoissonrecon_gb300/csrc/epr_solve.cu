@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(kThreads) gn_matvec_kernel(LevelPtrs<Real> L, 
         gather_element<D, Real>(g, nc, i, A, dxy, dx, dy);
         element_gn<D, Real>(x, y, dx, dy, A, s);
     }
-    const Real sc = (Real)(2.0 * wedge_scale<D>(g.r));
+    const Real sc = (Real)wedge_scale<D>(g.r);
     Real ox = s[0] * sc, oy = s[1] * sc;
     constexpr int S = Dims<D>::S;
     for (int o = 0; o < S; o++)
