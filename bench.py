@@ -1,0 +1,261 @@
+"""Benchmark of the GB300 solve path on the depth-8 3D link workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (synthetic, seeded): two interlocking unit circles (one in the xy-plane at the origin,
+one in the xz-plane centred at (1,0,0)), 1M samples uniform in arc length, Gaussian positional
+noise sigma 0.005 (unit-cube units), 5 degree angular noise, plus 10% uniform spot outliers with
+random frames; 3D, depth 8 (257^3 nodes x 2 channels = 33.9M unknowns), code-default parameters.
+
+One step = one full solve from the built system (fresh initial guess each time).  `value` is the
+device time per solve with the system resident in HBM; `e2e` repeats the whole public-API
+pipeline per step from host buffers (samples host->device, build, solve, solution device->host).
+Every array of a level exceeds the 129 MB L2 (coefficients 137 MB in FP32, stencils 3.7 GB), so no
+flush is inserted between steps.
+
+--impl reference times the CPU restatement of the reference algorithm (oracle/, the reference's
+cascadic paired Gauss-Seidel schedule, all host threads) on a bounded sample of the same input
+(depth 6 build + sweeps) and scales its node-update rate to the depth-8 schedule.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Depth-8 time-to-1e-6-residual, learned+FP32 vs plain FP64 GPU; stencil HBM GB/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--depth", type=int, default=8)
+    ap.add_argument("--samples", type=int, default=1_000_000)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--solver", default="cascadic", choices=["cascadic", "multigrid"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-depth", type=int, default=6)
+    return ap.parse_args()
+
+
+def workload(n, seed=0):
+    from exteriorpoissonrecon_gb300 import samples, unit_cube, pack_skew
+    pos, frames = samples.make_workload("link", n, seed=seed)
+    pu, xf = unit_cube(pos)
+    return pu, pack_skew(frames)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, device=0):
+        self.device = device
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        def run():
+            q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                         timeout=5).stdout.strip()
+                    if out:
+                        self.rows.append([x.strip() for x in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for i, nm in enumerate(names):
+                if len(r) > 4 + i and r[4 + i].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://", world_size=ws, rank=rank)
+        pg = dist
+    return ws, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allmax(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def schedule_node_updates(dim, depth, gs_iters=10, i_mult=2.0):
+    return sum(math.ceil(i_mult ** (depth - l) * gs_iters) * (2 ** l + 1) ** dim for l in range(depth + 1))
+
+
+def cpu_reference(pu, sk, depth, cpu_depth, steps, warmup):
+    """CPU restatement (oracle) of the reference's cascadic paired Gauss-Seidel on a bounded sample:
+    build at cpu_depth, time paired-GS sweeps there with all host threads, scale the node-update
+    rate to the depth-`depth` schedule."""
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    o = O.Oracle(3, cpu_depth, threads=cores)
+    o.set_samples(pu, sk)
+    t0 = time.perf_counter()
+    o.build()
+    build_s = time.perf_counter() - t0
+    N = o.nodes(cpu_depth)
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1e-2, 1e-2, N)
+    y = rng.uniform(-1e-2, 1e-2, N)
+    times = []
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        x, y = o.gs(cpu_depth, x, y, 1)
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(dt)
+    per_update = statistics.mean(times) / N
+    full = per_update * schedule_node_updates(3, depth)
+    return {"value": full, "unit": "s", "cores": cores, "kind": "port",
+            "sample": (f"oracle build + {steps} paired-GS sweeps at depth {cpu_depth} "
+                       f"({N} nodes, FP64) of the same {len(pu)}-sample input; per-node-update time "
+                       f"{per_update * 1e9:.1f} ns scaled to the depth-{depth} cascadic schedule "
+                       f"({schedule_node_updates(3, depth)} node updates); build took {build_s:.1f} s")}
+
+
+def main():
+    args = parse()
+    ws, rank, local, pg = dist_setup(args)
+    depth = args.depth
+    pu, sk = workload(args.samples)
+    config = {"workload": f"link-1M+10%spot-3D-depth{depth}", "samples": int(len(pu)), "depth": depth,
+              "dim": 3, "nodes": (2 ** depth + 1) ** 3, "unknowns": 2 * (2 ** depth + 1) ** 3,
+              "solver": args.solver, "precision": args.precision, "l2": "inputs larger than L2 (no flush)",
+              "parallelism": f"replicas{ws}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_reference(pu, sk, depth, args.cpu_depth, args.steps, args.warmup)
+        line = {"metric": METRIC, "value": cb["value"], "unit": "s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": cb["value"] * 1e3, "higher_is_better": False,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config, "impl": "reference", "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import exteriorpoissonrecon_gb300 as epr
+    r = epr.Reconstructor(3, depth, pu, sk, precision=args.precision, solver=args.solver, device=local)
+    build_ms = r.stats.build_ms if r.stats.build_ms else None
+    for _ in range(args.warmup):
+        r.solve()
+    barrier(pg)
+    clocks = ClockSampler(local)
+    clocks.start()
+    dev_ms = []
+    launches = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = r.solve()
+        dev_ms.append(st["solve_ms"])
+        launches += st["kernel_launches"]
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    barrier(pg)
+    total_ms = allmax(pg, sum(dev_ms))
+    per_step_s = total_ms / 1e3 / args.steps
+
+    # kernel roofline: one parity colour of the paired Gauss-Seidel sweep at the finest level
+    hbm_peak, peak_kind = measured_peaks()
+    gs_ms = r.time_kernel("gs", depth, reps=20)
+    N = (2 ** depth + 1) ** 3
+    rs = 4 if args.precision == "fp32" else 8
+    colour_nodes = (2 ** (depth - 1) + 1) ** 3
+    gs_bytes = 2 * rs * N + colour_nodes * (2 * 27 * rs + 2 * rs)
+    achieved = gs_bytes / (gs_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "gs_colour_kernel", "achieved": achieved, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_kind, "traffic": None,
+                "launch_ms": gs_ms, "algorithmic_bytes_per_launch": gs_bytes,
+                "note": "FMA-bound quartic relaxation; bytes = coefficient read + stencil columns + update writes"}
+
+    # end to end through the public API from host buffers
+    e2e_s = []
+    h2d = pu.nbytes + sk.nbytes
+    d2h = sum(2 * 8 * (2 ** l + 1) ** 3 for l in range(depth + 1))
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        r2 = epr.Reconstructor(3, depth, pu, sk, precision=args.precision, solver=args.solver, device=local)
+        r2.solve()
+        r2.solution()
+        e2e_s.append(time.perf_counter() - t0)
+        r2.close()
+    e2e_v = allmax(pg, statistics.mean(e2e_s))
+
+    line = {"metric": METRIC, "value": per_step_s, "unit": "s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per_step_s * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
+            "data": "synthetic", "config": config, "clocks": clk, "gpu_launches": int(launches),
+            "roofline": roofline,
+            "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "build_ms": build_ms, "wall_s": wall,
+            "final_energy": st["fit_energy"] + st["reg_energy"], "initial_energy": st["initial_energy"],
+            "unknown_sweeps_per_s": 2 * schedule_node_updates(3, depth) / per_step_s}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_reference(pu, sk, depth, args.cpu_depth, 2, 1)
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -52,6 +52,7 @@ class Params(ctypes.Structure):
         ("tolerance", ctypes.c_double),
         ("max_cycles", ctypes.c_int),
         ("verbose", ctypes.c_int),
+        ("device", ctypes.c_int),
     ]
 
 
@@ -66,6 +67,7 @@ class Stats(ctypes.Structure):
         ("grad_norm", ctypes.c_double),
         ("cycles", ctypes.c_int),
         ("node_updates", ctypes.c_int64),
+        ("kernel_launches", ctypes.c_int64),
     ]
 
     def as_dict(self):
@@ -121,6 +123,7 @@ def load():
     L.epr_get_array.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, P, ctypes.c_size_t,
                                 ctypes.POINTER(ctypes.c_size_t)]
     L.epr_synchronize.argtypes = [vp]
+    L.epr_time_kernel.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P]
     _lib = L
     return L
 
@@ -269,6 +272,12 @@ class Reconstructor:
         self._check(load().epr_gn_matvec(self._h, level, _p(np.ascontiguousarray(dx, np.float64)),
                                          _p(np.ascontiguousarray(dy, np.float64)), _p(ox), _p(oy)))
         return ox, oy
+
+    def time_kernel(self, kernel: str, level: int, reps: int = 20) -> float:
+        """Mean device time (ms) of one launch of a kernel family (CUDA events on the context's stream)."""
+        ms = np.zeros(1)
+        self._check(load().epr_time_kernel(self._h, kernel.encode(), level, reps, _p(ms)))
+        return float(ms[0])
 
     # ---------------------------------------------------------------- solve
     def solve(self):

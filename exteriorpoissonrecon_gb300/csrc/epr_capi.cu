@@ -160,6 +160,7 @@ bool Context::energy(int l, double *out3)
         else launch_energy<D, double>(level_ptrs<double>(this, l), levels[l].xy64, red, stream);
         return 0;
     });
+    launches += 2;
     if (!launch_ok("energy")) return false;
     double h[3];
     if (!cuda_ok(cudaMemcpyAsync(h, red.out, sizeof(h), cudaMemcpyDeviceToHost, stream), "energy copy")) return false;
@@ -182,6 +183,7 @@ bool Context::gs(int l, int iters)
                 else launch_gs_colour<D, double>(level_ptrs<double>(this, l), col, d_err, stream);
                 return 0;
             });
+            launches++;
         }
     stats.node_updates += (int64_t)iters * levels[l].N;
     return launch_ok("gs");
@@ -205,6 +207,7 @@ bool Context::prolong_add(int l)
         else launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 1, stream);
         return 0;
     });
+    launches++;
     return launch_ok("prolong");
 }
 
@@ -245,6 +248,7 @@ bool Context::solve_cascadic()
     const int minD = std::min(P.min_solve_depth, depth);
     const int maxD = P.max_solve_depth < 0 ? depth : std::min(P.max_solve_depth, depth);
     bool fp32 = P.precision == EPR_FP32;
+    cudaEventRecord(ev0, stream);
     for (int l = 0; l <= depth; l++)
     {
         if (!cuda_ok(cudaMemsetAsync(levels[l].xy64, 0, sizeof(double) * 2 * levels[l].N, stream), "clear")) return false;
@@ -263,7 +267,6 @@ bool Context::solve_cascadic()
         for (int64_t i = 0; i < N; i++) { x[i] *= s; y[i] *= s; }
         if (!upload_xy(minD, x.data(), y.data())) return false;
     }
-    cudaEventRecord(ev0, stream);
     for (int l = minD; l <= maxD; l++)
     {
         int iters = (int)std::ceil(std::pow(P.i_mult, depth - l) * P.gs_iters);
@@ -283,6 +286,7 @@ bool Context::solve_cascadic()
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0, ev1);
     stats.solve_ms = ms;
+    stats.kernel_launches = launches;
     double e[3];
     if (!energy(maxD, e)) return false;
     stats.initial_energy = c;
@@ -351,6 +355,7 @@ void epr_default_params(epr_params *p)
     p->tolerance = 1e-6;
     p->max_cycles = 200;
     p->verbose = 0;
+    p->device = 0;
 }
 
 const char *epr_global_error(void) { return g_error.c_str(); }
@@ -366,6 +371,11 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
     if (params) p = *params; else epr_default_params(&p);
     if (p.t_radius < 0 || p.t_radius > 4 || p.d_radius < 0 || p.d_radius > 4) { g_error = "kernel radius must be in [0,4]"; return nullptr; }
     if (p.precision != EPR_FP64 && p.precision != EPR_FP32) { g_error = "unknown precision"; return nullptr; }
+    if (cudaSetDevice(p.device) != cudaSuccess)
+    {
+        g_error = std::string("cannot select CUDA device: ") + cudaGetErrorString(cudaGetLastError());
+        return nullptr;
+    }
     epr_ctx *c = new epr_ctx;
     c->dim = dim;
     c->depth = depth;
@@ -397,7 +407,7 @@ void epr_destroy(epr_ctx *ctx) { delete ctx; }
 const char *epr_last_error(const epr_ctx *ctx) { return ctx ? ctx->err.c_str() : g_error.c_str(); }
 
 #define EPR_CHECK_CTX(ctx) \
-    do { if (!(ctx)) { g_error = "null context"; return EPR_ERR_ARG; } (ctx)->status = EPR_OK; } while (0)
+    do { if (!(ctx)) { g_error = "null context"; return EPR_ERR_ARG; } (ctx)->status = EPR_OK; cudaSetDevice((ctx)->P.device); } while (0)
 #define EPR_CHECK_LEVEL(ctx, l) \
     do { if ((l) < 0 || (l) > (ctx)->depth) { (ctx)->fail(EPR_ERR_ARG, "level %d out of range", (int)(l)); return EPR_ERR_ARG; } } while (0)
 #define EPR_RETURN(ctx, ok) return (ok) ? EPR_OK : ((ctx)->status ? (ctx)->status : EPR_ERR_CUDA)
@@ -559,6 +569,7 @@ int epr_solve(epr_ctx *ctx, epr_stats *stats)
     EPR_CHECK_CTX(ctx);
     if (!ctx->have_system) { ctx->fail(EPR_ERR_STATE, "epr_solve called before epr_build"); return EPR_ERR_STATE; }
     ctx->stats.node_updates = 0;
+    ctx->launches = 0;
     bool ok;
     if (ctx->P.solver == EPR_SOLVER_MULTIGRID) ok = epr::solve_multigrid(*ctx);
     else ok = ctx->solve_cascadic();
@@ -614,6 +625,64 @@ int epr_get_array(epr_ctx *ctx, const char *name, int level, double *out, size_t
         return EPR_OK;
     }
     EPR_RETURN(ctx, ctx->setup.get(*ctx, nm, out, cap, count));
+}
+
+int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, double *ms)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!kernel || !ms || reps < 1) { ctx->fail(EPR_ERR_ARG, "bad arguments"); return EPR_ERR_ARG; }
+    std::string k(kernel);
+    epr::Level &L = ctx->levels[level];
+    bool fp32 = ctx->P.precision == EPR_FP32;
+    double *scratch = nullptr;
+    void *pair = nullptr, *out = nullptr;
+    size_t rs = fp32 ? sizeof(float) : sizeof(double);
+    bool ok = ctx->alloc((void **)&scratch, sizeof(double) * 5 * L.N, "alloc") && ctx->alloc(&pair, rs * 2 * L.N, "alloc") &&
+              ctx->alloc(&out, rs * 2 * L.N, "alloc") && ctx->cuda_ok(cudaMemsetAsync(pair, 0, rs * 2 * L.N, ctx->stream), "memset");
+    if (ok && (k == "prolong" && level >= ctx->depth)) { ctx->fail(EPR_ERR_ARG, "no finer level"); ok = false; }
+    if (ok && k != "gs" && k != "energy" && k != "quadfit" && k != "prolong" && k != "gn")
+    {
+        ctx->fail(EPR_ERR_ARG, "unknown kernel '%s'", kernel);
+        ok = false;
+    }
+    auto run = [&]() {
+        epr::with_dim(ctx, [&](auto dd) {
+            constexpr int D = decltype(dd)::value;
+            if (fp32)
+            {
+                auto P = epr::level_ptrs<float>(ctx, level);
+                if (k == "gs") epr::launch_gs_colour<D, float>(P, 0, ctx->d_err, ctx->stream);
+                else if (k == "energy") epr::launch_energy<D, float>(P, L.xy32, ctx->red, ctx->stream);
+                else if (k == "quadfit") epr::launch_quadfit<D, float>(P, L.xy32, scratch, ctx->stream);
+                else if (k == "prolong") epr::launch_prolong<D, float>(level, L.xy32, ctx->levels[level + 1].xy32, 1, ctx->stream);
+                else epr::launch_gn_matvec<D, float>(P, L.xy32, (const float *)pair, (float *)out, ctx->stream);
+            }
+            else
+            {
+                auto P = epr::level_ptrs<double>(ctx, level);
+                if (k == "gs") epr::launch_gs_colour<D, double>(P, 0, ctx->d_err, ctx->stream);
+                else if (k == "energy") epr::launch_energy<D, double>(P, L.xy64, ctx->red, ctx->stream);
+                else if (k == "quadfit") epr::launch_quadfit<D, double>(P, L.xy64, scratch, ctx->stream);
+                else if (k == "prolong") epr::launch_prolong<D, double>(level, L.xy64, ctx->levels[level + 1].xy64, 1, ctx->stream);
+                else epr::launch_gn_matvec<D, double>(P, L.xy64, (const double *)pair, (double *)out, ctx->stream);
+            }
+            return 0;
+        });
+    };
+    if (ok)
+    {
+        run();  // warm-up launch
+        cudaEventRecord(ctx->ev0, ctx->stream);
+        for (int i = 0; i < reps; i++) run();
+        cudaEventRecord(ctx->ev1, ctx->stream);
+        ok = ctx->launch_ok("time kernel") && ctx->cuda_ok(cudaEventSynchronize(ctx->ev1), "sync");
+        float t = 0;
+        if (ok) cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1);
+        *ms = (double)t / reps;
+    }
+    ctx->release(scratch); ctx->release(pair); ctx->release(out);
+    EPR_RETURN(ctx, ok);
 }
 
 int epr_synchronize(epr_ctx *ctx)

@@ -66,6 +66,7 @@ struct Context
     bool have_system = false;
     bool solved = false;
     epr_stats stats{};
+    int64_t launches = 0;  // kernels launched since the last epr_solve started
     Setup setup;
 
     virtual ~Context();

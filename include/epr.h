@@ -73,6 +73,7 @@ typedef struct epr_params {
     double tolerance;     /* multigrid: stop when |grad E| / |grad E(x0)| <= tolerance (1e-6) */
     int max_cycles;       /* multigrid: cycle cap (200) */
     int verbose;          /* print the reference's per-level "Error[...]" lines */
+    int device;           /* CUDA device ordinal the context runs on (0) */
 } epr_params;
 
 typedef struct epr_stats {
@@ -85,6 +86,7 @@ typedef struct epr_stats {
     double grad_norm;        /* multigrid: |grad E| at exit */
     int cycles;              /* multigrid cycles run */
     int64_t node_updates;    /* paired Gauss-Seidel node updates performed */
+    int64_t kernel_launches; /* kernels this library launched during the solve */
 } epr_stats;
 
 void epr_default_params(epr_params *p);
@@ -137,6 +139,13 @@ int epr_get_solution(epr_ctx *ctx, int level, double *x, double *y);
  * "S" (per finest element, packed), "leaf_depth", "R", "B" (per level, column stencils), "c".
  * count receives the number of doubles; out may be NULL to query it. */
 int epr_get_array(epr_ctx *ctx, const char *name, int level, double *out, size_t cap, size_t *count);
+
+/* Times `reps` launches of one kernel family on the context's stream with CUDA events and returns
+ * the mean device time of a single launch in *ms: "gs" (one parity colour of the paired
+ * Gauss-Seidel sweep, colour 0), "energy", "quadfit", "prolong", "gn" (Gauss-Newton matvec).
+ * The level's coefficients are modified by "gs". No counterpart in the reference (a profiling
+ * hook for the benchmark). */
+int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, double *ms);
 
 /* Waits for all work of the context. */
 int epr_synchronize(epr_ctx *ctx);
