@@ -124,6 +124,9 @@ def load():
                                 ctypes.POINTER(ctypes.c_size_t)]
     L.epr_synchronize.argtypes = [vp]
     L.epr_time_kernel.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P]
+    L.epr_energy_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp,
+                                     ctypes.c_double, vp, vp]
+    L.epr_noalloc_last_error.restype = ctypes.c_char_p
     _lib = L
     return L
 

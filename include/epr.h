@@ -147,6 +147,24 @@ int epr_get_array(epr_ctx *ctx, const char *name, int level, double *out, size_t
  * hook for the benchmark). */
 int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, double *ms);
 
+/* Energy of one level computed without allocating anything, for callers that cannot call
+ * cudaMalloc where they need the value (inside a stream capture that must not gain allocation
+ * nodes, under an external memory pool or arena, in allocation-free real-time loops).  It has no
+ * counterpart in the reference.  All pointers are device memory owned by the caller:
+ *   xy    interleaved (x, y) coefficients, 2 (2^level+1)^dim values of the precision's type;
+ *   A, B  the level's column stencils R + dWeight K and B, offset-major (value of offset o at
+ *         node i at [o * N + i]), 3^dim N values of the precision's type;
+ *   out3  3 doubles: fitting energy, regularisation energy, wedge square norm (as epr_energy).
+ * The work is enqueued on `stream` (NULL = default stream) of `device`; the caller synchronises.
+ * The block partial sums use a fixed 128 KiB device array inside the library (one copy per GPU,
+ * held until exit); levels up to 10 (3D) / 7 (4D) fit, anything needing more is rejected.  The
+ * first call on a device looks the array's address up and caches it, so make that first call
+ * before any stream capture.  Calls that overlap on the GPU share the array and race: serialise
+ * them.  Errors: epr_noalloc_last_error(). */
+int epr_energy_noalloc(int device, int dim, int level, int precision, const void *xy, const void *A,
+                       const void *B, double c, double *out3, void *stream);
+const char *epr_noalloc_last_error(void);
+
 /* Waits for all work of the context. */
 int epr_synchronize(epr_ctx *ctx);
 
