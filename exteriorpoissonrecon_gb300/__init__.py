@@ -53,6 +53,7 @@ class Params(ctypes.Structure):
         ("max_cycles", ctypes.c_int),
         ("verbose", ctypes.c_int),
         ("device", ctypes.c_int),
+        ("fp64_levels", ctypes.c_int),
     ]
 
 

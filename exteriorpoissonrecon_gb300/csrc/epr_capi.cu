@@ -87,9 +87,11 @@ bool Context::ensure_level(int l)
     return true;
 }
 
+bool Context::lvl32(int l) const { return P.precision == EPR_FP32 && l >= P.fp64_levels; }
+
 bool Context::sync_system32(int l)
 {
-    if (P.precision != EPR_FP32) return true;
+    if (!lvl32(l)) return true;
     Level &L = levels[l];
     size_t S = (size_t)stencil();
     launch_convert_d2f(L.A64, L.A32, (int64_t)S * L.N, stream);
@@ -100,13 +102,13 @@ bool Context::sync_system32(int l)
 // device coefficients <-> the precision the solve works in
 bool Context::push_xy(int l)
 {
-    if (P.precision != EPR_FP32) return true;
+    if (!lvl32(l)) return true;
     launch_convert_d2f(levels[l].xy64, levels[l].xy32, 2 * levels[l].N, stream);
     return launch_ok("convert xy");
 }
 bool Context::pull_xy(int l)
 {
-    if (P.precision != EPR_FP32) return true;
+    if (!lvl32(l)) return true;
     launch_convert_f2d(levels[l].xy32, levels[l].xy64, 2 * levels[l].N, stream);
     return launch_ok("convert xy");
 }
@@ -153,7 +155,7 @@ LevelPtrs<Real> level_ptrs(Context *c, int l)
 
 bool Context::energy(int l, double *out3)
 {
-    bool fp32 = P.precision == EPR_FP32;
+    bool fp32 = lvl32(l);
     with_dim(this, [&](auto dd) {
         constexpr int D = decltype(dd)::value;
         if (fp32) launch_energy<D, float>(level_ptrs<float>(this, l), levels[l].xy32, red, stream);
@@ -173,18 +175,12 @@ bool Context::energy(int l, double *out3)
 
 bool Context::gs(int l, int iters)
 {
-    bool fp32 = P.precision == EPR_FP32;
-    for (int it = 0; it < iters; it++)
-        for (int col = 0; col < (1 << dim); col++)
-        {
-            with_dim(this, [&](auto dd) {
-                constexpr int D = decltype(dd)::value;
-                if (fp32) launch_gs_colour<D, float>(level_ptrs<float>(this, l), col, d_err, stream);
-                else launch_gs_colour<D, double>(level_ptrs<double>(this, l), col, d_err, stream);
-                return 0;
-            });
-            launches++;
-        }
+    bool fp32 = lvl32(l);
+    launches += with_dim(this, [&](auto dd) {
+        constexpr int D = decltype(dd)::value;
+        if (fp32) return launch_gs_sweeps<D, float>(level_ptrs<float>(this, l), iters, d_err, stream);
+        return launch_gs_sweeps<D, double>(level_ptrs<double>(this, l), iters, d_err, stream);
+    });
     stats.node_updates += (int64_t)iters * levels[l].N;
     return launch_ok("gs");
 }
@@ -200,11 +196,23 @@ bool Context::check_errors()
 
 bool Context::prolong_add(int l)
 {
-    bool fp32 = P.precision == EPR_FP32;
+    bool c32 = lvl32(l), f32 = lvl32(l + 1);
     with_dim(this, [&](auto dd) {
         constexpr int D = decltype(dd)::value;
-        if (fp32) launch_prolong<D, float>(l, levels[l].xy32, levels[l + 1].xy32, 1, stream);
-        else launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 1, stream);
+        if (c32 && f32) launch_prolong<D, float>(l, levels[l].xy32, levels[l + 1].xy32, 1, stream);
+        else
+        {
+            // a double coarse level feeding a float fine level: prolong in double, then refresh
+            // the float copy of the fine level
+            if (!f32) launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 1, stream);
+            else
+            {
+                launch_convert_f2d(levels[l + 1].xy32, levels[l + 1].xy64, 2 * levels[l + 1].N, stream);
+                launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 1, stream);
+                launch_convert_d2f(levels[l + 1].xy64, levels[l + 1].xy32, 2 * levels[l + 1].N, stream);
+                launches += 2;
+            }
+        }
         return 0;
     });
     launches++;
@@ -356,6 +364,7 @@ void epr_default_params(epr_params *p)
     p->max_cycles = 200;
     p->verbose = 0;
     p->device = 0;
+    p->fp64_levels = 0;
 }
 
 const char *epr_global_error(void) { return g_error.c_str(); }
@@ -485,7 +494,7 @@ int epr_quadfit(epr_ctx *ctx, int level, double *out)
     bool ok = ctx->alloc((void **)&d, sizeof(double) * 5 * L.N, "alloc fit");
     if (ok)
     {
-        bool fp32 = ctx->P.precision == EPR_FP32;
+        bool fp32 = ctx->lvl32(level);
         epr::with_dim(ctx, [&](auto dd) {
             constexpr int D = decltype(dd)::value;
             if (fp32) epr::launch_quadfit<D, float>(epr::level_ptrs<float>(ctx, level), L.xy32, d, ctx->stream);
@@ -537,7 +546,7 @@ int epr_gn_matvec(epr_ctx *ctx, int level, const double *dx, const double *dy, d
     for (int64_t i = 0; i < L.N; i++) { h[2 * i] = dx[i]; h[2 * i + 1] = dy[i]; }
     double *d64 = nullptr, *o64 = nullptr;
     float *d32 = nullptr, *o32 = nullptr;
-    bool fp32 = ctx->P.precision == EPR_FP32;
+    bool fp32 = ctx->lvl32(level);
     bool ok = ctx->alloc((void **)&d64, sizeof(double) * 2 * L.N, "alloc") && ctx->alloc((void **)&o64, sizeof(double) * 2 * L.N, "alloc") &&
               ctx->cuda_ok(cudaMemcpyAsync(d64, h.data(), sizeof(double) * 2 * L.N, cudaMemcpyHostToDevice, ctx->stream), "upload");
     if (ok && fp32)
@@ -634,7 +643,7 @@ int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, doubl
     if (!kernel || !ms || reps < 1) { ctx->fail(EPR_ERR_ARG, "bad arguments"); return EPR_ERR_ARG; }
     std::string k(kernel);
     epr::Level &L = ctx->levels[level];
-    bool fp32 = ctx->P.precision == EPR_FP32;
+    bool fp32 = ctx->lvl32(level);
     double *scratch = nullptr;
     void *pair = nullptr, *out = nullptr;
     size_t rs = fp32 ? sizeof(float) : sizeof(double);

@@ -78,6 +78,7 @@ struct Context
     int64_t nodes(int level) const;
     int stencil() const;
     bool ensure_level(int l);
+    bool lvl32(int l) const;  // level l computes in float
     bool sync_system32(int l);
     bool push_xy(int l);
     bool pull_xy(int l);

@@ -33,6 +33,11 @@ template <int D, typename Real>
 void launch_quadfit(const LevelPtrs<Real> &L, const Real *xy, double *out, cudaStream_t s);
 template <int D, typename Real>
 void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, cudaStream_t s);
+// iters full sweeps (all 2^D colours in order); levels of at most kPersistentMaxNodes nodes run all
+// sweeps inside one thread block.  Returns the number of kernels launched.
+constexpr int64_t kPersistentMaxNodes = 729;
+template <int D, typename Real>
+int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s);
 template <int D, typename Real>
 void launch_gn_matvec(const LevelPtrs<Real> &L, const Real *xy, const Real *dxy, Real *out, cudaStream_t s);
 // fine (2 N_f) = P coarse (2 N_c), pairs; add != 0 accumulates

@@ -241,14 +241,10 @@ __global__ void __launch_bounds__(kThreads) quadfit_kernel(LevelPtrs<Real> L, co
     for (int k = 0; k < 5; k++) out[i * 5 + k] = (double)q[k];
 }
 
-// Paired Gauss-Seidel update of one parity colour: same-colour nodes share no element, so all of
-// them are updated in parallel exactly as the reference's per-colour ParallelFor does.
+// Paired Gauss-Seidel update of node j of a parity colour.
 template <int D, typename Real>
-__global__ void __launch_bounds__(kThreads) gs_colour_kernel(LevelPtrs<Real> L, Colour<D> col, unsigned int *err)
+__device__ __forceinline__ void gs_update(const LevelPtrs<Real> &L, const Grid<D> &g, const Colour<D> &col, int64_t j, unsigned int *err)
 {
-    Grid<D> g(L.level);
-    int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (j >= col.n) return;
     NodeCtx<D> nc;
     col.node(j, nc.I);
 #pragma unroll
@@ -269,6 +265,35 @@ __global__ void __launch_bounds__(kThreads) gs_colour_kernel(LevelPtrs<Real> L, 
         if (!isfinite((double)v.x) || !isfinite((double)v.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
         reinterpret_cast<Real2<Real> *>(L.xy)[i] = v;
     }
+}
+
+// One parity colour: same-colour nodes share no element, so all of them are updated in parallel
+// exactly as the reference's per-colour ParallelFor does.
+template <int D, typename Real>
+__global__ void __launch_bounds__(kThreads) gs_colour_kernel(LevelPtrs<Real> L, Colour<D> col, unsigned int *err)
+{
+    Grid<D> g(L.level);
+    int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= col.n) return;
+    gs_update<D, Real>(L, g, col, j, err);
+}
+
+// All sweeps of a small level in one thread block: the colours follow each other behind a block
+// barrier, which also makes each colour's writes visible to the next.  Used for the coarse levels
+// of the cascadic schedule, whose thousands of tiny sweeps would otherwise be bound by launch
+// latency.
+constexpr int kPersistentThreads = 256;
+template <int D, typename Real>
+__global__ void __launch_bounds__(kPersistentThreads) gs_level_kernel(LevelPtrs<Real> L, int iters, unsigned int *err)
+{
+    Grid<D> g(L.level);
+    for (int it = 0; it < iters; it++)
+        for (int c = 0; c < (1 << D); c++)
+        {
+            Colour<D> col(g, c);
+            for (int64_t j = threadIdx.x; j < col.n; j += blockDim.x) gs_update<D, Real>(L, g, col, j, err);
+            __syncthreads();
+        }
 }
 
 template <int D, typename Real>
@@ -437,6 +462,22 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
 }
 
 template <int D, typename Real>
+int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s)
+{
+    Grid<D> g(L.level);
+    if (iters <= 0) return 0;
+    if (g.N <= kPersistentMaxNodes)
+    {
+        gs_level_kernel<D, Real><<<1, kPersistentThreads, 0, s>>>(L, iters, err);
+        return 1;
+    }
+    int n = 0;
+    for (int it = 0; it < iters; it++)
+        for (int c = 0; c < (1 << D); c++) { launch_gs_colour<D, Real>(L, c, err, s); n++; }
+    return n;
+}
+
+template <int D, typename Real>
 void launch_gn_matvec(const LevelPtrs<Real> &L, const Real *xy, const Real *dxy, Real *out, cudaStream_t s)
 {
     Grid<D> g(L.level);
@@ -480,6 +521,7 @@ void launch_convert_f2d(const float *in, double *out, int64_t n, cudaStream_t st
     template void launch_energy<D, R>(const LevelPtrs<R> &, const R *, const Reduce &, cudaStream_t);   \
     template void launch_quadfit<D, R>(const LevelPtrs<R> &, const R *, double *, cudaStream_t);        \
     template void launch_gs_colour<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t);      \
+    template int launch_gs_sweeps<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t);       \
     template void launch_gn_matvec<D, R>(const LevelPtrs<R> &, const R *, const R *, R *, cudaStream_t); \
     template void launch_prolong<D, R>(int, const R *, R *, int, cudaStream_t);                         \
     template void launch_restrict<D, R>(int, const R *, R *, cudaStream_t);

@@ -74,6 +74,7 @@ typedef struct epr_params {
     int max_cycles;       /* multigrid: cycle cap (200) */
     int verbose;          /* print the reference's per-level "Error[...]" lines */
     int device;           /* CUDA device ordinal the context runs on (0) */
+    int fp64_levels;      /* EPR_FP32 only: levels below this one still run in double (0) */
 } epr_params;
 
 typedef struct epr_stats {

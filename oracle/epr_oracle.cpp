@@ -984,7 +984,7 @@ struct Oracle
 
     // paired Gauss-Seidel (ExteriorPoissonSolvers.h:156-196), colours by per-axis parity
     // (ExteriorPoisson.h:161-169): colour bit d set when node index on axis d is odd.
-    void gs(int level, double *x, double *y, int iters) const
+    void gs(int level, double *x, double *y, int iters, const double *tx = nullptr, const double *ty = nullptr) const
     {
         GridIdx<D> g(1 << level);
         size_t N = g.nodes();
@@ -1007,6 +1007,7 @@ struct Oracle
                     size_t i = list[j];
                     double q[5];
                     quadfitNode(level, g, i, x, y, q);
+                    if (tx) { q[3] -= tx[i]; q[4] -= ty[i]; }
                     double h00 = 2 * q[0], h11 = 2 * q[1], h01 = q[2];
                     double det = h00 * h11 - h01 * h01;
                     if (std::fabs(det) > 1e-20)
@@ -1051,6 +1052,30 @@ struct Oracle
                 if (d < 0) break;
             }
             xf[i] = s;
+        }
+    }
+
+    // restriction v_c = P^T v_f (the transpose of prolong)
+    void restrictT(int level, const double *vf, double *vc) const
+    {
+        GridIdx<D> gc(1 << level), gf(1 << (level + 1));
+        size_t Nc = gc.nodes();
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < (long)Nc; i++)
+        {
+            int I[D];
+            gc.node((size_t)i, I);
+            double s = 0;
+            for (int o = 0; o < T::S; o++)
+            {
+                int off[D], F[D];
+                StencilOffset<D>(o, off);
+                bool ok = true;
+                double w = 1.;
+                for (int d = 0; d < D; d++) { F[d] = 2 * I[d] + off[d]; if (F[d] < 0 || F[d] > gf.r) ok = false; if (off[d]) w *= 0.5; }
+                if (ok) s += w * vf[gf.node(F)];
+            }
+            vc[i] = s;
         }
     }
 
@@ -1365,6 +1390,20 @@ int epr_oracle_gs(epr_oracle *o, int level, double *x, double *y, int iters)
 {
     if (!o) return -1;
     DISPATCH(o, { self->gs(level, x, y, iters); });
+    return 0;
+}
+
+int epr_oracle_gs_shifted(epr_oracle *o, int level, double *x, double *y, int iters, const double *tx, const double *ty)
+{
+    if (!o) return -1;
+    DISPATCH(o, { self->gs(level, x, y, iters, tx, ty); });
+    return 0;
+}
+
+int epr_oracle_restrict(epr_oracle *o, int level, const double *fine, double *coarse)
+{
+    if (!o) return -1;
+    DISPATCH(o, { self->restrictT(level, fine, coarse); });
     return 0;
 }
 

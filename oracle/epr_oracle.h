@@ -68,6 +68,10 @@ int epr_oracle_quadfit(epr_oracle *o, int level, const double *x, const double *
 int epr_oracle_gradient(epr_oracle *o, int level, const double *x, const double *y, double *gx, double *gy);
 /* paired Gauss-Seidel, iters full sweeps over the 2^Dim parity colours (ExteriorPoissonSolvers.h:156-196) */
 int epr_oracle_gs(epr_oracle *o, int level, double *x, double *y, int iters);
+/* paired Gauss-Seidel on the shifted energy E - <tx, x> - <ty, y> (tx, ty per node) */
+int epr_oracle_gs_shifted(epr_oracle *o, int level, double *x, double *y, int iters, const double *tx, const double *ty);
+/* restriction coarse = P^T fine of a level-(level+1) vector to level `level` */
+int epr_oracle_restrict(epr_oracle *o, int level, const double *fine, double *coarse);
 /* prolongation of a level-`level` vector to level+1 (Hat.scalars.inl:1747-1779) */
 int epr_oracle_prolong(epr_oracle *o, int level, const double *coarse, double *fine);
 /* Gauss-Newton matvec of the energy's quadratic model at (x,y) applied to (dx,dy) */

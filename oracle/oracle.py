@@ -63,6 +63,8 @@ def lib():
         L.epr_oracle_gradient.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, P]
         L.epr_oracle_gs.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, ctypes.c_int]
         L.epr_oracle_prolong.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P]
+        L.epr_oracle_gs_shifted.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, ctypes.c_int, P, P]
+        L.epr_oracle_restrict.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P]
         L.epr_oracle_gn_matvec.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, P, P, P]
         L.epr_oracle_solve.argtypes = [ctypes.c_void_p, P, P, P]
         _lib = L
@@ -161,6 +163,18 @@ class Oracle:
         y = np.array(y, dtype=np.float64)
         lib().epr_oracle_gs(self._h, level, _p(x), _p(y), iters)
         return x, y
+
+    def gs_shifted(self, level, x, y, tx, ty, iters=1):
+        x = np.array(x, dtype=np.float64)
+        y = np.array(y, dtype=np.float64)
+        lib().epr_oracle_gs_shifted(self._h, level, _p(x), _p(y), iters,
+                                    _p(np.ascontiguousarray(tx, np.float64)), _p(np.ascontiguousarray(ty, np.float64)))
+        return x, y
+
+    def restrict(self, level, vf):
+        out = np.zeros(self.nodes(level))
+        lib().epr_oracle_restrict(self._h, level, _p(np.ascontiguousarray(vf, np.float64)), _p(out))
+        return out
 
     def prolong(self, level, xc):
         out = np.zeros(self.nodes(level + 1))
