@@ -240,7 +240,7 @@ def main():
         r2.solution()
         e2e_s.append(time.perf_counter() - t0)
         r2.close()
-    e2e_v = allmax(pg, statistics.mean(e2e_s))
+    e2e_v = allmax(pg, statistics.mean(e2e_s)) if e2e_s else None
 
     line = {"metric": METRIC, "value": per_step_s, "unit": "s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step_s * 1e3, "higher_is_better": False,

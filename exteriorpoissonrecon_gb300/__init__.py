@@ -54,6 +54,8 @@ class Params(ctypes.Structure):
         ("verbose", ctypes.c_int),
         ("device", ctypes.c_int),
         ("fp64_levels", ctypes.c_int),
+        ("single_level", ctypes.c_int),
+        ("separate", ctypes.c_int),
     ]
 
 
@@ -80,6 +82,7 @@ _FLAG_NAMES = {
     "sWeight": "s_weight", "dWeight": "d_weight", "nSigma": "n_sigma", "iMult": "i_mult",
     "tRadius": "t_radius", "dRadius": "d_radius", "gsIters": "gs_iters",
     "minSolveDepth": "min_solve_depth", "maxSolveDepth": "max_solve_depth", "seed": "seed",
+    "singleLevel": "single_level", "separate": "separate",
 }
 
 

@@ -59,7 +59,24 @@ def build(verbose_ptxas: bool = False, force: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_cli()
     return LIB
+
+
+CLI_SRC = os.path.join(HERE, "host", "epr_recon.cpp")
+CLI = os.path.join(HERE, "epr_recon")
+
+
+def build_cli() -> str:
+    """The ExteriorPoissonRecon-compatible command line (host C++ over the C ABI)."""
+    if os.path.exists(CLI) and os.path.getmtime(CLI) > max(os.path.getmtime(CLI_SRC), os.path.getmtime(LIB)):
+        return CLI
+    cxx = os.environ.get("CXX", "g++")
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-o", CLI, CLI_SRC, "-L" + HERE, "-lepr_cuda", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CLI build failed:\n{r.stdout}\n{r.stderr}")
+    return CLI
 
 
 if __name__ == "__main__":

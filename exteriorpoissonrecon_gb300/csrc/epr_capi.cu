@@ -178,8 +178,8 @@ bool Context::gs(int l, int iters)
     bool fp32 = lvl32(l);
     launches += with_dim(this, [&](auto dd) {
         constexpr int D = decltype(dd)::value;
-        if (fp32) return launch_gs_sweeps<D, float>(level_ptrs<float>(this, l), iters, d_err, stream);
-        return launch_gs_sweeps<D, double>(level_ptrs<double>(this, l), iters, d_err, stream);
+        if (fp32) return launch_gs_sweeps<D, float>(level_ptrs<float>(this, l), iters, d_err, stream, P.separate);
+        return launch_gs_sweeps<D, double>(level_ptrs<double>(this, l), iters, d_err, stream, P.separate);
     });
     stats.node_updates += (int64_t)iters * levels[l].N;
     return launch_ok("gs");
@@ -275,7 +275,33 @@ bool Context::solve_cascadic()
         for (int64_t i = 0; i < N; i++) { x[i] *= s; y[i] *= s; }
         if (!upload_xy(minD, x.data(), y.data())) return false;
     }
-    for (int l = minD; l <= maxD; l++)
+    if (P.single_level)
+    {
+        // prolong the initial guess to the finest solve level, clear the coarser levels and relax
+        // only there with gsIters sweeps (ExteriorPoisson.h:342-360)
+        for (int l = minD; l < maxD; l++)
+        {
+            with_dim(this, [&](auto dd) {
+                constexpr int D = decltype(dd)::value;
+                launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 0, stream);
+                return 0;
+            });
+            launches++;
+        }
+        for (int l = minD; l < maxD; l++)
+            if (!cuda_ok(cudaMemsetAsync(levels[l].xy64, 0, sizeof(double) * 2 * levels[l].N, stream), "clear")) return false;
+        if (!push_xy(maxD)) return false;
+        double e0[3] = {0, 0, 0};
+        if (P.verbose && !energy(maxD, e0)) return false;
+        if (!gs(maxD, P.gs_iters)) return false;
+        if (P.verbose)
+        {
+            double e1[3];
+            if (!energy(maxD, e1)) return false;
+            printf("Error[%2d]: %9.5f -> %.5f = %.5f + %.5f\n", 1 << maxD, e0[0] + e0[1], e1[0] + e1[1], e1[0], e1[1]);
+        }
+    }
+    for (int l = minD; !P.single_level && l <= maxD; l++)
     {
         int iters = (int)std::ceil(std::pow(P.i_mult, depth - l) * P.gs_iters);
         double e0[3] = {0, 0, 0};
@@ -365,6 +391,8 @@ void epr_default_params(epr_params *p)
     p->verbose = 0;
     p->device = 0;
     p->fp64_levels = 0;
+    p->single_level = 0;
+    p->separate = 0;
 }
 
 const char *epr_global_error(void) { return g_error.c_str(); }
@@ -385,6 +413,7 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
         g_error = std::string("cannot select CUDA device: ") + cudaGetErrorString(cudaGetLastError());
         return nullptr;
     }
+    if (const char *v = getenv("EPR_GS_VARIANT")) epr::set_gs_variant(atoi(v));
     epr_ctx *c = new epr_ctx;
     c->dim = dim;
     c->depth = depth;

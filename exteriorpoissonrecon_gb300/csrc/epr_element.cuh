@@ -215,6 +215,43 @@ __device__ __forceinline__ void element_fit(const Real *x, const Real *y, int A,
 }
 
 // ---------------------------------------------------------------------------------------------
+// Canonical orientation.  Mirroring an element along axis d (xi_d -> 1 - xi_d) flips the sign of
+// every d-derivative; each component of W, U and V carries exactly one derivative along each of
+// its two axes, so all the products in the fit integrals keep their sign.  Any corner A can
+// therefore be evaluated as corner 0 of the element mirrored along the axes where A has a 1 bit,
+// which makes every hat factor a compile-time constant.
+// ---------------------------------------------------------------------------------------------
+template <int D, typename Real>
+struct Corners
+{
+    Real x[1 << D];
+    Real y[1 << D];
+};
+template <typename Real>
+struct Fit5
+{
+    Real h[5];
+};
+
+template <int D, typename Real>
+__device__ __noinline__ Fit5<Real> element_fit_canonical(Corners<D, Real> c)
+{
+    Fit5<Real> f;
+#pragma unroll
+    for (int k = 0; k < 5; k++) f.h[k] = 0;
+    component_fit<D, 0>(c.x, c.y, 0, f.h);
+    component_fit<D, 1>(c.x, c.y, 0, f.h);
+    component_fit<D, 2>(c.x, c.y, 0, f.h);
+    if constexpr (D == 4)
+    {
+        component_fit<D, 3>(c.x, c.y, 0, f.h);
+        component_fit<D, 4>(c.x, c.y, 0, f.h);
+        component_fit<D, 5>(c.x, c.y, 0, f.h);
+    }
+    return f;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Gauss-Newton products for corner A: J(d) = W(dx, y) + W(x, dy);
 //   s[0] = sum <J(d), U>,  s[1] = sum <J(d), V>   (reference units)
 // ---------------------------------------------------------------------------------------------

@@ -31,13 +31,16 @@ void launch_energy(const LevelPtrs<Real> &L, const Real *xy, const Reduce &red, 
 // writes N x 5 doubles (Q20, Q02, Q11, Q10, Q01)
 template <int D, typename Real>
 void launch_quadfit(const LevelPtrs<Real> &L, const Real *xy, double *out, cudaStream_t s);
+// separate != 0: the reference's SeparateGaussSeidelSolve update (x first, then y with the new x)
 template <int D, typename Real>
-void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, cudaStream_t s);
+void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, cudaStream_t s, int separate = 0);
+// selects the colour-kernel variant (0: one thread per node, 1: 2^D lanes per node)
+void set_gs_variant(int v);
 // iters full sweeps (all 2^D colours in order); levels of at most kPersistentMaxNodes nodes run all
 // sweeps inside one thread block.  Returns the number of kernels launched.
 constexpr int64_t kPersistentMaxNodes = 729;
 template <int D, typename Real>
-int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s);
+int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s, int separate = 0);
 template <int D, typename Real>
 void launch_gn_matvec(const LevelPtrs<Real> &L, const Real *xy, const Real *dxy, Real *out, cudaStream_t s);
 // fine (2 N_f) = P coarse (2 N_c), pairs; add != 0 accumulates

@@ -228,72 +228,222 @@ struct SplatArgs
     int depth;  // finest depth
     int t;      // tree depth of the grid
     int KR;     // kernel radius (B-spline degree 2 KR + 1)
+    const int *rlo = nullptr, *rhi = nullptr;  // occupied-cell range of every depth-t cell, by Morton code
 };
 
 // range of occupied cells inside the depth-t cell C
 template <int D>
 __device__ inline void cell_range(const SplatArgs &a, const int *C, int64_t &lo, int64_t &hi)
 {
-    int s = a.depth + 1 - a.t;  // levels between depth-t cells and finest cells
+    if (a.rlo)
+    {
+        const int res = 1 << (a.t - 1);
+        int64_t li = 0;
+        for (int d = 0; d < D; d++) li = li * res + C[d];
+        lo = a.rlo[li];
+        hi = a.rhi[li];
+        return;
+    }
     int64_t m = morton<D>(C, a.t - 1);
+    int s = a.depth + 1 - a.t;  // levels between depth-t cells and finest cells
     lo = lower_bound(a.cellKey, a.ncells, m << (D * s));
     hi = lower_bound(a.cellKey, a.ncells, (m + 1) << (D * s));
 }
 
-// Density splat of the merged cells (TreeSplatter::_addSample, GridSamples.inl:458-491 with the
-// depth weight of TreeEstimator, GridSamples.inl:749-760).
+// Occupied-cell range of every depth-t cell: the occupied finest cells are sorted by Morton key, so
+// the ones below a depth-t cell are contiguous; mark where each ancestor's run starts and ends.
+// (stored by the row-major index of the depth-t cell)
 template <int D>
-__global__ void density_gather_kernel(SplatArgs a, const double *mean, const double *datum, double depthWeight, double *grid)
+__global__ void level_ranges_kernel(const int64_t *cellKey, int64_t ncells, int t, int shift, int *rlo, int *rhi)
 {
-    constexpr int W = 1 + D + D * D;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= ncells) return;
+    int64_t anc = cellKey[k] >> shift;
+    int C[D];
+    demorton<D>(anc, t - 1, C);
+    const int res = 1 << (t - 1);
+    int64_t li = 0;
+    for (int d = 0; d < D; d++) li = li * res + C[d];
+    if (k == 0 || (cellKey[k - 1] >> shift) != anc) rlo[li] = (int)k;
+    if (k == ncells - 1 || (cellKey[k + 1] >> shift) != anc) rhi[li] = (int)(k + 1);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Chunked gathers for the coarse tree levels.  There a vertex's window covers a large part of the
+// domain, so one warp per vertex would walk hundreds of thousands of items.  Instead each vertex's
+// item list (the concatenation, in window order, of the items of its window cells) is cut into
+// chunks of kChunk items, one warp reduces each chunk into a partial sum, and a final pass adds a
+// vertex's partials in chunk order: the result is still deterministic.
+// ---------------------------------------------------------------------------------------------
+constexpr int kChunk = 2048;
+
+// Item range of one window cell: occupied-cell indices (merged density data) or sample positions
+// in the sorted order (frame samples).
+template <int D, bool Samples>
+__device__ inline void item_range(const SplatArgs &a, const int *C, int &lo, int &hi)
+{
+    int64_t l, h;
+    cell_range<D>(a, C, l, h);
+    if (Samples) { lo = a.cellStart[l]; hi = a.cellStart[h]; }
+    else { lo = (int)l; hi = (int)h; }
+}
+
+template <int D>
+__device__ inline void vertex_of(int64_t vi, int nv, int *v)
+{
+    for (int d = D - 1; d >= 0; d--) { v[d] = (int)(vi % nv); vi /= nv; }
+}
+
+template <int D>
+__device__ inline bool window_next(int *C, const int *clo, const int *chi)
+{
+    int d = D - 1;
+    for (; d >= 0; d--) { if (++C[d] <= chi[d]) return true; C[d] = clo[d]; }
+    return false;
+}
+
+template <int D, bool Samples>
+__global__ void vertex_chunks_kernel(SplatArgs a, int *nchunks)
+{
     int res = 1 << (a.t - 1), nv = res + 1;
     int64_t NV = 1;
     for (int d = 0; d < D; d++) NV *= nv;
-    if (warp >= NV) return;
-    int v[D];
+    int64_t vi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (vi >= NV) return;
+    int v[D], clo[D], chi[D], C[D];
+    vertex_of<D>(vi, nv, v);
+    for (int d = 0; d < D; d++) { clo[d] = max(0, v[d] - a.KR - 1); chi[d] = min(res - 1, v[d] + a.KR); C[d] = clo[d]; }
+    int64_t count = 0;
+    do
     {
-        int64_t t = warp;
-        for (int d = D - 1; d >= 0; d--) { v[d] = (int)(t % nv); t /= nv; }
-    }
-    const int deg = 2 * a.KR + 1;
-    int clo[D], chi[D], C[D];
-    for (int d = 0; d < D; d++)
+        int lo, hi;
+        item_range<D, Samples>(a, C, lo, hi);
+        count += hi - lo;
+    } while (window_next<D>(C, clo, chi));
+    nchunks[vi] = (int)((count + kChunk - 1) / kChunk);
+}
+
+// Contribution of item `it` to vertex v through window cell C, added to acc.
+// Density: a merged cell (mean position, summed (1, p, p p^T)) splatted with the degree 2 KR + 1
+// B-spline weights of its mean and the estimator's depth weight (TreeSplatter::_addSample,
+// GridSamples.inl:458-491; TreeEstimator ctor :749-760).  The window is centred on the depth-t
+// ancestor of the item's cell while the weights come from floor(p res), as in the reference.
+template <int D>
+struct DensityItem
+{
+    static constexpr int W = 1 + D + D * D;
+    const double *mean, *datum;
+    double depthWeight;
+    __device__ void operator()(const SplatArgs &a, int it, const int *v, const int *C, double *acc) const
     {
-        clo[d] = max(0, v[d] - a.KR - 1);
-        chi[d] = min(res - 1, v[d] + a.KR);
-        C[d] = clo[d];
+        const int deg = 2 * a.KR + 1, res = 1 << (a.t - 1);
+        double wt = depthWeight;
+        for (int d = 0; d < D; d++)
+        {
+            double bs[kMaxDeg + 1];
+            double pr = mean[(int64_t)it * D + d] * res;
+            int e = (int)floor(pr);
+            bspline_eval(deg, pr - e, bs);
+            wt *= bs[v[d] - (C[d] - a.KR)];
+        }
+        for (int w = 0; w < W; w++) acc[w] += wt * datum[(int64_t)it * W + w];
     }
+};
+
+// Frame sample: normalised frame times the sample's measure and 2^(2 depth), split between the two
+// tree depths bracketing its estimated depth with weights 2^((d-1) D) (ExteriorPoisson.h:181-228,
+// GridSamples.inl:436-456), B-spline weights of the sample position.
+template <int D>
+struct SkewItem
+{
+    static constexpr int W = D * (D - 1) / 2;
+    const double *pos, *skew, *measure, *sdepth;
+    const int *order;
+    __device__ void operator()(const SplatArgs &a, int j, const int *v, const int *C, double *acc) const
+    {
+        const int deg = 2 * a.KR + 1, res = 1 << (a.t - 1), maxT = a.depth + 1;
+        int s = order[j];
+        double dd = sdepth[s] + 1.;
+        double lw = 0;
+        if (dd >= maxT) lw = (a.t == maxT) ? (double)(1ull << (a.depth * D)) : 0.;
+        else if (dd <= 1) lw = (a.t == 1) ? 1. : 0.;
+        else
+        {
+            int d1 = (int)floor(dd), d2 = d1 + 1;
+            double f = dd - d1;
+            if (a.t == d1) lw = (1. - f) * (double)(1ull << ((d1 - 1) * D));
+            else if (a.t == d2) lw = f * (double)(1ull << ((d2 - 1) * D));
+        }
+        if (lw == 0) return;
+        const double *q = pos + (int64_t)s * D;
+        double wt = lw;
+        for (int d = 0; d < D; d++)
+        {
+            double bs[kMaxDeg + 1];
+            double pr = q[d] * res;
+            int e = (int)floor(pr);
+            bspline_eval(deg, pr - e, bs);
+            wt *= bs[v[d] - (C[d] - a.KR)];
+        }
+        const double *sk = skew + (int64_t)s * W;
+        double nrm = 0;
+        for (int k = 0; k < W; k++) nrm += 2 * sk[k] * sk[k];
+        nrm = sqrt(nrm);
+        double m = measure[s], sc = (double)(1ull << (a.depth * 2));
+        for (int k = 0; k < W; k++) acc[k] += wt * (sk[k] / nrm * m * sc);
+    }
+};
+
+// one warp per chunk
+template <int D, bool Samples, class Item>
+__global__ void chunk_gather_kernel(SplatArgs a, Item item, const int *chunkStart, int64_t NV, int64_t nchunks, double *partial)
+{
+    constexpr int W = Item::W;
+    int64_t chunk = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (chunk >= nchunks) return;
+    // vertex owning the chunk: last vi with chunkStart[vi] <= chunk
+    int64_t lo = 0, hi = NV;
+    while (hi - lo > 1)
+    {
+        int64_t mid = (lo + hi) >> 1;
+        if (chunkStart[mid] <= chunk) lo = mid; else hi = mid;
+    }
+    const int64_t vi = lo;
+    const int64_t first = (chunk - chunkStart[vi]) * kChunk, last = first + kChunk;
+    int res = 1 << (a.t - 1), nv = res + 1;
+    int v[D], clo[D], chi[D], C[D];
+    vertex_of<D>(vi, nv, v);
+    for (int d = 0; d < D; d++) { clo[d] = max(0, v[d] - a.KR - 1); chi[d] = min(res - 1, v[d] + a.KR); C[d] = clo[d]; }
     double acc[W];
     for (int w = 0; w < W; w++) acc[w] = 0;
-    while (true)
+    int64_t base = 0;
+    do
     {
-        int64_t lo, hi;
-        cell_range<D>(a, C, lo, hi);
-        for (int64_t k = lo + lane; k < hi; k += 32)
-        {
-            double wt = depthWeight;
-            for (int d = 0; d < D; d++)
-            {
-                double bs[kMaxDeg + 1];
-                double pr = mean[k * D + d] * res;
-                int e = (int)floor(pr);
-                bspline_eval(deg, pr - e, bs);
-                int i = v[d] - (C[d] - a.KR);
-                wt *= bs[i];
-            }
-            for (int w = 0; w < W; w++) acc[w] += wt * datum[k * W + w];
-        }
-        int d = D - 1;
-        for (; d >= 0; d--) { if (++C[d] <= chi[d]) break; C[d] = clo[d]; }
-        if (d < 0) break;
-    }
+        int ilo, ihi;
+        item_range<D, Samples>(a, C, ilo, ihi);
+        int64_t sz = ihi - ilo;
+        int64_t b0 = max(base, first), b1 = min(base + sz, last);
+        for (int64_t o = b0 + lane; o < b1; o += 32) item(a, (int)(ilo + (o - base)), v, C, acc);
+        base += sz;
+    } while (base < last && window_next<D>(C, clo, chi));
     for (int w = 0; w < W; w++)
     {
-        double s = warp_sum(acc[w]);
-        if (lane == 0) grid[warp * W + w] = s;
+        double sum = warp_sum(acc[w]);
+        if (lane == 0) partial[chunk * W + w] = sum;
     }
+}
+
+template <int W>
+__global__ void chunk_finish_kernel(const int *chunkStart, int64_t NV, const double *partial, double scale, double *grid)
+{
+    int64_t vi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (vi >= NV) return;
+    double acc[W];
+    for (int w = 0; w < W; w++) acc[w] = 0;
+    for (int c = chunkStart[vi]; c < chunkStart[vi + 1]; c++)
+        for (int w = 0; w < W; w++) acc[w] += partial[(int64_t)c * W + w];
+    for (int w = 0; w < W; w++) grid[vi * W + w] = acc[w] * scale;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -437,90 +587,6 @@ __global__ void estimator_kernel(DensityGrids<D> G, const double *pos, int64_t n
     for (int d = 0; d < D; d++) { sum += ev[d]; if (d < 2) low += ev[d]; }
     noise[i] = (low * D) / (sum * 2);
     sdepth[i] = dd - 1.;  // depth(p) of the estimator: leaf of a sample is at the finest depth
-}
-
-// ---------------------------------------------------------------------------------------------
-// frame splat gather (ExteriorPoisson.h:181-228 -> GridSamples.inl:393-456)
-// ---------------------------------------------------------------------------------------------
-template <int D>
-__global__ void skew_gather_kernel(SplatArgs a, const double *pos, const double *skew, const int *order, const double *measure,
-                                   const double *sdepth, double *grid)
-{
-    constexpr int K = D * (D - 1) / 2;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    int res = 1 << (a.t - 1), nv = res + 1;
-    int64_t NV = 1;
-    for (int d = 0; d < D; d++) NV *= nv;
-    if (warp >= NV) return;
-    int v[D];
-    {
-        int64_t t = warp;
-        for (int d = D - 1; d >= 0; d--) { v[d] = (int)(t % nv); t /= nv; }
-    }
-    const int deg = 2 * a.KR + 1;
-    const double sampleScale = (double)(1ull << (a.depth * 2));
-    int clo[D], chi[D], C[D];
-    for (int d = 0; d < D; d++)
-    {
-        clo[d] = max(0, v[d] - a.KR - 1);
-        chi[d] = min(res - 1, v[d] + a.KR);
-        C[d] = clo[d];
-    }
-    double acc[K];
-    for (int k = 0; k < K; k++) acc[k] = 0;
-    const int maxT = a.depth + 1;
-    while (true)
-    {
-        int64_t lo, hi;
-        cell_range<D>(a, C, lo, hi);
-        if (lo < hi)
-        {
-            int j0 = a.cellStart[lo], j1 = a.cellStart[hi];
-            for (int j = j0 + lane; j < j1; j += 32)
-            {
-                int s = order[j];
-                // level weight of this sample at tree depth t
-                double dd = sdepth[s] + 1.;
-                double lw = 0;
-                if (dd >= maxT) lw = (a.t == maxT) ? (double)(1ull << (a.depth * D)) : 0.;
-                else if (dd <= 1) lw = (a.t == 1) ? 1. : 0.;
-                else
-                {
-                    int d1 = (int)floor(dd), d2 = d1 + 1;
-                    double f = dd - d1;
-                    if (a.t == d1) lw = (1. - f) * (double)(1ull << ((d1 - 1) * D));
-                    else if (a.t == d2) lw = f * (double)(1ull << ((d2 - 1) * D));
-                }
-                if (lw == 0) continue;
-                const double *q = pos + (int64_t)s * D;
-                double wt = lw;
-                for (int d = 0; d < D; d++)
-                {
-                    double bs[kMaxDeg + 1];
-                    double pr = q[d] * res;
-                    int e = (int)floor(pr);
-                    bspline_eval(deg, pr - e, bs);
-                    wt *= bs[v[d] - (C[d] - a.KR)];
-                }
-                const double *sk = skew + (int64_t)s * K;
-                double nrm = 0;
-                for (int k = 0; k < K; k++) nrm += 2 * sk[k] * sk[k];
-                nrm = sqrt(nrm);
-                double m = measure[s];
-                for (int k = 0; k < K; k++) acc[k] += wt * (sk[k] / nrm * m * sampleScale);
-            }
-        }
-        int d = D - 1;
-        for (; d >= 0; d--) { if (++C[d] <= chi[d]) break; C[d] = clo[d]; }
-        if (d < 0) break;
-    }
-    const double finalScale = pow(pow(0.5, a.depth), 1.5 * 2);
-    for (int k = 0; k < K; k++)
-    {
-        double s = warp_sum(acc[k]);
-        if (lane == 0) grid[warp * K + k] = s * finalScale;
-    }
 }
 
 // S(E) at element centres, summed over tree depths down to the leaf containing the centre
@@ -739,39 +805,45 @@ __global__ void dirichlet_kernel(int level, double w, double *dst)
     int I[D];
     g.node(i, I);
     const double h = 1. / g.r;
+    // The elements shared by nodes I and J form a tensor product of per-axis sets, so
+    // int grad phi_I . grad phi_J = sum_k prod_d (k == d ? s_d : m_d) with the per-axis sums of the
+    // 1-D stiffness (s_d) and mass (m_d) entries over the shared 1-D elements.
+    double sd[D][3], md[D][3];
+    for (int d = 0; d < D; d++)
+        for (int o = -1; o <= 1; o++)
+        {
+            int J = I[d] + o;
+            double sv = 0, mv = 0;
+            if (J >= 0 && J <= g.r)
+            {
+                int lo = max(max(I[d], J) - 1, 0), hi = min(min(I[d], J), g.r - 1);
+                for (int e = lo; e <= hi; e++)
+                {
+                    int a = I[d] - e, b = J - e;
+                    sv += stiff1(a, b) / h;
+                    mv += mass1(a, b) * h;
+                }
+            }
+            sd[d][o + 1] = sv;
+            md[d][o + 1] = mv;
+        }
     for (int o = 0; o < S; o++)
     {
-        int off[D], J[D];
+        int off[D];
         stencil_offset<D>(o, off);
         bool ok = true;
-        int lo[D], hi[D];
         for (int d = 0; d < D; d++)
         {
-            J[d] = I[d] + off[d];
-            if (J[d] < 0 || J[d] > g.r) ok = false;
-            lo[d] = max(max(I[d], J[d]) - 1, 0);
-            hi[d] = min(min(I[d], J[d]), g.r - 1);
-            if (lo[d] > hi[d]) ok = false;
+            int J = I[d] + off[d];
+            if (J < 0 || J > g.r) ok = false;
         }
         if (!ok) continue;
         double sum = 0;
-        int E[D];
-        for (int d = 0; d < D; d++) E[d] = lo[d];
-        while (true)
+        for (int k = 0; k < D; k++)
         {
-            for (int k = 0; k < D; k++)
-            {
-                double v = 1.;
-                for (int d = 0; d < D; d++)
-                {
-                    int a = I[d] - E[d], b = J[d] - E[d];
-                    v *= (d == k) ? stiff1(a, b) / h : mass1(a, b) * h;
-                }
-                sum += v;
-            }
-            int d = D - 1;
-            for (; d >= 0; d--) { if (++E[d] <= hi[d]) break; E[d] = lo[d]; }
-            if (d < 0) break;
+            double v = 1.;
+            for (int d = 0; d < D; d++) v *= (d == k) ? sd[d][off[d] + 1] : md[d][off[d] + 1];
+            sum += v;
         }
         dst[(int64_t)o * g.N + i] += w * sum;
     }
@@ -847,6 +919,72 @@ bool device_sum(Context &c, const double *v, int64_t n, int comps, double *out)
     sum_finish_kernel<<<1, 32, 0, c.stream>>>(partial, nb, out);
     c.release(partial);
     return c.launch_ok("sum");
+}
+
+// Chunked gather of one tree level into grid (NV x W); returns false on a CUDA error.
+template <int D, bool Samples, class Item>
+bool chunked_level(Context &c, const SplatArgs &a, const Item &item, double scale, double *grid)
+{
+    constexpr int W = Item::W;
+    cudaStream_t s = c.stream;
+    int nv = (1 << (a.t - 1)) + 1;
+    int64_t NV = 1;
+    for (int d = 0; d < D; d++) NV *= nv;
+    int *nch = nullptr, *start = nullptr;
+    if (!dalloc(c, &nch, NV + 1, "chunks") || !dalloc(c, &start, NV + 1, "chunks")) return false;
+    cudaMemsetAsync(nch + NV, 0, sizeof(int), s);
+    vertex_chunks_kernel<D, Samples><<<nblocks(NV, 128), 128, 0, s>>>(a, nch);
+    {
+        size_t tmpBytes = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tmpBytes, nch, start, (int)(NV + 1), s);
+        void *tmp = nullptr;
+        if (!c.alloc(&tmp, tmpBytes, "scan tmp")) return false;
+        cub::DeviceScan::ExclusiveSum(tmp, tmpBytes, nch, start, (int)(NV + 1), s);
+        c.release(tmp);
+    }
+    int total = 0;
+    if (!c.cuda_ok(cudaMemcpyAsync(&total, start + NV, sizeof(int), cudaMemcpyDeviceToHost, s), "copy") ||
+        !c.cuda_ok(cudaStreamSynchronize(s), "sync"))
+        return false;
+    double *partial = nullptr;
+    if (total > 0)
+    {
+        if (!dalloc(c, &partial, (size_t)total * W, "partials")) return false;
+        chunk_gather_kernel<D, Samples, Item><<<nblocks((int64_t)total * 32, 256), 256, 0, s>>>(a, item, start, NV, total, partial);
+    }
+    chunk_finish_kernel<W><<<nblocks(NV, 128), 128, 0, s>>>(start, NV, partial, scale, grid);
+    c.release(partial);
+    c.release(nch);
+    c.release(start);
+    return c.launch_ok("chunked gather");
+}
+
+// levels with at most this many vertices use the chunked gather (all levels: the item counts of
+// the vertices near the samples vary too much for one thread or warp per vertex)
+constexpr int64_t kChunkedMaxVertices = (int64_t)1 << 40;
+
+// Fine levels: one thread per vertex (most windows hold no or few items), fixed window order.
+template <int D, bool Samples, class Item>
+__global__ void vertex_gather_kernel(SplatArgs a, Item item, double scale, double *grid)
+{
+    constexpr int W = Item::W;
+    int res = 1 << (a.t - 1), nv = res + 1;
+    int64_t NV = 1;
+    for (int d = 0; d < D; d++) NV *= nv;
+    int64_t vi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (vi >= NV) return;
+    int v[D], clo[D], chi[D], C[D];
+    vertex_of<D>(vi, nv, v);
+    for (int d = 0; d < D; d++) { clo[d] = max(0, v[d] - a.KR - 1); chi[d] = min(res - 1, v[d] + a.KR); C[d] = clo[d]; }
+    double acc[W];
+    for (int w = 0; w < W; w++) acc[w] = 0;
+    do
+    {
+        int lo, hi;
+        item_range<D, Samples>(a, C, lo, hi);
+        for (int it = lo; it < hi; it++) item(a, it, v, C, acc);
+    } while (window_next<D>(C, clo, chi));
+    for (int w = 0; w < W; w++) grid[vi * W + w] = acc[w] * scale;
 }
 
 template <int D>
@@ -927,6 +1065,18 @@ bool build_impl(Context &c, Setup &st)
     if (!buildRefined(st.refinedD, c.P.d_radius)) return false;
     if (!buildRefined(st.refinedS, c.P.t_radius)) return false;
 
+    // ---- occupied-cell ranges of every depth-t cell (shared by both trees) ----
+    std::vector<int *> rlo(depth + 2, nullptr), rhi(depth + 2, nullptr);
+    for (int t = 1; t <= depth + 1; t++)
+    {
+        int64_t cells = (int64_t)1 << (D * (t - 1));
+        if (!dalloc(c, &rlo[t], cells, "ranges") || !dalloc(c, &rhi[t], cells, "ranges")) return false;
+        cudaMemsetAsync(rlo[t], 0, sizeof(int) * cells, s);
+        cudaMemsetAsync(rhi[t], 0, sizeof(int) * cells, s);
+        level_ranges_kernel<D><<<nblocks(nc, 256), 256, 0, s>>>(st.cellKey, nc, t, D * (depth + 1 - t), rlo[t], rhi[t]);
+    }
+    if (!c.launch_ok("level ranges")) return false;
+
     // ---- density splat of the merged cells ----
     double *mean = nullptr, *datum = nullptr;
     if (!dalloc(c, &mean, nc * D, "mean") || !dalloc(c, &datum, nc * W, "datum")) return false;
@@ -955,9 +1105,18 @@ bool build_impl(Context &c, Setup &st)
         {
             Grid<D> gl(t - 1);
             if (!dalloc(c, &st.density[t - 1], gl.N * W, "density")) return false;
-            SplatArgs a{st.cellKey, st.cellStart, nc, depth, t, KR};
+            SplatArgs a{st.cellKey, st.cellStart, nc, depth, t, KR, rlo[t], rhi[t]};
             double dw = scale / std::pow(std::pow(0.5, t - 1), D - 2);
-            density_gather_kernel<D><<<nblocks(gl.N * 32, 256), 256, 0, s>>>(a, mean, datum, dw, st.density[t - 1]);
+            if (gl.N <= kChunkedMaxVertices)
+            {
+                DensityItem<D> item{mean, datum, dw};
+                if (!chunked_level<D, false>(c, a, item, 1.0, st.density[t - 1])) return false;
+            }
+            else
+            {
+                DensityItem<D> item{mean, datum, dw};
+                vertex_gather_kernel<D, false><<<nblocks(gl.N, 128), 128, 0, s>>>(a, item, 1.0, st.density[t - 1]);
+            }
         }
     }
     c.release(mean); c.release(datum);
@@ -979,10 +1138,22 @@ bool build_impl(Context &c, Setup &st)
     {
         Grid<D> gl(t - 1);
         if (!dalloc(c, &st.skewGrid[t - 1], gl.N * K, "skew grid")) return false;
-        SplatArgs a{st.cellKey, st.cellStart, nc, depth, t, c.P.t_radius};
-        skew_gather_kernel<D><<<nblocks(gl.N * 32, 256), 256, 0, s>>>(a, st.pos, st.skew, st.order, st.measure, st.sdepth, st.skewGrid[t - 1]);
+        SplatArgs a{st.cellKey, st.cellStart, nc, depth, t, c.P.t_radius, rlo[t], rhi[t]};
+        if (gl.N <= kChunkedMaxVertices)
+        {
+            SkewItem<D> item{st.pos, st.skew, st.measure, st.sdepth, st.order};
+            if (!chunked_level<D, true>(c, a, item, std::pow(std::pow(0.5, depth), 1.5 * 2), st.skewGrid[t - 1])) return false;
+        }
+        else
+        {
+            SkewItem<D> item{st.pos, st.skew, st.measure, st.sdepth, st.order};
+            vertex_gather_kernel<D, true><<<nblocks(gl.N, 128), 128, 0, s>>>(a, item, std::pow(std::pow(0.5, depth), 1.5 * 2),
+                                                                           st.skewGrid[t - 1]);
+        }
     }
     if (!c.launch_ok("frame splat")) return false;
+
+    for (int t = 1; t <= depth + 1; t++) { c.release(rlo[t]); c.release(rhi[t]); }
 
     // ---- S(E), leaf depths, c ----
     if (!dalloc(c, &st.S, gfine.NE * K, "S") || !dalloc(c, &st.leaf, gfine.NE, "leaf")) return false;

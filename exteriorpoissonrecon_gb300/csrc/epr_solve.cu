@@ -62,18 +62,91 @@ __device__ __forceinline__ bool gather_element(const Grid<D> &g, const NodeCtx<D
     return true;
 }
 
+// stencil index of the neighbour at offset (o_0, ..., o_{D-1}), o_d in {-1, 0, 1}
+template <int D>
+__host__ __device__ constexpr int nb_index(const int *off)
+{
+    int o = 0;
+    for (int d = 0; d < D; d++) o = o * 3 + (off[d] + 1);
+    return o;
+}
+
+// Wedge part of the quadratic model of node i, elements in canonical orientation.
+template <int D, typename Real>
+__device__ __forceinline__ void node_wedge_fit(const Grid<D> &g, const NodeCtx<D> &nc, int64_t i, const Real *xy, Real *h)
+{
+    if constexpr (D == 3)
+    {
+        // the 27-node neighbourhood in registers; out-of-domain neighbours are never used
+        Real2<Real> nb[27];
+#pragma unroll
+        for (int o = 0; o < 27; o++)
+        {
+            const int o0 = o / 9 - 1, o1 = (o / 3) % 3 - 1, o2 = o % 3 - 1;
+            bool ok = (nc.I[0] + o0 >= 0) && (nc.I[0] + o0 <= g.r) && (nc.I[1] + o1 >= 0) && (nc.I[1] + o1 <= g.r) &&
+                      (nc.I[2] + o2 >= 0) && (nc.I[2] + o2 <= g.r);
+            int64_t j = i + o0 * nc.stride[0] + o1 * nc.stride[1] + o2 * nc.stride[2];
+            nb[o] = ok ? ld2(xy, j) : Real2<Real>{0, 0};
+        }
+#pragma unroll
+        for (int A = 0; A < 8; A++)
+        {
+            const int a0 = (A >> 2) & 1, a1 = (A >> 1) & 1, a2 = A & 1;
+            bool ok = (nc.I[0] - a0 >= 0) && (nc.I[0] - a0 < g.r) && (nc.I[1] - a1 >= 0) && (nc.I[1] - a1 < g.r) &&
+                      (nc.I[2] - a2 >= 0) && (nc.I[2] - a2 < g.r);
+            if (!ok) continue;
+            Corners<3, Real> c;
+#pragma unroll
+            for (int cc = 0; cc < 8; cc++)
+            {
+                int off[3] = {(a0 ? -1 : 1) * ((cc >> 2) & 1), (a1 ? -1 : 1) * ((cc >> 1) & 1), (a2 ? -1 : 1) * (cc & 1)};
+                Real2<Real> v = nb[nb_index<3>(off)];
+                c.x[cc] = v.x;
+                c.y[cc] = v.y;
+            }
+            Fit5<Real> f = element_fit_canonical<3, Real>(c);
+#pragma unroll
+            for (int k = 0; k < 5; k++) h[k] += f.h[k];
+        }
+    }
+    else
+    {
+#pragma unroll 1
+        for (int A = 0; A < (1 << D); A++)
+        {
+            bool ok = true;
+#pragma unroll
+            for (int d = 0; d < D; d++)
+            {
+                int e = nc.I[d] - cbit<D>(A, d);
+                ok = ok && e >= 0 && e < g.r;
+            }
+            if (!ok) continue;
+            Corners<D, Real> c;
+#pragma unroll
+            for (int cc = 0; cc < (1 << D); cc++)
+            {
+                int64_t j = i;
+#pragma unroll
+                for (int d = 0; d < D; d++) j += (int64_t)(cbit<D>(A, d) ? -cbit<D>(cc, d) : cbit<D>(cc, d)) * nc.stride[d];
+                Real2<Real> v = ld2(xy, j);
+                c.x[cc] = v.x;
+                c.y[cc] = v.y;
+            }
+            Fit5<Real> f = element_fit_canonical<D, Real>(c);
+#pragma unroll
+            for (int k = 0; k < 5; k++) h[k] += f.h[k];
+        }
+    }
+}
+
 // Quadratic model of E(x + s e_i, y + t e_i): q = (Q20, Q02, Q11, Q10, Q01)
 template <int D, typename Real>
 __device__ __forceinline__ void node_fit(const LevelPtrs<Real> &L, const Grid<D> &g, const NodeCtx<D> &nc, int64_t i,
                                          const Real *xy, Real *q)
 {
     Real h[5] = {0, 0, 0, 0, 0};
-#pragma unroll 1
-    for (int A = 0; A < (1 << D); A++)
-    {
-        Real x[1 << D], y[1 << D];
-        if (gather_element<D, Real>(g, nc, i, A, xy, x, y)) element_fit<D, Real>(x, y, A, h);
-    }
+    node_wedge_fit<D, Real>(g, nc, i, xy, h);
     const Real sc = (Real)wedge_scale<D>(g.r);
     q[0] = h[0] * sc;
     q[1] = h[1] * sc;
@@ -241,9 +314,33 @@ __global__ void __launch_bounds__(kThreads) quadfit_kernel(LevelPtrs<Real> L, co
     for (int k = 0; k < 5; k++) out[i * 5 + k] = (double)q[k];
 }
 
+// Node step from the quadratic model q = (Q20, Q02, Q11, Q10, Q01) with H = [[2 Q20, Q11], [Q11, 2 Q02]]
+// and grad = (Q10, Q01).  Paired (ExteriorPoissonSolvers.h:173-181): -H^{-1} grad / 2 when
+// |det H| > 1e-20.  Separate (ExteriorPoissonSolvers.h:216-235): p0 = -grad0 / (2 H00) when
+// H00 > 1e-20, then p1 = -((H10 + H01) p0 + grad1) / (2 H11) when H11 > 1e-20.
+template <typename Real>
+__device__ __forceinline__ bool node_step(const Real *q, int separate, Real &p0, Real &p1)
+{
+    Real h00 = (Real)2 * q[0], h11 = (Real)2 * q[1], h01 = q[2];
+    if (separate)
+    {
+        p0 = 0;
+        p1 = 0;
+        if ((double)h00 > 1e-20) p0 = -((h01 + h01) * p1 + q[3]) / ((Real)2 * h00);
+        if ((double)h11 > 1e-20) p1 = -((h01 + h01) * p0 + q[4]) / ((Real)2 * h11);
+        return true;
+    }
+    Real det = h00 * h11 - h01 * h01;
+    if (!(fabs((double)det) > 1e-20)) return false;
+    p0 = -(h11 * q[3] - h01 * q[4]) / det / (Real)2;
+    p1 = -(-h01 * q[3] + h00 * q[4]) / det / (Real)2;
+    return true;
+}
+
 // Paired Gauss-Seidel update of node j of a parity colour.
 template <int D, typename Real>
-__device__ __forceinline__ void gs_update(const LevelPtrs<Real> &L, const Grid<D> &g, const Colour<D> &col, int64_t j, unsigned int *err)
+__device__ __forceinline__ void gs_update(const LevelPtrs<Real> &L, const Grid<D> &g, const Colour<D> &col, int64_t j, unsigned int *err,
+                                          int separate)
 {
     NodeCtx<D> nc;
     col.node(j, nc.I);
@@ -252,13 +349,9 @@ __device__ __forceinline__ void gs_update(const LevelPtrs<Real> &L, const Grid<D
     int64_t i = g.node(nc.I);
     Real q[5];
     node_fit<D, Real>(L, g, nc, i, L.xy, q);
-    // H = [[2 Q20, Q11], [Q11, 2 Q02]], grad = (Q10, Q01); step = -H^{-1} grad / 2
-    Real h00 = (Real)2 * q[0], h11 = (Real)2 * q[1], h01 = q[2];
-    Real det = h00 * h11 - h01 * h01;
-    if (fabs((double)det) > 1e-20)
+    Real p0, p1;
+    if (node_step<Real>(q, separate, p0, p1))
     {
-        Real p0 = -(h11 * q[3] - h01 * q[4]) / det / (Real)2;
-        Real p1 = -(-h01 * q[3] + h00 * q[4]) / det / (Real)2;
         Real2<Real> v = ld2(L.xy, i);
         v.x += p0;
         v.y += p1;
@@ -270,12 +363,145 @@ __device__ __forceinline__ void gs_update(const LevelPtrs<Real> &L, const Grid<D
 // One parity colour: same-colour nodes share no element, so all of them are updated in parallel
 // exactly as the reference's per-colour ParallelFor does.
 template <int D, typename Real>
-__global__ void __launch_bounds__(kThreads) gs_colour_kernel(LevelPtrs<Real> L, Colour<D> col, unsigned int *err)
+__global__ void __launch_bounds__(kThreads) gs_colour_kernel(LevelPtrs<Real> L, Colour<D> col, unsigned int *err, int separate)
 {
     Grid<D> g(L.level);
     int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= col.n) return;
-    gs_update<D, Real>(L, g, col, j, err);
+    gs_update<D, Real>(L, g, col, j, err, separate);
+}
+
+// Lane-parallel variant: a group of 2^D consecutive lanes updates one node, lane A integrating the
+// node's element A (canonical orientation) and a share of its stencil column; the group reduces
+// with shuffles in a fixed order and its first lane writes the update.
+template <int D>
+__device__ __forceinline__ float group_sum(float v)
+{
+#pragma unroll
+    for (int o = (1 << D) / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, 1 << D);
+    return v;
+}
+template <int D>
+__device__ __forceinline__ double group_sum(double v)
+{
+#pragma unroll
+    for (int o = (1 << D) / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, 1 << D);
+    return v;
+}
+
+template <int D, typename Real>
+__device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Real *xy, const Grid<D> &g, const int *I, bool active,
+                                                   int A, unsigned int *err, int separate = 0)
+{
+    constexpr int C = 1 << D, S = Dims<D>::S;
+    NodeCtx<D> nc;
+    int64_t i = 0;
+    Real h[5] = {0, 0, 0, 0, 0};
+    Real ax = 0, ay = 0, bx = 0, by = 0, acen = 0;
+    if (active)
+    {
+#pragma unroll
+        for (int d = 0; d < D; d++) { nc.I[d] = I[d]; nc.stride[d] = g.stride(d); }
+        i = g.node(nc.I);
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < D; d++)
+        {
+            int e = nc.I[d] - cbit<D>(A, d);
+            ok = ok && e >= 0 && e < g.r;
+        }
+        if (ok)
+        {
+            Real x[C], y[C];
+#pragma unroll
+            for (int cc = 0; cc < C; cc++)
+            {
+                int64_t jj = i;
+#pragma unroll
+                for (int d = 0; d < D; d++) jj += (int64_t)(cbit<D>(A, d) ? -cbit<D>(cc, d) : cbit<D>(cc, d)) * nc.stride[d];
+                Real2<Real> v = ld2(xy, jj);
+                x[cc] = v.x;
+                y[cc] = v.y;
+            }
+            element_fit<D, Real>(x, y, 0, h);
+        }
+        for (int o = A; o < S; o += C)
+        {
+            int off[D];
+            stencil_offset<D>(o, off);
+            bool in = true;
+            int64_t jj = i;
+#pragma unroll
+            for (int d = 0; d < D; d++)
+            {
+                int t = nc.I[d] + off[d];
+                in = in && (t >= 0) && (t <= g.r);
+                jj += (int64_t)off[d] * nc.stride[d];
+            }
+            if (!in) continue;
+            Real a = L.A[(int64_t)o * L.N + i];
+            Real b = L.B[(int64_t)o * L.N + i];
+            Real2<Real> v = ld2(xy, jj);
+            ax += a * v.x;
+            ay += a * v.y;
+            if (o == Dims<D>::CENTER) acen = a;
+            else { bx += b * v.x; by += b * v.y; }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++) h[k] = group_sum<D>(h[k]);
+    ax = group_sum<D>(ax); ay = group_sum<D>(ay); bx = group_sum<D>(bx); by = group_sum<D>(by); acen = group_sum<D>(acen);
+    if (!active || A != 0) return;
+    const Real sc = (Real)wedge_scale<D>(g.r);
+    Real q[5];
+    q[0] = h[0] * sc + acen;
+    q[1] = h[1] * sc + acen;
+    q[2] = (Real)2 * h[2] * sc;
+    q[3] = (Real)2 * h[3] * sc + (Real)2 * ax - (Real)2 * by;
+    q[4] = (Real)2 * h[4] * sc + (Real)2 * ay + (Real)2 * bx;
+    Real p0, p1;
+    if (node_step<Real>(q, separate, p0, p1))
+    {
+        Real2<Real> v = ld2(xy, i);
+        v.x += p0;
+        v.y += p1;
+        if (!isfinite((double)v.x) || !isfinite((double)v.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
+        reinterpret_cast<Real2<Real> *>(xy)[i] = v;
+    }
+}
+
+template <int D, typename Real>
+__device__ __forceinline__ void gs_update_lanes(const LevelPtrs<Real> &L, const Grid<D> &g, const Colour<D> &col, int64_t j,
+                                                bool active, int A, unsigned int *err)
+{
+    int I[D];
+    if (active) col.node(j, I);
+    else
+        for (int d = 0; d < D; d++) I[d] = 0;
+    gs_update_lanes_at<D, Real>(L, L.xy, g, I, active, A, err);
+}
+
+// Launch geometry without 64-bit index division: block = (128 >> D) nodes along the last axis
+// times 2^D lanes; grid.y = the colour's count on axis D-2; grid.z = the counts on the remaining
+// leading axes.
+template <int D, typename Real>
+__global__ void __launch_bounds__(kThreads) gs_colour_lanes_kernel(LevelPtrs<Real> L, Colour<D> col, unsigned int *err, int separate)
+{
+    Grid<D> g(L.level);
+    constexpr int NPB = kThreads >> D;
+    const int A = threadIdx.x & ((1 << D) - 1);
+    const int tl = blockIdx.x * NPB + (threadIdx.x >> D);
+    int I[D];
+    I[D - 1] = 2 * tl + col.par[D - 1];
+    I[D - 2] = 2 * (int)blockIdx.y + col.par[D - 2];
+    if constexpr (D == 3) I[0] = 2 * (int)blockIdx.z + col.par[0];
+    else
+    {
+        int z = (int)blockIdx.z;
+        I[1] = 2 * (z % col.cnt[1]) + col.par[1];
+        I[0] = 2 * (z / col.cnt[1]) + col.par[0];
+    }
+    gs_update_lanes_at<D, Real>(L, L.xy, g, I, tl < col.cnt[D - 1], A, err, separate);
 }
 
 // All sweeps of a small level in one thread block: the colours follow each other behind a block
@@ -284,16 +510,33 @@ __global__ void __launch_bounds__(kThreads) gs_colour_kernel(LevelPtrs<Real> L, 
 // latency.
 constexpr int kPersistentThreads = 256;
 template <int D, typename Real>
-__global__ void __launch_bounds__(kPersistentThreads) gs_level_kernel(LevelPtrs<Real> L, int iters, unsigned int *err)
+__global__ void __launch_bounds__(kPersistentThreads) gs_level_kernel(LevelPtrs<Real> L, int iters, unsigned int *err, int separate)
 {
     Grid<D> g(L.level);
+    // the level's coefficients live in shared memory for the whole schedule
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Real *xy = reinterpret_cast<Real *>(smem_raw);
+    for (int64_t k = threadIdx.x; k < 2 * g.N; k += blockDim.x) xy[k] = L.xy[k];
+    __syncthreads();
     for (int it = 0; it < iters; it++)
         for (int c = 0; c < (1 << D); c++)
         {
             Colour<D> col(g, c);
-            for (int64_t j = threadIdx.x; j < col.n; j += blockDim.x) gs_update<D, Real>(L, g, col, j, err);
+            const int per = blockDim.x >> D;  // nodes per pass of the block
+            const int A = threadIdx.x & ((1 << D) - 1);
+            for (int64_t j0 = 0; j0 < col.n; j0 += per)
+            {
+                int64_t j = j0 + (threadIdx.x >> D);
+                bool active = j < col.n;
+                int I[D];
+                if (active) col.node(j, I);
+                else
+                    for (int d = 0; d < D; d++) I[d] = 0;
+                gs_update_lanes_at<D, Real>(L, xy, g, I, active, A, err, separate);
+            }
             __syncthreads();
         }
+    for (int64_t k = threadIdx.x; k < 2 * g.N; k += blockDim.x) L.xy[k] = xy[k];
 }
 
 template <int D, typename Real>
@@ -427,6 +670,8 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n)
 
 inline unsigned int blocks_for(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
 
+int g_gs_variant = 1;  // 0: one thread per node, 1: 2^D lanes per node
+
 }  // namespace
 
 // ---------------------------------------------------------------------------------------------
@@ -453,27 +698,36 @@ void launch_quadfit(const LevelPtrs<Real> &L, const Real *xy, double *out, cudaS
 }
 
 template <int D, typename Real>
-void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, cudaStream_t s)
+void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, cudaStream_t s, int separate)
 {
     Grid<D> g(L.level);
     Colour<D> col(g, colour);
     if (col.n == 0) return;
-    gs_colour_kernel<D, Real><<<blocks_for(col.n), kThreads, 0, s>>>(L, col, err);
+    if (g_gs_variant == 0) gs_colour_kernel<D, Real><<<blocks_for(col.n), kThreads, 0, s>>>(L, col, err, separate);
+    else
+    {
+        constexpr int NPB = kThreads >> D;
+        dim3 grid((unsigned)((col.cnt[D - 1] + NPB - 1) / NPB), (unsigned)col.cnt[D - 2],
+                  (unsigned)(D == 3 ? col.cnt[0] : col.cnt[0] * col.cnt[1]));
+        gs_colour_lanes_kernel<D, Real><<<grid, kThreads, 0, s>>>(L, col, err, separate);
+    }
 }
 
+void set_gs_variant(int v) { g_gs_variant = v; }
+
 template <int D, typename Real>
-int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s)
+int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s, int separate)
 {
     Grid<D> g(L.level);
     if (iters <= 0) return 0;
     if (g.N <= kPersistentMaxNodes)
     {
-        gs_level_kernel<D, Real><<<1, kPersistentThreads, 0, s>>>(L, iters, err);
+        gs_level_kernel<D, Real><<<1, kPersistentThreads, (size_t)(2 * g.N * sizeof(Real)), s>>>(L, iters, err, separate);
         return 1;
     }
     int n = 0;
     for (int it = 0; it < iters; it++)
-        for (int c = 0; c < (1 << D); c++) { launch_gs_colour<D, Real>(L, c, err, s); n++; }
+        for (int c = 0; c < (1 << D); c++) { launch_gs_colour<D, Real>(L, c, err, s, separate); n++; }
     return n;
 }
 
@@ -520,8 +774,8 @@ void launch_convert_f2d(const float *in, double *out, int64_t n, cudaStream_t st
 #define EPR_INSTANTIATE(D, R)                                                                          \
     template void launch_energy<D, R>(const LevelPtrs<R> &, const R *, const Reduce &, cudaStream_t);   \
     template void launch_quadfit<D, R>(const LevelPtrs<R> &, const R *, double *, cudaStream_t);        \
-    template void launch_gs_colour<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t);      \
-    template int launch_gs_sweeps<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t);       \
+    template void launch_gs_colour<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t, int); \
+    template int launch_gs_sweeps<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t, int);  \
     template void launch_gn_matvec<D, R>(const LevelPtrs<R> &, const R *, const R *, R *, cudaStream_t); \
     template void launch_prolong<D, R>(int, const R *, R *, int, cudaStream_t);                         \
     template void launch_restrict<D, R>(int, const R *, R *, cudaStream_t);

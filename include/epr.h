@@ -75,6 +75,8 @@ typedef struct epr_params {
     int verbose;          /* print the reference's per-level "Error[...]" lines */
     int device;           /* CUDA device ordinal the context runs on (0) */
     int fp64_levels;      /* EPR_FP32 only: levels below this one still run in double (0) */
+    int single_level;     /* --singleLevel: prolong the initial guess and relax only the finest solve level */
+    int separate;         /* --separate: update x then y per node instead of the paired 2x2 step */
 } epr_params;
 
 typedef struct epr_stats {

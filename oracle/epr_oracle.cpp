@@ -1009,6 +1009,16 @@ struct Oracle
                     quadfitNode(level, g, i, x, y, q);
                     if (tx) { q[3] -= tx[i]; q[4] -= ty[i]; }
                     double h00 = 2 * q[0], h11 = 2 * q[1], h01 = q[2];
+                    if (P.separate)
+                    {
+                        // SeparateGaussSeidelSolve (ExteriorPoissonSolvers.h:216-235)
+                        double p0 = 0, p1 = 0;
+                        if (h00 > 1e-20) p0 = -((h01 + h01) * p1 + q[3]) / (2 * h00);
+                        if (h11 > 1e-20) p1 = -((h01 + h01) * p0 + q[4]) / (2 * h11);
+                        x[i] += p0;
+                        y[i] += p1;
+                        continue;
+                    }
                     double det = h00 * h11 - h01 * h01;
                     if (std::fabs(det) > 1e-20)
                     {
@@ -1172,7 +1182,22 @@ struct Oracle
             double s = std::sqrt(std::sqrt(c / e[2]));
             for (size_t i = 0; i < X[minD].size(); i++) { X[minD][i] *= s; Y[minD][i] *= s; }
         }
-        for (int l = minD; l <= maxD; l++)
+        if (P.single_level)
+        {
+            // ExteriorPoisson.h:342-360
+            for (int l = minD; l < maxD; l++)
+            {
+                prolong(l, X[l].data(), X[l + 1].data());
+                prolong(l, Y[l].data(), Y[l + 1].data());
+            }
+            for (int l = minD; l < maxD; l++)
+            {
+                std::fill(X[l].begin(), X[l].end(), 0.);
+                std::fill(Y[l].begin(), Y[l].end(), 0.);
+            }
+            gs(maxD, X[maxD].data(), Y[maxD].data(), P.gs_iters);
+        }
+        for (int l = minD; !P.single_level && l <= maxD; l++)
         {
             int iters = (int)std::ceil(std::pow(P.i_mult, depth - l) * P.gs_iters);
             gs(l, X[l].data(), Y[l].data(), iters);
@@ -1268,6 +1293,8 @@ void epr_oracle_default_params(epr_oracle_params *p)
     p->max_solve_depth = -1;
     p->seed = 0;
     p->threads = 0;
+    p->single_level = 0;
+    p->separate = 0;
 }
 
 int epr_oracle_unit_cube(int dim, size_t n, double scale, double *pos, double *xform)

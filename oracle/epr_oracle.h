@@ -32,6 +32,8 @@ typedef struct epr_oracle_params {
     int max_solve_depth;  /* --maxSolveDepth (-1 = depth) */
     unsigned int seed;    /* --seed */
     int threads;          /* OpenMP threads (0 = all) */
+    int single_level;     /* --singleLevel */
+    int separate;         /* --separate */
 } epr_oracle_params;
 
 void epr_oracle_default_params(epr_oracle_params *p);

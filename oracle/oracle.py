@@ -29,6 +29,8 @@ class Params(ctypes.Structure):
         ("max_solve_depth", ctypes.c_int),
         ("seed", ctypes.c_uint),
         ("threads", ctypes.c_int),
+        ("single_level", ctypes.c_int),
+        ("separate", ctypes.c_int),
     ]
 
 

@@ -85,6 +85,7 @@ struct Params
     double sWeight = 100., dWeight = 0.00625, nSigma = 0.25, iMult = 2., scale = 1.1;
     unsigned int tRadius = 1, dRadius = 1, gsIters = 10, seed = 0, minSolveDepth = 0;
     int solve = 1;
+    int separate = 0, singleLevel = 0;
 };
 
 template <unsigned int Dim>
@@ -338,7 +339,11 @@ static void Run(const std::string &in, unsigned int depth, const std::string &ou
         std::streambuf *old = std::cout.rdbuf();
         std::stringstream sink;
         std::cout.rdbuf(sink.rdbuf());
-        recon.solve(false, P.iMult, P.gsIters, false, false);
+        // Levels below minSolveDepth are never written by the reference's solve (Eigen resize leaves
+        // them uninitialised, ExteriorPoisson.h:158-159, 349-351) yet enter its hierarchical output;
+        // zero them so that the dump is well defined.
+        for (unsigned int d = 0; d < P.minSolveDepth && d <= depth; d++) { recon._x[d].setZero(); recon._y[d].setZero(); }
+        recon.solve(P.singleLevel != 0, P.iMult, P.gsIters, P.separate != 0, false);
         std::cout.rdbuf(old);
         for (unsigned int d = 0; d <= depth; d++)
         {
@@ -391,6 +396,8 @@ int main(int argc, char **argv)
         else if (k == "--seed") P.seed = (unsigned int)v;
         else if (k == "--minSolveDepth") P.minSolveDepth = (unsigned int)v;
         else if (k == "--solve") P.solve = (int)v;
+        else if (k == "--separate") P.separate = (int)v;
+        else if (k == "--singleLevel") P.singleLevel = (int)v;
         else { fprintf(stderr, "unknown flag %s\n", k.c_str()); return 2; }
     }
     mkdir(out.c_str(), 0755);

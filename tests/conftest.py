@@ -19,3 +19,18 @@ GOLDEN_CASES = ["knot3_d4", "link3_d4", "cliff4_d3"]
 def load_golden(name):
     import numpy as np
     return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+
+
+VARIANT_CASES = ["knot3_d4_separate", "knot3_d4_single", "knot3_d4_seed7_min2"]
+
+
+def variant_params(flags):
+    """Harness flags of a variant fixture -> parameter keywords (the reference's flag names)."""
+    conv = {"--separate": ("separate", int), "--singleLevel": ("singleLevel", int), "--gsIters": ("gsIters", int),
+            "--seed": ("seed", int), "--minSolveDepth": ("minSolveDepth", int), "--iMult": ("iMult", float)}
+    flags = [str(f) for f in flags]
+    out = {}
+    for k, v in zip(flags[0::2], flags[1::2]):
+        name, cast = conv[k]
+        out[name] = cast(v)
+    return out

@@ -28,6 +28,7 @@ sys.path.insert(0, ROOT)
 from exteriorpoissonrecon_gb300 import samples  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+REF_CLI = os.path.join(ROOT, "oracle", "_ref", "ExteriorPoissonRecon")
 
 # name, workload, sample count, seed, depth, levels whose full stencils are stored
 CASES = [
@@ -35,6 +36,32 @@ CASES = [
     ("link3_d4", "link", 6000, 3, 4, [1, 4]),
     ("cliff4_d3", "clifford", 4000, 5, 3, [1, 2]),
 ]
+
+# solver variants of the reference's CLI: name, base case, extra harness flags
+VARIANTS = [
+    ("knot3_d4_separate", "knot", 4096, 0, 4, ["--separate", "1"]),
+    ("knot3_d4_single", "knot", 4096, 0, 4, ["--singleLevel", "1", "--gsIters", "40"]),
+    ("knot3_d4_seed7_min2", "knot", 4096, 0, 4, ["--seed", "7", "--minSolveDepth", "2", "--iMult", "1.5"]),
+]
+
+
+def make_variant(name, workload, n, seed, depth, flags):
+    """Solve results only (the system is the base case's)."""
+    pos, frames = samples.make_workload(workload, n, seed=seed)
+    with tempfile.TemporaryDirectory() as td:
+        ply = os.path.join(td, "in.ply")
+        samples.write_ply(ply, pos, frames)
+        out = os.path.join(td, "dump")
+        subprocess.run([HARNESS, ply, str(depth), out] + flags, check=True)
+        L = lambda k: np.load(os.path.join(out, k + ".npy"))  # noqa: E731
+        fx = {"depth": np.array(depth), "pos": L("pos"), "skew": L("skew"), "flags": np.array(flags),
+              "sol_energies": L("sol_energies"), "solX": L("solX"), "solY": L("solY")}
+        for l in range(depth + 1):
+            fx[f"solx_d{l}"] = L(f"solx_d{l}")
+            fx[f"soly_d{l}"] = L(f"soly_d{l}")
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **fx)
+    print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB")
 
 
 def make(name, workload, n, seed, depth, stencil_levels):
@@ -89,8 +116,29 @@ def make(name, workload, n, seed, depth, stencil_levels):
     print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+def make_tree(name, workload, n, seed, depth, flags):
+    """The reference command line's own .tree output for a PLY input (frames stored in full)."""
+    pos, frames = samples.make_workload(workload, n, seed=seed)
+    with tempfile.TemporaryDirectory() as td:
+        ply = os.path.join(td, "in.ply")
+        samples.write_ply(ply, pos, frames)
+        out = os.path.join(td, "out")
+        subprocess.run([REF_CLI, "--in", ply, "--out", out, "--depth", str(depth), "--aRadius", "-1"] + flags,
+                       check=True, capture_output=True)
+        with open(out + ".tree", "rb") as f:
+            tree = np.frombuffer(f.read(), dtype=np.uint8)
+    fx = {"depth": np.array(depth), "world_pos": pos, "frames": frames, "flags": np.array(flags, dtype=str), "tree": tree}
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **fx)
+    print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: make -C oracle ref")
     for case in CASES:
         make(*case)
+    for v in VARIANTS:
+        make_variant(*v)
+    make_tree("knot3_d4_tree", "knot", 4096, 0, 4, [])
+    make_tree("cliff4_d3_tree", "clifford", 3000, 9, 3, ["--gsIters", "5"])

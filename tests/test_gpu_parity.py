@@ -141,3 +141,20 @@ def test_against_oracle_larger(dim, depth, workload, n):
     mx, my = r.gn_matvec(depth, dx, dy)
     omx, omy = o.gn_matvec(depth, x, y, dx, dy)
     assert rel(mx, omx) < 1e-11 and rel(my, omy) < 1e-11
+
+
+@pytest.mark.parametrize("name", ["knot3_d4_separate", "knot3_d4_single", "knot3_d4_seed7_min2"])
+def test_solver_variants(name):
+    """--separate, --singleLevel and seed/minSolveDepth/iMult schedules against the reference."""
+    from conftest import variant_params
+    g = load_golden(name)
+    depth = int(g["depth"])
+    r = epr.Reconstructor(3, depth, g["pos"], g["skew"], **variant_params(g["flags"]))
+    st = r.solve()
+    ref = g["sol_energies"]
+    assert abs(st["fit_energy"] - ref[0]) < 1e-10 * ref[0]
+    assert abs(st["reg_energy"] - ref[1]) < 1e-10 * ref[1]
+    xs, ys = r.solution()
+    for l in range(depth + 1):
+        assert rel(xs[l], g[f"solx_d{l}"]) < 1e-9
+        assert rel(ys[l], g[f"soly_d{l}"]) < 1e-9

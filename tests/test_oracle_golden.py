@@ -106,3 +106,25 @@ def test_cascadic_solve(case):
     for l in range(depth + 1):
         assert rel(xs[l], g[f"solx_d{l}"]) < 1e-9
         assert rel(ys[l], g[f"soly_d{l}"]) < 1e-9
+
+
+ORACLE_NAMES = {"separate": "separate", "singleLevel": "single_level", "gsIters": "gs_iters", "seed": "seed",
+                "minSolveDepth": "min_solve_depth", "iMult": "i_mult"}
+
+
+@pytest.mark.parametrize("name", ["knot3_d4_separate", "knot3_d4_single", "knot3_d4_seed7_min2"])
+def test_solver_variants(name):
+    from conftest import variant_params
+    g = load_golden(name)
+    depth = int(g["depth"])
+    kw = {ORACLE_NAMES[k]: v for k, v in variant_params(g["flags"]).items()}
+    o = O.Oracle(3, depth, **kw)
+    o.set_samples(g["pos"], g["skew"])
+    o.build()
+    xs, ys, e = o.solve()
+    ref = g["sol_energies"]
+    assert abs(e[1] - ref[0]) < 1e-10 * ref[0]
+    assert abs(e[2] - ref[1]) < 1e-10 * ref[1]
+    for l in range(depth + 1):
+        assert rel(xs[l], g[f"solx_d{l}"]) < 1e-9
+        assert rel(ys[l], g[f"soly_d{l}"]) < 1e-9
