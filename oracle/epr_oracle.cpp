@@ -1156,6 +1156,142 @@ struct Oracle
         }
     }
 
+    // -------------------------------------------------------------------------------------------
+    // Linear multigrid on column stencils (MG.h:37-195)
+    // -------------------------------------------------------------------------------------------
+    // one coloured Gauss-Seidel sweep of M x = b (GSRelaxer::operator() with colours, MG.h:57-72):
+    // x_i += (b_i - sum_j M(j,i) x_j) / M(i,i), colours in order, nodes of a colour in parallel
+    void linearGS(int level, const double *M, const double *b, double *x) const
+    {
+        GridIdx<D> g(1 << level);
+        size_t N = g.nodes();
+        const int oc = (T::S - 1) / 2;
+        for (int col = 0; col < (1 << D); col++)
+        {
+#pragma omp parallel for schedule(static)
+            for (long i = 0; i < (long)N; i++)
+            {
+                int I[D];
+                g.node((size_t)i, I);
+                int m = 0;
+                for (int d = 0; d < D; d++) if (I[d] & 1) m |= 1 << d;
+                if (m != col) continue;
+                double v = ColumnDot(g, &M[(size_t)i * T::S], I, x);
+                x[i] += (b[i] - v) / M[(size_t)i * T::S + oc];
+            }
+        }
+    }
+
+    // out = M x (matrix rows: M(i,j) is entry -off of node j's column, j = i + off)
+    void applyRows(int level, const double *M, const double *x, double *out) const
+    {
+        GridIdx<D> g(1 << level);
+        size_t N = g.nodes();
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < (long)N; i++)
+        {
+            int I[D];
+            g.node((size_t)i, I);
+            double s = 0;
+            for (int o = 0; o < T::S; o++)
+            {
+                int off[D], J[D];
+                StencilOffset<D>(o, off);
+                bool ok = true;
+                for (int d = 0; d < D; d++) { J[d] = I[d] + off[d]; if (J[d] < 0 || J[d] > g.r) ok = false; }
+                if (!ok) continue;
+                size_t j = g.node(J);
+                s += M[j * T::S + (T::S - 1 - o)] * x[j];
+            }
+            out[i] = s;
+        }
+    }
+
+    // dense LDL^T solve of the coarsest level (stands in for SimplicialLDLT, MG.h:105,131)
+    static void DenseSolve(const GridIdx<D> &g, const double *M, const double *b, double *x)
+    {
+        size_t N = g.nodes();
+        std::vector<double> A(N * N, 0.), L(N * N, 0.), Dg(N, 0.), z(N);
+        for (size_t i = 0; i < N; i++)
+        {
+            int I[D];
+            g.node(i, I);
+            for (int o = 0; o < T::S; o++)
+            {
+                int off[D], J[D];
+                StencilOffset<D>(o, off);
+                bool ok = true;
+                for (int d = 0; d < D; d++) { J[d] = I[d] + off[d]; if (J[d] < 0 || J[d] > g.r) ok = false; }
+                if (ok) A[g.node(J) * N + i] = M[i * T::S + o];  // A(row j, col i)
+            }
+        }
+        for (size_t j = 0; j < N; j++)
+        {
+            double d = A[j * N + j];
+            for (size_t k = 0; k < j; k++) d -= L[j * N + k] * L[j * N + k] * Dg[k];
+            Dg[j] = d;
+            L[j * N + j] = 1.;
+            for (size_t i = j + 1; i < N; i++)
+            {
+                double v = A[i * N + j];
+                for (size_t k = 0; k < j; k++) v -= L[i * N + k] * L[j * N + k] * Dg[k];
+                L[i * N + j] = v / d;
+            }
+        }
+        for (size_t i = 0; i < N; i++)
+        {
+            double v = b[i];
+            for (size_t k = 0; k < i; k++) v -= L[i * N + k] * z[k];
+            z[i] = v;
+        }
+        for (size_t i = 0; i < N; i++) z[i] /= Dg[i];
+        for (size_t ii = N; ii-- > 0;)
+        {
+            double v = z[ii];
+            for (size_t k = ii + 1; k < N; k++) v -= L[k * N + ii] * x[k];
+            x[ii] = v;
+        }
+    }
+
+    void prolongScalar(int level, const double *c, double *f) const { prolong(level, c, f); }
+
+    // V-cycle (MGSolver::vCycle with colours, MG.h:150-187) of M x = b on levels 0..top, with the
+    // Galerkin hierarchy Ms (Ms[top] = M)
+    void vcycle(const std::vector<std::vector<double>> &Ms, int top, const double *b, double *x, int iters) const
+    {
+        std::vector<std::vector<double>> Bs(top + 1), Xs(top + 1);
+        for (int l = 0; l <= top; l++) { Bs[l].assign(NumNodes(D, l), 0.); Xs[l].assign(NumNodes(D, l), 0.); }
+        std::copy(b, b + NumNodes(D, top), Bs[top].begin());
+        std::copy(x, x + NumNodes(D, top), Xs[top].begin());
+        for (int l = top; l > 0; l--)
+        {
+            for (int i = 0; i < iters; i++) linearGS(l, Ms[l].data(), Bs[l].data(), Xs[l].data());
+            std::vector<double> r(NumNodes(D, l));
+            applyRows(l, Ms[l].data(), Xs[l].data(), r.data());
+            for (size_t i = 0; i < r.size(); i++) r[i] = Bs[l][i] - r[i];
+            restrictT(l - 1, r.data(), Bs[l - 1].data());
+            std::fill(Xs[l - 1].begin(), Xs[l - 1].end(), 0.);
+        }
+        DenseSolve(GridIdx<D>(1), Ms[0].data(), Bs[0].data(), Xs[0].data());
+        for (int l = 1; l <= top; l++)
+        {
+            std::vector<double> p(NumNodes(D, l));
+            prolong(l - 1, Xs[l - 1].data(), p.data());
+            for (size_t i = 0; i < p.size(); i++) Xs[l][i] += p[i];
+            for (int i = 0; i < iters; i++) linearGS(l, Ms[l].data(), Bs[l].data(), Xs[l].data());
+        }
+        std::copy(Xs[top].begin(), Xs[top].end(), x);
+    }
+
+    // Galerkin hierarchy of a finest-level operator (MGSolver ctor, MG.h:93-107)
+    std::vector<std::vector<double>> hierarchy(const double *M, int top) const
+    {
+        std::vector<std::vector<double>> Ms(top + 1);
+        Ms[top].assign(M, M + NumNodes(D, top) * T::S);
+        for (int l = top; l > 0; l--) Ms[l - 1] = galerkin(Ms[l], l);
+        return Ms;
+    }
+
     // Random<double> (Misha/Geometry.inl:430-438) on the C library generator
     static double RandomDouble()
     {
@@ -1424,6 +1560,23 @@ int epr_oracle_gs_shifted(epr_oracle *o, int level, double *x, double *y, int it
 {
     if (!o) return -1;
     DISPATCH(o, { self->gs(level, x, y, iters, tx, ty); });
+    return 0;
+}
+
+int epr_oracle_linear_gs(epr_oracle *o, int level, const double *M, const double *b, double *x)
+{
+    if (!o) return -1;
+    DISPATCH(o, { self->linearGS(level, M, b, x); });
+    return 0;
+}
+
+int epr_oracle_mg_vcycle(epr_oracle *o, int level, const double *M, const double *b, double *x, int iters, int cycles)
+{
+    if (!o) return -1;
+    DISPATCH(o, {
+        auto Ms = self->hierarchy(M, level);
+        for (int c = 0; c < cycles; c++) self->vcycle(Ms, level, b, x, iters);
+    });
     return 0;
 }
 

@@ -72,6 +72,11 @@ int epr_oracle_gradient(epr_oracle *o, int level, const double *x, const double 
 int epr_oracle_gs(epr_oracle *o, int level, double *x, double *y, int iters);
 /* paired Gauss-Seidel on the shifted energy E - <tx, x> - <ty, y> (tx, ty per node) */
 int epr_oracle_gs_shifted(epr_oracle *o, int level, double *x, double *y, int iters, const double *tx, const double *ty);
+/* one coloured Gauss-Seidel sweep of M x = b with a column-stencil M (GSRelaxer, MG.h:57-72) */
+int epr_oracle_linear_gs(epr_oracle *o, int level, const double *M, const double *b, double *x);
+/* `cycles` V-cycles (MGSolver::vCycle, MG.h:150-187, iters relaxations per level) of M x = b with the
+ * Galerkin hierarchy of the column stencil M of `level`; x is updated in place */
+int epr_oracle_mg_vcycle(epr_oracle *o, int level, const double *M, const double *b, double *x, int iters, int cycles);
 /* restriction coarse = P^T fine of a level-(level+1) vector to level `level` */
 int epr_oracle_restrict(epr_oracle *o, int level, const double *fine, double *coarse);
 /* prolongation of a level-`level` vector to level+1 (Hat.scalars.inl:1747-1779) */

@@ -67,6 +67,8 @@ def lib():
         L.epr_oracle_prolong.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P]
         L.epr_oracle_gs_shifted.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, ctypes.c_int, P, P]
         L.epr_oracle_restrict.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P]
+        L.epr_oracle_linear_gs.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P]
+        L.epr_oracle_mg_vcycle.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, ctypes.c_int, ctypes.c_int]
         L.epr_oracle_gn_matvec.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, P, P, P]
         L.epr_oracle_solve.argtypes = [ctypes.c_void_p, P, P, P]
         _lib = L
@@ -172,6 +174,18 @@ class Oracle:
         lib().epr_oracle_gs_shifted(self._h, level, _p(x), _p(y), iters,
                                     _p(np.ascontiguousarray(tx, np.float64)), _p(np.ascontiguousarray(ty, np.float64)))
         return x, y
+
+    def linear_gs(self, level, M, b, x):
+        x = np.array(x, dtype=np.float64)
+        lib().epr_oracle_linear_gs(self._h, level, _p(np.ascontiguousarray(M, np.float64)),
+                                   _p(np.ascontiguousarray(b, np.float64)), _p(x))
+        return x
+
+    def mg_vcycle(self, level, M, b, x, iters=2, cycles=1):
+        x = np.array(x, dtype=np.float64)
+        lib().epr_oracle_mg_vcycle(self._h, level, _p(np.ascontiguousarray(M, np.float64)),
+                                   _p(np.ascontiguousarray(b, np.float64)), _p(x), iters, cycles)
+        return x
 
     def restrict(self, level, vf):
         out = np.zeros(self.nodes(level))

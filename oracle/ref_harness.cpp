@@ -333,6 +333,34 @@ static void Run(const std::string &in, unsigned int depth, const std::string &ou
         }
     }
 
+    // Linear multigrid of the reference (MG.h:37-195) on the finest level's screening+Dirichlet
+    // operator M = R + dWeight K, with the reference's prolongations and parity colours:
+    // one coloured GSRelaxer sweep and two V-cycles (2 relaxations per level) from x = 0.
+    {
+        const Energy &E = recon._energies[depth];
+        Eigen::SparseMatrix<double> K = E.scalars.stiffness(E.indexer);
+        Eigen::SparseMatrix<double> M = E._R + K * P.dWeight;
+        size_t N = (size_t)M.rows();
+        Eigen::VectorXd b(N);
+        for (size_t i = 0; i < N; i++) b[i] = U(rng);
+        auto MCI = [&](unsigned int d) -> const std::vector<std::vector<unsigned int>> & { return recon._mcIndices[d]; };
+        Eigen::VectorXd g = Eigen::VectorXd::Zero(N);
+        GSRelaxer relaxer(M);
+        relaxer(b, g, recon._mcIndices[depth]);
+        std::vector<Eigen::SparseMatrix<double>> Ps(depth);
+        for (unsigned int d = 0; d < depth; d++) Ps[d] = recon._energies[d]._sP;  // level d -> d+1 lives on the coarser energy
+        MGSolver mg(M, [&](unsigned int i) { return Ps[i]; }, depth);
+        Eigen::VectorXd x1 = Eigen::VectorXd::Zero(N);
+        mg.vCycle(b, x1, 2, MCI);
+        Eigen::VectorXd x2 = x1;
+        mg.vCycle(b, x2, 2, MCI);
+        SaveF64(path("mg_M"), ColumnStencil<Dim>(M, 1u << depth), {N, (size_t)std::pow(3, Dim)});
+        SaveF64(path("mg_b"), ToVec(b), {N});
+        SaveF64(path("mg_gs1"), ToVec(g), {N});
+        SaveF64(path("mg_v1"), ToVec(x1), {N});
+        SaveF64(path("mg_v2"), ToVec(x2), {N});
+    }
+
     if (P.solve)
     {
         // Cascadic solve with the reference schedule (ExteriorPoisson.h:315-409)

@@ -128,3 +128,15 @@ def test_solver_variants(name):
     for l in range(depth + 1):
         assert rel(xs[l], g[f"solx_d{l}"]) < 1e-9
         assert rel(ys[l], g[f"soly_d{l}"]) < 1e-9
+
+
+def test_linear_multigrid(case):
+    """GSRelaxer sweep and MGSolver V-cycles (MG.h:57-72, 150-187) on M = R + dWeight K."""
+    g, o, dim, depth = case
+    M, b = g["mg_M"], g["mg_b"]
+    x = o.linear_gs(depth, M, b, np.zeros_like(b))
+    assert rel(x, g["mg_gs1"]) < 1e-12
+    x1 = o.mg_vcycle(depth, M, b, np.zeros_like(b), 2, 1)
+    assert rel(x1, g["mg_v1"]) < 1e-10
+    x2 = o.mg_vcycle(depth, M, b, x1, 2, 1)
+    assert rel(x2, g["mg_v2"]) < 1e-10
