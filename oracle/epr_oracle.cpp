@@ -153,6 +153,130 @@ struct DenseTree
     std::vector<std::vector<uint8_t>> refined; // per tree depth t (0..D+1): cells (2^t)^D, 1 if children exist
 };
 
+// -------------------------------------------------------------------------------------------
+// Line searches on the bi-quadratic fit (SystemEnergy.h:256-303).  q[i*3+j] = coefficient of
+// s^i t^j.  Real roots of polynomials up to degree 3 follow Polynomial::Roots
+// (Misha/Polynomial.inl:653-708: a constant term below 1e-14 in magnitude is taken as the root 0
+// and the polynomial deflated; a vanishing leading coefficient lowers the degree) and, for the
+// cubic, the trigonometric / Cardano method for x^3 + a x^2 + b x + c (three real roots when
+// R^2 <= Q^3 + eps, Q = (a^2 - 3b)/9, R = (2a^3 - 9ab + 27c)/54; otherwise one real root, or a
+// double root when the imaginary part falls below eps).
+// -------------------------------------------------------------------------------------------
+static int RealRoots(const double *p, int degree, double *r, double eps = 1e-14)
+{
+    if (degree == 0) return 0;
+    if (std::fabs(p[0]) < eps)
+    {
+        r[0] = 0;
+        return RealRoots(p + 1, degree - 1, r + 1, eps) + 1;
+    }
+    if (degree == 1) { if (p[1] == 0) return 0; r[0] = -p[0] / p[1]; return 1; }
+    if (p[degree] == 0) return RealRoots(p, degree - 1, r, eps);
+    if (degree == 2)
+    {
+        double disc = p[1] * p[1] - 4. * p[0] * p[2];
+        if (disc < 0) return 0;
+        if (disc == 0) { r[0] = -p[1] / (2 * p[2]); return 1; }
+        disc = std::sqrt(disc);
+        r[0] = (-p[1] - disc) / (2 * p[2]);
+        r[1] = (-p[1] + disc) / (2 * p[2]);
+        return 2;
+    }
+    double a = p[2] / p[3], b = p[1] / p[3], cc = p[0] / p[3];
+    double Qv = (a * a - 3 * b) / 9, Rv = (a * (2 * a * a - 9 * b) + 27 * cc) / 54;
+    double Q3 = Qv * Qv * Qv, R2 = Rv * Rv;
+    if (R2 <= Q3 + eps)
+    {
+        double t = Rv / std::sqrt(Q3);
+        t = std::max(-1., std::min(1., t));
+        double th = std::acos(t), m = -2 * std::sqrt(Qv);
+        const double twoPi = 6.283185307179586476925286766559;
+        r[0] = m * std::cos(th / 3) - a / 3;
+        r[1] = m * std::cos((th + twoPi) / 3) - a / 3;
+        r[2] = m * std::cos((th - twoPi) / 3) - a / 3;
+        return 3;
+    }
+    double Av = -std::cbrt(std::fabs(Rv) + std::sqrt(R2 - Q3));
+    if (Rv < 0) Av = -Av;
+    double Bv = Av == 0 ? 0 : Qv / Av;
+    r[0] = (Av + Bv) - a / 3;
+    double im = 0.5 * std::sqrt(3.) * (Av - Bv);
+    if (std::fabs(im) < eps) { r[1] = -0.5 * (Av + Bv) - a / 3; return 2; }
+    return 1;
+}
+
+// coefficients (degree 4) of s -> P(c0 + s d0, c1 + s d1)
+static void PullBack(const double *q, double c0, double d0, double c1, double d1, double *out)
+{
+    for (int k = 0; k < 5; k++) out[k] = 0;
+    double ps[3][3] = {{1, 0, 0}, {c0, d0, 0}, {c0 * c0, 2 * c0 * d0, d0 * d0}};  // (c0 + s d0)^i
+    double pt[3][3] = {{1, 0, 0}, {c1, d1, 0}, {c1 * c1, 2 * c1 * d1, d1 * d1}};
+    for (int i = 0; i <= 2; i++)
+        for (int j = 0; j <= 2; j++)
+            for (int a = 0; a <= 2; a++)
+                for (int b = 0; b <= 2; b++) out[a + b] += q[i * 3 + j] * ps[i][a] * pt[j][b];
+}
+
+static double Poly1(const double *p, int deg, double s)
+{
+    double v = 0;
+    for (int k = deg; k >= 0; k--) v = v * s + p[k];
+    return v;
+}
+
+// the minimiser of the quartic p among the real roots of its derivative
+static double QuarticArgMin(const double *p)
+{
+    double dp[4] = {p[1], 2 * p[2], 3 * p[3], 4 * p[4]}, roots[3];
+    int n = RealRoots(dp, 3, roots);
+    if (n <= 0) return 0;
+    double s = roots[0];
+    for (int i = 1; i < n; i++) if (Poly1(p, 4, roots[i]) < Poly1(p, 4, s)) s = roots[i];
+    return s;
+}
+
+// stepSize (SystemEnergy.h:256-270): argmin over s of P(s, s)
+static double StepSize(const double *q)
+{
+    double p[5];
+    PullBack(q, 0, 1, 0, 1, p);
+    return QuarticArgMin(p);
+}
+
+// newtonUpdate (SystemEnergy.h:272-303): Newton directions from (0,0), each followed by an exact
+// line search along the direction
+static void NewtonUpdate(const double *q, int steps, double *st)
+{
+    double c0 = 0, c1 = 0;
+    for (int k = 0; k < steps; k++)
+    {
+        auto Q = [&](int i, int j) { return q[i * 3 + j]; };
+        // gradient and Hessian of sum q_ij s^i t^j at (c0, c1)
+        double g0 = 0, g1 = 0, h00 = 0, h01 = 0, h11 = 0;
+        for (int i = 0; i <= 2; i++)
+            for (int j = 0; j <= 2; j++)
+            {
+                double v = Q(i, j);
+                double si = std::pow(c0, i), tj = std::pow(c1, j);
+                if (i >= 1) g0 += v * i * std::pow(c0, i - 1) * tj;
+                if (j >= 1) g1 += v * j * si * std::pow(c1, j - 1);
+                if (i >= 2) h00 += v * i * (i - 1) * std::pow(c0, i - 2) * tj;
+                if (j >= 2) h11 += v * j * (j - 1) * si * std::pow(c1, j - 2);
+                if (i >= 1 && j >= 1) h01 += v * i * j * std::pow(c0, i - 1) * std::pow(c1, j - 1);
+            }
+        double det = h00 * h11 - h01 * h01;
+        double d0 = -(h11 * g0 - h01 * g1) / det, d1 = -(-h01 * g0 + h00 * g1) / det;
+        if (d0 * d0 + d1 * d1 < 1e-20) break;
+        double p[5];
+        PullBack(q, c0, d0, c1, d1, p);
+        double s = QuarticArgMin(p);
+        c0 += d0 * s;
+        c1 += d1 * s;
+    }
+    st[0] = c0;
+    st[1] = c1;
+}
+
 template <int D>
 struct Oracle
 {
@@ -1292,6 +1416,220 @@ struct Oracle
         return Ms;
     }
 
+    // -------------------------------------------------------------------------------------------
+    // Alternating solve (ExteriorPoissonSolvers.h:86-154)
+    // -------------------------------------------------------------------------------------------
+    // Gram matrix of the wedge with a fixed field f as a column stencil:
+    //   G(j, i) = int <W(f, phi_j), W(f, phi_i)>_F,   so that  |W(f, v)|^2 = v^T G v
+    // (and |W(v, f)|^2 too: W is antisymmetric in its arguments).
+    void wedgeGram(int level, const double *f, double *G) const
+    {
+        int r = 1 << level;
+        GridIdx<D> g(r);
+        size_t N = g.nodes();
+        double vol = std::pow(1. / r, D);
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < (long)N; i++)
+        {
+            int I[D];
+            g.node((size_t)i, I);
+            double *col = &G[(size_t)i * T::S];
+            for (int o = 0; o < T::S; o++) col[o] = 0;
+            for (int A = 0; A < (1 << D); A++)
+            {
+                int E[D];
+                bool ok = true;
+                for (int d = 0; d < D; d++) { E[d] = I[d] - ((A >> (D - 1 - d)) & 1); if (E[d] < 0 || E[d] >= r) ok = false; }
+                if (!ok) continue;
+                double fc[1 << D], dummy[1 << D];
+                gatherElement(g, E, f, f, fc, dummy);
+                for (int q = 0; q < T::Q; q++)
+                {
+                    double xi[D], w = vol;
+                    int t = q;
+                    for (int d = D - 1; d >= 0; d--) { xi[d] = GQ_X[t % 3]; w *= GQ_W[t % 3]; t /= 3; }
+                    double gf[D], ga[D];
+                    CornerGrad(fc, xi, r, gf);
+                    HatGrad(A, xi, r, ga);
+                    for (int Bc = 0; Bc < (1 << D); Bc++)
+                    {
+                        double gb[D];
+                        HatGrad(Bc, xi, r, gb);
+                        double s = 0;
+                        for (int a = 0; a < D; a++)
+                            for (int b = 0; b < a; b++)
+                            {
+                                double Va = 0.5 * (ga[a] * gf[b] - gf[a] * ga[b]);
+                                double Vb = 0.5 * (gb[a] * gf[b] - gf[a] * gb[b]);
+                                s += 2 * Va * Vb;
+                            }
+                        int off[D];
+                        for (int d = 0; d < D; d++) off[d] = ((Bc >> (D - 1 - d)) & 1) - ((A >> (D - 1 - d)) & 1);
+                        col[StencilOffsetIndex<D>(off)] += w * s;
+                    }
+                }
+            }
+        }
+    }
+
+    // sum_j B(j, i) v_j without the diagonal (B is antisymmetric, so this is also -(B v)_i)
+    double BColumnDot(const GridIdx<D> &g, const double *col, const int *I, const double *v) const
+    {
+        double s = 0;
+        for (int o = 0; o < T::S; o++)
+        {
+            if (o == (T::S - 1) / 2 || col[o] == 0) continue;
+            int off[D], J[D];
+            StencilOffset<D>(o, off);
+            bool ok = true;
+            for (int d = 0; d < D; d++) { J[d] = I[d] + off[d]; if (J[d] < 0 || J[d] > g.r) ok = false; }
+            if (ok) s += col[o] * v[g.node(J)];
+        }
+        return s;
+    }
+
+    // The linear system of one alternating half-step, as AlternatingSolve forms it from a
+    // quadratic approximation q (q.q *= 2, q.l = -q.l; ExteriorPoissonSolvers.h:101-104, 120-123):
+    //   which == 1 (y free, x fixed):  2 (G_x + A) y = 2 B x
+    //   which == 0 (x free, y fixed):  2 (G_y + A) x = 2 B^T y
+    // from E = |W(x,y)|^2 - 2 y^T B x + c + x^T A x + y^T A y.
+    void alternatingSystem(int level, const double *x, const double *y, int which, double *M, double *b) const
+    {
+        const LevelSystem &L = levels[level];
+        GridIdx<D> g(1 << level);
+        size_t N = g.nodes();
+        wedgeGram(level, which ? x : y, M);
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < (long)N; i++)
+        {
+            int I[D];
+            g.node((size_t)i, I);
+            for (int o = 0; o < T::S; o++) M[(size_t)i * T::S + o] = 2. * (M[(size_t)i * T::S + o] + L.A[(size_t)i * T::S + o]);
+            const double *bc = &L.B[(size_t)i * T::S];
+            b[i] = which ? -2. * BColumnDot(g, bc, I, x) : 2. * BColumnDot(g, bc, I, y);
+        }
+    }
+
+    // AlternatingSolve with sType MULTIGRID (V-cycles on the Galerkin hierarchy down to level 0)
+    // or SINGLE_LEVEL (gsIters * vCycles coloured GS sweeps)
+    void alternatingSolve(int level, double *x, double *y, int iters, int vCycles, int gsIters, bool singleLevel) const
+    {
+        size_t N = NumNodes(D, level);
+        std::vector<double> M(N * T::S), b(N);
+        for (int it = 0; it < iters; it++)
+        {
+            for (int which = 1; which >= 0; which--)
+            {
+                double *v = which ? y : x;
+                alternatingSystem(level, x, y, which, M.data(), b.data());
+                if (singleLevel)
+                    for (int k = 0; k < gsIters * vCycles; k++) linearGS(level, M.data(), b.data(), v);
+                else
+                {
+                    auto Ms = hierarchy(M.data(), level);
+                    for (int k = 0; k < vCycles; k++) vcycle(Ms, level, b.data(), v, gsIters);
+                }
+            }
+        }
+    }
+
+    // -------------------------------------------------------------------------------------------
+    // Bi-quadratic fit P(s,t) = E(x + s dx, y + t dy); q[i*3 + j] is the coefficient of s^i t^j.
+    // asReference reproduces SingleCycleCascadicSystemEnergy::biQuadraticFit (SystemEnergy.h:
+    // 499-540) term by term, which differs from the exact expansion in two places:
+    //   * the s t^2 coefficient is 2 <W(dx,dy), W(x,y)> (SystemEnergy.h:506) where the expansion
+    //     has 2 <W(dx,dy), W(x,dy)>;
+    //   * the stiffness term enters with weight 1 (SystemEnergy.h:522-530) where energies() weights
+    //     it by sWeight (= dWeight, SystemEnergy.h:494).
+    // -------------------------------------------------------------------------------------------
+    void biQuadraticFit(int level, const double *x, const double *y, const double *dx, const double *dy, double *q,
+                        bool asReference = false) const
+    {
+        const LevelSystem &L = levels[level];
+        std::vector<double> Aref;
+        const double *Abase = L.A.data();
+        if (asReference)
+        {
+            std::vector<double> K = stiffnessStencil(level);
+            Aref.resize(L.A.size());
+            for (size_t i = 0; i < Aref.size(); i++) Aref[i] = L.A[i] + (1. - P.d_weight) * K[i];
+            Abase = Aref.data();
+        }
+        int r = 1 << level;
+        GridIdx<D> g(r);
+        size_t NE = g.elems(), N = g.nodes();
+        double vol = std::pow(1. / r, D);
+        // <P,Q> of the four wedges W(x,y), W(dx,y), W(x,dy), W(dx,dy)
+        double w00 = 0, w20 = 0, w02 = 0, w22 = 0, w21 = 0, w12 = 0, w11a = 0, w11b = 0, w10 = 0, w01 = 0;
+#pragma omp parallel for schedule(static) reduction(+ : w00, w20, w02, w22, w21, w12, w11a, w11b, w10, w01)
+        for (long e = 0; e < (long)NE; e++)
+        {
+            int E[D];
+            g.elem((size_t)e, E);
+            double xc[1 << D], yc[1 << D], dxc[1 << D], dyc[1 << D];
+            gatherElement(g, E, x, y, xc, yc);
+            gatherElement(g, E, dx, dy, dxc, dyc);
+            for (int qp = 0; qp < T::Q; qp++)
+            {
+                double xi[D], w = vol;
+                int t = qp;
+                for (int d = D - 1; d >= 0; d--) { xi[d] = GQ_X[t % 3]; w *= GQ_W[t % 3]; t /= 3; }
+                double gx[D], gy[D], gdx[D], gdy[D];
+                CornerGrad(xc, xi, r, gx);
+                CornerGrad(yc, xi, r, gy);
+                CornerGrad(dxc, xi, r, gdx);
+                CornerGrad(dyc, xi, r, gdy);
+                for (int a = 0; a < D; a++)
+                    for (int b = 0; b < a; b++)
+                    {
+                        auto W = [&](const double *u, const double *v) { return 0.5 * (v[a] * u[b] - u[a] * v[b]); };
+                        double Wxy = W(gx, gy), WXy = W(gdx, gy), WxY = W(gx, gdy), WXY = W(gdx, gdy);
+                        double s = 2 * w;
+                        w22 += s * WXY * WXY;
+                        w21 += s * WXY * WXy;
+                        w12 += s * WXY * WxY;
+                        w20 += s * WXy * WXy;
+                        w02 += s * WxY * WxY;
+                        w11a += s * WXy * WxY;
+                        w11b += s * WXY * Wxy;
+                        w10 += s * WXy * Wxy;
+                        w01 += s * WxY * Wxy;
+                        w00 += s * Wxy * Wxy;
+                    }
+            }
+        }
+        double aXX = 0, axX = 0, axx = 0, aYY = 0, ayY = 0, ayy = 0, bYX = 0, bYx = 0, byX = 0, byx = 0;
+#pragma omp parallel for schedule(static) reduction(+ : aXX, axX, axx, aYY, ayY, ayy, bYX, bYx, byX, byx)
+        for (long i = 0; i < (long)N; i++)
+        {
+            int I[D];
+            g.node((size_t)i, I);
+            const double *a = &Abase[(size_t)i * T::S], *b = &L.B[(size_t)i * T::S];
+            double Adx = ColumnDot(g, a, I, dx), Ax = ColumnDot(g, a, I, x);
+            double Ady = ColumnDot(g, a, I, dy), Ay = ColumnDot(g, a, I, y);
+            double Bdy = ColumnDot(g, b, I, dy), By = ColumnDot(g, b, I, y);
+            aXX += dx[i] * Adx; axX += x[i] * Adx; axx += x[i] * Ax;
+            aYY += dy[i] * Ady; ayY += y[i] * Ady; ayy += y[i] * Ay;
+            // y^T B x = sum_i x_i sum_j B(j,i) y_j, as in energy()
+            bYX += dx[i] * Bdy; bYx += x[i] * Bdy; byX += dx[i] * By; byx += x[i] * By;
+        }
+        for (int k = 0; k < 9; k++) q[k] = 0;
+        auto Q = [&](int i, int j) -> double & { return q[i * 3 + j]; };
+        Q(2, 2) += w22;
+        Q(2, 1) += 2 * w21;
+        Q(1, 2) += 2 * (asReference ? w11b : w12);
+        Q(2, 0) += w20;
+        Q(0, 2) += w02;
+        Q(1, 1) += 2 * w11a + 2 * w11b;
+        Q(1, 0) += 2 * w10;
+        Q(0, 1) += 2 * w01;
+        Q(0, 0) += w00;
+        Q(2, 0) += aXX; Q(1, 0) += 2 * axX; Q(0, 0) += axx;
+        Q(0, 2) += aYY; Q(0, 1) += 2 * ayY; Q(0, 0) += ayy;
+        Q(1, 1) += -2 * bYX; Q(0, 1) += -2 * bYx; Q(1, 0) += -2 * byX; Q(0, 0) += -2 * byx;
+        Q(0, 0) += c;
+    }
+
     // Random<double> (Misha/Geometry.inl:430-438) on the C library generator
     static double RandomDouble()
     {
@@ -1579,6 +1917,39 @@ int epr_oracle_mg_vcycle(epr_oracle *o, int level, const double *M, const double
     });
     return 0;
 }
+
+int epr_oracle_wedge_gram(epr_oracle *o, int level, const double *f, double *G)
+{
+    if (!o) return -1;
+    DISPATCH(o, { self->wedgeGram(level, f, G); });
+    return 0;
+}
+
+int epr_oracle_alternating_system(epr_oracle *o, int level, const double *x, const double *y, int which, double *M, double *b)
+{
+    if (!o) return -1;
+    DISPATCH(o, { self->alternatingSystem(level, x, y, which, M, b); });
+    return 0;
+}
+
+int epr_oracle_alternating_solve(epr_oracle *o, int level, double *x, double *y, int iters, int vcycles, int gs_iters, int single_level)
+{
+    if (!o) return -1;
+    DISPATCH(o, { self->alternatingSolve(level, x, y, iters, vcycles, gs_iters, single_level != 0); });
+    return 0;
+}
+
+int epr_oracle_biquadratic_fit(epr_oracle *o, int level, const double *x, const double *y, const double *dx, const double *dy, double *q9,
+                               int as_reference)
+{
+    if (!o) return -1;
+    DISPATCH(o, { self->biQuadraticFit(level, x, y, dx, dy, q9, as_reference != 0); });
+    return 0;
+}
+
+double epr_oracle_step_size(const double *q9) { return StepSize(q9); }
+
+void epr_oracle_newton_update(const double *q9, int steps, double *st) { NewtonUpdate(q9, steps, st); }
 
 int epr_oracle_restrict(epr_oracle *o, int level, const double *fine, double *coarse)
 {

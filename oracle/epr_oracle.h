@@ -77,6 +77,20 @@ int epr_oracle_linear_gs(epr_oracle *o, int level, const double *M, const double
 /* `cycles` V-cycles (MGSolver::vCycle, MG.h:150-187, iters relaxations per level) of M x = b with the
  * Galerkin hierarchy of the column stencil M of `level`; x is updated in place */
 int epr_oracle_mg_vcycle(epr_oracle *o, int level, const double *M, const double *b, double *x, int iters, int cycles);
+/* wedge Gram matrix of a fixed field f (column stencil, N x 3^dim): v^T G v = |W(f, v)|^2 */
+int epr_oracle_wedge_gram(epr_oracle *o, int level, const double *f, double *G);
+/* system of one alternating half-step (ExteriorPoissonSolvers.h:96-131): which 1 -> y free,
+ * which 0 -> x free; M (N x 3^dim column stencil) and right-hand side b */
+int epr_oracle_alternating_system(epr_oracle *o, int level, const double *x, const double *y, int which, double *M, double *b);
+/* AlternatingSolve (ExteriorPoissonSolvers.h:86-154) on (x, y) in place */
+int epr_oracle_alternating_solve(epr_oracle *o, int level, double *x, double *y, int iters, int vcycles, int gs_iters, int single_level);
+/* q9[i*3+j] = coefficient of s^i t^j of E(x+s dx, y+t dy); as_reference != 0 reproduces the
+ * reference's biQuadraticFit (SystemEnergy.h:499-540) including its two deviations */
+int epr_oracle_biquadratic_fit(epr_oracle *o, int level, const double *x, const double *y, const double *dx, const double *dy, double *q9,
+                               int as_reference);
+/* stepSize / newtonUpdate (SystemEnergy.h:256-303) on a bi-quadratic fit */
+double epr_oracle_step_size(const double *q9);
+void epr_oracle_newton_update(const double *q9, int steps, double *st);
 /* restriction coarse = P^T fine of a level-(level+1) vector to level `level` */
 int epr_oracle_restrict(epr_oracle *o, int level, const double *fine, double *coarse);
 /* prolongation of a level-`level` vector to level+1 (Hat.scalars.inl:1747-1779) */

@@ -68,6 +68,14 @@ def lib():
         L.epr_oracle_gs_shifted.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, ctypes.c_int, P, P]
         L.epr_oracle_restrict.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P]
         L.epr_oracle_linear_gs.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P]
+        L.epr_oracle_wedge_gram.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P]
+        L.epr_oracle_alternating_system.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, ctypes.c_int, P, P]
+        L.epr_oracle_alternating_solve.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int,
+                                                   ctypes.c_int, ctypes.c_int]
+        L.epr_oracle_biquadratic_fit.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, P, P, ctypes.c_int]
+        L.epr_oracle_step_size.argtypes = [P]
+        L.epr_oracle_step_size.restype = ctypes.c_double
+        L.epr_oracle_newton_update.argtypes = [P, ctypes.c_int, P]
         L.epr_oracle_mg_vcycle.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, ctypes.c_int, ctypes.c_int]
         L.epr_oracle_gn_matvec.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, P, P, P]
         L.epr_oracle_solve.argtypes = [ctypes.c_void_p, P, P, P]
@@ -186,6 +194,42 @@ class Oracle:
         lib().epr_oracle_mg_vcycle(self._h, level, _p(np.ascontiguousarray(M, np.float64)),
                                    _p(np.ascontiguousarray(b, np.float64)), _p(x), iters, cycles)
         return x
+
+    def wedge_gram(self, level, f):
+        N = int(((1 << level) + 1) ** self.dim)
+        G = np.zeros((N, 3 ** self.dim))
+        lib().epr_oracle_wedge_gram(self._h, level, _p(np.ascontiguousarray(f, np.float64)), _p(G))
+        return G
+
+    def alternating_system(self, level, x, y, which):
+        N = int(((1 << level) + 1) ** self.dim)
+        M = np.zeros((N, 3 ** self.dim))
+        b = np.zeros(N)
+        lib().epr_oracle_alternating_system(self._h, level, _p(np.ascontiguousarray(x, np.float64)),
+                                            _p(np.ascontiguousarray(y, np.float64)), which, _p(M), _p(b))
+        return M, b
+
+    def alternating_solve(self, level, x, y, iters=1, vcycles=1, gs_iters=2, single_level=False):
+        x = np.array(x, dtype=np.float64)
+        y = np.array(y, dtype=np.float64)
+        lib().epr_oracle_alternating_solve(self._h, level, _p(x), _p(y), iters, vcycles, gs_iters, int(single_level))
+        return x, y
+
+    def biquadratic_fit(self, level, x, y, dx, dy, as_reference=False):
+        q = np.zeros((3, 3))
+        c = lambda v: _p(np.ascontiguousarray(v, np.float64))  # noqa: E731
+        lib().epr_oracle_biquadratic_fit(self._h, level, c(x), c(y), c(dx), c(dy), _p(q), int(as_reference))
+        return q
+
+    @staticmethod
+    def step_size(q):
+        return float(lib().epr_oracle_step_size(_p(np.ascontiguousarray(q, np.float64))))
+
+    @staticmethod
+    def newton_update(q, steps=10):
+        st = np.zeros(2)
+        lib().epr_oracle_newton_update(_p(np.ascontiguousarray(q, np.float64)), steps, _p(st))
+        return st
 
     def restrict(self, level, vf):
         out = np.zeros(self.nodes(level))

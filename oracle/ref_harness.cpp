@@ -361,6 +361,48 @@ static void Run(const std::string &in, unsigned int depth, const std::string &ou
         SaveF64(path("mg_v2"), ToVec(x2), {N});
     }
 
+    // Quadratic models of the alternating solve (ExteriorPoissonSolvers.h:96-131) for the energy
+    // the reconstructor uses.  SingleCycleCascadicSystemEnergy does not implement
+    // quadraticApproximation1/2 (the SystemEnergy defaults abort, SystemEnergy.h:322-334), and the
+    // product mass matrix (ProductFunctions::mass, Hat.products.h:136) does not compile, so the
+    // wedge Gram matrices G_x (u^T G_x v = <x^u, x^v>) and G_y (<u^y, v^y>) are pinned through the
+    // reference's own bilinear wedge integral wedges(indexer, _wMStencil, a, b, c, d) = <a^b, c^d>
+    // (Hat.products.inl:189-231) on random probe pairs (u_k, v_k).  Then biQuadraticFit, stepSize
+    // and newtonUpdate (SystemEnergy.h:256-303, 499-540) for random directions (dx, dy).
+    {
+        const unsigned int ql = depth, K = 6;
+        const Energy &E = recon._energies[ql];
+        unsigned int res = 1u << ql;
+        size_t N = (size_t)std::pow(res + 1, Dim);
+        Eigen::VectorXd x(N), y(N), dx(N), dy(N);
+        for (size_t i = 0; i < N; i++) x[i] = U(rng), y[i] = U(rng), dx[i] = U(rng), dy[i] = U(rng);
+        std::vector<double> us(K * N), vs(K * N), gx(K), gy(K);
+        for (unsigned int k = 0; k < K; k++)
+        {
+            Eigen::VectorXd u(N), v(N);
+            for (size_t i = 0; i < N; i++) u[i] = U(rng), v[i] = U(rng);
+            for (size_t i = 0; i < N; i++) us[k * N + i] = u[i], vs[k * N + i] = v[i];
+            gx[k] = E.wedges(E.indexer, E._wMStencil, x, u, x, v);
+            gy[k] = E.wedges(E.indexer, E._wMStencil, u, y, v, y);
+        }
+        SaveF64(path("qa_x"), ToVec(x), {N});
+        SaveF64(path("qa_y"), ToVec(y), {N});
+        SaveF64(path("qa_dx"), ToVec(dx), {N});
+        SaveF64(path("qa_dy"), ToVec(dy), {N});
+        SaveF64(path("qa_u"), us, {K, N});
+        SaveF64(path("qa_v"), vs, {K, N});
+        SaveF64(path("qa_gx"), gx, {K});
+        SaveF64(path("qa_gy"), gy, {K});
+        Polynomial::Polynomial2D<4> Q = E.biQuadraticFit(x, y, dx, dy);
+        std::vector<double> q(9);
+        for (unsigned int i = 0; i <= 2; i++) for (unsigned int j = 0; j <= 2; j++) q[i * 3 + j] = Q.coefficient(i, j);
+        SaveF64(path("qa_biquad"), q, {3, 3});
+        std::vector<double> st = {E.stepSize(x, y, dx, dy)};
+        SaveF64(path("qa_step"), st, {1});
+        Point<double, 2> nu = E.newtonUpdate(x, y, dx, dy, 10);
+        SaveF64(path("qa_newton"), std::vector<double>{nu[0], nu[1]}, {2});
+    }
+
     if (P.solve)
     {
         // Cascadic solve with the reference schedule (ExteriorPoisson.h:315-409)

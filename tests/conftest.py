@@ -34,3 +34,19 @@ def variant_params(flags):
         name, cast = conv[k]
         out[name] = cast(v)
     return out
+
+
+def stencil_apply(G, v, dim, level):
+    """out_j = sum_i G(j, i) v_i for a column stencil G[i, o] = G(i + off(o), i) (numpy, tests only)."""
+    import numpy as np
+    r = 1 << level
+    N = (r + 1) ** dim
+    idx = np.array(np.unravel_index(np.arange(N), (r + 1,) * dim)).T
+    out = np.zeros(N)
+    for o in range(3 ** dim):
+        off = np.array(np.unravel_index(o, (3,) * dim)) - 1
+        J = idx + off
+        ok = np.all((J >= 0) & (J <= r), axis=1)
+        j = np.ravel_multi_index(J[ok].T, (r + 1,) * dim)
+        np.add.at(out, j, G[ok, o] * v[ok])
+    return out

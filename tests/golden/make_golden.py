@@ -111,7 +111,8 @@ def make(name, workload, n, seed, depth, stencil_levels):
         for l in range(depth + 1):
             fx[f"density_l{l}"] = L(f"density_l{l}")
             fx[f"skew_l{l}"] = L(f"skew_l{l}")
-        for k in ("mg_M", "mg_b", "mg_gs1", "mg_v1", "mg_v2"):
+        for k in ("mg_M", "mg_b", "mg_gs1", "mg_v1", "mg_v2", "qa_x", "qa_y", "qa_dx", "qa_dy", "qa_u", "qa_v",
+                  "qa_gx", "qa_gy", "qa_biquad", "qa_step", "qa_newton"):
             fx[k] = L(k)
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **fx)

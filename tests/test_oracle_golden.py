@@ -140,3 +140,54 @@ def test_linear_multigrid(case):
     assert rel(x1, g["mg_v1"]) < 1e-10
     x2 = o.mg_vcycle(depth, M, b, x1, 2, 1)
     assert rel(x2, g["mg_v2"]) < 1e-10
+
+
+def test_wedge_gram(case):
+    """u^T G_x v = <x^u, x^v> and <u^y, v^y> against the reference's bilinear wedge integral."""
+    from conftest import stencil_apply
+    g, o, dim, depth = case
+    Gx = o.wedge_gram(depth, g["qa_x"])
+    Gy = o.wedge_gram(depth, g["qa_y"])
+    U, V = g["qa_u"], g["qa_v"]
+    gx = [U[k] @ stencil_apply(Gx, V[k], dim, depth) for k in range(len(U))]
+    gy = [U[k] @ stencil_apply(Gy, V[k], dim, depth) for k in range(len(U))]
+    assert rel(gx, g["qa_gx"]) < 1e-12
+    assert rel(gy, g["qa_gy"]) < 1e-12
+
+
+def test_biquadratic_fit_and_line_searches(case):
+    g, o, dim, depth = case
+    x, y, dx, dy = g["qa_x"], g["qa_y"], g["qa_dx"], g["qa_dy"]
+    q = o.biquadratic_fit(depth, x, y, dx, dy, as_reference=True)
+    assert rel(q, g["qa_biquad"]) < 1e-12
+    assert abs(O.Oracle.step_size(q) - g["qa_step"][0]) < 1e-9 * abs(g["qa_step"][0])
+    assert np.abs(O.Oracle.newton_update(q, 10) - g["qa_newton"]).max() < 1e-9 * np.abs(g["qa_newton"]).max()
+    # the exact expansion reproduces E(x + s dx, y + t dy)
+    qe = o.biquadratic_fit(depth, x, y, dx, dy)
+    for s, t in [(0.3, -0.7), (-1.1, 0.4), (0.05, 0.02)]:
+        e = o.energy(depth, x + s * dx, y + t * dy)
+        p = sum(qe[i, j] * s ** i * t ** j for i in range(3) for j in range(3))
+        assert abs(p - (e[0] + e[1])) < 1e-11 * abs(p)
+
+
+def test_alternating_system_and_solve(case):
+    """The half-step systems are the exact quadratic models of E in one field (checked against the
+    exact bi-quadratic expansion); AlternatingSolve never increases the energy."""
+    from conftest import stencil_apply
+    g, o, dim, depth = case
+    x, y, d = g["qa_x"], g["qa_y"], g["qa_dx"]
+    zero = np.zeros_like(x)
+    for which in (0, 1):
+        M, b = o.alternating_system(depth, x, y, which)
+        v = y if which else x
+        q = o.biquadratic_fit(depth, x, y, zero if which else d, d if which else zero)
+        quad, lin = (q[0, 2], q[0, 1]) if which else (q[2, 0], q[1, 0])
+        Md = stencil_apply(M, d, dim, depth)
+        assert abs(0.5 * d @ Md - quad) < 1e-12 * abs(quad)
+        assert abs(d @ (stencil_apply(M, v, dim, depth) - b) - lin) < 1e-10 * (abs(lin) + abs(d @ b))
+    lev = max(depth - 1, 1)
+    xs, ys = 0.01 * g[f"xr_d{lev}"], 0.01 * g[f"yr_d{lev}"]
+    e0 = o.energy(lev, xs, ys)
+    x1, y1 = o.alternating_solve(lev, xs, ys, iters=2, vcycles=2, gs_iters=2)
+    e1 = o.energy(lev, x1, y1)
+    assert e1[0] + e1[1] < e0[0] + e0[1]
