@@ -131,6 +131,13 @@ def load():
     L.epr_energy_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp,
                                      ctypes.c_double, vp, vp]
     L.epr_noalloc_last_error.restype = ctypes.c_char_p
+    L.epr_linear_gs.argtypes = [vp, ctypes.c_int, P, P, P, ctypes.c_int]
+    L.epr_mg_vcycle.argtypes = [vp, ctypes.c_int, P, P, P, ctypes.c_int, ctypes.c_int]
+    L.epr_alternating_system.argtypes = [vp, ctypes.c_int, ctypes.c_int, P, P]
+    L.epr_alternating_solve.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.epr_biquadratic_fit.argtypes = [vp, ctypes.c_int, P, P, ctypes.c_int, P]
+    L.epr_step_size.argtypes = [P, P]
+    L.epr_newton_update.argtypes = [P, ctypes.c_int, P]
     _lib = L
     return L
 
@@ -138,6 +145,24 @@ def load():
 def _p(a: np.ndarray):
     assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def step_size(q) -> float:
+    """stepSize (SystemEnergy.h:256-270) on a 3 x 3 bi-quadratic fit."""
+    s = np.zeros(1)
+    rc = load().epr_step_size(_p(np.ascontiguousarray(q, np.float64)), _p(s))
+    if rc != EPR_OK:
+        raise EprError(f"[{rc}] step size")
+    return float(s[0])
+
+
+def newton_update(q, steps=10) -> np.ndarray:
+    """newtonUpdate (SystemEnergy.h:272-303) on a 3 x 3 bi-quadratic fit."""
+    st = np.zeros(2)
+    rc = load().epr_newton_update(_p(np.ascontiguousarray(q, np.float64)), steps, _p(st))
+    if rc != EPR_OK:
+        raise EprError(f"[{rc}] newton update")
+    return st
 
 
 def default_params(**kw) -> Params:
@@ -279,6 +304,40 @@ class Reconstructor:
         self._check(load().epr_gn_matvec(self._h, level, _p(np.ascontiguousarray(dx, np.float64)),
                                          _p(np.ascontiguousarray(dy, np.float64)), _p(ox), _p(oy)))
         return ox, oy
+
+    # ---------------------------------------------------------------- linear multigrid / alternating solve
+    def linear_gs(self, level, M, b, v, iters=1):
+        """iters coloured Gauss-Seidel sweeps of M v = b (GSRelaxer, MG.h:57-72); returns v."""
+        v = np.array(v, dtype=np.float64)
+        self._check(load().epr_linear_gs(self._h, level, _p(np.ascontiguousarray(M, np.float64)),
+                                         _p(np.ascontiguousarray(b, np.float64)), _p(v), iters))
+        return v
+
+    def mg_vcycle(self, level, M, b, v, gs_iters=2, cycles=1):
+        """cycles V-cycles of M v = b (MGSolver::vCycle, MG.h:150-187); returns v."""
+        v = np.array(v, dtype=np.float64)
+        self._check(load().epr_mg_vcycle(self._h, level, _p(np.ascontiguousarray(M, np.float64)),
+                                         _p(np.ascontiguousarray(b, np.float64)), _p(v), gs_iters, cycles))
+        return v
+
+    def alternating_system(self, level, which):
+        """(M, b) of one alternating half-step: which 1 solves for y, 0 for x."""
+        M = np.zeros((self.nodes(level), 3 ** self.dim))
+        b = np.zeros(self.nodes(level))
+        self._check(load().epr_alternating_system(self._h, level, which, _p(M), _p(b)))
+        return M, b
+
+    def alternating_solve(self, level, iters=1, vcycles=1, gs_iters=2, single_level=False):
+        """AlternatingSolve (ExteriorPoissonSolvers.h:86-154) on the level's coefficients."""
+        self._check(load().epr_alternating_solve(self._h, level, iters, vcycles, gs_iters, int(single_level)))
+        return self.coefficients(level)
+
+    def biquadratic_fit(self, level, dx, dy, as_reference=False):
+        """3 x 3 coefficients q[i, j] of s^i t^j of E(x + s dx, y + t dy)."""
+        q = np.zeros((3, 3))
+        self._check(load().epr_biquadratic_fit(self._h, level, _p(np.ascontiguousarray(dx, np.float64)),
+                                               _p(np.ascontiguousarray(dy, np.float64)), int(as_reference), _p(q)))
+        return q
 
     def time_kernel(self, kernel: str, level: int, reps: int = 20) -> float:
         """Mean device time (ms) of one launch of a kernel family (CUDA events on the context's stream)."""

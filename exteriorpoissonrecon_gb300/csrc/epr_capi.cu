@@ -14,6 +14,8 @@
 #include "epr_common.cuh"
 #include "epr_context.h"
 #include "epr_kernels.h"
+#include "epr_mg.h"
+#include "epr_poly.h"
 #include "epr_setup.h"
 
 namespace {
@@ -124,6 +126,7 @@ Context::~Context()
         }
         release(red.partial); release(red.out); release(d_err); release(d_fit);
         setup.release(*this);
+        release_mg(*this);
         cudaStreamSynchronize(stream);
         cudaStreamDestroy(stream);
     }
@@ -721,6 +724,72 @@ int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, doubl
     }
     ctx->release(scratch); ctx->release(pair); ctx->release(out);
     EPR_RETURN(ctx, ok);
+}
+
+int epr_linear_gs(epr_ctx *ctx, int level, const double *M, const double *b, double *v, int iters)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!M || !b || !v || iters < 0) { ctx->fail(EPR_ERR_ARG, "bad arguments"); return EPR_ERR_ARG; }
+    EPR_RETURN(ctx, epr::linear_gs(*ctx, level, M, b, v, iters));
+}
+
+int epr_mg_vcycle(epr_ctx *ctx, int level, const double *M, const double *b, double *v, int gs_iters, int cycles)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!M || !b || !v || gs_iters < 0 || cycles < 0) { ctx->fail(EPR_ERR_ARG, "bad arguments"); return EPR_ERR_ARG; }
+    EPR_RETURN(ctx, epr::mg_vcycles(*ctx, level, M, b, v, gs_iters, cycles));
+}
+
+int epr_alternating_system(epr_ctx *ctx, int level, int which, double *M, double *b)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!M || !b || (which != 0 && which != 1)) { ctx->fail(EPR_ERR_ARG, "bad arguments"); return EPR_ERR_ARG; }
+    if (!ctx->have_system) { ctx->fail(EPR_ERR_STATE, "no system (call epr_build or epr_set_level_system)"); return EPR_ERR_STATE; }
+    EPR_RETURN(ctx, epr::alternating_system(*ctx, level, which, M, b));
+}
+
+int epr_alternating_solve(epr_ctx *ctx, int level, int iters, int vcycles, int gs_iters, int single_level)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (iters < 0 || vcycles < 0 || gs_iters < 0) { ctx->fail(EPR_ERR_ARG, "negative iteration count"); return EPR_ERR_ARG; }
+    if (!ctx->have_system) { ctx->fail(EPR_ERR_STATE, "no system (call epr_build or epr_set_level_system)"); return EPR_ERR_STATE; }
+    EPR_RETURN(ctx, epr::alternating_solve(*ctx, level, iters, vcycles, gs_iters, single_level != 0) &&
+                        ctx->cuda_ok(cudaStreamSynchronize(ctx->stream), "sync"));
+}
+
+int epr_biquadratic_fit(epr_ctx *ctx, int level, const double *dx, const double *dy, int as_reference, double *q9)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    if (!dx || !dy || !q9) { ctx->fail(EPR_ERR_ARG, "null argument"); return EPR_ERR_ARG; }
+    if (!ctx->have_system) { ctx->fail(EPR_ERR_STATE, "no system (call epr_build or epr_set_level_system)"); return EPR_ERR_STATE; }
+    epr::Level &L = ctx->levels[level];
+    std::vector<double> h(2 * L.N);
+    for (int64_t i = 0; i < L.N; i++) { h[2 * i] = dx[i]; h[2 * i + 1] = dy[i]; }
+    double *d = nullptr;
+    bool ok = ctx->alloc((void **)&d, sizeof(double) * 2 * L.N, "alloc direction") &&
+              ctx->cuda_ok(cudaMemcpyAsync(d, h.data(), sizeof(double) * 2 * L.N, cudaMemcpyHostToDevice, ctx->stream), "upload") &&
+              epr::biquadratic_fit(*ctx, level, d, as_reference != 0, q9);
+    ctx->release(d);
+    EPR_RETURN(ctx, ok);
+}
+
+int epr_step_size(const double *q9, double *s)
+{
+    if (!q9 || !s) { g_error = "null argument"; return EPR_ERR_ARG; }
+    *s = epr::poly::step_size(q9);
+    return std::isfinite(*s) ? EPR_OK : EPR_ERR_NUMERIC;
+}
+
+int epr_newton_update(const double *q9, int steps, double *st2)
+{
+    if (!q9 || !st2 || steps < 0) { g_error = "bad arguments"; return EPR_ERR_ARG; }
+    epr::poly::newton_update(q9, steps, st2);
+    return std::isfinite(st2[0]) && std::isfinite(st2[1]) ? EPR_OK : EPR_ERR_NUMERIC;
 }
 
 int epr_synchronize(epr_ctx *ctx)

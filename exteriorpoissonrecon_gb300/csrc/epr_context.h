@@ -12,6 +12,7 @@
 namespace epr {
 
 struct Context;
+struct MGHierarchy;
 
 // Device storage of one level of the hierarchy.
 struct Level
@@ -68,6 +69,7 @@ struct Context
     epr_stats stats{};
     int64_t launches = 0;  // kernels launched since the last epr_solve started
     Setup setup;
+    MGHierarchy *mg = nullptr;  // linear multigrid storage (epr_mg.cu), allocated on first use
 
     virtual ~Context();
     void fail(int code, const char *fmt, ...);

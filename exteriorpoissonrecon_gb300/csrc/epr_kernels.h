@@ -50,6 +50,10 @@ void launch_prolong(int coarseLevel, const Real *coarse, Real *fine, int add, cu
 template <int D, typename Real>
 void launch_restrict(int coarseLevel, const Real *fine, Real *coarse, cudaStream_t s);
 
+// coarse = P^T fine P of a column stencil (offset-major, double), fine level -> fineLevel - 1
+template <int D>
+void launch_galerkin(int fineLevel, const double *Mf, double *Mc, cudaStream_t s);
+
 // elementwise helpers
 template <typename Real>
 void launch_scale(Real *v, int64_t n, double s, cudaStream_t st);

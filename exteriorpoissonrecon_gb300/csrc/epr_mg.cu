@@ -1,7 +1,901 @@
-// Multigrid solver driver (filled in below the cascadic path).
+// Linear multigrid and the solvers built on it.
+//
+// Reference correspondence:
+//   linear GS sweep     GSRelaxer::operator()(b, x, mcIndices)        MG.h:57-72
+//   V-cycle             MGSolver ctor (Galerkin hierarchy) / vCycle   MG.h:81-187
+//   half-step systems   quadraticApproximation1/2 as AlternatingSolve uses them
+//                                                                     ExteriorPoissonSolvers.h:96-131
+//   alternating solve   AlternatingSolve                              ExteriorPoissonSolvers.h:86-154
+//   bi-quadratic fit    SingleCycleCascadicSystemEnergy::biQuadraticFit SystemEnergy.h:499-540
+//   line searches       stepSize / newtonUpdate                       SystemEnergy.h:256-303
+//
+// Layout.  The Galerkin hierarchy is built in double from natural offset-major column stencils
+// (coef[o * N + i]).  Each level is then re-laid out *colour-blocked* for relaxation: the nodes of
+// parity colour c are numbered j = 0 .. n_c - 1 (axis 0 slowest) and coefficient o of node j sits
+// at block_c + o * n_c + j, so one colour sweep streams its own coefficients contiguously (the
+// natural layout would touch every other 32-byte sector).  Vectors stay in natural order.  In the
+// float mode the colour-blocked copies are float, the coarsest level (resolution 1) is solved in
+// double, and the finest-level residual and update are double (iterative refinement), so a V-cycle
+// of M x = b computes x += V(b - M x) with V the float V-cycle of the residual equation from zero.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/epr.h"
+#include "epr_common.cuh"
 #include "epr_context.h"
+#include "epr_element.cuh"
+#include "epr_kernels.h"
+#include "epr_mg.h"
 
 namespace epr {
+
+namespace {
+
+constexpr int kThreads = 256;
+inline unsigned int blocks(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
+
+template <int D>
+struct ColourBlocks
+{
+    int64_t base[1 << D];   // first coefficient of colour c's block
+    int64_t count[1 << D];  // nodes of colour c
+};
+
+template <int D>
+ColourBlocks<D> colour_blocks(int level)
+{
+    Grid<D> g(level);
+    ColourBlocks<D> cb;
+    int64_t at = 0;
+    for (int c = 0; c < (1 << D); c++)
+    {
+        Colour<D> col(g, c);
+        cb.base[c] = at;
+        cb.count[c] = col.n;
+        at += col.n * Dims<D>::S;
+    }
+    return cb;
+}
+
+// neighbour of node i at stencil offset o, or -1 outside the grid
+template <int D>
+__device__ __forceinline__ int64_t neighbour(const Grid<D> &g, const int *I, int64_t i, int o)
+{
+    int64_t j = i, s = 1;
+    int t = o;
+#pragma unroll
+    for (int d = D - 1; d >= 0; d--)
+    {
+        int off = t % 3 - 1;
+        t /= 3;
+        int q = I[d] + off;
+        if (q < 0 || q > g.r) return -1;
+        j += off * s;
+        s *= g.r + 1;
+    }
+    return j;
+}
+
+// natural offset-major double stencil -> colour-blocked Real stencil; grid.y = colour
+template <int D, typename Real>
+__global__ void to_colour_blocks_kernel(int level, const double *M, ColourBlocks<D> cb, Real *out)
+{
+    const int c = blockIdx.y;
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= cb.count[c]) return;
+    Grid<D> g(level);
+    Colour<D> col(g, c);
+    int I[D];
+    col.node(j, I);
+    const int64_t i = g.node(I);
+    Real *dst = out + cb.base[c] + j;
+    const int64_t n = cb.count[c];
+    for (int o = 0; o < Dims<D>::S; o++) dst[o * n] = (Real)M[(int64_t)o * g.N + i];
+}
+
+// x_i += (b_i - sum_j M(j, i) x_j) / M(i, i) for the nodes of one colour (the GSRelaxer update,
+// which reads column i of M; M is symmetric)
+template <int D, typename Real>
+__global__ void __launch_bounds__(kThreads) linear_gs_colour_kernel(int level, int colour, const Real *Mc, int64_t n,
+                                                                     const Real *b, Real *x)
+{
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    Grid<D> g(level);
+    Colour<D> col(g, colour);
+    int I[D];
+    col.node(j, I);
+    const int64_t i = g.node(I);
+    Real s = 0;
+#pragma unroll 27
+    for (int o = 0; o < Dims<D>::S; o++)
+    {
+        int64_t k = neighbour<D>(g, I, i, o);
+        if (k >= 0) s += Mc[o * n + j] * x[k];
+    }
+    x[i] += (b[i] - s) / Mc[Dims<D>::CENTER * n + j];
+}
+
+// r = b - M x over every node, colour-blocked coefficients; grid.y = colour
+template <int D, typename Real>
+__global__ void __launch_bounds__(kThreads) residual_cb_kernel(int level, const Real *M, ColourBlocks<D> cb, const Real *b,
+                                                                const Real *x, Real *r)
+{
+    const int c = blockIdx.y;
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t n = cb.count[c];
+    if (j >= n) return;
+    Grid<D> g(level);
+    Colour<D> col(g, c);
+    int I[D];
+    col.node(j, I);
+    const int64_t i = g.node(I);
+    const Real *Mc = M + cb.base[c];
+    Real s = 0;
+#pragma unroll 27
+    for (int o = 0; o < Dims<D>::S; o++)
+    {
+        int64_t k = neighbour<D>(g, I, i, o);
+        if (k >= 0) s += Mc[o * n + j] * x[k];
+    }
+    r[i] = b[i] - s;
+}
+
+// r = b - M x with the natural double stencil (the refinement residual of the float mode)
+template <int D>
+__global__ void __launch_bounds__(kThreads) residual_nat_kernel(int level, const double *M, const double *b, const double *x,
+                                                                 float *r)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    Grid<D> g(level);
+    if (i >= g.N) return;
+    int I[D];
+    g.node(i, I);
+    double s = 0;
+#pragma unroll 27
+    for (int o = 0; o < Dims<D>::S; o++)
+    {
+        int64_t k = neighbour<D>(g, I, i, o);
+        if (k >= 0) s += M[o * g.N + i] * x[k];
+    }
+    r[i] = (float)(b[i] - s);
+}
+
+// coarse = P^T fine (scalar)
+template <int D, typename Real>
+__global__ void restrict1_kernel(int coarseLevel, const Real *fine, Real *coarse)
+{
+    Grid<D> gc(coarseLevel), gf(coarseLevel + 1);
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= gc.N) return;
+    int I[D];
+    gc.node(i, I);
+    Real s = 0;
+    for (int o = 0; o < Dims<D>::S; o++)
+    {
+        int off[D], F[D];
+        stencil_offset<D>(o, off);
+        bool ok = true;
+        Real w = 1;
+#pragma unroll
+        for (int d = 0; d < D; d++)
+        {
+            F[d] = 2 * I[d] + off[d];
+            ok = ok && F[d] >= 0 && F[d] <= gf.r;
+            if (off[d]) w *= (Real)0.5;
+        }
+        if (ok) s += w * fine[gf.node(F)];
+    }
+    coarse[i] = s;
+}
+
+// fine += P coarse (scalar)
+template <int D, typename Real>
+__global__ void prolong_add1_kernel(int coarseLevel, const Real *coarse, Real *fine)
+{
+    Grid<D> gc(coarseLevel), gf(coarseLevel + 1);
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= gf.N) return;
+    int F[D];
+    gf.node(i, F);
+    Real s = 0;
+#pragma unroll
+    for (int c = 0; c < (1 << D); c++)
+    {
+        bool use = true;
+        Real w = 1;
+        int I[D];
+#pragma unroll
+        for (int d = 0; d < D; d++)
+        {
+            int bit = (c >> d) & 1;
+            if (F[d] & 1) { I[d] = (F[d] >> 1) + bit; w *= (Real)0.5; }
+            else { I[d] = F[d] >> 1; if (bit) use = false; }
+        }
+        if (use) s += w * coarse[gc.node(I)];
+    }
+    fine[i] += s;
+}
+
+// Exact solve at resolution 1 (2^D nodes) by a dense LDL^T factorisation in double, one thread;
+// stands in for the SimplicialLDLT of the coarsest MGSolver level (MG.h:105, 131).
+template <int D, typename Real>
+__global__ void coarse_solve_kernel(const double *M, const Real *b, Real *x)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    constexpr int N = 1 << D;
+    Grid<D> g(0);
+    double A[N][N], L[N][N], Dg[N], z[N];
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++) { A[i][j] = 0; L[i][j] = 0; }
+    for (int i = 0; i < N; i++)
+    {
+        int I[D];
+        g.node(i, I);
+        for (int o = 0; o < Dims<D>::S; o++)
+        {
+            int64_t k = neighbour<D>(g, I, i, o);
+            if (k >= 0) A[k][i] = M[(int64_t)o * N + i];
+        }
+    }
+    for (int j = 0; j < N; j++)
+    {
+        double d = A[j][j];
+        for (int k = 0; k < j; k++) d -= L[j][k] * L[j][k] * Dg[k];
+        Dg[j] = d;
+        L[j][j] = 1.;
+        for (int i = j + 1; i < N; i++)
+        {
+            double v = A[i][j];
+            for (int k = 0; k < j; k++) v -= L[i][k] * L[j][k] * Dg[k];
+            L[i][j] = v / d;
+        }
+    }
+    for (int i = 0; i < N; i++)
+    {
+        double v = (double)b[i];
+        for (int k = 0; k < i; k++) v -= L[i][k] * z[k];
+        z[i] = v;
+    }
+    for (int i = 0; i < N; i++) z[i] /= Dg[i];
+    double xs[N];
+    for (int ii = N - 1; ii >= 0; ii--)
+    {
+        double v = z[ii];
+        for (int k = ii + 1; k < N; k++) v -= L[k][ii] * xs[k];
+        xs[ii] = v;
+    }
+    for (int i = 0; i < N; i++) x[i] = (Real)xs[i];
+}
+
+template <typename Real>
+__global__ void component_get_kernel(const double *xy, int which, int64_t n, Real *v)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (Real)xy[2 * i + which];
+}
+__global__ void component_set_kernel(double *xy, int which, int64_t n, const double *v)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) xy[2 * i + which] = v[i];
+}
+__global__ void add_f2d_kernel(double *y, const float *x, int64_t n)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] += (double)x[i];
+}
+
+// ---------------------------------------------------------------------------------------------
+// Half-step systems of the alternating solve.  For a fixed field f the wedge is linear in the
+// other one: |W(f, v)|^2 = v^T G_f v with G_f(j, i) = int <W(f, phi_j), W(f, phi_i)>.  The Gram
+// column of node i is integrated per incident element in the canonical orientation (node i at
+// corner 0; mirroring flips the sign of both W(f, phi_j) and W(f, phi_i), so each product keeps
+// its sign) with the same exact Gauss rule as the energy.
+// ---------------------------------------------------------------------------------------------
+template <int D, int K>
+__device__ __forceinline__ void component_gram(const double *f, double *loc)
+{
+    using Cp = Component<D, K>;
+    constexpr int M = Cp::M;
+    constexpr int NG = ipow(3, M);
+    constexpr int C = 1 << D;
+    double fP[2 * NG], fQ[2 * NG];
+    derivative_table<D, K, true, double>(f, fP);
+    derivative_table<D, K, false, double>(f, fQ);
+#pragma unroll
+    for (int go = 0; go < NG; go++)
+    {
+        const double wo = other_weight<M>(go);
+#pragma unroll
+        for (int gp = 0; gp < 2; gp++)
+#pragma unroll
+            for (int gq = 0; gq < 2; gq++)
+            {
+                const double w = Gauss::W2(gp) * Gauss::W2(gq) * wo;
+                const double xp = fP[gq * NG + go], xq = fQ[gp * NG + go];
+                double V[C];
+#pragma unroll
+                for (int B = 0; B < C; B++)
+                {
+                    const int bP = cbit<D>(B, Cp::P), bQ = cbit<D>(B, Cp::Q);
+                    double lo;
+                    if constexpr (M == 1) lo = hat3<double>(cbit<D>(B, Cp::other(0)), go);
+                    else lo = hat3<double>(cbit<D>(B, Cp::other(0)), go / 3) * hat3<double>(cbit<D>(B, Cp::other(1)), go % 3);
+                    const double phP = (bP ? 1. : -1.) * hat2<double>(bQ, gq) * lo;
+                    const double phQ = (bQ ? 1. : -1.) * hat2<double>(bP, gp) * lo;
+                    V[B] = phP * xq - xp * phQ;
+                }
+#pragma unroll
+                for (int B = 0; B < C; B++) loc[B] += w * V[0] * V[B];
+            }
+    }
+}
+
+template <int D>
+__device__ __noinline__ void element_gram_canonical(const double *f, double *loc)
+{
+#pragma unroll
+    for (int B = 0; B < (1 << D); B++) loc[B] = 0;
+    component_gram<D, 0>(f, loc);
+    component_gram<D, 1>(f, loc);
+    component_gram<D, 2>(f, loc);
+    if constexpr (D == 4)
+    {
+        component_gram<D, 3>(f, loc);
+        component_gram<D, 4>(f, loc);
+        component_gram<D, 5>(f, loc);
+    }
+}
+
+// sum_j B(j, i) v_j over the off-diagonal neighbours (natural offset-major B)
+template <int D>
+__device__ __forceinline__ double b_column_dot(const Grid<D> &g, const int *I, int64_t i, const double *B, const double *xy,
+                                               int comp)
+{
+    double s = 0;
+    for (int o = 0; o < Dims<D>::S; o++)
+    {
+        if (o == Dims<D>::CENTER) continue;
+        int64_t k = neighbour<D>(g, I, i, o);
+        if (k >= 0) s += B[(int64_t)o * g.N + i] * xy[2 * k + comp];
+    }
+    return s;
+}
+
+// M = 2 (G_f + A) and b of one half-step: which 1 -> y free (f = x, b = 2 B x), which 0 -> x
+// free (f = y, b = 2 B^T y); B x = -(column sums) since B is antisymmetric.
+template <int D>
+__global__ void __launch_bounds__(128) alternating_system_kernel(int level, const double *xy, int which, const double *A,
+                                                                  const double *B, double *M, double *b)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    Grid<D> g(level);
+    if (i >= g.N) return;
+    constexpr int S = Dims<D>::S;
+    int I[D];
+    g.node(i, I);
+    const int fc = which ? 0 : 1;  // component of the fixed field
+    double col[S];
+#pragma unroll
+    for (int o = 0; o < S; o++) col[o] = 0;
+#pragma unroll 1
+    for (int mirror = 0; mirror < (1 << D); mirror++)
+    {
+        // element whose corner `mirror` is node i (bit D-1-d of mirror: node is the upper corner on axis d)
+        bool ok = true;
+        for (int d = 0; d < D; d++)
+        {
+            int e = I[d] - cbit<D>(mirror, d);
+            ok = ok && e >= 0 && e < g.r;
+        }
+        if (!ok) continue;
+        double f[1 << D], loc[1 << D];
+#pragma unroll
+        for (int cc = 0; cc < (1 << D); cc++)
+        {
+            int64_t j = i, s = 1;
+            for (int d = D - 1; d >= 0; d--)
+            {
+                int step = cbit<D>(cc, d);
+                j += (cbit<D>(mirror, d) ? -step : step) * s;
+                s *= g.r + 1;
+            }
+            f[cc] = xy[2 * j + fc];
+        }
+        element_gram_canonical<D>(f, loc);
+#pragma unroll
+        for (int B2 = 0; B2 < (1 << D); B2++)
+        {
+            int o = 0;
+            for (int d = 0; d < D; d++) o = o * 3 + 1 + (cbit<D>(mirror, d) ? -cbit<D>(B2, d) : cbit<D>(B2, d));
+            col[o] += loc[B2];
+        }
+    }
+    const double sc = (D == 3 ? (double)g.r : 1.0) * 0.5;
+    for (int o = 0; o < S; o++) M[(int64_t)o * g.N + i] = 2. * (col[o] * sc + A[(int64_t)o * g.N + i]);
+    const double bd = b_column_dot<D>(g, I, i, B, xy, which ? 0 : 1);
+    b[i] = which ? -2. * bd : 2. * bd;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Bi-quadratic fit: 10 wedge products per element and 10 stencil forms per node, block sums
+// ---------------------------------------------------------------------------------------------
+constexpr int kBQ = 20;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int D, int K>
+__device__ __forceinline__ void component_biquad(const double *x, const double *y, const double *dx, const double *dy,
+                                                 double *acc)
+{
+    constexpr int NG = ipow(3, D - 2);
+    double xP[2 * NG], xQ[2 * NG], yP[2 * NG], yQ[2 * NG], XP[2 * NG], XQ[2 * NG], YP[2 * NG], YQ[2 * NG];
+    derivative_table<D, K, true, double>(x, xP);
+    derivative_table<D, K, false, double>(x, xQ);
+    derivative_table<D, K, true, double>(y, yP);
+    derivative_table<D, K, false, double>(y, yQ);
+    derivative_table<D, K, true, double>(dx, XP);
+    derivative_table<D, K, false, double>(dx, XQ);
+    derivative_table<D, K, true, double>(dy, YP);
+    derivative_table<D, K, false, double>(dy, YQ);
+#pragma unroll
+    for (int gp = 0; gp < 2; gp++)
+#pragma unroll
+        for (int gq = 0; gq < 2; gq++)
+#pragma unroll
+            for (int go = 0; go < NG; go++)
+            {
+                const double w = Gauss::W2(gp) * Gauss::W2(gq) * other_weight<D - 2>(go);
+                const int ip = gq * NG + go, iq = gp * NG + go;
+                // W(u, v) = d_P v d_Q u - d_P u d_Q v (reference units, the 1/2 folded into the scale)
+                const double Wxy = yP[ip] * xQ[iq] - xP[ip] * yQ[iq];
+                const double WXy = yP[ip] * XQ[iq] - XP[ip] * yQ[iq];
+                const double WxY = YP[ip] * xQ[iq] - xP[ip] * YQ[iq];
+                const double WXY = YP[ip] * XQ[iq] - XP[ip] * YQ[iq];
+                acc[0] += w * WXY * WXY;
+                acc[1] += w * WXY * WXy;
+                acc[2] += w * WXY * WxY;
+                acc[3] += w * WXy * WXy;
+                acc[4] += w * WxY * WxY;
+                acc[5] += w * WXy * WxY;
+                acc[6] += w * WXY * Wxy;
+                acc[7] += w * WXy * Wxy;
+                acc[8] += w * WxY * Wxy;
+                acc[9] += w * Wxy * Wxy;
+            }
+}
+
+// xy: current (x, y) pairs; dxy: direction pairs.  A = R + dWeight K; K2 (optional) adds kw K.
+template <int D>
+__global__ void __launch_bounds__(128) biquad_kernel(int level, const double *xy, const double *dxy, const double *A,
+                                                      const double *K2, double kw, const double *B, double *partial)
+{
+    Grid<D> g(level);
+    double acc[kBQ];
+#pragma unroll
+    for (int k = 0; k < kBQ; k++) acc[k] = 0;
+    const int64_t total = g.N > g.NE ? g.N : g.NE;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x)
+    {
+        if (t < g.NE)
+        {
+            int E[D];
+            g.elem(t, E);
+            double x[1 << D], y[1 << D], X[1 << D], Y[1 << D];
+            int64_t base = 0;
+            for (int d = 0; d < D; d++) base = base * (g.r + 1) + E[d];
+#pragma unroll
+            for (int c = 0; c < (1 << D); c++)
+            {
+                int64_t j = base;
+                for (int d = 0; d < D; d++) j += cbit<D>(c, d) * g.stride(d);
+                x[c] = xy[2 * j];
+                y[c] = xy[2 * j + 1];
+                X[c] = dxy[2 * j];
+                Y[c] = dxy[2 * j + 1];
+            }
+            component_biquad<D, 0>(x, y, X, Y, acc);
+            component_biquad<D, 1>(x, y, X, Y, acc);
+            component_biquad<D, 2>(x, y, X, Y, acc);
+            if constexpr (D == 4)
+            {
+                component_biquad<D, 3>(x, y, X, Y, acc);
+                component_biquad<D, 4>(x, y, X, Y, acc);
+                component_biquad<D, 5>(x, y, X, Y, acc);
+            }
+        }
+        if (t < g.N)
+        {
+            int I[D];
+            g.node(t, I);
+            double Adx = 0, Ax = 0, Ady = 0, Ay = 0, Bdy = 0, By = 0;
+            for (int o = 0; o < Dims<D>::S; o++)
+            {
+                int64_t k = neighbour<D>(g, I, t, o);
+                if (k < 0) continue;
+                double a = A[(int64_t)o * g.N + t];
+                if (K2) a += kw * K2[(int64_t)o * g.N + t];
+                const double b = B[(int64_t)o * g.N + t];
+                Adx += a * dxy[2 * k];
+                Ax += a * xy[2 * k];
+                Ady += a * dxy[2 * k + 1];
+                Ay += a * xy[2 * k + 1];
+                Bdy += b * dxy[2 * k + 1];
+                By += b * xy[2 * k + 1];
+            }
+            const double xi = xy[2 * t], yi = xy[2 * t + 1], Xi = dxy[2 * t], Yi = dxy[2 * t + 1];
+            acc[10] += Xi * Adx;  // dx A dx
+            acc[11] += xi * Adx;  // x A dx
+            acc[12] += xi * Ax;   // x A x
+            acc[13] += Yi * Ady;  // dy A dy
+            acc[14] += yi * Ady;  // y A dy
+            acc[15] += yi * Ay;   // y A y
+            acc[16] += Xi * Bdy;  // dy^T B dx
+            acc[17] += xi * Bdy;  // dy^T B x
+            acc[18] += Xi * By;   // y^T B dx
+            acc[19] += xi * By;   // y^T B x
+        }
+    }
+    __shared__ double sh[kBQ][4];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kBQ; k++)
+    {
+        double v = warp_sum(acc[k]);
+        if (lane == 0) sh[k][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kBQ)
+    {
+        double s = 0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += sh[threadIdx.x][q];
+        partial[(int64_t)blockIdx.x * kBQ + threadIdx.x] = s;
+    }
+}
+
+__global__ void biquad_finish_kernel(const double *partial, int nblocks, double *out)
+{
+    const int v = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (v >= kBQ) return;
+    double s = 0;
+    for (int b = lane; b < nblocks; b += 32) s += partial[(int64_t)b * kBQ + v];
+    s = warp_sum(s);
+    if (lane == 0) out[v] = s;
+}
+
+}  // namespace
+
+// =============================================================================================
+// Host side
+// =============================================================================================
+
+// Per-level storage of the linear multigrid
+struct MGLevel
+{
+    int64_t N = 0;
+    double *M64 = nullptr;  // natural offset-major stencil (double)
+    void *Mcb = nullptr;    // colour-blocked stencil (working precision)
+    void *x = nullptr, *b = nullptr, *r = nullptr;  // working-precision vectors
+};
+
+struct MGHierarchy
+{
+    int top = -1;
+    bool fp32 = false;
+    std::vector<MGLevel> L;
+    double *x64 = nullptr, *b64 = nullptr;  // finest-level double vectors (solution, right-hand side)
+};
+
+void release_mg(Context &c)
+{
+    if (!c.mg) return;
+    for (MGLevel &l : c.mg->L)
+    {
+        c.release(l.M64); c.release(l.Mcb); c.release(l.x); c.release(l.b); c.release(l.r);
+    }
+    c.release(c.mg->x64);
+    c.release(c.mg->b64);
+    delete c.mg;
+    c.mg = nullptr;
+}
+
+// (re)allocates the hierarchy for levels 0..top in the context's working precision
+static bool mg_prepare(Context &c, int top)
+{
+    const bool fp32 = c.P.precision == EPR_FP32;
+    if (c.mg && c.mg->top >= top && c.mg->fp32 == fp32) return true;
+    release_mg(c);
+    c.mg = new MGHierarchy;
+    MGHierarchy &h = *c.mg;
+    h.top = top;
+    h.fp32 = fp32;
+    h.L.resize(top + 1);
+    const size_t S = (size_t)c.stencil(), rs = fp32 ? sizeof(float) : sizeof(double);
+    for (int l = 0; l <= top; l++)
+    {
+        MGLevel &m = h.L[l];
+        m.N = c.nodes(l);
+        if (!c.alloc((void **)&m.M64, sizeof(double) * S * m.N, "alloc mg stencil") ||
+            !c.alloc(&m.Mcb, rs * S * m.N, "alloc mg stencil") || !c.alloc(&m.x, rs * m.N, "alloc mg x") ||
+            !c.alloc(&m.b, rs * m.N, "alloc mg b") || !c.alloc(&m.r, rs * m.N, "alloc mg r"))
+            return false;
+    }
+    const int64_t N = h.L[top].N;
+    return c.alloc((void **)&h.x64, sizeof(double) * N, "alloc mg x64") && c.alloc((void **)&h.b64, sizeof(double) * N, "alloc mg b64");
+}
+
+template <typename F>
+static int mg_dim(Context &c, F &&f)
+{
+    if (c.dim == 3) return f(std::integral_constant<int, 3>{});
+    return f(std::integral_constant<int, 4>{});
+}
+
+// Galerkin hierarchy of L[top].M64 down to level 0 and the colour-blocked copies of levels
+// lo..top (lo = top for relaxation only)
+static bool mg_build(Context &c, int top, int lo)
+{
+    MGHierarchy &h = *c.mg;
+    mg_dim(c, [&](auto dd) {
+        constexpr int D = decltype(dd)::value;
+        if (lo < top)
+            for (int l = top; l > 0; l--) launch_galerkin<D>(l, h.L[l].M64, h.L[l - 1].M64, c.stream);
+        for (int l = std::max(lo, 1); l <= top; l++)
+        {
+            ColourBlocks<D> cb = colour_blocks<D>(l);
+            dim3 grid(blocks(cb.count[0]), 1 << D);
+            if (h.fp32) to_colour_blocks_kernel<D, float><<<grid, kThreads, 0, c.stream>>>(l, h.L[l].M64, cb, (float *)h.L[l].Mcb);
+            else to_colour_blocks_kernel<D, double><<<grid, kThreads, 0, c.stream>>>(l, h.L[l].M64, cb, (double *)h.L[l].Mcb);
+            c.launches++;
+        }
+        c.launches += (lo < top) ? top : 0;
+        return 0;
+    });
+    return c.launch_ok("mg hierarchy");
+}
+
+template <int D, typename Real>
+static void mg_sweeps(Context &c, int l, const Real *b, Real *x, int iters)
+{
+    MGLevel &m = c.mg->L[l];
+    ColourBlocks<D> cb = colour_blocks<D>(l);
+    for (int it = 0; it < iters; it++)
+        for (int col = 0; col < (1 << D); col++)
+        {
+            linear_gs_colour_kernel<D, Real><<<blocks(cb.count[col]), kThreads, 0, c.stream>>>(
+                l, col, (const Real *)m.Mcb + cb.base[col], cb.count[col], b, x);
+            c.launches++;
+        }
+}
+
+// One V-cycle (MGSolver::vCycle, MG.h:150-187) of M x = b on levels 0..top with the vectors of
+// L[top] as b and x.
+template <int D, typename Real>
+static void mg_vcycle(Context &c, int top, int iters)
+{
+    MGHierarchy &h = *c.mg;
+    for (int l = top; l > 0; l--)
+    {
+        MGLevel &m = h.L[l], &mc = h.L[l - 1];
+        mg_sweeps<D, Real>(c, l, (const Real *)m.b, (Real *)m.x, iters);
+        ColourBlocks<D> cb = colour_blocks<D>(l);
+        residual_cb_kernel<D, Real><<<dim3(blocks(cb.count[0]), 1 << D), kThreads, 0, c.stream>>>(
+            l, (const Real *)m.Mcb, cb, (const Real *)m.b, (const Real *)m.x, (Real *)m.r);
+        restrict1_kernel<D, Real><<<blocks(mc.N), kThreads, 0, c.stream>>>(l - 1, (const Real *)m.r, (Real *)mc.b);
+        cudaMemsetAsync(mc.x, 0, sizeof(Real) * mc.N, c.stream);
+        c.launches += 2;
+    }
+    coarse_solve_kernel<D, Real><<<1, 32, 0, c.stream>>>(h.L[0].M64, (const Real *)h.L[0].b, (Real *)h.L[0].x);
+    c.launches++;
+    for (int l = 1; l <= top; l++)
+    {
+        MGLevel &m = h.L[l];
+        prolong_add1_kernel<D, Real><<<blocks(m.N), kThreads, 0, c.stream>>>(l - 1, (const Real *)h.L[l - 1].x, (Real *)m.x);
+        c.launches++;
+        mg_sweeps<D, Real>(c, l, (const Real *)m.b, (Real *)m.x, iters);
+    }
+}
+
+// cycles V-cycles of L[top].M64 x64 = b64 (x64 updated in place); in the float mode each cycle
+// relaxes the residual equation in float and adds the correction in double.
+static bool mg_cycles(Context &c, int top, int iters, int cycles)
+{
+    MGHierarchy &h = *c.mg;
+    MGLevel &m = h.L[top];
+    mg_dim(c, [&](auto dd) {
+        constexpr int D = decltype(dd)::value;
+        for (int k = 0; k < cycles; k++)
+        {
+            if (!h.fp32)
+            {
+                cudaMemcpyAsync(m.x, h.x64, sizeof(double) * m.N, cudaMemcpyDeviceToDevice, c.stream);
+                cudaMemcpyAsync(m.b, h.b64, sizeof(double) * m.N, cudaMemcpyDeviceToDevice, c.stream);
+                if (top == 0)
+                {
+                    coarse_solve_kernel<D, double><<<1, 32, 0, c.stream>>>(h.L[0].M64, (const double *)m.b, (double *)m.x);
+                    c.launches++;
+                }
+                else mg_vcycle<D, double>(c, top, iters);
+                cudaMemcpyAsync(h.x64, m.x, sizeof(double) * m.N, cudaMemcpyDeviceToDevice, c.stream);
+            }
+            else
+            {
+                residual_nat_kernel<D><<<blocks(m.N), kThreads, 0, c.stream>>>(top, m.M64, h.b64, h.x64, (float *)m.b);
+                cudaMemsetAsync(m.x, 0, sizeof(float) * m.N, c.stream);
+                if (top == 0) coarse_solve_kernel<D, float><<<1, 32, 0, c.stream>>>(h.L[0].M64, (const float *)m.b, (float *)m.x);
+                else mg_vcycle<D, float>(c, top, iters);
+                add_f2d_kernel<<<blocks(m.N), kThreads, 0, c.stream>>>(h.x64, (const float *)m.x, m.N);
+                c.launches += 3;
+            }
+        }
+        return 0;
+    });
+    return c.launch_ok("mg v-cycle");
+}
+
+// iters coloured GS sweeps of L[top].M64 x64 = b64 (colour-blocked copy of top must be current)
+static bool mg_relax(Context &c, int top, int iters)
+{
+    MGHierarchy &h = *c.mg;
+    MGLevel &m = h.L[top];
+    mg_dim(c, [&](auto dd) {
+        constexpr int D = decltype(dd)::value;
+        if (!h.fp32)
+        {
+            mg_sweeps<D, double>(c, top, h.b64, h.x64, iters);
+        }
+        else
+        {
+            launch_convert_d2f(h.x64, (float *)m.x, m.N, c.stream);
+            launch_convert_d2f(h.b64, (float *)m.b, m.N, c.stream);
+            mg_sweeps<D, float>(c, top, (const float *)m.b, (float *)m.x, iters);
+            launch_convert_f2d((const float *)m.x, h.x64, m.N, c.stream);
+            c.launches += 3;
+        }
+        return 0;
+    });
+    return c.launch_ok("mg relax");
+}
+
+// host node-major stencil -> L[top].M64, host vectors -> b64 / x64
+static bool mg_upload(Context &c, int top, const double *M, const double *b, const double *x)
+{
+    MGHierarchy &h = *c.mg;
+    const int64_t N = h.L[top].N;
+    const size_t S = (size_t)c.stencil();
+    std::vector<double> t(S * N);
+    for (int64_t i = 0; i < N; i++)
+        for (size_t o = 0; o < S; o++) t[o * N + i] = M[i * S + o];
+    return c.cuda_ok(cudaMemcpyAsync(h.L[top].M64, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, c.stream), "upload M") &&
+           c.cuda_ok(cudaMemcpyAsync(h.b64, b, sizeof(double) * N, cudaMemcpyHostToDevice, c.stream), "upload b") &&
+           c.cuda_ok(cudaMemcpyAsync(h.x64, x, sizeof(double) * N, cudaMemcpyHostToDevice, c.stream), "upload x") &&
+           c.cuda_ok(cudaStreamSynchronize(c.stream), "sync");
+}
+
+bool linear_gs(Context &c, int level, const double *M, const double *b, double *x, int iters)
+{
+    if (!mg_prepare(c, level) || !mg_upload(c, level, M, b, x) || !mg_build(c, level, level) || !mg_relax(c, level, iters)) return false;
+    return c.cuda_ok(cudaMemcpyAsync(x, c.mg->x64, sizeof(double) * c.mg->L[level].N, cudaMemcpyDeviceToHost, c.stream), "download x") &&
+           c.cuda_ok(cudaStreamSynchronize(c.stream), "sync");
+}
+
+bool mg_vcycles(Context &c, int level, const double *M, const double *b, double *x, int iters, int cycles)
+{
+    if (!mg_prepare(c, level) || !mg_upload(c, level, M, b, x) || !mg_build(c, level, 0) || !mg_cycles(c, level, iters, cycles)) return false;
+    return c.cuda_ok(cudaMemcpyAsync(x, c.mg->x64, sizeof(double) * c.mg->L[level].N, cudaMemcpyDeviceToHost, c.stream), "download x") &&
+           c.cuda_ok(cudaStreamSynchronize(c.stream), "sync");
+}
+
+// assembles the half-step system of `which` from the level's double coefficients into
+// L[level].M64 and b64
+static bool assemble_system(Context &c, int level, int which)
+{
+    MGHierarchy &h = *c.mg;
+    Level &Lv = c.levels[level];
+    mg_dim(c, [&](auto dd) {
+        constexpr int D = decltype(dd)::value;
+        alternating_system_kernel<D><<<blocks(Lv.N, 128), 128, 0, c.stream>>>(level, Lv.xy64, which, Lv.A64, Lv.B64,
+                                                                               h.L[level].M64, h.b64);
+        return 0;
+    });
+    c.launches++;
+    return c.launch_ok("alternating system");
+}
+
+bool alternating_system(Context &c, int level, int which, double *M, double *b)
+{
+    if (!mg_prepare(c, level) || !c.pull_xy(level) || !assemble_system(c, level, which)) return false;
+    const int64_t N = c.levels[level].N;
+    const size_t S = (size_t)c.stencil();
+    std::vector<double> t(S * N);
+    if (!c.cuda_ok(cudaMemcpyAsync(t.data(), c.mg->L[level].M64, sizeof(double) * t.size(), cudaMemcpyDeviceToHost, c.stream), "download M") ||
+        !c.cuda_ok(cudaMemcpyAsync(b, c.mg->b64, sizeof(double) * N, cudaMemcpyDeviceToHost, c.stream), "download b") ||
+        !c.cuda_ok(cudaStreamSynchronize(c.stream), "sync"))
+        return false;
+    for (int64_t i = 0; i < N; i++)
+        for (size_t o = 0; o < S; o++) M[i * S + o] = t[o * N + i];
+    return true;
+}
+
+// AlternatingSolve (ExteriorPoissonSolvers.h:86-154) on the level's coefficients: iters rounds of
+// (y with x fixed, then x with y fixed), each vCycles V-cycles of gsIters relaxations (MULTIGRID)
+// or gsIters * vCycles sweeps (SINGLE_LEVEL).
+bool alternating_solve(Context &c, int level, int iters, int vcycles, int gsIters, bool singleLevel)
+{
+    if (!mg_prepare(c, level) || !c.pull_xy(level)) return false;
+    MGHierarchy &h = *c.mg;
+    Level &Lv = c.levels[level];
+    for (int it = 0; it < iters; it++)
+        for (int which = 1; which >= 0; which--)
+        {
+            if (!assemble_system(c, level, which)) return false;
+            component_get_kernel<double><<<blocks(Lv.N), kThreads, 0, c.stream>>>(Lv.xy64, which, Lv.N, h.x64);
+            c.launches++;
+            bool ok = singleLevel ? (mg_build(c, level, level) && mg_relax(c, level, gsIters * vcycles))
+                                  : (mg_build(c, level, 0) && mg_cycles(c, level, gsIters, vcycles));
+            if (!ok) return false;
+            component_set_kernel<<<blocks(Lv.N), kThreads, 0, c.stream>>>(Lv.xy64, which, Lv.N, h.x64);
+            c.launches++;
+        }
+    if (!c.push_xy(level)) return false;
+    return c.launch_ok("alternating solve");
+}
+
+// q[i*3+j]: coefficient of s^i t^j of E(x + s dx, y + t dy) at the level's coefficients
+bool biquadratic_fit(Context &c, int level, const double *ddxy, bool asReference, double *q)
+{
+    if (!c.pull_xy(level)) return false;
+    Level &Lv = c.levels[level];
+    const size_t S = (size_t)c.stencil();
+    const int nb = 1024;
+    double *partial = nullptr, *out = nullptr, *K = nullptr;
+    bool ok = c.alloc((void **)&partial, sizeof(double) * kBQ * nb, "alloc partial") && c.alloc((void **)&out, sizeof(double) * kBQ, "alloc out");
+    if (ok && asReference)
+        ok = c.alloc((void **)&K, sizeof(double) * S * Lv.N, "alloc K") &&
+             c.cuda_ok(cudaMemsetAsync(K, 0, sizeof(double) * S * Lv.N, c.stream), "memset K") && add_dirichlet_to(c, level, K, 1.0);
+    double h[kBQ];
+    if (ok)
+    {
+        mg_dim(c, [&](auto dd) {
+            constexpr int D = decltype(dd)::value;
+            biquad_kernel<D><<<nb, 128, 0, c.stream>>>(level, Lv.xy64, ddxy, Lv.A64, K, 1.0 - c.P.d_weight, Lv.B64, partial);
+            biquad_finish_kernel<<<1, 32 * kBQ, 0, c.stream>>>(partial, nb, out);
+            return 0;
+        });
+        c.launches += 2;
+        ok = c.launch_ok("biquadratic fit") && c.cuda_ok(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, c.stream), "copy") &&
+             c.cuda_ok(cudaStreamSynchronize(c.stream), "sync");
+    }
+    c.release(partial); c.release(out); c.release(K);
+    if (!ok) return false;
+    const double sc = (c.dim == 3 ? (double)(1 << level) : 1.0) * 0.5;
+    double w[10];
+    for (int k = 0; k < 10; k++) w[k] = h[k] * sc;
+    for (int k = 0; k < 9; k++) q[k] = 0;
+    auto Q = [&](int i, int j) -> double & { return q[i * 3 + j]; };
+    Q(2, 2) += w[0];
+    Q(2, 1) += 2 * w[1];
+    Q(1, 2) += 2 * (asReference ? w[6] : w[2]);
+    Q(2, 0) += w[3];
+    Q(0, 2) += w[4];
+    Q(1, 1) += 2 * w[5] + 2 * w[6];
+    Q(1, 0) += 2 * w[7];
+    Q(0, 1) += 2 * w[8];
+    Q(0, 0) += w[9];
+    Q(2, 0) += h[10]; Q(1, 0) += 2 * h[11]; Q(0, 0) += h[12];
+    Q(0, 2) += h[13]; Q(0, 1) += 2 * h[14]; Q(0, 0) += h[15];
+    Q(1, 1) += -2 * h[16]; Q(0, 1) += -2 * h[17]; Q(1, 0) += -2 * h[18]; Q(0, 0) += -2 * h[19];
+    Q(0, 0) += c.c;
+    return true;
+}
 
 bool solve_multigrid(Context &c)
 {

@@ -1279,6 +1279,16 @@ bool Setup::get(Context &c, const std::string &name, double *out, size_t cap, si
     return false;
 }
 
+// Galerkin coarsening of any column stencil (used by the linear multigrid of epr_mg.cu)
+template <int D>
+void launch_galerkin(int fineLevel, const double *Mf, double *Mc, cudaStream_t s)
+{
+    Grid<D> gc(fineLevel - 1);
+    galerkin_kernel<D><<<nblocks(gc.N, 64), 64, 0, s>>>(fineLevel, Mf, Mc);
+}
+template void launch_galerkin<3>(int, const double *, double *, cudaStream_t);
+template void launch_galerkin<4>(int, const double *, double *, cudaStream_t);
+
 void Setup::release(Context &c)
 {
     c.release(pos); c.release(skew); c.release(order); c.release(cellKey); c.release(cellStart); c.release(cellOfFinest);

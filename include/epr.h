@@ -28,6 +28,19 @@
  *   epr_gn_matvec
  *       the matrix of SystemEnergy::quadraticApproximation1/2 applied to a vector
  *                                                           Include/SystemEnergy.h:80-84 (q.q * x, MG.h:120)
+ *   epr_linear_gs
+ *       GSRelaxer::operator()(b, x, mcIndices)              Include/MG.h:39-72
+ *   epr_mg_vcycle
+ *       MGSolver::MGSolver + vCycle                         Include/MG.h:74-187
+ *   epr_alternating_system
+ *       quadraticApproximation1/2 as AlternatingSolve uses them (q.q *= 2, q.l = -q.l)
+ *                                                           ExteriorPoissonRecon/ExteriorPoissonSolvers.h:96-131
+ *   epr_alternating_solve
+ *       ExteriorPoissonSolvers::AlternatingSolve            ExteriorPoissonSolvers.h:66-68,86-154
+ *   epr_biquadratic_fit
+ *       SystemEnergy::biQuadraticFit                        Include/SystemEnergy.h:78,499-540
+ *   epr_step_size / epr_newton_update
+ *       SystemEnergy::stepSize / newtonUpdate               Include/SystemEnergy.h:66-69,256-303
  *   epr_get_array
  *       read-only views of the reference's internal state (TreeEstimator::measure/noise/depth
  *       GridSamples.inl:838-862, S(E) ExteriorPoisson.h:290-307, _R/_B SystemEnergy.h:172-175)
@@ -53,7 +66,8 @@ extern "C" {
 #define EPR_FP32 1  /* smoothing / matvecs in float; energies, norms and the coarse solve in double */
 
 #define EPR_SOLVER_CASCADIC 0   /* the reference schedule: coarse-to-fine paired Gauss-Seidel */
-#define EPR_SOLVER_MULTIGRID 1  /* nonlinear multigrid V-cycles to a gradient tolerance */
+#define EPR_SOLVER_MULTIGRID 1  /* cascadic, each level relaxed by the alternating solve with linear
+                                   multigrid V-cycles (AlternatingSolve, sType MULTIGRID) */
 
 typedef struct epr_ctx epr_ctx;
 
@@ -167,6 +181,36 @@ int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, doubl
 int epr_energy_noalloc(int device, int dim, int level, int precision, const void *xy, const void *A,
                        const void *B, double c, double *out3, void *stream);
 const char *epr_noalloc_last_error(void);
+
+/* Linear multigrid on a host system M v = b, M a symmetric column stencil of `level` (N x 3^dim,
+ * node-major, entry o of node i holds M(i+off(o), i)), v updated in place.  In EPR_FP32 mode the
+ * relaxation runs in float; epr_mg_vcycle then forms the residual and adds each correction in
+ * double.
+ *   epr_linear_gs:  iters coloured Gauss-Seidel sweeps (colours by per-axis parity, in order);
+ *   epr_mg_vcycle:  cycles V-cycles with gs_iters relaxations before and after the coarse
+ *                   correction on every level, Galerkin operators P^T M P, exact solve at
+ *                   resolution 1. */
+int epr_linear_gs(epr_ctx *ctx, int level, const double *M, const double *b, double *v, int iters);
+int epr_mg_vcycle(epr_ctx *ctx, int level, const double *M, const double *b, double *v, int gs_iters, int cycles);
+
+/* The linear system of one half-step of the alternating solve at the level's coefficients, as
+ * AlternatingSolve forms it: which = 1 solves for y with x fixed, M = 2 (G_x + A), b = 2 B x;
+ * which = 0 solves for x with y fixed, M = 2 (G_y + A), b = 2 B^T y; G_f is the wedge Gram matrix
+ * (|f ^ v|^2 = v^T G_f v).  M: N x 3^dim node-major column stencil, b: N doubles. */
+int epr_alternating_system(epr_ctx *ctx, int level, int which, double *M, double *b);
+/* AlternatingSolve on the level's coefficients (in place): iters rounds of (y, then x), each
+ * vcycles V-cycles of gs_iters relaxations, or gs_iters * vcycles sweeps when single_level != 0. */
+int epr_alternating_solve(epr_ctx *ctx, int level, int iters, int vcycles, int gs_iters, int single_level);
+
+/* q9[3i + j] = coefficient of s^i t^j of E(x + s dx, y + t dy) at the level's coefficients.
+ * as_reference != 0 reproduces the reference's biQuadraticFit term by term, which deviates from
+ * the exact expansion twice: its s t^2 coefficient is 2 <dx^dy, x^y> (SystemEnergy.h:506) and its
+ * stiffness term has weight 1 instead of dWeight (SystemEnergy.h:522-530). */
+int epr_biquadratic_fit(epr_ctx *ctx, int level, const double *dx, const double *dy, int as_reference, double *q9);
+/* stepSize: the s minimising P(s, s) among the critical points; newtonUpdate: `steps` Newton
+ * steps on P from (0, 0), each followed by an exact line search.  Host arithmetic only. */
+int epr_step_size(const double *q9, double *s);
+int epr_newton_update(const double *q9, int steps, double *st2);
 
 /* Waits for all work of the context. */
 int epr_synchronize(epr_ctx *ctx);

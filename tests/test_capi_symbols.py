@@ -26,3 +26,22 @@ def test_params_struct_matches_defaults():
     q = epr.default_params(sWeight=50, gsIters=20, precision="fp32")
     assert q.s_weight == 50 and q.gs_iters == 20 and q.precision == epr.EPR_FP32
     assert ctypes.sizeof(epr.Params) == 96
+
+
+def test_line_searches_host_only():
+    """stepSize / newtonUpdate are host arithmetic in the library (no CUDA call): they reproduce the
+    reference's values for the reference's own bi-quadratic fits."""
+    import numpy as np
+    from conftest import GOLDEN_CASES, load_golden
+    for name in GOLDEN_CASES:
+        g = load_golden(name)
+        q = g["qa_biquad"]
+        assert abs(epr.step_size(q) - g["qa_step"][0]) <= 1e-10 * abs(g["qa_step"][0])
+        assert np.abs(epr.newton_update(q, 10) - g["qa_newton"]).max() <= 1e-10 * np.abs(g["qa_newton"]).max()
+    # a cubic derivative with a single real root and one whose constant term vanishes
+    q = np.zeros((3, 3))
+    q[2, 2], q[1, 0] = 1.0, -1.0
+    assert abs(epr.step_size(q) - 0.25 ** (1 / 3)) < 1e-14  # argmin of s^4 - s
+    q = np.zeros((3, 3))
+    q[2, 0], q[0, 2] = 1.0, 1.0
+    assert epr.step_size(q) == 0.0
