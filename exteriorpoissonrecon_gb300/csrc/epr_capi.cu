@@ -253,7 +253,9 @@ bool Context::download_xy(int l, double *x, double *y, bool fromSolution)
     return true;
 }
 
-// The reference's cascadic schedule (ExteriorPoisson.h:315-409)
+// The reference's cascadic schedule (ExteriorPoisson.h:315-409).  Each level is relaxed by paired
+// Gauss-Seidel (EPR_SOLVER_CASCADIC, the reference) or by alternating-solve rounds with linear
+// multigrid V-cycles until the gradient falls by `tolerance` (EPR_SOLVER_MULTIGRID).
 bool Context::solve_cascadic()
 {
     const int minD = std::min(P.min_solve_depth, depth);
@@ -296,7 +298,7 @@ bool Context::solve_cascadic()
         if (!push_xy(maxD)) return false;
         double e0[3] = {0, 0, 0};
         if (P.verbose && !energy(maxD, e0)) return false;
-        if (!gs(maxD, P.gs_iters)) return false;
+        if (P.solver == EPR_SOLVER_MULTIGRID ? !relax_alternating(*this, maxD, true) : !gs(maxD, P.gs_iters)) return false;
         if (P.verbose)
         {
             double e1[3];
@@ -309,7 +311,7 @@ bool Context::solve_cascadic()
         int iters = (int)std::ceil(std::pow(P.i_mult, depth - l) * P.gs_iters);
         double e0[3] = {0, 0, 0};
         if (P.verbose && !energy(l, e0)) return false;
-        if (!gs(l, iters)) return false;
+        if (P.solver == EPR_SOLVER_MULTIGRID ? !relax_alternating(*this, l, l == maxD) : !gs(l, iters)) return false;
         if (P.verbose)
         {
             double e1[3];
@@ -411,6 +413,8 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
     if (params) p = *params; else epr_default_params(&p);
     if (p.t_radius < 0 || p.t_radius > 4 || p.d_radius < 0 || p.d_radius > 4) { g_error = "kernel radius must be in [0,4]"; return nullptr; }
     if (p.precision != EPR_FP64 && p.precision != EPR_FP32) { g_error = "unknown precision"; return nullptr; }
+    if (p.solver != EPR_SOLVER_CASCADIC && p.solver != EPR_SOLVER_MULTIGRID) { g_error = "unknown solver"; return nullptr; }
+    if (p.solver == EPR_SOLVER_MULTIGRID && (p.max_cycles < 0 || !(p.tolerance >= 0))) { g_error = "bad multigrid cycle cap or tolerance"; return nullptr; }
     if (cudaSetDevice(p.device) != cudaSuccess)
     {
         g_error = std::string("cannot select CUDA device: ") + cudaGetErrorString(cudaGetLastError());
@@ -611,9 +615,8 @@ int epr_solve(epr_ctx *ctx, epr_stats *stats)
     if (!ctx->have_system) { ctx->fail(EPR_ERR_STATE, "epr_solve called before epr_build"); return EPR_ERR_STATE; }
     ctx->stats.node_updates = 0;
     ctx->launches = 0;
-    bool ok;
-    if (ctx->P.solver == EPR_SOLVER_MULTIGRID) ok = epr::solve_multigrid(*ctx);
-    else ok = ctx->solve_cascadic();
+    ctx->stats.cycles = 0;
+    bool ok = ctx->solve_cascadic();
     if (ok && stats) *stats = ctx->stats;
     EPR_RETURN(ctx, ok);
 }
@@ -674,6 +677,11 @@ int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, doubl
     EPR_CHECK_LEVEL(ctx, level);
     if (!kernel || !ms || reps < 1) { ctx->fail(EPR_ERR_ARG, "bad arguments"); return EPR_ERR_ARG; }
     std::string k(kernel);
+    if (k == "lgs" || k == "residual" || k == "assemble" || k == "biquad")
+    {
+        if (!ctx->have_system) { ctx->fail(EPR_ERR_STATE, "no system"); return EPR_ERR_STATE; }
+        EPR_RETURN(ctx, epr::time_mg_kernel(*ctx, kernel, level, reps, ms));
+    }
     epr::Level &L = ctx->levels[level];
     bool fp32 = ctx->lvl32(level);
     double *scratch = nullptr;

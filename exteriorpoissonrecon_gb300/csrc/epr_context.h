@@ -97,7 +97,5 @@ struct Context
 // resolution-1 stencil table, see epr_setup.cu)
 bool add_dirichlet(Context &c, int level);
 bool add_dirichlet_to(Context &c, int level, double *dst, double w);
-// Nonlinear multigrid driver (epr_mg.cu)
-bool solve_multigrid(Context &c);
 
 }  // namespace epr

@@ -28,6 +28,9 @@ struct Reduce
 
 template <int D, typename Real>
 void launch_energy(const LevelPtrs<Real> &L, const Real *xy, const Reduce &red, cudaStream_t s);
+// red.out[0] = sum_i (dE/dx_i)^2 + (dE/dy_i)^2
+template <int D, typename Real>
+void launch_grad_norm(const LevelPtrs<Real> &L, const Real *xy, const Reduce &red, cudaStream_t s);
 // writes N x 5 doubles (Q20, Q02, Q11, Q10, Q01)
 template <int D, typename Real>
 void launch_quadfit(const LevelPtrs<Real> &L, const Real *xy, double *out, cudaStream_t s);

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "../../include/epr.h"
@@ -897,10 +898,113 @@ bool biquadratic_fit(Context &c, int level, const double *ddxy, bool asReference
     return true;
 }
 
-bool solve_multigrid(Context &c)
+// Times `reps` launches of one multigrid kernel at `level` on the context's stream (CUDA events):
+//   "lgs"       one colour (0) of the linear Gauss-Seidel sweep on the y half-step system,
+//   "residual"  the colour-blocked residual of that system,
+//   "assemble"  the half-step system assembly,
+//   "biquad"    the bi-quadratic fit reduction along (x, y).
+bool time_mg_kernel(Context &c, const char *kernel, int level, int reps, double *ms)
 {
-    c.fail(EPR_ERR_STATE, "multigrid solver not available in this build");
-    return false;
+    std::string k(kernel);
+    if (k != "lgs" && k != "residual" && k != "assemble" && k != "biquad")
+    {
+        c.fail(EPR_ERR_ARG, "unknown kernel '%s'", kernel);
+        return false;
+    }
+    if (!mg_prepare(c, level) || !c.pull_xy(level) || !assemble_system(c, level, 1) || !mg_build(c, level, level)) return false;
+    MGHierarchy &h = *c.mg;
+    Level &Lv = c.levels[level];
+    MGLevel &m = h.L[level];
+    if (h.fp32) launch_convert_d2f(h.b64, (float *)m.b, m.N, c.stream);
+    else cudaMemcpyAsync(m.b, h.b64, sizeof(double) * m.N, cudaMemcpyDeviceToDevice, c.stream);
+    cudaMemsetAsync(m.x, 0, (h.fp32 ? sizeof(float) : sizeof(double)) * m.N, c.stream);
+    double *partial = nullptr;
+    if (k == "biquad" && !c.alloc((void **)&partial, sizeof(double) * kBQ * 1024, "alloc partial")) return false;
+    auto run = [&]() {
+        mg_dim(c, [&](auto dd) {
+            constexpr int D = decltype(dd)::value;
+            ColourBlocks<D> cb = colour_blocks<D>(level);
+            if (k == "lgs")
+            {
+                if (h.fp32)
+                    linear_gs_colour_kernel<D, float><<<blocks(cb.count[0]), kThreads, 0, c.stream>>>(
+                        level, 0, (const float *)m.Mcb, cb.count[0], (const float *)m.b, (float *)m.x);
+                else
+                    linear_gs_colour_kernel<D, double><<<blocks(cb.count[0]), kThreads, 0, c.stream>>>(
+                        level, 0, (const double *)m.Mcb, cb.count[0], (const double *)m.b, (double *)m.x);
+            }
+            else if (k == "residual")
+            {
+                dim3 grid(blocks(cb.count[0]), 1 << D);
+                if (h.fp32)
+                    residual_cb_kernel<D, float><<<grid, kThreads, 0, c.stream>>>(level, (const float *)m.Mcb, cb, (const float *)m.b,
+                                                                                 (const float *)m.x, (float *)m.r);
+                else
+                    residual_cb_kernel<D, double><<<grid, kThreads, 0, c.stream>>>(level, (const double *)m.Mcb, cb, (const double *)m.b,
+                                                                                  (const double *)m.x, (double *)m.r);
+            }
+            else if (k == "assemble")
+                alternating_system_kernel<D><<<blocks(Lv.N, 128), 128, 0, c.stream>>>(level, Lv.xy64, 1, Lv.A64, Lv.B64, m.M64, h.b64);
+            else
+                biquad_kernel<D><<<1024, 128, 0, c.stream>>>(level, Lv.xy64, Lv.xy64, Lv.A64, nullptr, 0.0, Lv.B64, partial);
+            return 0;
+        });
+    };
+    run();
+    cudaEventRecord(c.ev0, c.stream);
+    for (int i = 0; i < reps; i++) run();
+    cudaEventRecord(c.ev1, c.stream);
+    bool ok = c.launch_ok("time mg kernel") && c.cuda_ok(cudaEventSynchronize(c.ev1), "sync");
+    float t = 0;
+    if (ok) cudaEventElapsedTime(&t, c.ev0, c.ev1);
+    *ms = (double)t / reps;
+    c.release(partial);
+    return ok;
+}
+
+bool grad_norm(Context &c, int level, double *out)
+{
+    if (!c.pull_xy(level)) return false;
+    Level &Lv = c.levels[level];
+    LevelPtrs<double> P;
+    P.level = level;
+    P.N = Lv.N;
+    P.xy = Lv.xy64;
+    P.A = Lv.A64;
+    P.B = Lv.B64;
+    mg_dim(c, [&](auto dd) {
+        constexpr int D = decltype(dd)::value;
+        launch_grad_norm<D, double>(P, Lv.xy64, c.red, c.stream);
+        return 0;
+    });
+    c.launches += 2;
+    double h = 0;
+    if (!c.launch_ok("gradient norm") || !c.cuda_ok(cudaMemcpyAsync(&h, c.red.out, sizeof(double), cudaMemcpyDeviceToHost, c.stream), "copy") ||
+        !c.cuda_ok(cudaStreamSynchronize(c.stream), "sync"))
+        return false;
+    *out = std::sqrt(h);
+    return true;
+}
+
+bool relax_alternating(Context &c, int level, bool finest)
+{
+    double g0 = 0, g = 0;
+    if (!grad_norm(c, level, &g0)) return false;
+    g = g0;
+    int rounds = 0;
+    while (rounds < c.P.max_cycles && g > c.P.tolerance * g0)
+    {
+        if (!alternating_solve(c, level, 1, 1, c.P.gs_iters, false) || !grad_norm(c, level, &g)) return false;
+        rounds++;
+        if (c.P.verbose) printf("\t\tGradient[%d][%d]: %g\n", 1 << level, rounds, g);
+    }
+    c.stats.cycles += rounds;
+    if (finest)
+    {
+        c.stats.grad_norm0 = g0;
+        c.stats.grad_norm = g;
+    }
+    return true;
 }
 
 }  // namespace epr

@@ -17,6 +17,13 @@ bool mg_vcycles(Context &c, int level, const double *M, const double *b, double 
 bool alternating_system(Context &c, int level, int which, double *M, double *b);
 // AlternatingSolve on the level's coefficients
 bool alternating_solve(Context &c, int level, int iters, int vcycles, int gsIters, bool singleLevel);
+// relaxation of one level of the multigrid solver: alternating rounds (one V-cycle of gs_iters
+// relaxations per half-step) until |grad E| <= tolerance |grad E(start)| or max_cycles rounds
+bool relax_alternating(Context &c, int level, bool finest);
+// CUDA-event time of one launch of a multigrid kernel family ("lgs", "residual", "assemble", "biquad")
+bool time_mg_kernel(Context &c, const char *kernel, int level, int reps, double *ms);
+// |grad E| of the level's double coefficients
+bool grad_norm(Context &c, int level, double *out);
 // bi-quadratic fit along the device direction pairs ddxy (2N doubles)
 bool biquadratic_fit(Context &c, int level, const double *ddxy, bool asReference, double *q);
 

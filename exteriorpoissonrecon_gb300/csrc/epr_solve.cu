@@ -314,6 +314,23 @@ __global__ void __launch_bounds__(kThreads) quadfit_kernel(LevelPtrs<Real> L, co
     for (int k = 0; k < 5; k++) out[i * 5 + k] = (double)q[k];
 }
 
+// sum over the nodes of |dE/dx_i|^2 + |dE/dy_i|^2 (the linear coefficients of the node fits)
+template <int D, typename Real>
+__global__ void __launch_bounds__(kThreads) grad_norm_kernel(LevelPtrs<Real> L, const Real *xy, double *partial)
+{
+    Grid<D> g(L.level);
+    double acc[1] = {0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < g.N; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        NodeCtx<D> nc;
+        make_ctx<D>(g, i, nc);
+        Real q[5];
+        node_fit<D, Real>(L, g, nc, i, xy, q);
+        acc[0] += (double)q[3] * (double)q[3] + (double)q[4] * (double)q[4];
+    }
+    block_sum_store<1>(acc, partial + 4 * blockIdx.x);
+}
+
 // Node step from the quadratic model q = (Q20, Q02, Q11, Q10, Q01) with H = [[2 Q20, Q11], [Q11, 2 Q02]]
 // and grad = (Q10, Q01).  Paired (ExteriorPoissonSolvers.h:173-181): -H^{-1} grad / 2 when
 // |det H| > 1e-20.  Separate (ExteriorPoissonSolvers.h:216-235): p0 = -grad0 / (2 H00) when
@@ -691,6 +708,17 @@ void launch_energy(const LevelPtrs<Real> &L, const Real *xy, const Reduce &red, 
 }
 
 template <int D, typename Real>
+void launch_grad_norm(const LevelPtrs<Real> &L, const Real *xy, const Reduce &red, cudaStream_t s)
+{
+    Grid<D> g(L.level);
+    int nb = (int)blocks_for(g.N);
+    if (nb > Reduce::kMaxBlocks) nb = Reduce::kMaxBlocks;
+    if (nb < 1) nb = 1;
+    grad_norm_kernel<D, Real><<<nb, kThreads, 0, s>>>(L, xy, red.partial);
+    finish_kernel<<<1, 32, 0, s>>>(red.partial, nb, 1, red.out, 1.0);
+}
+
+template <int D, typename Real>
 void launch_quadfit(const LevelPtrs<Real> &L, const Real *xy, double *out, cudaStream_t s)
 {
     Grid<D> g(L.level);
@@ -774,6 +802,7 @@ void launch_convert_f2d(const float *in, double *out, int64_t n, cudaStream_t st
 #define EPR_INSTANTIATE(D, R)                                                                          \
     template void launch_energy<D, R>(const LevelPtrs<R> &, const R *, const Reduce &, cudaStream_t);   \
     template void launch_quadfit<D, R>(const LevelPtrs<R> &, const R *, double *, cudaStream_t);        \
+    template void launch_grad_norm<D, R>(const LevelPtrs<R> &, const R *, const Reduce &, cudaStream_t); \
     template void launch_gs_colour<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t, int); \
     template int launch_gs_sweeps<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t, int);  \
     template void launch_gn_matvec<D, R>(const LevelPtrs<R> &, const R *, const R *, R *, cudaStream_t); \

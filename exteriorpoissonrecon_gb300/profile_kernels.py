@@ -4,7 +4,8 @@
 
 Builds the named synthetic workload on the GPU, sets seeded random coefficients on the finest
 level and times `reps` launches of the kernel (plus one warm-up launch) with CUDA events through
-epr_time_kernel.  Kernel families: gs, energy, quadfit, prolong, gn.
+epr_time_kernel.  Kernel families: gs, energy, quadfit, prolong, gn, and the multigrid families
+lgs, residual, assemble, biquad.
 """
 from __future__ import annotations
 

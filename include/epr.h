@@ -159,7 +159,10 @@ int epr_get_array(epr_ctx *ctx, const char *name, int level, double *out, size_t
 
 /* Times `reps` launches of one kernel family on the context's stream with CUDA events and returns
  * the mean device time of a single launch in *ms: "gs" (one parity colour of the paired
- * Gauss-Seidel sweep, colour 0), "energy", "quadfit", "prolong", "gn" (Gauss-Newton matvec).
+ * Gauss-Seidel sweep, colour 0), "energy", "quadfit", "prolong", "gn" (Gauss-Newton matvec),
+ * "lgs" (one colour of the linear Gauss-Seidel sweep on the alternating y-system, colour-blocked
+ * stencil), "residual" (that system's residual), "assemble" (its assembly), "biquad" (the
+ * bi-quadratic fit reduction).
  * The level's coefficients are modified by "gs". No counterpart in the reference (a profiling
  * hook for the benchmark). */
 int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, double *ms);

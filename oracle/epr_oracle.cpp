@@ -1674,7 +1674,8 @@ struct Oracle
         for (int l = minD; !P.single_level && l <= maxD; l++)
         {
             int iters = (int)std::ceil(std::pow(P.i_mult, depth - l) * P.gs_iters);
-            gs(l, X[l].data(), Y[l].data(), iters);
+            if (P.alt_rounds > 0) alternatingSolve(l, X[l].data(), Y[l].data(), P.alt_rounds, 1, P.gs_iters, false);
+            else gs(l, X[l].data(), Y[l].data(), iters);
             if (l < maxD)
             {
                 std::vector<double> px(X[l + 1].size()), py(Y[l + 1].size());
@@ -1769,6 +1770,7 @@ void epr_oracle_default_params(epr_oracle_params *p)
     p->threads = 0;
     p->single_level = 0;
     p->separate = 0;
+    p->alt_rounds = 0;
 }
 
 int epr_oracle_unit_cube(int dim, size_t n, double scale, double *pos, double *xform)

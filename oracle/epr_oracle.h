@@ -34,6 +34,8 @@ typedef struct epr_oracle_params {
     int threads;          /* OpenMP threads (0 = all) */
     int single_level;     /* --singleLevel */
     int separate;         /* --separate */
+    int alt_rounds;       /* > 0: relax every level with this many AlternatingSolve rounds (one
+                             V-cycle of gs_iters relaxations per half-step) instead of paired GS */
 } epr_oracle_params;
 
 void epr_oracle_default_params(epr_oracle_params *p);

@@ -31,6 +31,7 @@ class Params(ctypes.Structure):
         ("threads", ctypes.c_int),
         ("single_level", ctypes.c_int),
         ("separate", ctypes.c_int),
+        ("alt_rounds", ctypes.c_int),
     ]
 
 

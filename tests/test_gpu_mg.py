@@ -50,11 +50,13 @@ def test_vcycles_fp32(built):
     M, b = g["mg_M"], g["mg_b"]
     assert rel(r32.linear_gs(depth, M, b, np.zeros_like(b), iters=1), g["mg_gs1"]) < 1e-5
     assert rel(r32.mg_vcycle(depth, M, b, np.zeros_like(b), gs_iters=2, cycles=2), g["mg_v2"]) < 1e-5
-    # float relaxation with double residuals converges to the double solution
-    from scipy.sparse.linalg import spsolve
-    x = spsolve(sparse(M, dim, depth), b)
-    v = r32.mg_vcycle(depth, M, b, np.zeros_like(b), gs_iters=2, cycles=40)
-    assert rel(v, x) < 1e-9
+    # float relaxation with double residuals tracks the double iteration (the V-cycle contracts
+    # slowly on these high-contrast operators, ~0.95 per cycle, so rounding would show here)
+    v64 = r.mg_vcycle(depth, M, b, np.zeros_like(b), gs_iters=2, cycles=30)
+    v32 = r32.mg_vcycle(depth, M, b, np.zeros_like(b), gs_iters=2, cycles=30)
+    assert rel(v32, v64) < 1e-5
+    A = sparse(M, dim, depth)
+    assert np.linalg.norm(A @ v32 - b) < 0.7 * np.linalg.norm(A @ g["mg_v2"] - b)
 
 
 def sparse(M, dim, level):
@@ -129,3 +131,25 @@ def test_alternating_solve_matches_oracle(built, single):
     xo, yo = o.alternating_solve(lev, x0, y0, iters=2, vcycles=2, gs_iters=2, single_level=single)
     assert rel(x, xo) < 1e-9
     assert rel(y, yo) < 1e-9
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_multigrid_solver_matches_oracle(precision):
+    """EPR_SOLVER_MULTIGRID: the cascadic schedule with every level relaxed by alternating-solve
+    rounds (fixed round count: tolerance 0) against the oracle's same schedule."""
+    g = load_golden("knot3_d4")
+    depth = int(g["depth"])
+    r = epr.Reconstructor(3, depth, g["pos"], g["skew"], solver="multigrid", tolerance=0.0, max_cycles=2,
+                          gsIters=2, precision=precision)
+    st = r.solve()
+    assert st["cycles"] == 2 * (depth + 1)
+    xs, ys = r.solution()
+    o = O.Oracle(3, depth, alt_rounds=2, gs_iters=2)
+    o.set_samples(g["pos"], g["skew"])
+    o.build()
+    xo, yo, eo = o.solve()
+    tol = 1e-8 if precision == "fp64" else 1e-4
+    for l in range(depth + 1):
+        assert rel(xs[l], xo[l]) < tol, l
+        assert rel(ys[l], yo[l]) < tol, l
+    assert abs(st["fit_energy"] + st["reg_energy"] - (eo[1] + eo[2])) < tol * (eo[1] + eo[2])
