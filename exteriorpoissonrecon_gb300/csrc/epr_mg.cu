@@ -165,10 +165,11 @@ __global__ void __launch_bounds__(kThreads) residual_nat_kernel(int level, const
     r[i] = (float)(b[i] - s);
 }
 
-// coarse = P^T fine (scalar)
-template <int D, typename Real>
-__global__ void restrict1_kernel(int coarseLevel, const Real *fine, Real *coarse)
+// coarse = P^T fine (scalar; the sum runs in the wider of the two precisions)
+template <int D, typename RF, typename RC>
+__global__ void restrict1_kernel(int coarseLevel, const RF *fine, RC *coarse)
 {
+    using Real = decltype(RF() + RC());
     Grid<D> gc(coarseLevel), gf(coarseLevel + 1);
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= gc.N) return;
@@ -188,15 +189,16 @@ __global__ void restrict1_kernel(int coarseLevel, const Real *fine, Real *coarse
             ok = ok && F[d] >= 0 && F[d] <= gf.r;
             if (off[d]) w *= (Real)0.5;
         }
-        if (ok) s += w * fine[gf.node(F)];
+        if (ok) s += w * (Real)fine[gf.node(F)];
     }
-    coarse[i] = s;
+    coarse[i] = (RC)s;
 }
 
 // fine += P coarse (scalar)
-template <int D, typename Real>
-__global__ void prolong_add1_kernel(int coarseLevel, const Real *coarse, Real *fine)
+template <int D, typename RC, typename RF>
+__global__ void prolong_add1_kernel(int coarseLevel, const RC *coarse, RF *fine)
 {
+    using Real = decltype(RF() + RC());
     Grid<D> gc(coarseLevel), gf(coarseLevel + 1);
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= gf.N) return;
@@ -216,9 +218,9 @@ __global__ void prolong_add1_kernel(int coarseLevel, const Real *coarse, Real *f
             if (F[d] & 1) { I[d] = (F[d] >> 1) + bit; w *= (Real)0.5; }
             else { I[d] = F[d] >> 1; if (bit) use = false; }
         }
-        if (use) s += w * coarse[gc.node(I)];
+        if (use) s += w * (Real)coarse[gc.node(I)];
     }
-    fine[i] += s;
+    fine[i] = (RF)((Real)fine[i] + s);
 }
 
 // Exact solve at resolution 1 (2^D nodes) by a dense LDL^T factorisation in double, one thread;
@@ -578,19 +580,25 @@ __global__ void biquad_finish_kernel(const double *partial, int nblocks, double 
 // Host side
 // =============================================================================================
 
+// Levels with fewer nodes than this relax in double even in the float mode: they cost nothing,
+// and the coarse Galerkin systems are the ill-conditioned ones, where a float right-hand side
+// would be amplified by the exact coarse solve.
+constexpr int64_t kFloatMinNodes = 1 << 15;
+
 // Per-level storage of the linear multigrid
 struct MGLevel
 {
     int64_t N = 0;
+    bool f32 = false;       // the level relaxes in float
     double *M64 = nullptr;  // natural offset-major stencil (double)
-    void *Mcb = nullptr;    // colour-blocked stencil (working precision)
-    void *x = nullptr, *b = nullptr, *r = nullptr;  // working-precision vectors
+    void *Mcb = nullptr;    // colour-blocked stencil (the level's precision)
+    void *x = nullptr, *b = nullptr, *r = nullptr;  // the level's vectors
 };
 
 struct MGHierarchy
 {
     int top = -1;
-    bool fp32 = false;
+    int mode = -1;  // precision and fp64_levels the levels were allocated for
     std::vector<MGLevel> L;
     double *x64 = nullptr, *b64 = nullptr;  // finest-level double vectors (solution, right-hand side)
 };
@@ -608,22 +616,24 @@ void release_mg(Context &c)
     c.mg = nullptr;
 }
 
-// (re)allocates the hierarchy for levels 0..top in the context's working precision
+// (re)allocates the hierarchy for levels 0..top
 static bool mg_prepare(Context &c, int top)
 {
-    const bool fp32 = c.P.precision == EPR_FP32;
-    if (c.mg && c.mg->top >= top && c.mg->fp32 == fp32) return true;
+    const int mode = c.P.precision * 1024 + c.P.fp64_levels;
+    if (c.mg && c.mg->top >= top && c.mg->mode == mode) return true;
     release_mg(c);
     c.mg = new MGHierarchy;
     MGHierarchy &h = *c.mg;
     h.top = top;
-    h.fp32 = fp32;
+    h.mode = mode;
     h.L.resize(top + 1);
-    const size_t S = (size_t)c.stencil(), rs = fp32 ? sizeof(float) : sizeof(double);
+    const size_t S = (size_t)c.stencil();
     for (int l = 0; l <= top; l++)
     {
         MGLevel &m = h.L[l];
         m.N = c.nodes(l);
+        m.f32 = c.P.precision == EPR_FP32 && m.N >= kFloatMinNodes && l >= c.P.fp64_levels;
+        const size_t rs = m.f32 ? sizeof(float) : sizeof(double);
         if (!c.alloc((void **)&m.M64, sizeof(double) * S * m.N, "alloc mg stencil") ||
             !c.alloc(&m.Mcb, rs * S * m.N, "alloc mg stencil") || !c.alloc(&m.x, rs * m.N, "alloc mg x") ||
             !c.alloc(&m.b, rs * m.N, "alloc mg b") || !c.alloc(&m.r, rs * m.N, "alloc mg r"))
@@ -640,6 +650,14 @@ static int mg_dim(Context &c, F &&f)
     return f(std::integral_constant<int, 4>{});
 }
 
+// calls f(float{}) or f(double{})
+template <typename F>
+static void with_real(bool f32, F &&f)
+{
+    if (f32) f(0.0f);
+    else f(0.0);
+}
+
 // Galerkin hierarchy of L[top].M64 down to level 0 and the colour-blocked copies of levels
 // lo..top (lo = top for relaxation only)
 static bool mg_build(Context &c, int top, int lo)
@@ -653,8 +671,10 @@ static bool mg_build(Context &c, int top, int lo)
         {
             ColourBlocks<D> cb = colour_blocks<D>(l);
             dim3 grid(blocks(cb.count[0]), 1 << D);
-            if (h.fp32) to_colour_blocks_kernel<D, float><<<grid, kThreads, 0, c.stream>>>(l, h.L[l].M64, cb, (float *)h.L[l].Mcb);
-            else to_colour_blocks_kernel<D, double><<<grid, kThreads, 0, c.stream>>>(l, h.L[l].M64, cb, (double *)h.L[l].Mcb);
+            with_real(h.L[l].f32, [&](auto rv) {
+                using R = decltype(rv);
+                to_colour_blocks_kernel<D, R><<<grid, kThreads, 0, c.stream>>>(l, h.L[l].M64, cb, (R *)h.L[l].Mcb);
+            });
             c.launches++;
         }
         c.launches += (lo < top) ? top : 0;
@@ -678,35 +698,50 @@ static void mg_sweeps(Context &c, int l, const Real *b, Real *x, int iters)
 }
 
 // One V-cycle (MGSolver::vCycle, MG.h:150-187) of M x = b on levels 0..top with the vectors of
-// L[top] as b and x.
-template <int D, typename Real>
+// L[top] as b and x; every level computes in its own precision.
+template <int D>
 static void mg_vcycle(Context &c, int top, int iters)
 {
     MGHierarchy &h = *c.mg;
     for (int l = top; l > 0; l--)
     {
         MGLevel &m = h.L[l], &mc = h.L[l - 1];
-        mg_sweeps<D, Real>(c, l, (const Real *)m.b, (Real *)m.x, iters);
-        ColourBlocks<D> cb = colour_blocks<D>(l);
-        residual_cb_kernel<D, Real><<<dim3(blocks(cb.count[0]), 1 << D), kThreads, 0, c.stream>>>(
-            l, (const Real *)m.Mcb, cb, (const Real *)m.b, (const Real *)m.x, (Real *)m.r);
-        restrict1_kernel<D, Real><<<blocks(mc.N), kThreads, 0, c.stream>>>(l - 1, (const Real *)m.r, (Real *)mc.b);
-        cudaMemsetAsync(mc.x, 0, sizeof(Real) * mc.N, c.stream);
+        with_real(m.f32, [&](auto rv) {
+            using R = decltype(rv);
+            mg_sweeps<D, R>(c, l, (const R *)m.b, (R *)m.x, iters);
+            ColourBlocks<D> cb = colour_blocks<D>(l);
+            residual_cb_kernel<D, R><<<dim3(blocks(cb.count[0]), 1 << D), kThreads, 0, c.stream>>>(
+                l, (const R *)m.Mcb, cb, (const R *)m.b, (const R *)m.x, (R *)m.r);
+            with_real(mc.f32, [&](auto cv) {
+                using RC = decltype(cv);
+                restrict1_kernel<D, R, RC><<<blocks(mc.N), kThreads, 0, c.stream>>>(l - 1, (const R *)m.r, (RC *)mc.b);
+                cudaMemsetAsync(mc.x, 0, sizeof(RC) * mc.N, c.stream);
+            });
+        });
         c.launches += 2;
     }
-    coarse_solve_kernel<D, Real><<<1, 32, 0, c.stream>>>(h.L[0].M64, (const Real *)h.L[0].b, (Real *)h.L[0].x);
+    with_real(h.L[0].f32, [&](auto rv) {
+        using R = decltype(rv);
+        coarse_solve_kernel<D, R><<<1, 32, 0, c.stream>>>(h.L[0].M64, (const R *)h.L[0].b, (R *)h.L[0].x);
+    });
     c.launches++;
     for (int l = 1; l <= top; l++)
     {
-        MGLevel &m = h.L[l];
-        prolong_add1_kernel<D, Real><<<blocks(m.N), kThreads, 0, c.stream>>>(l - 1, (const Real *)h.L[l - 1].x, (Real *)m.x);
+        MGLevel &m = h.L[l], &mc = h.L[l - 1];
+        with_real(m.f32, [&](auto rv) {
+            using R = decltype(rv);
+            with_real(mc.f32, [&](auto cv) {
+                using RC = decltype(cv);
+                prolong_add1_kernel<D, RC, R><<<blocks(m.N), kThreads, 0, c.stream>>>(l - 1, (const RC *)mc.x, (R *)m.x);
+            });
+            mg_sweeps<D, R>(c, l, (const R *)m.b, (R *)m.x, iters);
+        });
         c.launches++;
-        mg_sweeps<D, Real>(c, l, (const Real *)m.b, (Real *)m.x, iters);
     }
 }
 
-// cycles V-cycles of L[top].M64 x64 = b64 (x64 updated in place); in the float mode each cycle
-// relaxes the residual equation in float and adds the correction in double.
+// cycles V-cycles of L[top].M64 x64 = b64 (x64 updated in place).  A float top level relaxes the
+// residual equation (residual formed in double) and adds each correction in double.
 static bool mg_cycles(Context &c, int top, int iters, int cycles)
 {
     MGHierarchy &h = *c.mg;
@@ -715,7 +750,7 @@ static bool mg_cycles(Context &c, int top, int iters, int cycles)
         constexpr int D = decltype(dd)::value;
         for (int k = 0; k < cycles; k++)
         {
-            if (!h.fp32)
+            if (!m.f32)
             {
                 cudaMemcpyAsync(m.x, h.x64, sizeof(double) * m.N, cudaMemcpyDeviceToDevice, c.stream);
                 cudaMemcpyAsync(m.b, h.b64, sizeof(double) * m.N, cudaMemcpyDeviceToDevice, c.stream);
@@ -724,17 +759,16 @@ static bool mg_cycles(Context &c, int top, int iters, int cycles)
                     coarse_solve_kernel<D, double><<<1, 32, 0, c.stream>>>(h.L[0].M64, (const double *)m.b, (double *)m.x);
                     c.launches++;
                 }
-                else mg_vcycle<D, double>(c, top, iters);
+                else mg_vcycle<D>(c, top, iters);
                 cudaMemcpyAsync(h.x64, m.x, sizeof(double) * m.N, cudaMemcpyDeviceToDevice, c.stream);
             }
             else
             {
                 residual_nat_kernel<D><<<blocks(m.N), kThreads, 0, c.stream>>>(top, m.M64, h.b64, h.x64, (float *)m.b);
                 cudaMemsetAsync(m.x, 0, sizeof(float) * m.N, c.stream);
-                if (top == 0) coarse_solve_kernel<D, float><<<1, 32, 0, c.stream>>>(h.L[0].M64, (const float *)m.b, (float *)m.x);
-                else mg_vcycle<D, float>(c, top, iters);
+                mg_vcycle<D>(c, top, iters);
                 add_f2d_kernel<<<blocks(m.N), kThreads, 0, c.stream>>>(h.x64, (const float *)m.x, m.N);
-                c.launches += 3;
+                c.launches += 2;
             }
         }
         return 0;
@@ -749,7 +783,7 @@ static bool mg_relax(Context &c, int top, int iters)
     MGLevel &m = h.L[top];
     mg_dim(c, [&](auto dd) {
         constexpr int D = decltype(dd)::value;
-        if (!h.fp32)
+        if (!m.f32)
         {
             mg_sweeps<D, double>(c, top, h.b64, h.x64, iters);
         }
@@ -915,9 +949,9 @@ bool time_mg_kernel(Context &c, const char *kernel, int level, int reps, double 
     MGHierarchy &h = *c.mg;
     Level &Lv = c.levels[level];
     MGLevel &m = h.L[level];
-    if (h.fp32) launch_convert_d2f(h.b64, (float *)m.b, m.N, c.stream);
+    if (m.f32) launch_convert_d2f(h.b64, (float *)m.b, m.N, c.stream);
     else cudaMemcpyAsync(m.b, h.b64, sizeof(double) * m.N, cudaMemcpyDeviceToDevice, c.stream);
-    cudaMemsetAsync(m.x, 0, (h.fp32 ? sizeof(float) : sizeof(double)) * m.N, c.stream);
+    cudaMemsetAsync(m.x, 0, (m.f32 ? sizeof(float) : sizeof(double)) * m.N, c.stream);
     double *partial = nullptr;
     if (k == "biquad" && !c.alloc((void **)&partial, sizeof(double) * kBQ * 1024, "alloc partial")) return false;
     auto run = [&]() {
@@ -926,7 +960,7 @@ bool time_mg_kernel(Context &c, const char *kernel, int level, int reps, double 
             ColourBlocks<D> cb = colour_blocks<D>(level);
             if (k == "lgs")
             {
-                if (h.fp32)
+                if (m.f32)
                     linear_gs_colour_kernel<D, float><<<blocks(cb.count[0]), kThreads, 0, c.stream>>>(
                         level, 0, (const float *)m.Mcb, cb.count[0], (const float *)m.b, (float *)m.x);
                 else
@@ -936,7 +970,7 @@ bool time_mg_kernel(Context &c, const char *kernel, int level, int reps, double 
             else if (k == "residual")
             {
                 dim3 grid(blocks(cb.count[0]), 1 << D);
-                if (h.fp32)
+                if (m.f32)
                     residual_cb_kernel<D, float><<<grid, kThreads, 0, c.stream>>>(level, (const float *)m.Mcb, cb, (const float *)m.b,
                                                                                  (const float *)m.x, (float *)m.r);
                 else
