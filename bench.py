@@ -229,6 +229,17 @@ def main():
                 "launch_ms": gs_ms, "algorithmic_bytes_per_launch": gs_bytes,
                 "note": "FMA-bound quartic relaxation; bytes = coefficient read + stencil columns + update writes"}
 
+    # stored-stencil relaxation (the smoother of the linear multigrid, MG.h GSRelaxer): one colour of
+    # the linear Gauss-Seidel sweep on the alternating y-system of the finest level, colour-blocked
+    # 27-point stencil; bytes = the colour's coefficients, right-hand side and update plus one read
+    # of the whole x vector (every node neighbours the colour)
+    lgs_ms = r.time_kernel("lgs", depth, reps=20)
+    lgs_bytes = colour_nodes * (27 + 2) * rs + N * rs
+    lgs_achieved = lgs_bytes / (lgs_ms * 1e-3) / 1e9
+    stencil_roofline = {"bound": "hbm", "kernel": "linear_gs_colour_kernel", "achieved": lgs_achieved, "peak": hbm_peak,
+                        "unit": "GB/s", "frac": lgs_achieved / hbm_peak, "peak_source": peak_kind, "traffic": None,
+                        "launch_ms": lgs_ms, "algorithmic_bytes_per_launch": lgs_bytes}
+
     # end to end through the public API from host buffers
     e2e_s = []
     h2d = pu.nbytes + sk.nbytes
@@ -246,7 +257,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": per_step_s * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
             "data": "synthetic", "config": config, "clocks": clk, "gpu_launches": int(launches),
-            "roofline": roofline,
+            "roofline": roofline, "stencil_roofline": stencil_roofline,
             "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "build_ms": build_ms, "wall_s": wall,
             "final_energy": st["fit_energy"] + st["reg_energy"], "initial_energy": st["initial_energy"],

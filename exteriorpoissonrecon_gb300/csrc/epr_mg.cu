@@ -97,27 +97,99 @@ __global__ void to_colour_blocks_kernel(int level, const double *M, ColourBlocks
     for (int o = 0; o < Dims<D>::S; o++) dst[o * n] = (Real)M[(int64_t)o * g.N + i];
 }
 
+// component d of stencil offset o (axis 0 slowest), in {-1, 0, 1}
+template <int D>
+__host__ __device__ constexpr int offset_of(int o, int d)
+{
+    for (int k = D - 1; k > d; k--) o /= 3;
+    return o % 3 - 1;
+}
+
+// Node I (and its index) of the j-th node of a parity colour; 32-bit arithmetic (every supported
+// grid has fewer than 2^32 nodes)
+template <int D>
+__device__ __forceinline__ uint32_t colour_node(const Colour<D> &col, const uint32_t *st, uint32_t j, int *I)
+{
+    uint32_t i = 0;
+#pragma unroll
+    for (int d = D - 1; d >= 0; d--)
+    {
+        const uint32_t c = (uint32_t)col.cnt[d];
+        const uint32_t q = j / c;
+        I[d] = 2 * (int)(j - q * c) + col.par[d];
+        i += (uint32_t)I[d] * st[d];
+        j = q;
+    }
+    return i;
+}
+
+// sum_o M[o] x[i + off(o)] over the stencil of node i: interior nodes take the unrolled path with
+// compile-time offsets, boundary nodes check every neighbour.
+template <int D, typename Real>
+__device__ __forceinline__ Real stencil_dot(const Real *__restrict__ Mc, int64_t n, int64_t j, const Real *x, uint32_t i,
+                                            const int *I, const uint32_t *st, int r)
+{
+    constexpr int S = Dims<D>::S;
+    bool interior = true;
+#pragma unroll
+    for (int d = 0; d < D; d++) interior = interior && I[d] > 0 && I[d] < r;
+    Real s = 0;
+    if (interior)
+    {
+#pragma unroll
+        for (int o = 0; o < S; o++)
+        {
+            int64_t k = (int64_t)i;
+#pragma unroll
+            for (int d = 0; d < D; d++) k += (int64_t)offset_of<D>(o, d) * (int64_t)st[d];
+            s += __ldg(Mc + (int64_t)o * n + j) * x[k];
+        }
+    }
+    else
+    {
+#pragma unroll 9
+        for (int o = 0; o < S; o++)
+        {
+            int64_t k = (int64_t)i;
+            bool ok = true;
+#pragma unroll
+            for (int d = 0; d < D; d++)
+            {
+                const int off = offset_of<D>(o, d), q = I[d] + off;
+                ok = ok && q >= 0 && q <= r;
+                k += (int64_t)off * (int64_t)st[d];
+            }
+            if (ok) s += __ldg(Mc + (int64_t)o * n + j) * x[k];
+        }
+    }
+    return s;
+}
+
+template <int D>
+__device__ __forceinline__ void node_strides(int r, uint32_t *st)
+{
+    st[D - 1] = 1;
+#pragma unroll
+    for (int d = D - 2; d >= 0; d--) st[d] = st[d + 1] * (uint32_t)(r + 1);
+}
+
 // x_i += (b_i - sum_j M(j, i) x_j) / M(i, i) for the nodes of one colour (the GSRelaxer update,
 // which reads column i of M; M is symmetric)
 template <int D, typename Real>
-__global__ void __launch_bounds__(kThreads) linear_gs_colour_kernel(int level, int colour, const Real *Mc, int64_t n,
-                                                                     const Real *b, Real *x)
+__global__ void __launch_bounds__(kThreads) linear_gs_colour_kernel(int level, int colour, const Real *__restrict__ Mc, int64_t n,
+                                                                     const Real *__restrict__ b, Real *x)
 {
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= n) return;
+    const int r = 1 << level;
     Grid<D> g(level);
     Colour<D> col(g, colour);
+    uint32_t st[D];
+    node_strides<D>(r, st);
     int I[D];
-    col.node(j, I);
-    const int64_t i = g.node(I);
-    Real s = 0;
-#pragma unroll 27
-    for (int o = 0; o < Dims<D>::S; o++)
-    {
-        int64_t k = neighbour<D>(g, I, i, o);
-        if (k >= 0) s += Mc[o * n + j] * x[k];
-    }
-    x[i] += (b[i] - s) / Mc[Dims<D>::CENTER * n + j];
+    const uint32_t i = colour_node<D>(col, st, (uint32_t)j, I);
+    const Real s = stencil_dot<D, Real>(Mc, n, j, x, i, I, st, r);
+    x[i] += (__ldg(b + i) - s) / __ldg(Mc + (int64_t)Dims<D>::CENTER * n + j);
 }
 
 // r = b - M x over every node, colour-blocked coefficients; grid.y = colour
@@ -129,20 +201,14 @@ __global__ void __launch_bounds__(kThreads) residual_cb_kernel(int level, const 
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t n = cb.count[c];
     if (j >= n) return;
+    const int res = 1 << level;
     Grid<D> g(level);
     Colour<D> col(g, c);
+    uint32_t st[D];
+    node_strides<D>(res, st);
     int I[D];
-    col.node(j, I);
-    const int64_t i = g.node(I);
-    const Real *Mc = M + cb.base[c];
-    Real s = 0;
-#pragma unroll 27
-    for (int o = 0; o < Dims<D>::S; o++)
-    {
-        int64_t k = neighbour<D>(g, I, i, o);
-        if (k >= 0) s += Mc[o * n + j] * x[k];
-    }
-    r[i] = b[i] - s;
+    const uint32_t i = colour_node<D>(col, st, (uint32_t)j, I);
+    r[i] = b[i] - stencil_dot<D, Real>(M + cb.base[c], n, j, x, i, I, st, res);
 }
 
 // r = b - M x with the natural double stencil (the refinement residual of the float mode)
@@ -298,58 +364,59 @@ __global__ void add_f2d_kernel(double *y, const float *x, int64_t n)
 // corner 0; mirroring flips the sign of both W(f, phi_j) and W(f, phi_i), so each product keeps
 // its sign) with the same exact Gauss rule as the energy.
 // ---------------------------------------------------------------------------------------------
-template <int D, int K>
-__device__ __forceinline__ void component_gram(const double *f, double *loc)
+template <int D, int K, typename Real>
+__device__ __forceinline__ void component_gram(const Real *f, Real *loc)
 {
     using Cp = Component<D, K>;
     constexpr int M = Cp::M;
     constexpr int NG = ipow(3, M);
     constexpr int C = 1 << D;
-    double fP[2 * NG], fQ[2 * NG];
-    derivative_table<D, K, true, double>(f, fP);
-    derivative_table<D, K, false, double>(f, fQ);
+    Real fP[2 * NG], fQ[2 * NG];
+    derivative_table<D, K, true, Real>(f, fP);
+    derivative_table<D, K, false, Real>(f, fQ);
 #pragma unroll
     for (int go = 0; go < NG; go++)
     {
-        const double wo = other_weight<M>(go);
+        const Real wo = (Real)other_weight<M>(go);
 #pragma unroll
         for (int gp = 0; gp < 2; gp++)
 #pragma unroll
             for (int gq = 0; gq < 2; gq++)
             {
-                const double w = Gauss::W2(gp) * Gauss::W2(gq) * wo;
-                const double xp = fP[gq * NG + go], xq = fQ[gp * NG + go];
-                double V[C];
+                const Real w = (Real)(Gauss::W2(gp) * Gauss::W2(gq)) * wo;
+                const Real xp = fP[gq * NG + go], xq = fQ[gp * NG + go];
+                Real V[C];
 #pragma unroll
                 for (int B = 0; B < C; B++)
                 {
                     const int bP = cbit<D>(B, Cp::P), bQ = cbit<D>(B, Cp::Q);
-                    double lo;
-                    if constexpr (M == 1) lo = hat3<double>(cbit<D>(B, Cp::other(0)), go);
-                    else lo = hat3<double>(cbit<D>(B, Cp::other(0)), go / 3) * hat3<double>(cbit<D>(B, Cp::other(1)), go % 3);
-                    const double phP = (bP ? 1. : -1.) * hat2<double>(bQ, gq) * lo;
-                    const double phQ = (bQ ? 1. : -1.) * hat2<double>(bP, gp) * lo;
+                    Real lo;
+                    if constexpr (M == 1) lo = hat3<Real>(cbit<D>(B, Cp::other(0)), go);
+                    else lo = hat3<Real>(cbit<D>(B, Cp::other(0)), go / 3) * hat3<Real>(cbit<D>(B, Cp::other(1)), go % 3);
+                    const Real phP = (bP ? (Real)1 : (Real)-1) * hat2<Real>(bQ, gq) * lo;
+                    const Real phQ = (bQ ? (Real)1 : (Real)-1) * hat2<Real>(bP, gp) * lo;
                     V[B] = phP * xq - xp * phQ;
                 }
+                const Real wV0 = w * V[0];
 #pragma unroll
-                for (int B = 0; B < C; B++) loc[B] += w * V[0] * V[B];
+                for (int B = 0; B < C; B++) loc[B] += wV0 * V[B];
             }
     }
 }
 
-template <int D>
-__device__ __noinline__ void element_gram_canonical(const double *f, double *loc)
+template <int D, typename Real>
+__device__ __noinline__ void element_gram_canonical(const Real *f, Real *loc)
 {
 #pragma unroll
     for (int B = 0; B < (1 << D); B++) loc[B] = 0;
-    component_gram<D, 0>(f, loc);
-    component_gram<D, 1>(f, loc);
-    component_gram<D, 2>(f, loc);
+    component_gram<D, 0, Real>(f, loc);
+    component_gram<D, 1, Real>(f, loc);
+    component_gram<D, 2, Real>(f, loc);
     if constexpr (D == 4)
     {
-        component_gram<D, 3>(f, loc);
-        component_gram<D, 4>(f, loc);
-        component_gram<D, 5>(f, loc);
+        component_gram<D, 3, Real>(f, loc);
+        component_gram<D, 4, Real>(f, loc);
+        component_gram<D, 5, Real>(f, loc);
     }
 }
 
@@ -370,7 +437,9 @@ __device__ __forceinline__ double b_column_dot(const Grid<D> &g, const int *I, i
 
 // M = 2 (G_f + A) and b of one half-step: which 1 -> y free (f = x, b = 2 B x), which 0 -> x
 // free (f = y, b = 2 B^T y); B x = -(column sums) since B is antisymmetric.
-template <int D>
+// The Gram integrals run in Real (float in the float mode: the half-step system only steers the
+// outer iteration, whose gradient is evaluated in double); M and b are written in double.
+template <int D, typename Real>
 __global__ void __launch_bounds__(128) alternating_system_kernel(int level, const double *xy, int which, const double *A,
                                                                   const double *B, double *M, double *b)
 {
@@ -381,7 +450,7 @@ __global__ void __launch_bounds__(128) alternating_system_kernel(int level, cons
     int I[D];
     g.node(i, I);
     const int fc = which ? 0 : 1;  // component of the fixed field
-    double col[S];
+    Real col[S];
 #pragma unroll
     for (int o = 0; o < S; o++) col[o] = 0;
 #pragma unroll 1
@@ -395,7 +464,7 @@ __global__ void __launch_bounds__(128) alternating_system_kernel(int level, cons
             ok = ok && e >= 0 && e < g.r;
         }
         if (!ok) continue;
-        double f[1 << D], loc[1 << D];
+        Real f[1 << D], loc[1 << D];
 #pragma unroll
         for (int cc = 0; cc < (1 << D); cc++)
         {
@@ -406,9 +475,9 @@ __global__ void __launch_bounds__(128) alternating_system_kernel(int level, cons
                 j += (cbit<D>(mirror, d) ? -step : step) * s;
                 s *= g.r + 1;
             }
-            f[cc] = xy[2 * j + fc];
+            f[cc] = (Real)xy[2 * j + fc];
         }
-        element_gram_canonical<D>(f, loc);
+        element_gram_canonical<D, Real>(f, loc);
 #pragma unroll
         for (int B2 = 0; B2 < (1 << D); B2++)
         {
@@ -418,7 +487,7 @@ __global__ void __launch_bounds__(128) alternating_system_kernel(int level, cons
         }
     }
     const double sc = (D == 3 ? (double)g.r : 1.0) * 0.5;
-    for (int o = 0; o < S; o++) M[(int64_t)o * g.N + i] = 2. * (col[o] * sc + A[(int64_t)o * g.N + i]);
+    for (int o = 0; o < S; o++) M[(int64_t)o * g.N + i] = 2. * ((double)col[o] * sc + A[(int64_t)o * g.N + i]);
     const double bd = b_column_dot<D>(g, I, i, B, xy, which ? 0 : 1);
     b[i] = which ? -2. * bd : 2. * bd;
 }
@@ -837,8 +906,11 @@ static bool assemble_system(Context &c, int level, int which)
     Level &Lv = c.levels[level];
     mg_dim(c, [&](auto dd) {
         constexpr int D = decltype(dd)::value;
-        alternating_system_kernel<D><<<blocks(Lv.N, 128), 128, 0, c.stream>>>(level, Lv.xy64, which, Lv.A64, Lv.B64,
-                                                                               h.L[level].M64, h.b64);
+        with_real(h.L[level].f32, [&](auto rv) {
+            using R = decltype(rv);
+            alternating_system_kernel<D, R><<<blocks(Lv.N, 128), 128, 0, c.stream>>>(level, Lv.xy64, which, Lv.A64, Lv.B64,
+                                                                                     h.L[level].M64, h.b64);
+        });
         return 0;
     });
     c.launches++;
@@ -978,7 +1050,12 @@ bool time_mg_kernel(Context &c, const char *kernel, int level, int reps, double 
                                                                                   (const double *)m.x, (double *)m.r);
             }
             else if (k == "assemble")
-                alternating_system_kernel<D><<<blocks(Lv.N, 128), 128, 0, c.stream>>>(level, Lv.xy64, 1, Lv.A64, Lv.B64, m.M64, h.b64);
+            {
+                if (m.f32)
+                    alternating_system_kernel<D, float><<<blocks(Lv.N, 128), 128, 0, c.stream>>>(level, Lv.xy64, 1, Lv.A64, Lv.B64, m.M64, h.b64);
+                else
+                    alternating_system_kernel<D, double><<<blocks(Lv.N, 128), 128, 0, c.stream>>>(level, Lv.xy64, 1, Lv.A64, Lv.B64, m.M64, h.b64);
+            }
             else
                 biquad_kernel<D><<<1024, 128, 0, c.stream>>>(level, Lv.xy64, Lv.xy64, Lv.A64, nullptr, 0.0, Lv.B64, partial);
             return 0;

@@ -153,3 +153,36 @@ def test_multigrid_solver_matches_oracle(precision):
         assert rel(xs[l], xo[l]) < tol, l
         assert rel(ys[l], yo[l]) < tol, l
     assert abs(st["fit_energy"] + st["reg_energy"] - (eo[1] + eo[2])) < tol * (eo[1] + eo[2])
+
+
+@pytest.fixture(scope="module")
+def link6():
+    pos, fr = epr.samples.make_workload("link", 100000, seed=1)
+    pu, _ = epr.unit_cube(pos)
+    return pu, epr.pack_skew(fr)
+
+
+def test_float_levels_track_double(link6):
+    """At depth 6 the fine levels relax in float (>= 32768 nodes); V-cycles with double residuals
+    track the double V-cycles, and the multigrid solver's float result has the double energy."""
+    pu, sk = link6
+    depth = 6
+    r64 = epr.Reconstructor(3, depth, pu, sk)
+    r32 = epr.Reconstructor(3, depth, pu, sk, precision="fp32")
+    n = r64.nodes(depth)
+    rng = np.random.default_rng(0)
+    r64.set_coefficients(depth, rng.uniform(-0.1, 0.1, n), rng.uniform(-0.1, 0.1, n))
+    M, b = r64.alternating_system(depth, 1)
+    for cycles, tol in ((1, 1e-5), (20, 1e-7)):
+        v64 = r64.mg_vcycle(depth, M, b, np.zeros(n), gs_iters=2, cycles=cycles)
+        v32 = r32.mg_vcycle(depth, M, b, np.zeros(n), gs_iters=2, cycles=cycles)
+        assert rel(v32, v64) < tol
+    e = {}
+    sol = {}
+    for prec in ("fp64", "fp32"):
+        r = epr.Reconstructor(3, depth, pu, sk, solver="multigrid", tolerance=0.0, max_cycles=3, gsIters=2, precision=prec)
+        st = r.solve()
+        e[prec] = st["fit_energy"] + st["reg_energy"]
+        sol[prec] = r.solution()[0][depth]
+    assert abs(e["fp32"] - e["fp64"]) < 1e-5 * e["fp64"]
+    assert np.linalg.norm(sol["fp32"] - sol["fp64"]) < 1e-3 * np.linalg.norm(sol["fp64"])
