@@ -197,9 +197,9 @@ def main():
 
     import exteriorpoissonrecon_gb300 as epr
     r = epr.Reconstructor(3, depth, pu, sk, precision=args.precision, solver=args.solver, device=local)
-    build_ms = r.stats.build_ms if r.stats.build_ms else None
     for _ in range(args.warmup):
         r.solve()
+    build_ms = r.stats.build_ms  # device time of epr_build (filled in by the first solve's stats copy)
     barrier(pg)
     clocks = ClockSampler(local)
     clocks.start()

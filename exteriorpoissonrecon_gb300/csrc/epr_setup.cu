@@ -328,71 +328,100 @@ __global__ void vertex_chunks_kernel(SplatArgs a, int *nchunks)
 // B-spline weights of its mean and the estimator's depth weight (TreeSplatter::_addSample,
 // GridSamples.inl:458-491; TreeEstimator ctor :749-760).  The window is centred on the depth-t
 // ancestor of the item's cell while the weights come from floor(p res), as in the reference.
+// The per-axis B-spline values of every item at the level are tabulated once (item_bspline_kernel)
+// instead of once per (vertex, item) pair; the products keep the reference's order.
 template <int D>
 struct DensityItem
 {
     static constexpr int W = 1 + D + D * D;
-    const double *mean, *datum;
+    const double *bs;  // per item: D x (deg + 1) B-spline values at this level
+    const double *datum;
     double depthWeight;
     __device__ void operator()(const SplatArgs &a, int it, const int *v, const int *C, double *acc) const
     {
-        const int deg = 2 * a.KR + 1, res = 1 << (a.t - 1);
+        const int nb = 2 * a.KR + 2;
         double wt = depthWeight;
-        for (int d = 0; d < D; d++)
-        {
-            double bs[kMaxDeg + 1];
-            double pr = mean[(int64_t)it * D + d] * res;
-            int e = (int)floor(pr);
-            bspline_eval(deg, pr - e, bs);
-            wt *= bs[v[d] - (C[d] - a.KR)];
-        }
+        const double *b = bs + (int64_t)it * D * nb;
+        for (int d = 0; d < D; d++) wt *= b[d * nb + v[d] - (C[d] - a.KR)];
         for (int w = 0; w < W; w++) acc[w] += wt * datum[(int64_t)it * W + w];
     }
 };
 
 // Frame sample: normalised frame times the sample's measure and 2^(2 depth), split between the two
 // tree depths bracketing its estimated depth with weights 2^((d-1) D) (ExteriorPoisson.h:181-228,
-// GridSamples.inl:436-456), B-spline weights of the sample position.
+// GridSamples.inl:436-456), B-spline weights of the sample position.  Per sorted sample: the
+// level weight and B-spline values (skew_level_kernel) and the scaled frame (skew_frame_kernel).
 template <int D>
 struct SkewItem
 {
     static constexpr int W = D * (D - 1) / 2;
-    const double *pos, *skew, *measure, *sdepth;
-    const int *order;
+    const double *bs;     // per sorted sample: D x (deg + 1) B-spline values at this level
+    const double *lw;     // per sorted sample: level weight at this level
+    const double *frame;  // per sorted sample: W scaled frame values
     __device__ void operator()(const SplatArgs &a, int j, const int *v, const int *C, double *acc) const
     {
-        const int deg = 2 * a.KR + 1, res = 1 << (a.t - 1), maxT = a.depth + 1;
-        int s = order[j];
-        double dd = sdepth[s] + 1.;
-        double lw = 0;
-        if (dd >= maxT) lw = (a.t == maxT) ? (double)(1ull << (a.depth * D)) : 0.;
-        else if (dd <= 1) lw = (a.t == 1) ? 1. : 0.;
-        else
-        {
-            int d1 = (int)floor(dd), d2 = d1 + 1;
-            double f = dd - d1;
-            if (a.t == d1) lw = (1. - f) * (double)(1ull << ((d1 - 1) * D));
-            else if (a.t == d2) lw = f * (double)(1ull << ((d2 - 1) * D));
-        }
-        if (lw == 0) return;
-        const double *q = pos + (int64_t)s * D;
-        double wt = lw;
-        for (int d = 0; d < D; d++)
-        {
-            double bs[kMaxDeg + 1];
-            double pr = q[d] * res;
-            int e = (int)floor(pr);
-            bspline_eval(deg, pr - e, bs);
-            wt *= bs[v[d] - (C[d] - a.KR)];
-        }
-        const double *sk = skew + (int64_t)s * W;
-        double nrm = 0;
-        for (int k = 0; k < W; k++) nrm += 2 * sk[k] * sk[k];
-        nrm = sqrt(nrm);
-        double m = measure[s], sc = (double)(1ull << (a.depth * 2));
-        for (int k = 0; k < W; k++) acc[k] += wt * (sk[k] / nrm * m * sc);
+        const double l = lw[j];
+        if (l == 0) return;
+        const int nb = 2 * a.KR + 2;
+        double wt = l;
+        const double *b = bs + (int64_t)j * D * nb;
+        for (int d = 0; d < D; d++) wt *= b[d * nb + v[d] - (C[d] - a.KR)];
+        for (int k = 0; k < W; k++) acc[k] += wt * frame[(int64_t)j * W + k];
     }
 };
+
+// per-axis B-spline values of n points (pts[idx[j]] or pts[j]) at the resolution of tree depth t
+template <int D>
+__global__ void item_bspline_kernel(const double *pts, const int *idx, int64_t n, int t, int deg, const double *lw, double *bs)
+{
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    if (lw && lw[j] == 0) return;
+    const int64_t s = idx ? idx[j] : j;
+    const int res = 1 << (t - 1);
+    for (int d = 0; d < D; d++)
+    {
+        double pr = pts[s * D + d] * res;
+        int e = (int)floor(pr);
+        bspline_eval(deg, pr - e, bs + (j * D + d) * (deg + 1));
+    }
+}
+
+// level weight of every sorted frame sample at tree depth t
+__global__ void skew_level_kernel(const double *sdepth, const int *order, int64_t n, int t, int depth, int D, double *lw)
+{
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int maxT = depth + 1;
+    double dd = sdepth[order[j]] + 1.;
+    double w = 0;
+    if (dd >= maxT) w = (t == maxT) ? (double)(1ull << (depth * D)) : 0.;
+    else if (dd <= 1) w = (t == 1) ? 1. : 0.;
+    else
+    {
+        int d1 = (int)floor(dd), d2 = d1 + 1;
+        double f = dd - d1;
+        if (t == d1) w = (1. - f) * (double)(1ull << ((d1 - 1) * D));
+        else if (t == d2) w = f * (double)(1ull << ((d2 - 1) * D));
+    }
+    lw[j] = w;
+}
+
+// normalised frame times measure and 2^(2 depth), per sorted sample
+template <int D>
+__global__ void skew_frame_kernel(const double *skew, const double *measure, const int *order, int64_t n, int depth, double *frame)
+{
+    constexpr int W = D * (D - 1) / 2;
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int s = order[j];
+    const double *sk = skew + (int64_t)s * W;
+    double nrm = 0;
+    for (int k = 0; k < W; k++) nrm += 2 * sk[k] * sk[k];
+    nrm = sqrt(nrm);
+    double m = measure[s], sc = (double)(1ull << (depth * 2));
+    for (int k = 0; k < W; k++) frame[j * W + k] = sk[k] / nrm * m * sc;
+}
 
 // one warp per chunk
 template <int D, bool Samples, class Item>
@@ -1101,23 +1130,24 @@ bool build_impl(Context &c, Setup &st)
             bsv = v;
         }
         double scale = std::pow(1. / bsv[KR + 1], 2);
+        double *bs = nullptr;
+        if (!dalloc(c, &bs, (size_t)nc * D * (2 * KR + 2), "bspline table")) return false;
         for (int t = 1; t <= depth + 1; t++)
         {
             Grid<D> gl(t - 1);
             if (!dalloc(c, &st.density[t - 1], gl.N * W, "density")) return false;
             SplatArgs a{st.cellKey, st.cellStart, nc, depth, t, KR, rlo[t], rhi[t]};
             double dw = scale / std::pow(std::pow(0.5, t - 1), D - 2);
+            item_bspline_kernel<D><<<nblocks(nc, 256), 256, 0, s>>>(mean, nullptr, nc, t, 2 * KR + 1, nullptr, bs);
+            DensityItem<D> item{bs, datum, dw};
             if (gl.N <= kChunkedMaxVertices)
             {
-                DensityItem<D> item{mean, datum, dw};
                 if (!chunked_level<D, false>(c, a, item, 1.0, st.density[t - 1])) return false;
             }
             else
-            {
-                DensityItem<D> item{mean, datum, dw};
                 vertex_gather_kernel<D, false><<<nblocks(gl.N, 128), 128, 0, s>>>(a, item, 1.0, st.density[t - 1]);
-            }
         }
+        c.release(bs);
     }
     c.release(mean); c.release(datum);
     if (!c.launch_ok("density splat")) return false;
@@ -1134,22 +1164,30 @@ bool build_impl(Context &c, Setup &st)
 
     // ---- frame splat ----
     st.skewGrid.assign(depth + 1, nullptr);
-    for (int t = 1; t <= depth + 1; t++)
     {
-        Grid<D> gl(t - 1);
-        if (!dalloc(c, &st.skewGrid[t - 1], gl.N * K, "skew grid")) return false;
-        SplatArgs a{st.cellKey, st.cellStart, nc, depth, t, c.P.t_radius, rlo[t], rhi[t]};
-        if (gl.N <= kChunkedMaxVertices)
+        const int TR = c.P.t_radius;
+        double *bs = nullptr, *lw = nullptr, *frame = nullptr;
+        if (!dalloc(c, &bs, (size_t)n * D * (2 * TR + 2), "bspline table") || !dalloc(c, &lw, n, "level weights") ||
+            !dalloc(c, &frame, (size_t)n * K, "frames"))
+            return false;
+        skew_frame_kernel<D><<<nblocks(n, 256), 256, 0, s>>>(st.skew, st.measure, st.order, n, depth, frame);
+        for (int t = 1; t <= depth + 1; t++)
         {
-            SkewItem<D> item{st.pos, st.skew, st.measure, st.sdepth, st.order};
-            if (!chunked_level<D, true>(c, a, item, std::pow(std::pow(0.5, depth), 1.5 * 2), st.skewGrid[t - 1])) return false;
+            Grid<D> gl(t - 1);
+            if (!dalloc(c, &st.skewGrid[t - 1], gl.N * K, "skew grid")) return false;
+            SplatArgs a{st.cellKey, st.cellStart, nc, depth, t, TR, rlo[t], rhi[t]};
+            skew_level_kernel<<<nblocks(n, 256), 256, 0, s>>>(st.sdepth, st.order, n, t, depth, D, lw);
+            item_bspline_kernel<D><<<nblocks(n, 256), 256, 0, s>>>(st.pos, st.order, n, t, 2 * TR + 1, lw, bs);
+            SkewItem<D> item{bs, lw, frame};
+            if (gl.N <= kChunkedMaxVertices)
+            {
+                if (!chunked_level<D, true>(c, a, item, std::pow(std::pow(0.5, depth), 1.5 * 2), st.skewGrid[t - 1])) return false;
+            }
+            else
+                vertex_gather_kernel<D, true><<<nblocks(gl.N, 128), 128, 0, s>>>(a, item, std::pow(std::pow(0.5, depth), 1.5 * 2),
+                                                                               st.skewGrid[t - 1]);
         }
-        else
-        {
-            SkewItem<D> item{st.pos, st.skew, st.measure, st.sdepth, st.order};
-            vertex_gather_kernel<D, true><<<nblocks(gl.N, 128), 128, 0, s>>>(a, item, std::pow(std::pow(0.5, depth), 1.5 * 2),
-                                                                           st.skewGrid[t - 1]);
-        }
+        c.release(bs); c.release(lw); c.release(frame);
     }
     if (!c.launch_ok("frame splat")) return false;
 

@@ -8,6 +8,8 @@
 //   GS colour     PairedGaussSeidelSolve (one parity colour)         ExteriorPoissonSolvers.h:156-196
 //   prolongation  ScalarFunctions::prolongation                      Hat.scalars.inl:1747-1779
 //   restriction   its transpose (the Galerkin restriction of MG.h:120-127)
+#include <algorithm>
+
 #include "epr_common.cuh"
 #include "epr_element.cuh"
 #include "epr_kernels.h"
@@ -524,16 +526,27 @@ __global__ void __launch_bounds__(kThreads) gs_colour_lanes_kernel(LevelPtrs<Rea
 // All sweeps of a small level in one thread block: the colours follow each other behind a block
 // barrier, which also makes each colour's writes visible to the next.  Used for the coarse levels
 // of the cascadic schedule, whose thousands of tiny sweeps would otherwise be bound by launch
-// latency.
-constexpr int kPersistentThreads = 256;
+// latency.  The level's coefficients, and its stencils when they fit, live in shared memory for the
+// whole schedule.  The block holds up to MaxThreads threads (1024 where the lane update fits in 64
+// registers: 3D float) so that a colour takes as few passes as possible.
 template <int D, typename Real>
-__global__ void __launch_bounds__(kPersistentThreads) gs_level_kernel(LevelPtrs<Real> L, int iters, unsigned int *err, int separate)
+constexpr int persistent_threads() { return (D == 3 && sizeof(Real) == 4) ? 1024 : 256; }
+template <int D, typename Real, bool SmemStencil, int MaxThreads>
+__global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L, int iters, unsigned int *err, int separate)
 {
     Grid<D> g(L.level);
-    // the level's coefficients live in shared memory for the whole schedule
+    constexpr int S = Dims<D>::S;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Real *xy = reinterpret_cast<Real *>(smem_raw);
     for (int64_t k = threadIdx.x; k < 2 * g.N; k += blockDim.x) xy[k] = L.xy[k];
+    LevelPtrs<Real> Ls = L;
+    if constexpr (SmemStencil)
+    {
+        Real *A = xy + 2 * g.N, *B = A + S * g.N;
+        for (int64_t k = threadIdx.x; k < S * g.N; k += blockDim.x) { A[k] = L.A[k]; B[k] = L.B[k]; }
+        Ls.A = A;
+        Ls.B = B;
+    }
     __syncthreads();
     for (int it = 0; it < iters; it++)
         for (int c = 0; c < (1 << D); c++)
@@ -549,7 +562,7 @@ __global__ void __launch_bounds__(kPersistentThreads) gs_level_kernel(LevelPtrs<
                 if (active) col.node(j, I);
                 else
                     for (int d = 0; d < D; d++) I[d] = 0;
-                gs_update_lanes_at<D, Real>(L, xy, g, I, active, A, err, separate);
+                gs_update_lanes_at<D, Real>(Ls, xy, g, I, active, A, err, separate);
             }
             __syncthreads();
         }
@@ -750,7 +763,24 @@ int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cud
     if (iters <= 0) return 0;
     if (g.N <= kPersistentMaxNodes)
     {
-        gs_level_kernel<D, Real><<<1, kPersistentThreads, (size_t)(2 * g.N * sizeof(Real)), s>>>(L, iters, err, separate);
+        // one pass per colour (the colour of even nodes is the largest), whole warps
+        const int64_t lanes = Colour<D>(g, 0).n << D;
+        constexpr int MT = persistent_threads<D, Real>();
+        const int threads = (int)std::min<int64_t>(MT, (lanes + 31) / 32 * 32);
+        const size_t xyBytes = 2 * g.N * sizeof(Real), stBytes = 2 * (size_t)Dims<D>::S * g.N * sizeof(Real);
+        constexpr size_t kSmemLimit = 200 * 1024;
+        if (xyBytes + stBytes <= kSmemLimit)
+        {
+            static bool attr = false;
+            if (!attr)
+            {
+                cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+                attr = true;
+            }
+            gs_level_kernel<D, Real, true, MT><<<1, threads, xyBytes + stBytes, s>>>(L, iters, err, separate);
+        }
+        else
+            gs_level_kernel<D, Real, false, MT><<<1, threads, xyBytes, s>>>(L, iters, err, separate);
         return 1;
     }
     int n = 0;
