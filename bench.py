@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--solver", default="cascadic", choices=["cascadic", "multigrid"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true")
     ap.add_argument("--cpu-depth", type=int, default=6)
     return ap.parse_args()
 
@@ -262,6 +263,18 @@ def main():
             "build_ms": build_ms, "wall_s": wall,
             "final_energy": st["fit_energy"] + st["reg_energy"], "initial_energy": st["initial_energy"],
             "unknown_sweeps_per_s": 2 * schedule_node_updates(3, depth) / per_step_s}
+    # error of the result against the double-precision run of the same schedule (the CUDA FP64
+    # path reproduces the reference's algorithm to 1e-9 on the pinned cases)
+    if args.precision == "fp32" and not args.no_fp64_check:
+        xs32 = r.coefficients(depth)[0]
+        r64 = epr.Reconstructor(3, depth, pu, sk, precision="fp64", solver=args.solver, device=local)
+        st64 = r64.solve()
+        xs64 = r64.coefficients(depth)[0]
+        e32, e64 = line["final_energy"], st64["fit_energy"] + st64["reg_energy"]
+        line["error_vs_fp64"] = {"energy_fp64": e64, "energy_rel_diff": (e32 - e64) / e64,
+                                 "finest_x_rel_l2": float(np.linalg.norm(xs32 - xs64) / np.linalg.norm(xs64)),
+                                 "fp64_solve_s": st64["solve_ms"] / 1e3}
+        r64.close()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference(pu, sk, depth, args.cpu_depth, 2, 1)
     if rank == 0:
