@@ -36,6 +36,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Depth-8 time-to-1e-6-residual, learned+FP32 vs plain FP64 GPU; stencil HBM GB/s"
 
+# DRAM bytes (read + write) per colour node of one 3D FP32 colour launch, from ncu captures of the
+# depth-7 launch (profiles/gs_colour_lanes_kernel_link_depth7_fp32.txt,
+# profiles/linear_gs_colour_kernel_link_depth7_fp32.txt); a depth-8 launch's traffic is these times
+# its colour nodes (traffic grows in proportion with the nodes).
+GS_DRAM_BYTES_PER_COLOUR_NODE_FP32 = (156.35328e6 + 5.318144e6) / 274625
+LGS_DRAM_BYTES_PER_COLOUR_NODE_FP32 = (40.49792e6 + 1.28e3) / 274625
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -225,8 +232,10 @@ def main():
     colour_nodes = (2 ** (depth - 1) + 1) ** 3
     gs_bytes = 2 * rs * N + colour_nodes * (2 * 27 * rs + 2 * rs)
     achieved = gs_bytes / (gs_ms * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "gs_colour_kernel", "achieved": achieved, "peak": hbm_peak,
-                "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_kind, "traffic": None,
+    fp32 = args.precision == "fp32"
+    gs_traffic = GS_DRAM_BYTES_PER_COLOUR_NODE_FP32 * colour_nodes if fp32 else None
+    roofline = {"bound": "hbm", "kernel": "gs_colour_lanes_kernel", "achieved": achieved, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_kind, "traffic": gs_traffic,
                 "launch_ms": gs_ms, "algorithmic_bytes_per_launch": gs_bytes,
                 "note": "FMA-bound quartic relaxation; bytes = coefficient read + stencil columns + update writes"}
 
@@ -238,7 +247,8 @@ def main():
     lgs_bytes = colour_nodes * (27 + 2) * rs + N * rs
     lgs_achieved = lgs_bytes / (lgs_ms * 1e-3) / 1e9
     stencil_roofline = {"bound": "hbm", "kernel": "linear_gs_colour_kernel", "achieved": lgs_achieved, "peak": hbm_peak,
-                        "unit": "GB/s", "frac": lgs_achieved / hbm_peak, "peak_source": peak_kind, "traffic": None,
+                        "unit": "GB/s", "frac": lgs_achieved / hbm_peak, "peak_source": peak_kind,
+                        "traffic": LGS_DRAM_BYTES_PER_COLOUR_NODE_FP32 * colour_nodes if fp32 else None,
                         "launch_ms": lgs_ms, "algorithmic_bytes_per_launch": lgs_bytes}
 
     # end to end through the public API from host buffers
