@@ -489,6 +489,108 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
     }
 }
 
+// Warp-per-node variant for the coarsest 3D levels, where a colour has at most a few dozen nodes
+// and the update latency (not throughput) sets the pace: lane 3 A + K (A < 8, K < 3) integrates
+// component K of element A alone, lanes 24-31 take the stencil column.  Every (A, K) pair runs the
+// same code: the element is mirrored so that the node is its corner 0 and its axes are permuted so
+// that component K's axes (P, Q) and the remaining axis become component 0's (1, 0) and 2; the
+// integrals are invariant under both maps (each term carries one P- and one Q-derivative).
+template <typename Real>
+__device__ __forceinline__ Real warp_sum_all(Real v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename Real>
+__device__ __forceinline__ void gs_update_warp3(const LevelPtrs<Real> &L, Real *xy, const Grid<3> &g, const int *I, bool active,
+                                                unsigned int *err, int separate)
+{
+    constexpr int S = 27;
+    const int lane = threadIdx.x & 31;
+    Real h[5] = {0, 0, 0, 0, 0};
+    Real ax = 0, ay = 0, bx = 0, by = 0, acen = 0;
+    int64_t i = 0;
+    if (active)
+    {
+        const int64_t st[3] = {(int64_t)(g.r + 1) * (g.r + 1), (int64_t)(g.r + 1), 1};
+        i = I[0] * st[0] + I[1] * st[1] + I[2];
+        if (lane < 24)
+        {
+            const int A = lane / 3, K = lane - 3 * (lane / 3);
+            // physical axis of canonical axes 0, 1, 2 (= Q, P, R of component K)
+            const int p0 = (K == 2) ? 1 : 0, p1 = (K == 0) ? 1 : 2, p2 = (K == 0) ? 2 : (K == 1 ? 1 : 0);
+            const int pax[3] = {p0, p1, p2};
+            bool ok = true;
+#pragma unroll
+            for (int d = 0; d < 3; d++)
+            {
+                int e = I[d] - cbit<3>(A, d);
+                ok = ok && e >= 0 && e < g.r;
+            }
+            if (ok)
+            {
+                Real x[8], y[8];
+#pragma unroll
+                for (int cc = 0; cc < 8; cc++)
+                {
+                    int64_t jj = i;
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+                    {
+                        const int d = pax[a], b = cbit<3>(cc, a);
+                        jj += (cbit<3>(A, d) ? -b : b) * st[d];
+                    }
+                    Real2<Real> v = ld2(xy, jj);
+                    x[cc] = v.x;
+                    y[cc] = v.y;
+                }
+                component_fit<3, 0, Real>(x, y, 0, h);
+            }
+        }
+        else
+        {
+            for (int o = lane - 24; o < S; o += 8)
+            {
+                const int off[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+                bool in = true;
+#pragma unroll
+                for (int d = 0; d < 3; d++) { int t = I[d] + off[d]; in = in && t >= 0 && t <= g.r; }
+                if (!in) continue;
+                const int64_t jj = i + off[0] * st[0] + off[1] * st[1] + off[2];
+                Real a = L.A[(int64_t)o * L.N + i];
+                Real b = L.B[(int64_t)o * L.N + i];
+                Real2<Real> v = ld2(xy, jj);
+                ax += a * v.x;
+                ay += a * v.y;
+                if (o == 13) acen = a;
+                else { bx += b * v.x; by += b * v.y; }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++) h[k] = warp_sum_all(h[k]);
+    ax = warp_sum_all(ax); ay = warp_sum_all(ay); bx = warp_sum_all(bx); by = warp_sum_all(by); acen = warp_sum_all(acen);
+    if (!active || lane != 0) return;
+    const Real sc = (Real)wedge_scale<3>(g.r);
+    Real q[5];
+    q[0] = h[0] * sc + acen;
+    q[1] = h[1] * sc + acen;
+    q[2] = (Real)2 * h[2] * sc;
+    q[3] = (Real)2 * h[3] * sc + (Real)2 * ax - (Real)2 * by;
+    q[4] = (Real)2 * h[4] * sc + (Real)2 * ay + (Real)2 * bx;
+    Real p0, p1;
+    if (node_step<Real>(q, separate, p0, p1))
+    {
+        Real2<Real> v = ld2(xy, i);
+        v.x += p0;
+        v.y += p1;
+        if (!isfinite((double)v.x) || !isfinite((double)v.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
+        reinterpret_cast<Real2<Real> *>(xy)[i] = v;
+    }
+}
+
 template <int D, typename Real>
 __device__ __forceinline__ void gs_update_lanes(const LevelPtrs<Real> &L, const Grid<D> &g, const Colour<D> &col, int64_t j,
                                                 bool active, int A, unsigned int *err)
@@ -531,7 +633,7 @@ __global__ void __launch_bounds__(kThreads) gs_colour_lanes_kernel(LevelPtrs<Rea
 // registers: 3D float) so that a colour takes as few passes as possible.
 template <int D, typename Real>
 constexpr int persistent_threads() { return (D == 3 && sizeof(Real) == 4) ? 1024 : 256; }
-template <int D, typename Real, bool SmemStencil, int MaxThreads>
+template <int D, typename Real, bool SmemStencil, int MaxThreads, bool WarpPerNode>
 __global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L, int iters, unsigned int *err, int separate)
 {
     Grid<D> g(L.level);
@@ -552,17 +654,29 @@ __global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L,
         for (int c = 0; c < (1 << D); c++)
         {
             Colour<D> col(g, c);
-            const int per = blockDim.x >> D;  // nodes per pass of the block
-            const int A = threadIdx.x & ((1 << D) - 1);
-            for (int64_t j0 = 0; j0 < col.n; j0 += per)
+            if constexpr (WarpPerNode && D == 3)
             {
-                int64_t j = j0 + (threadIdx.x >> D);
-                bool active = j < col.n;
-                int I[D];
+                // one warp per node; the block holds a warp for every node of the largest colour
+                const int64_t j = threadIdx.x >> 5;
+                const bool active = j < col.n;
+                int I[3] = {0, 0, 0};
                 if (active) col.node(j, I);
-                else
-                    for (int d = 0; d < D; d++) I[d] = 0;
-                gs_update_lanes_at<D, Real>(Ls, xy, g, I, active, A, err, separate);
+                gs_update_warp3<Real>(Ls, xy, g, I, active, err, separate);
+            }
+            else
+            {
+                const int per = blockDim.x >> D;  // nodes per pass of the block
+                const int A = threadIdx.x & ((1 << D) - 1);
+                for (int64_t j0 = 0; j0 < col.n; j0 += per)
+                {
+                    int64_t j = j0 + (threadIdx.x >> D);
+                    bool active = j < col.n;
+                    int I[D];
+                    if (active) col.node(j, I);
+                    else
+                        for (int d = 0; d < D; d++) I[d] = 0;
+                    gs_update_lanes_at<D, Real>(Ls, xy, g, I, active, A, err, separate);
+                }
             }
             __syncthreads();
         }
@@ -763,24 +877,44 @@ int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cud
     if (iters <= 0) return 0;
     if (g.N <= kPersistentMaxNodes)
     {
-        // one pass per colour (the colour of even nodes is the largest), whole warps
-        const int64_t lanes = Colour<D>(g, 0).n << D;
         constexpr int MT = persistent_threads<D, Real>();
-        const int threads = (int)std::min<int64_t>(MT, (lanes + 31) / 32 * 32);
+        const int64_t colour0 = Colour<D>(g, 0).n;  // the colour of even nodes is the largest
         const size_t xyBytes = 2 * g.N * sizeof(Real), stBytes = 2 * (size_t)Dims<D>::S * g.N * sizeof(Real);
         constexpr size_t kSmemLimit = 200 * 1024;
-        if (xyBytes + stBytes <= kSmemLimit)
+        const bool smemStencil = xyBytes + stBytes <= kSmemLimit;
+        const size_t smem = xyBytes + (smemStencil ? stBytes : 0);
+        if (D == 3 && colour0 * 32 <= MT)
+        {
+            // a warp per node: the tiny levels, where the update latency sets the pace
+            const int threads = (int)colour0 * 32;
+            if (smemStencil)
+            {
+                static bool attr = false;
+                if (!attr)
+                {
+                    cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+                    attr = true;
+                }
+                gs_level_kernel<D, Real, true, MT, true><<<1, threads, smem, s>>>(L, iters, err, separate);
+            }
+            else
+                gs_level_kernel<D, Real, false, MT, true><<<1, threads, smem, s>>>(L, iters, err, separate);
+            return 1;
+        }
+        // lanes per node: one pass per colour where the block allows it, whole warps
+        const int threads = (int)std::min<int64_t>(MT, ((colour0 << D) + 31) / 32 * 32);
+        if (smemStencil)
         {
             static bool attr = false;
             if (!attr)
             {
-                cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+                cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
                 attr = true;
             }
-            gs_level_kernel<D, Real, true, MT><<<1, threads, xyBytes + stBytes, s>>>(L, iters, err, separate);
+            gs_level_kernel<D, Real, true, MT, false><<<1, threads, smem, s>>>(L, iters, err, separate);
         }
         else
-            gs_level_kernel<D, Real, false, MT><<<1, threads, xyBytes, s>>>(L, iters, err, separate);
+            gs_level_kernel<D, Real, false, MT, false><<<1, threads, smem, s>>>(L, iters, err, separate);
         return 1;
     }
     int n = 0;
