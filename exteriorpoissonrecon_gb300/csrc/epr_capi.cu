@@ -127,6 +127,7 @@ Context::~Context()
         release(red.partial); release(red.out); release(d_err); release(d_fit);
         setup.release(*this);
         release_mg(*this);
+        if (solve_graph) cudaGraphExecDestroy(solve_graph);
         cudaStreamSynchronize(stream);
         cudaStreamDestroy(stream);
     }
@@ -176,13 +177,13 @@ bool Context::energy(int l, double *out3)
     return true;
 }
 
-bool Context::gs(int l, int iters)
+bool Context::gs(int l, int iters, int64_t persistentMaxNodes)
 {
     bool fp32 = lvl32(l);
     launches += with_dim(this, [&](auto dd) {
         constexpr int D = decltype(dd)::value;
-        if (fp32) return launch_gs_sweeps<D, float>(level_ptrs<float>(this, l), iters, d_err, stream, P.separate);
-        return launch_gs_sweeps<D, double>(level_ptrs<double>(this, l), iters, d_err, stream, P.separate);
+        if (fp32) return launch_gs_sweeps<D, float>(level_ptrs<float>(this, l), iters, d_err, stream, P.separate, persistentMaxNodes);
+        return launch_gs_sweeps<D, double>(level_ptrs<double>(this, l), iters, d_err, stream, P.separate, persistentMaxNodes);
     });
     stats.node_updates += (int64_t)iters * levels[l].N;
     return launch_ok("gs");
@@ -253,6 +254,40 @@ bool Context::download_xy(int l, double *x, double *y, bool fromSolution)
     return true;
 }
 
+// The relaxation sequence of the cascadic schedule (GS on every solve level, prolongation to the
+// next), captured once into a CUDA graph and replayed: it is a fixed sequence of ~2,500 launches
+// with no host interaction.  In the graph only the two coarsest levels run their sweeps inside one
+// block; the others launch one kernel per colour, which the graph issues back to back.
+bool Context::relax_levels(int minD, int maxD, bool useGraph)
+{
+    const int64_t graphPersistentMax = dim == 3 ? 27 : 81;
+    if (useGraph && solve_graph)
+    {
+        launches += graph_launches;
+        stats.node_updates += graph_updates;
+        return cuda_ok(cudaGraphLaunch(solve_graph, stream), "graph launch");
+    }
+    const int64_t l0 = launches, u0 = stats.node_updates;
+    cudaGraph_t graph = nullptr;
+    if (useGraph && !cuda_ok(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture")) return false;
+    bool ok = true;
+    for (int l = minD; ok && l <= maxD; l++)
+    {
+        int iters = (int)std::ceil(std::pow(P.i_mult, depth - l) * P.gs_iters);
+        ok = gs(l, iters, useGraph ? graphPersistentMax : kPersistentMaxNodes);
+        if (ok && l < maxD) ok = prolong_add(l);
+    }
+    if (!useGraph) return ok;
+    cudaError_t e = cudaStreamEndCapture(stream, &graph);
+    if (!ok || !cuda_ok(e, "end capture")) { if (graph) cudaGraphDestroy(graph); return false; }
+    e = cudaGraphInstantiate(&solve_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (!cuda_ok(e, "graph instantiate")) { solve_graph = nullptr; return false; }
+    graph_launches = launches - l0;
+    graph_updates = stats.node_updates - u0;
+    return cuda_ok(cudaGraphLaunch(solve_graph, stream), "graph launch");
+}
+
 // The reference's cascadic schedule (ExteriorPoisson.h:315-409).  Each level is relaxed by paired
 // Gauss-Seidel (EPR_SOLVER_CASCADIC, the reference) or by alternating-solve rounds with linear
 // multigrid V-cycles until the gradient falls by `tolerance` (EPR_SOLVER_MULTIGRID).
@@ -306,7 +341,9 @@ bool Context::solve_cascadic()
             printf("Error[%2d]: %9.5f -> %.5f = %.5f + %.5f\n", 1 << maxD, e0[0] + e0[1], e1[0] + e1[1], e1[0], e1[1]);
         }
     }
-    for (int l = minD; !P.single_level && l <= maxD; l++)
+    const bool useGraph = !P.single_level && !P.verbose && P.solver == EPR_SOLVER_CASCADIC;
+    if (useGraph && !relax_levels(minD, maxD, true)) return false;
+    for (int l = minD; !P.single_level && !useGraph && l <= maxD; l++)
     {
         int iters = (int)std::ceil(std::pow(P.i_mult, depth - l) * P.gs_iters);
         double e0[3] = {0, 0, 0};
@@ -421,6 +458,12 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
         return nullptr;
     }
     if (const char *v = getenv("EPR_GS_VARIANT")) epr::set_gs_variant(atoi(v));
+    static uint64_t prepared = 0;  // devices whose kernel attributes are set
+    if (p.device >= 0 && p.device < 64 && !(prepared & (1ull << p.device)))
+    {
+        epr::prepare_gs_kernels();
+        prepared |= 1ull << p.device;
+    }
     epr_ctx *c = new epr_ctx;
     c->dim = dim;
     c->depth = depth;

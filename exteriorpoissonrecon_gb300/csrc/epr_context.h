@@ -70,6 +70,10 @@ struct Context
     int64_t launches = 0;  // kernels launched since the last epr_solve started
     Setup setup;
     MGHierarchy *mg = nullptr;  // linear multigrid storage (epr_mg.cu), allocated on first use
+    // the relaxation sequence of the cascadic solve captured as one CUDA graph (built on the first
+    // solve, replayed by the next ones), with the host-side counts of what it launches
+    cudaGraphExec_t solve_graph = nullptr;
+    int64_t graph_launches = 0, graph_updates = 0;
 
     virtual ~Context();
     void fail(int code, const char *fmt, ...);
@@ -85,7 +89,8 @@ struct Context
     bool push_xy(int l);
     bool pull_xy(int l);
     bool energy(int l, double *out3);
-    bool gs(int l, int iters);
+    bool gs(int l, int iters, int64_t persistentMaxNodes = kPersistentMaxNodes);
+    bool relax_levels(int minD, int maxD, bool useGraph);
     bool check_errors();
     bool prolong_add(int l);
     bool upload_xy(int l, const double *x, const double *y);

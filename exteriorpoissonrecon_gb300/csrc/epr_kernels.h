@@ -39,11 +39,16 @@ template <int D, typename Real>
 void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, cudaStream_t s, int separate = 0);
 // selects the colour-kernel variant (0: one thread per node, 1: 2^D lanes per node)
 void set_gs_variant(int v);
-// iters full sweeps (all 2^D colours in order); levels of at most kPersistentMaxNodes nodes run all
-// sweeps inside one thread block.  Returns the number of kernels launched.
+// iters full sweeps (all 2^D colours in order); levels of at most persistentMaxNodes nodes run all
+// sweeps inside one thread block, larger ones launch one kernel per colour.  Returns the number of
+// kernels launched.
 constexpr int64_t kPersistentMaxNodes = 729;
 template <int D, typename Real>
-int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s, int separate = 0);
+int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s, int separate = 0,
+                     int64_t persistentMaxNodes = kPersistentMaxNodes);
+// sets the shared-memory carve-out of the single-block level kernels (once per process, before
+// any stream capture)
+void prepare_gs_kernels();
 template <int D, typename Real>
 void launch_gn_matvec(const LevelPtrs<Real> &L, const Real *xy, const Real *dxy, Real *out, cudaStream_t s);
 // fine (2 N_f) = P coarse (2 N_c), pairs; add != 0 accumulates

@@ -870,51 +870,49 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
 
 void set_gs_variant(int v) { g_gs_variant = v; }
 
+// shared-memory carve-out of the single-block level kernels whose stencils live in shared memory
+constexpr size_t kLevelSmemLimit = 200 * 1024;
+
 template <int D, typename Real>
-int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s, int separate)
+static void prepare_level_kernels()
+{
+    constexpr int MT = persistent_threads<D, Real>();
+    cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLevelSmemLimit);
+    cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLevelSmemLimit);
+}
+
+void prepare_gs_kernels()
+{
+    prepare_level_kernels<3, float>();
+    prepare_level_kernels<3, double>();
+    prepare_level_kernels<4, float>();
+    prepare_level_kernels<4, double>();
+}
+
+template <int D, typename Real>
+int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s, int separate, int64_t persistentMaxNodes)
 {
     Grid<D> g(L.level);
     if (iters <= 0) return 0;
-    if (g.N <= kPersistentMaxNodes)
+    if (g.N <= persistentMaxNodes)
     {
         constexpr int MT = persistent_threads<D, Real>();
         const int64_t colour0 = Colour<D>(g, 0).n;  // the colour of even nodes is the largest
         const size_t xyBytes = 2 * g.N * sizeof(Real), stBytes = 2 * (size_t)Dims<D>::S * g.N * sizeof(Real);
-        constexpr size_t kSmemLimit = 200 * 1024;
-        const bool smemStencil = xyBytes + stBytes <= kSmemLimit;
+        const bool smemStencil = xyBytes + stBytes <= kLevelSmemLimit;
         const size_t smem = xyBytes + (smemStencil ? stBytes : 0);
-        if (D == 3 && colour0 * 32 <= MT)
+        if (D == 3 && colour0 <= 8 && colour0 * 32 <= MT)
         {
             // a warp per node: the tiny levels, where the update latency sets the pace
             const int threads = (int)colour0 * 32;
-            if (smemStencil)
-            {
-                static bool attr = false;
-                if (!attr)
-                {
-                    cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-                    attr = true;
-                }
-                gs_level_kernel<D, Real, true, MT, true><<<1, threads, smem, s>>>(L, iters, err, separate);
-            }
-            else
-                gs_level_kernel<D, Real, false, MT, true><<<1, threads, smem, s>>>(L, iters, err, separate);
+            if (smemStencil) gs_level_kernel<D, Real, true, MT, true><<<1, threads, smem, s>>>(L, iters, err, separate);
+            else gs_level_kernel<D, Real, false, MT, true><<<1, threads, smem, s>>>(L, iters, err, separate);
             return 1;
         }
         // lanes per node: one pass per colour where the block allows it, whole warps
         const int threads = (int)std::min<int64_t>(MT, ((colour0 << D) + 31) / 32 * 32);
-        if (smemStencil)
-        {
-            static bool attr = false;
-            if (!attr)
-            {
-                cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-                attr = true;
-            }
-            gs_level_kernel<D, Real, true, MT, false><<<1, threads, smem, s>>>(L, iters, err, separate);
-        }
-        else
-            gs_level_kernel<D, Real, false, MT, false><<<1, threads, smem, s>>>(L, iters, err, separate);
+        if (smemStencil) gs_level_kernel<D, Real, true, MT, false><<<1, threads, smem, s>>>(L, iters, err, separate);
+        else gs_level_kernel<D, Real, false, MT, false><<<1, threads, smem, s>>>(L, iters, err, separate);
         return 1;
     }
     int n = 0;
@@ -968,7 +966,7 @@ void launch_convert_f2d(const float *in, double *out, int64_t n, cudaStream_t st
     template void launch_quadfit<D, R>(const LevelPtrs<R> &, const R *, double *, cudaStream_t);        \
     template void launch_grad_norm<D, R>(const LevelPtrs<R> &, const R *, const Reduce &, cudaStream_t); \
     template void launch_gs_colour<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t, int); \
-    template int launch_gs_sweeps<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t, int);  \
+    template int launch_gs_sweeps<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t, int, int64_t); \
     template void launch_gn_matvec<D, R>(const LevelPtrs<R> &, const R *, const R *, R *, cudaStream_t); \
     template void launch_prolong<D, R>(int, const R *, R *, int, cudaStream_t);                         \
     template void launch_restrict<D, R>(int, const R *, R *, cudaStream_t);
