@@ -267,9 +267,13 @@ bool Context::relax_levels(int minD, int maxD, bool useGraph)
         stats.node_updates += graph_updates;
         return cuda_ok(cudaGraphLaunch(solve_graph, stream), "graph launch");
     }
+    // the first solve of a context launches directly (a one-off solve would not repay the graph's
+    // instantiation); the second one captures, with the same launch configuration, so every solve
+    // computes the same sequence of kernels
+    const bool capture = useGraph && solves_done > 0;
     const int64_t l0 = launches, u0 = stats.node_updates;
     cudaGraph_t graph = nullptr;
-    if (useGraph && !cuda_ok(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture")) return false;
+    if (capture && !cuda_ok(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture")) return false;
     bool ok = true;
     for (int l = minD; ok && l <= maxD; l++)
     {
@@ -277,7 +281,7 @@ bool Context::relax_levels(int minD, int maxD, bool useGraph)
         ok = gs(l, iters, useGraph ? graphPersistentMax : kPersistentMaxNodes);
         if (ok && l < maxD) ok = prolong_add(l);
     }
-    if (!useGraph) return ok;
+    if (!capture) return ok;
     cudaError_t e = cudaStreamEndCapture(stream, &graph);
     if (!ok || !cuda_ok(e, "end capture")) { if (graph) cudaGraphDestroy(graph); return false; }
     e = cudaGraphInstantiate(&solve_graph, graph, 0);
@@ -401,6 +405,7 @@ bool Context::solve_cascadic()
         if (!launch_ok("hierarchical")) return false;
     }
     solved = true;
+    solves_done++;
     return cuda_ok(cudaStreamSynchronize(stream), "solve sync");
 }
 

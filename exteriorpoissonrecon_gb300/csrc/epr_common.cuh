@@ -59,9 +59,12 @@ struct Grid
         for (int d = 0; d < D; d++) i = i * (r + 1) + I[d];
         return i;
     }
+    // 32-bit arithmetic: every supported grid (3D depth <= 10, 4D depth <= 7) has < 2^32 nodes
     __host__ __device__ void node(int64_t i, int *I) const
     {
-        for (int d = D - 1; d >= 0; d--) { I[d] = (int)(i % (r + 1)); i /= (r + 1); }
+        uint32_t u = (uint32_t)i;
+        const uint32_t n = (uint32_t)(r + 1);
+        for (int d = D - 1; d >= 0; d--) { uint32_t q = u / n; I[d] = (int)(u - q * n); u = q; }
     }
     __host__ __device__ int64_t elem(const int *E) const
     {
@@ -71,7 +74,9 @@ struct Grid
     }
     __host__ __device__ void elem(int64_t i, int *E) const
     {
-        for (int d = D - 1; d >= 0; d--) { E[d] = (int)(i % r); i /= r; }
+        uint32_t u = (uint32_t)i;
+        const uint32_t n = (uint32_t)r;
+        for (int d = D - 1; d >= 0; d--) { uint32_t q = u / n; E[d] = (int)(u - q * n); u = q; }
     }
     // node stride along axis d
     __host__ __device__ int64_t stride(int d) const
@@ -110,7 +115,13 @@ struct Colour
     // j-th node of the colour (axis 0 slowest)
     __host__ __device__ void node(int64_t j, int *I) const
     {
-        for (int d = D - 1; d >= 0; d--) { int t = (int)(j % cnt[d]); j /= cnt[d]; I[d] = 2 * t + par[d]; }
+        uint32_t u = (uint32_t)j;
+        for (int d = D - 1; d >= 0; d--)
+        {
+            const uint32_t c = (uint32_t)cnt[d], q = u / c;
+            I[d] = 2 * (int)(u - q * c) + par[d];
+            u = q;
+        }
     }
 };
 

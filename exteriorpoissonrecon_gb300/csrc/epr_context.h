@@ -74,6 +74,7 @@ struct Context
     // solve, replayed by the next ones), with the host-side counts of what it launches
     cudaGraphExec_t solve_graph = nullptr;
     int64_t graph_launches = 0, graph_updates = 0;
+    int solves_done = 0;
 
     virtual ~Context();
     void fail(int code, const char *fmt, ...);
