@@ -255,12 +255,17 @@ def main():
     e2e_s = []
     h2d = pu.nbytes + sk.nbytes
     d2h = sum(2 * 8 * (2 ** l + 1) ** 3 for l in range(depth + 1))
+    e2e_parts = []
     for _ in range(args.e2e_steps):
         t0 = time.perf_counter()
         r2 = epr.Reconstructor(3, depth, pu, sk, precision=args.precision, solver=args.solver, device=local)
+        t1 = time.perf_counter()
         r2.solve()
+        t2 = time.perf_counter()
         r2.solution()
-        e2e_s.append(time.perf_counter() - t0)
+        t3 = time.perf_counter()
+        e2e_s.append(t3 - t0)
+        e2e_parts.append({"create_upload_build_s": t1 - t0, "solve_s": t2 - t1, "download_s": t3 - t2})
         r2.close()
     e2e_v = allmax(pg, statistics.mean(e2e_s)) if e2e_s else None
 
@@ -269,7 +274,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
             "data": "synthetic", "config": config, "clocks": clk, "gpu_launches": int(launches),
             "roofline": roofline, "stencil_roofline": stencil_roofline,
-            "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "parts": e2e_parts[-1] if e2e_parts else None},
             "build_ms": build_ms, "wall_s": wall,
             "final_energy": st["fit_energy"] + st["reg_energy"], "initial_energy": st["initial_energy"],
             "unknown_sweeps_per_s": 2 * schedule_node_updates(3, depth) / per_step_s}

@@ -234,24 +234,37 @@ static double RandomDouble()
     return double(v) / RAND_MAX_SQUARED;
 }
 
+// host planar arrays <-> device pairs: the two arrays travel as they are and the (de)interleaving
+// runs on the device
 bool Context::upload_xy(int l, const double *x, const double *y)
 {
-    std::vector<double> h(2 * levels[l].N);
-    for (int64_t i = 0; i < levels[l].N; i++) { h[2 * i] = x[i]; h[2 * i + 1] = y[i]; }
-    if (!cuda_ok(cudaMemcpyAsync(levels[l].xy64, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, stream), "upload xy")) return false;
-    if (!push_xy(l)) return false;
-    return cuda_ok(cudaStreamSynchronize(stream), "upload sync");
+    const int64_t N = levels[l].N;
+    double *planar = nullptr;
+    if (!alloc((void **)&planar, sizeof(double) * 2 * N, "alloc planar")) return false;
+    bool ok = cuda_ok(cudaMemcpyAsync(planar, x, sizeof(double) * N, cudaMemcpyHostToDevice, stream), "upload x") &&
+              cuda_ok(cudaMemcpyAsync(planar + N, y, sizeof(double) * N, cudaMemcpyHostToDevice, stream), "upload y");
+    if (ok)
+    {
+        launch_merge_pairs(planar, planar + N, levels[l].xy64, N, stream);
+        ok = launch_ok("merge pairs") && push_xy(l);
+    }
+    release(planar);
+    return ok && cuda_ok(cudaStreamSynchronize(stream), "upload sync");
 }
 
 bool Context::download_xy(int l, double *x, double *y, bool fromSolution)
 {
-    std::vector<double> h(2 * levels[l].N);
+    const int64_t N = levels[l].N;
     double *src = fromSolution ? levels[l].tmp64 : levels[l].xy64;
     if (!fromSolution && !pull_xy(l)) return false;
-    if (!cuda_ok(cudaMemcpyAsync(h.data(), src, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream), "download xy")) return false;
-    if (!cuda_ok(cudaStreamSynchronize(stream), "download sync")) return false;
-    for (int64_t i = 0; i < levels[l].N; i++) { x[i] = h[2 * i]; y[i] = h[2 * i + 1]; }
-    return true;
+    double *planar = nullptr;
+    if (!alloc((void **)&planar, sizeof(double) * 2 * N, "alloc planar")) return false;
+    launch_split_pairs(src, planar, planar + N, N, stream);
+    bool ok = launch_ok("split pairs") &&
+              cuda_ok(cudaMemcpyAsync(x, planar, sizeof(double) * N, cudaMemcpyDeviceToHost, stream), "download x") &&
+              cuda_ok(cudaMemcpyAsync(y, planar + N, sizeof(double) * N, cudaMemcpyDeviceToHost, stream), "download y");
+    release(planar);
+    return ok && cuda_ok(cudaStreamSynchronize(stream), "download sync");
 }
 
 // The relaxation sequence of the cascadic schedule (GS on every solve level, prolongation to the
@@ -278,7 +291,10 @@ bool Context::relax_levels(int minD, int maxD, bool useGraph)
     for (int l = minD; ok && l <= maxD; l++)
     {
         int iters = (int)std::ceil(std::pow(P.i_mult, depth - l) * P.gs_iters);
-        ok = gs(l, iters, useGraph ? graphPersistentMax : kPersistentMaxNodes);
+        // the captured sequence launches one kernel per colour from level 2 on; a direct run keeps
+        // the single-block kernel up to 729 nodes (fewer host launches).  Both compute every node
+        // update with the same arithmetic, so the results are identical.
+        ok = gs(l, iters, capture ? graphPersistentMax : kPersistentMaxNodes);
         if (ok && l < maxD) ok = prolong_add(l);
     }
     if (!capture) return ok;

@@ -68,6 +68,9 @@ void launch_scale(Real *v, int64_t n, double s, cudaStream_t st);
 template <typename Real>
 void launch_axpy(Real *y, const Real *x, int64_t n, double a, cudaStream_t st);
 void launch_convert_d2f(const double *in, float *out, int64_t n, cudaStream_t st);
+// interleaved (x, y) pairs <-> two planar arrays
+void launch_split_pairs(const double *xy, double *x, double *y, int64_t n, cudaStream_t st);
+void launch_merge_pairs(const double *x, const double *y, double *xy, int64_t n, cudaStream_t st);
 void launch_convert_f2d(const float *in, double *out, int64_t n, cudaStream_t st);
 
 }  // namespace epr

@@ -952,6 +952,24 @@ void launch_axpy(Real *y, const Real *x, int64_t n, double a, cudaStream_t st)
 {
     if (n) axpy_kernel<Real><<<blocks_for(n, 256), 256, 0, st>>>(y, x, n, a);
 }
+__global__ void split_pairs_kernel(const double *xy, double *x, double *y, int64_t n)
+{
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) { double2 v = reinterpret_cast<const double2 *>(xy)[i]; x[i] = v.x; y[i] = v.y; }
+}
+__global__ void merge_pairs_kernel(const double *x, const double *y, double *xy, int64_t n)
+{
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) reinterpret_cast<double2 *>(xy)[i] = double2{x[i], y[i]};
+}
+void launch_split_pairs(const double *xy, double *x, double *y, int64_t n, cudaStream_t st)
+{
+    if (n) split_pairs_kernel<<<blocks_for(n, 256), 256, 0, st>>>(xy, x, y, n);
+}
+void launch_merge_pairs(const double *x, const double *y, double *xy, int64_t n, cudaStream_t st)
+{
+    if (n) merge_pairs_kernel<<<blocks_for(n, 256), 256, 0, st>>>(x, y, xy, n);
+}
 void launch_convert_d2f(const double *in, float *out, int64_t n, cudaStream_t st)
 {
     if (n) d2f_kernel<<<blocks_for(n, 256), 256, 0, st>>>(in, out, n);
