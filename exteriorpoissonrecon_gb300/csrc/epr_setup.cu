@@ -773,8 +773,10 @@ __global__ void screening_kernel(const double *pos, const double *noise, const i
 }
 
 // B(f2, f1) = sum_E sum_{a != b} S_E(b, a) int_E d_a phi_f1 d_b phi_f2 (column f1)
+// (elements whose frame is zero contribute nothing and are skipped; the element and corner loops
+// are unrolled so that the 3^D accumulators stay in registers)
 template <int D>
-__global__ void constraint_kernel(const double *Sel, int depth, double *B)
+__global__ void __launch_bounds__(128) constraint_kernel(const double *Sel, int depth, double *B)
 {
     constexpr int S = Dims<D>::S;
     Grid<D> g(depth);
@@ -783,8 +785,10 @@ __global__ void constraint_kernel(const double *Sel, int depth, double *B)
     int I[D];
     g.node(i, I);
     double acc[S];
+#pragma unroll
     for (int o = 0; o < S; o++) acc[o] = 0;
     const double invr = 1. / g.r;
+#pragma unroll
     for (int a = 0; a < (1 << D); a++)
     {
         int E[D];
@@ -792,6 +796,10 @@ __global__ void constraint_kernel(const double *Sel, int depth, double *B)
         for (int d = 0; d < D; d++) { E[d] = I[d] - ((a >> (D - 1 - d)) & 1); if (E[d] < 0 || E[d] >= g.r) ok = false; }
         if (!ok) continue;
         const double *s = Sel + g.elem(E) * Dims<D>::K;
+        bool zero = true;
+        for (int k = 0; k < Dims<D>::K; k++) zero = zero && s[k] == 0;
+        if (zero) continue;
+#pragma unroll
         for (int b = 0; b < (1 << D); b++)
         {
             int o = 0;
@@ -876,6 +884,56 @@ __global__ void dirichlet_kernel(int level, double w, double *dst)
         }
         dst[(int64_t)o * g.N + i] += w * sum;
     }
+}
+
+// 3D Galerkin with every index compile-time: for a coarse node J and fine offsets (go, fo) the
+// parity of F = 2 J + go + fo, hence the coarse parents of F relative to J, depend on go and fo
+// only, so the 27 accumulators stay in registers.  Same sums, same order as the generic kernel.
+__global__ void __launch_bounds__(64) galerkin3_kernel(int fineLevel, const double *Mf, double *Mc)
+{
+    constexpr int D = 3, S = 27;
+    Grid<D> gf(fineLevel), gc(fineLevel - 1);
+    int64_t J = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (J >= gc.N) return;
+    int Jc[D];
+    gc.node(J, Jc);
+    double acc[S];
+#pragma unroll
+    for (int o = 0; o < S; o++) acc[o] = 0;
+#pragma unroll
+    for (int go = 0; go < S; go++)
+    {
+        const int g0 = go / 9 - 1, g1 = (go / 3) % 3 - 1, g2 = go % 3 - 1;
+        const int G0 = 2 * Jc[0] + g0, G1 = 2 * Jc[1] + g1, G2 = 2 * Jc[2] + g2;
+        if (G0 < 0 || G0 > gf.r || G1 < 0 || G1 > gf.r || G2 < 0 || G2 > gf.r) continue;
+        const double wg = (g0 ? 0.5 : 1.) * (g1 ? 0.5 : 1.) * (g2 ? 0.5 : 1.);
+        const int64_t gi = ((int64_t)G0 * (gf.r + 1) + G1) * (gf.r + 1) + G2;
+#pragma unroll
+        for (int fo = 0; fo < S; fo++)
+        {
+            const double v = Mf[(int64_t)fo * gf.N + gi];
+            if (v == 0) continue;
+            const int f[3] = {g0 + fo / 9 - 1, g1 + (fo / 3) % 3 - 1, g2 + fo % 3 - 1};  // F - 2 J
+            const int n1 = (f[0] & 1) + (f[1] & 1) + (f[2] & 1);
+#pragma unroll
+            for (int c = 0; c < (1 << n1); c++)
+            {
+                double w = wg * v;
+                int o = 0, bit = 0;
+#pragma unroll
+                for (int d = 0; d < D; d++)
+                {
+                    int rel;  // coarse parent of F minus J, + 1
+                    if (f[d] & 1) { rel = ((f[d] - 1) >> 1) + ((c >> bit) & 1) + 1; bit++; w *= 0.5; }
+                    else rel = (f[d] >> 1) + 1;
+                    o = o * 3 + rel;
+                }
+                acc[o] += w;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 0; o < S; o++) Mc[(int64_t)o * gc.N + J] = acc[o];
 }
 
 // Galerkin P^T M P of a column stencil, one coarse column per thread
@@ -1229,8 +1287,8 @@ bool build_impl(Context &c, Setup &st)
     for (int l = depth; l > 0; l--)
     {
         Grid<D> gc(l - 1);
-        galerkin_kernel<D><<<nblocks(gc.N, 64), 64, 0, s>>>(l, c.levels[l].A64, c.levels[l - 1].A64);
-        galerkin_kernel<D><<<nblocks(gc.N, 64), 64, 0, s>>>(l, c.levels[l].B64, c.levels[l - 1].B64);
+        launch_galerkin<D>(l, c.levels[l].A64, c.levels[l - 1].A64, s);
+        launch_galerkin<D>(l, c.levels[l].B64, c.levels[l - 1].B64, s);
     }
     if (!c.launch_ok("galerkin")) return false;
     for (int l = 0; l <= depth; l++)
@@ -1322,7 +1380,8 @@ template <int D>
 void launch_galerkin(int fineLevel, const double *Mf, double *Mc, cudaStream_t s)
 {
     Grid<D> gc(fineLevel - 1);
-    galerkin_kernel<D><<<nblocks(gc.N, 64), 64, 0, s>>>(fineLevel, Mf, Mc);
+    if constexpr (D == 3) galerkin3_kernel<<<nblocks(gc.N, 64), 64, 0, s>>>(fineLevel, Mf, Mc);
+    else galerkin_kernel<D><<<nblocks(gc.N, 64), 64, 0, s>>>(fineLevel, Mf, Mc);
 }
 template void launch_galerkin<3>(int, const double *, double *, cudaStream_t);
 template void launch_galerkin<4>(int, const double *, double *, cudaStream_t);
