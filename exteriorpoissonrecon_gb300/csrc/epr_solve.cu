@@ -413,32 +413,39 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
                                                    int A, unsigned int *err, int separate = 0)
 {
     constexpr int C = 1 << D, S = Dims<D>::S;
-    NodeCtx<D> nc;
     int64_t i = 0;
     Real h[5] = {0, 0, 0, 0, 0};
     Real ax = 0, ay = 0, bx = 0, by = 0, acen = 0;
     if (active)
     {
+        // node indices in 32 bits (every supported grid has < 2^32 nodes); signed strides of the
+        // element mirrored so that the node is its corner 0
+        int st[D], sd[D];
+        st[D - 1] = 1;
 #pragma unroll
-        for (int d = 0; d < D; d++) { nc.I[d] = I[d]; nc.stride[d] = g.stride(d); }
-        i = g.node(nc.I);
+        for (int d = D - 2; d >= 0; d--) st[d] = st[d + 1] * (g.r + 1);
+        uint32_t iu = 0;
         bool ok = true;
 #pragma unroll
         for (int d = 0; d < D; d++)
         {
-            int e = nc.I[d] - cbit<D>(A, d);
+            iu += (uint32_t)I[d] * (uint32_t)st[d];
+            sd[d] = cbit<D>(A, d) ? -st[d] : st[d];
+            int e = I[d] - cbit<D>(A, d);
             ok = ok && e >= 0 && e < g.r;
         }
+        i = iu;
         if (ok)
         {
             Real x[C], y[C];
 #pragma unroll
             for (int cc = 0; cc < C; cc++)
             {
-                int64_t jj = i;
+                int jj = (int)iu;
 #pragma unroll
-                for (int d = 0; d < D; d++) jj += (int64_t)(cbit<D>(A, d) ? -cbit<D>(cc, d) : cbit<D>(cc, d)) * nc.stride[d];
-                Real2<Real> v = ld2(xy, jj);
+                for (int d = 0; d < D; d++)
+                    if (cbit<D>(cc, d)) jj += sd[d];
+                Real2<Real> v = ld2(xy, (int64_t)(uint32_t)jj);
                 x[cc] = v.x;
                 y[cc] = v.y;
             }
@@ -449,18 +456,18 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
             int off[D];
             stencil_offset<D>(o, off);
             bool in = true;
-            int64_t jj = i;
+            int jj = (int)iu;
 #pragma unroll
             for (int d = 0; d < D; d++)
             {
-                int t = nc.I[d] + off[d];
+                int t = I[d] + off[d];
                 in = in && (t >= 0) && (t <= g.r);
-                jj += (int64_t)off[d] * nc.stride[d];
+                jj += off[d] * st[d];
             }
             if (!in) continue;
             Real a = L.A[(int64_t)o * L.N + i];
             Real b = L.B[(int64_t)o * L.N + i];
-            Real2<Real> v = ld2(xy, jj);
+            Real2<Real> v = ld2(xy, (int64_t)(uint32_t)jj);
             ax += a * v.x;
             ay += a * v.y;
             if (o == Dims<D>::CENTER) acen = a;
@@ -623,6 +630,22 @@ __global__ void __launch_bounds__(kThreads) gs_colour_lanes_kernel(LevelPtrs<Rea
         I[0] = 2 * (z / col.cnt[1]) + col.par[0];
     }
     gs_update_lanes_at<D, Real>(L, L.xy, g, I, tl < col.cnt[D - 1], A, err, separate);
+}
+
+// Flat variant: consecutive groups of 2^D threads take consecutive nodes of the colour (32-bit
+// decomposition), so no block row is left partly empty.
+template <int D, typename Real>
+__global__ void __launch_bounds__(kThreads) gs_colour_flat_kernel(LevelPtrs<Real> L, Colour<D> col, unsigned int *err, int separate)
+{
+    Grid<D> g(L.level);
+    const int A = threadIdx.x & ((1 << D) - 1);
+    const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> D;
+    const bool active = j < col.n;
+    int I[D];
+    if (active) col.node(j, I);
+    else
+        for (int d = 0; d < D; d++) I[d] = 0;
+    gs_update_lanes_at<D, Real>(L, L.xy, g, I, active, A, err, separate);
 }
 
 // All sweeps of a small level in one thread block: the colours follow each other behind a block
@@ -814,7 +837,7 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n)
 
 inline unsigned int blocks_for(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
 
-int g_gs_variant = 1;  // 0: one thread per node, 1: 2^D lanes per node
+int g_gs_variant = 2;  // 0: one thread per node, 1: 2^D lanes per node (row grid), 2: 2^D lanes per node (flat grid)
 
 }  // namespace
 
@@ -859,6 +882,8 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
     Colour<D> col(g, colour);
     if (col.n == 0) return;
     if (g_gs_variant == 0) gs_colour_kernel<D, Real><<<blocks_for(col.n), kThreads, 0, s>>>(L, col, err, separate);
+    else if (g_gs_variant == 2)
+        gs_colour_flat_kernel<D, Real><<<blocks_for(col.n << D), kThreads, 0, s>>>(L, col, err, separate);
     else
     {
         constexpr int NPB = kThreads >> D;
