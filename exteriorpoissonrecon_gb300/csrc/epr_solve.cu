@@ -612,8 +612,13 @@ __device__ __forceinline__ void gs_update_lanes(const LevelPtrs<Real> &L, const 
 // Launch geometry without 64-bit index division: block = (128 >> D) nodes along the last axis
 // times 2^D lanes; grid.y = the colour's count on axis D-2; grid.z = the counts on the remaining
 // leading axes.
+// 3D float: cap registers at 48 (10 resident blocks, 40 warps per SM instead of 32 at 64 registers)
 template <int D, typename Real>
-__global__ void __launch_bounds__(kThreads) gs_colour_lanes_kernel(LevelPtrs<Real> L, Colour<D> col, unsigned int *err, int separate)
+constexpr int lanes_min_blocks() { return (D == 3 && sizeof(Real) == 4) ? 10 : 1; }
+
+template <int D, typename Real>
+__global__ void __launch_bounds__(kThreads, lanes_min_blocks<D, Real>()) gs_colour_lanes_kernel(LevelPtrs<Real> L, Colour<D> col,
+                                                                                                unsigned int *err, int separate)
 {
     Grid<D> g(L.level);
     constexpr int NPB = kThreads >> D;
@@ -837,7 +842,7 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n)
 
 inline unsigned int blocks_for(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
 
-int g_gs_variant = 2;  // 0: one thread per node, 1: 2^D lanes per node (row grid), 2: 2^D lanes per node (flat grid)
+int g_gs_variant = 1;  // 0: one thread per node, 1: 2^D lanes per node (row grid), 2: 2^D lanes per node (flat grid)
 
 }  // namespace
 
