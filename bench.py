@@ -1,4 +1,5 @@
-"""Benchmark of the GB300 solve path on the depth-8 3D link workload.
+"""Benchmark of the GB300 solve path on the depth-8 3D link workload (--dim 4: the depth-6 4D
+Clifford-torus workload, 1M samples, positional sigma 0.002, 2 degree angular noise).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -50,7 +51,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--depth", type=int, default=8)
+    ap.add_argument("--dim", type=int, default=3, choices=[3, 4])
+    ap.add_argument("--depth", type=int, default=None)
     ap.add_argument("--samples", type=int, default=1_000_000)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--solver", default="cascadic", choices=["cascadic", "multigrid"])
@@ -61,9 +63,9 @@ def parse():
     return ap.parse_args()
 
 
-def workload(n, seed=0):
+def workload(n, dim=3, seed=0):
     from exteriorpoissonrecon_gb300 import samples, unit_cube, pack_skew
-    pos, frames = samples.make_workload("link", n, seed=seed)
+    pos, frames = samples.make_workload("link" if dim == 3 else "clifford", n, seed=seed)
     pu, xf = unit_cube(pos)
     return pu, pack_skew(frames)
 
@@ -150,13 +152,13 @@ def schedule_node_updates(dim, depth, gs_iters=10, i_mult=2.0):
     return sum(math.ceil(i_mult ** (depth - l) * gs_iters) * (2 ** l + 1) ** dim for l in range(depth + 1))
 
 
-def cpu_reference(pu, sk, depth, cpu_depth, steps, warmup):
+def cpu_reference(pu, sk, depth, cpu_depth, steps, warmup, dim=3):
     """CPU restatement (oracle) of the reference's cascadic paired Gauss-Seidel on a bounded sample:
     build at cpu_depth, time paired-GS sweeps there with all host threads, scale the node-update
     rate to the depth-`depth` schedule."""
     from oracle import oracle as O
     cores = os.cpu_count() or 1
-    o = O.Oracle(3, cpu_depth, threads=cores)
+    o = O.Oracle(dim, cpu_depth, threads=cores)
     o.set_samples(pu, sk)
     t0 = time.perf_counter()
     o.build()
@@ -173,28 +175,31 @@ def cpu_reference(pu, sk, depth, cpu_depth, steps, warmup):
         if i >= warmup:
             times.append(dt)
     per_update = statistics.mean(times) / N
-    full = per_update * schedule_node_updates(3, depth)
+    full = per_update * schedule_node_updates(dim, depth)
     return {"value": full, "unit": "s", "cores": cores, "kind": "port",
             "sample": (f"oracle build + {steps} paired-GS sweeps at depth {cpu_depth} "
                        f"({N} nodes, FP64) of the same {len(pu)}-sample input; per-node-update time "
                        f"{per_update * 1e9:.1f} ns scaled to the depth-{depth} cascadic schedule "
-                       f"({schedule_node_updates(3, depth)} node updates); build took {build_s:.1f} s")}
+                       f"({schedule_node_updates(dim, depth)} node updates); build took {build_s:.1f} s")}
 
 
 def main():
     args = parse()
     ws, rank, local, pg = dist_setup(args)
-    depth = args.depth
-    pu, sk = workload(args.samples)
-    config = {"workload": f"link-1M+10%spot-3D-depth{depth}", "samples": int(len(pu)), "depth": depth,
-              "dim": 3, "nodes": (2 ** depth + 1) ** 3, "unknowns": 2 * (2 ** depth + 1) ** 3,
+    depth = args.depth if args.depth is not None else (8 if args.dim == 3 else 6)
+    cpu_depth = args.cpu_depth if args.dim == 3 else min(args.cpu_depth, 4)
+    dim = args.dim
+    pu, sk = workload(args.samples, dim)
+    name = f"link-1M+10%spot-3D-depth{depth}" if dim == 3 else f"clifford-torus-1M-4D-depth{depth}"
+    config = {"workload": name, "samples": int(len(pu)), "depth": depth,
+              "dim": dim, "nodes": (2 ** depth + 1) ** dim, "unknowns": 2 * (2 ** depth + 1) ** dim,
               "solver": args.solver, "precision": args.precision, "l2": "inputs larger than L2 (no flush)",
               "parallelism": f"replicas{ws}"}
 
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_reference(pu, sk, depth, args.cpu_depth, args.steps, args.warmup)
+        cb = cpu_reference(pu, sk, depth, cpu_depth, args.steps, args.warmup, dim)
         line = {"metric": METRIC, "value": cb["value"], "unit": "s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": cb["value"] * 1e3, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -204,7 +209,7 @@ def main():
         return
 
     import exteriorpoissonrecon_gb300 as epr
-    r = epr.Reconstructor(3, depth, pu, sk, precision=args.precision, solver=args.solver, device=local)
+    r = epr.Reconstructor(dim, depth, pu, sk, precision=args.precision, solver=args.solver, device=local)
     for _ in range(args.warmup):
         r.solve()
     build_ms = r.stats.build_ms  # device time of epr_build (filled in by the first solve's stats copy)
@@ -227,12 +232,13 @@ def main():
     # kernel roofline: one parity colour of the paired Gauss-Seidel sweep at the finest level
     hbm_peak, peak_kind = measured_peaks()
     gs_ms = r.time_kernel("gs", depth, reps=20)
-    N = (2 ** depth + 1) ** 3
+    N = (2 ** depth + 1) ** dim
+    S = 3 ** dim
     rs = 4 if args.precision == "fp32" else 8
-    colour_nodes = (2 ** (depth - 1) + 1) ** 3
-    gs_bytes = 2 * rs * N + colour_nodes * (2 * 27 * rs + 2 * rs)
+    colour_nodes = (2 ** (depth - 1) + 1) ** dim
+    gs_bytes = 2 * rs * N + colour_nodes * (2 * S * rs + 2 * rs)
     achieved = gs_bytes / (gs_ms * 1e-3) / 1e9
-    fp32 = args.precision == "fp32"
+    fp32 = args.precision == "fp32" and dim == 3  # the captures are of the 3D float kernels
     gs_traffic = GS_DRAM_BYTES_PER_COLOUR_NODE_FP32 * colour_nodes if fp32 else None
     roofline = {"bound": "hbm", "kernel": "gs_colour_lanes_kernel", "achieved": achieved, "peak": hbm_peak,
                 "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_kind, "traffic": gs_traffic,
@@ -244,7 +250,7 @@ def main():
     # 27-point stencil; bytes = the colour's coefficients, right-hand side and update plus one read
     # of the whole x vector (every node neighbours the colour)
     lgs_ms = r.time_kernel("lgs", depth, reps=20)
-    lgs_bytes = colour_nodes * (27 + 2) * rs + N * rs
+    lgs_bytes = colour_nodes * (S + 2) * rs + N * rs
     lgs_achieved = lgs_bytes / (lgs_ms * 1e-3) / 1e9
     stencil_roofline = {"bound": "hbm", "kernel": "linear_gs_colour_kernel", "achieved": lgs_achieved, "peak": hbm_peak,
                         "unit": "GB/s", "frac": lgs_achieved / hbm_peak, "peak_source": peak_kind,
@@ -254,11 +260,11 @@ def main():
     # end to end through the public API from host buffers
     e2e_s = []
     h2d = pu.nbytes + sk.nbytes
-    d2h = sum(2 * 8 * (2 ** l + 1) ** 3 for l in range(depth + 1))
+    d2h = sum(2 * 8 * (2 ** l + 1) ** dim for l in range(depth + 1))
     e2e_parts = []
     for _ in range(args.e2e_steps):
         t0 = time.perf_counter()
-        r2 = epr.Reconstructor(3, depth, pu, sk, precision=args.precision, solver=args.solver, device=local)
+        r2 = epr.Reconstructor(dim, depth, pu, sk, precision=args.precision, solver=args.solver, device=local)
         t1 = time.perf_counter()
         r2.solve()
         t2 = time.perf_counter()
@@ -278,12 +284,12 @@ def main():
                     "parts": e2e_parts[-1] if e2e_parts else None},
             "build_ms": build_ms, "wall_s": wall,
             "final_energy": st["fit_energy"] + st["reg_energy"], "initial_energy": st["initial_energy"],
-            "unknown_sweeps_per_s": 2 * schedule_node_updates(3, depth) / per_step_s}
+            "unknown_sweeps_per_s": 2 * schedule_node_updates(dim, depth) / per_step_s}
     # error of the result against the double-precision run of the same schedule (the CUDA FP64
     # path reproduces the reference's algorithm to 1e-9 on the pinned cases)
     if args.precision == "fp32" and not args.no_fp64_check:
         xs32 = r.coefficients(depth)[0]
-        r64 = epr.Reconstructor(3, depth, pu, sk, precision="fp64", solver=args.solver, device=local)
+        r64 = epr.Reconstructor(dim, depth, pu, sk, precision="fp64", solver=args.solver, device=local)
         st64 = r64.solve()
         xs64 = r64.coefficients(depth)[0]
         e32, e64 = line["final_energy"], st64["fit_energy"] + st64["reg_energy"]
@@ -292,7 +298,7 @@ def main():
                                  "fp64_solve_s": st64["solve_ms"] / 1e3}
         r64.close()
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_reference(pu, sk, depth, args.cpu_depth, 2, 1)
+        line["cpu_baseline"] = cpu_reference(pu, sk, depth, cpu_depth, 2, 1, dim)
     if rank == 0:
         print(json.dumps(line))
 
