@@ -239,11 +239,24 @@ def main():
     gs_bytes = 2 * rs * N + colour_nodes * (2 * S * rs + 2 * rs)
     achieved = gs_bytes / (gs_ms * 1e-3) / 1e9
     fp32 = args.precision == "fp32" and dim == 3  # the captures are of the 3D float kernels
+    # the quartic relaxation is bound by FP32/FP64 issue, not by HBM: its algorithmic FLOPs per node
+    # update (this formulation: per incident element and wedge component 4 derivative tables of
+    # ~34 flops and 2 x 2 x 3^(D-2) Gauss points of ~21 flops; plus the 3^D-point stencil column)
+    # against the nominal FP32 rate of 152 SMs x 128 lanes x 2 flops at the sampled SM clock
+    K = dim * (dim - 1) // 2
+    node_flops = (2 ** dim) * K * (4 * 34 + 4 * 3 ** (dim - 2) * 21) + 8 * S + 30
+    gs_flops = node_flops * colour_nodes
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     gs_traffic = GS_DRAM_BYTES_PER_COLOUR_NODE_FP32 * colour_nodes if fp32 else None
     roofline = {"bound": "hbm", "kernel": "gs_colour_lanes_kernel", "achieved": achieved, "peak": hbm_peak,
                 "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_kind, "traffic": gs_traffic,
                 "launch_ms": gs_ms, "algorithmic_bytes_per_launch": gs_bytes,
-                "note": "FMA-bound quartic relaxation; bytes = coefficient read + stencil columns + update writes"}
+                "note": "FMA-bound quartic relaxation; bytes = coefficient read + stencil columns + update writes",
+                "compute": {"algorithmic_flops_per_launch": gs_flops, "achieved_tflops": gs_flops / (gs_ms * 1e-3) / 1e12,
+                            "peak_tflops": fp32_peak if args.precision == "fp32" else None,
+                            "peak_source": "nominal FP32 at the sampled SM clock",
+                            "frac": (gs_flops / (gs_ms * 1e-3) / 1e12 / fp32_peak) if args.precision == "fp32" else None}}
 
     # stored-stencil relaxation (the smoother of the linear multigrid, MG.h GSRelaxer): one colour of
     # the linear Gauss-Seidel sweep on the alternating y-system of the finest level, colour-blocked

@@ -107,6 +107,43 @@ __device__ __forceinline__ void derivative_table(const Real *f, Real *out)
     }
 }
 
+// The two steps of derivative_table separately, for callers that evaluate the other-axis points
+// one at a time (fewer live registers in 4D): the A-differences interpolated along B ...
+template <int D, int K, bool AisP, typename Real>
+__device__ __forceinline__ void derivative_partial(const Real *f, Real (&t)[2][1 << (D - 2)])
+{
+    using Cp = Component<D, K>;
+    constexpr int NO = 1 << Cp::M;
+    Real dif[2][NO];
+#pragma unroll
+    for (int bB = 0; bB < 2; bB++)
+#pragma unroll
+        for (int bo = 0; bo < NO; bo++)
+        {
+            int c1 = AisP ? Cp::corner(1, bB, bo) : Cp::corner(bB, 1, bo);
+            int c0 = AisP ? Cp::corner(0, bB, bo) : Cp::corner(bB, 0, bo);
+            dif[bB][bo] = f[c1] - f[c0];
+        }
+#pragma unroll
+    for (int g = 0; g < 2; g++)
+#pragma unroll
+        for (int bo = 0; bo < NO; bo++) t[g][bo] = hat2<Real>(0, g) * dif[0][bo] + hat2<Real>(1, g) * dif[1][bo];
+}
+
+// ... and then at the other-axis Gauss point go (the same operations as derivative_table)
+template <int M, typename Real>
+__device__ __forceinline__ Real derivative_at(const Real *t, int go)
+{
+    if constexpr (M == 1) return hat3<Real>(0, go) * t[0] + hat3<Real>(1, go) * t[1];
+    else
+    {
+        const int g0 = go / 3, g1 = go % 3;
+        Real u0 = hat3<Real>(0, g0) * t[0] + hat3<Real>(1, g0) * t[2];
+        Real u1 = hat3<Real>(0, g0) * t[1] + hat3<Real>(1, g0) * t[3];
+        return hat3<Real>(0, g1) * u0 + hat3<Real>(1, g1) * u1;
+    }
+}
+
 template <int M>
 __device__ __forceinline__ double other_weight(int go)
 {
@@ -160,6 +197,54 @@ __device__ __forceinline__ void component_fit(const Real *x, const Real *y, int 
     using Cp = Component<D, K>;
     constexpr int M = Cp::M;
     constexpr int NG = ipow(3, M);
+    if constexpr (M == 2)
+    {
+        // 4D: derivatives evaluated per other-axis point (same values, same summation order)
+        Real txP[2][4], txQ[2][4], tyP[2][4], tyQ[2][4];
+        derivative_partial<D, K, true>(x, txP);
+        derivative_partial<D, K, false>(x, txQ);
+        derivative_partial<D, K, true>(y, tyP);
+        derivative_partial<D, K, false>(y, tyQ);
+        const int aP = cbit<D>(A, Cp::P), aQ = cbit<D>(A, Cp::Q);
+        const Real sP = aP ? (Real)1 : (Real)-1, sQ = aQ ? (Real)1 : (Real)-1;
+        const int ao0 = cbit<D>(A, Cp::other(0)), ao1 = cbit<D>(A, Cp::other(1));
+#pragma unroll
+        for (int go = 0; go < NG; go++)
+        {
+            const Real lo = hat3<Real>(ao0, go / 3) * hat3<Real>(ao1, go % 3);
+            const Real wo = (Real)other_weight<M>(go);
+            Real xPg[2], xQg[2], yPg[2], yQg[2];
+#pragma unroll
+            for (int g = 0; g < 2; g++)
+            {
+                xPg[g] = derivative_at<M, Real>(txP[g], go);
+                xQg[g] = derivative_at<M, Real>(txQ[g], go);
+                yPg[g] = derivative_at<M, Real>(tyP[g], go);
+                yQg[g] = derivative_at<M, Real>(tyQ[g], go);
+            }
+#pragma unroll
+            for (int gp = 0; gp < 2; gp++)
+#pragma unroll
+                for (int gq = 0; gq < 2; gq++)
+                {
+                    Real w = (Real)(Gauss::W2(gp) * Gauss::W2(gq)) * wo;
+                    Real phP = sP * hat2<Real>(aQ, gq) * lo;
+                    Real phQ = sQ * hat2<Real>(aP, gp) * lo;
+                    Real xp = xPg[gq], xq = xQg[gp];
+                    Real yp = yPg[gq], yq = yQg[gp];
+                    Real W = yp * xq - xp * yq;
+                    Real U = yp * phQ - phP * yq;
+                    Real V = phP * xq - xp * phQ;
+                    Real wU = w * U, wV = w * V;
+                    h[0] += wU * U;
+                    h[1] += wV * V;
+                    h[2] += wU * V;
+                    h[3] += wU * W;
+                    h[4] += wV * W;
+                }
+        }
+        return;
+    }
     Real xP[2 * NG], xQ[2 * NG], yP[2 * NG], yQ[2 * NG];
     derivative_table<D, K, true>(x, xP);
     derivative_table<D, K, false>(x, xQ);
