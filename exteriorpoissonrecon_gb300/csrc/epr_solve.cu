@@ -653,127 +653,6 @@ __global__ void __launch_bounds__(kThreads) gs_colour_flat_kernel(LevelPtrs<Real
     gs_update_lanes_at<D, Real>(L, L.xy, g, I, active, A, err, separate);
 }
 
-// 4D: one 128-thread block per node.  Warps 0-2: thread 6 A + K (A < 16 elements, K < 6 wedge
-// components) integrates component K of element A alone, every thread running component 0's code
-// on the element mirrored so that the node is its corner 0 and with its axes permuted so that
-// component K's (P, Q) and remaining axes become component 0's (1, 0) and (2, 3) — the integrals are
-// invariant under both maps.  Warp 3 takes the 81-point stencil column.  Each warp reduces with
-// shuffles, thread 0 adds the four warp sums in a fixed order and applies the paired step.
-template <typename Real>
-__global__ void __launch_bounds__(128, sizeof(Real) == 4 ? 8 : 2) gs_colour_node4_kernel(LevelPtrs<Real> L, Colour<4> col,
-                                                                                         unsigned int *err, int separate)
-{
-    constexpr int D = 4, S = 81;
-    // physical axes (Q, P, R0, R1) of component K (packing k = P(P-1)/2 + Q, Hat.inl:32-37)
-    constexpr int kAxes[6][4] = {{0, 1, 2, 3}, {0, 2, 1, 3}, {1, 2, 0, 3}, {0, 3, 1, 2}, {1, 3, 0, 2}, {2, 3, 0, 1}};
-    __shared__ Real part[4][10];
-    Grid<D> g(L.level);
-    const int64_t j = blockIdx.x;
-    if (j >= col.n) return;  // whole block
-    int I[D];
-    col.node(j, I);
-    int st[D];
-    st[D - 1] = 1;
-#pragma unroll
-    for (int d = D - 2; d >= 0; d--) st[d] = st[d + 1] * (g.r + 1);
-    uint32_t iu = 0;
-#pragma unroll
-    for (int d = 0; d < D; d++) iu += (uint32_t)I[d] * (uint32_t)st[d];
-    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    Real v[10];
-#pragma unroll
-    for (int k = 0; k < 10; k++) v[k] = 0;  // h0..h4, ax, ay, bx, by, acen
-    const Real *xy = L.xy;
-    if (warp < 3)
-    {
-        const int A = t / 6, K = t - 6 * (t / 6);
-        bool ok = true;
-#pragma unroll
-        for (int d = 0; d < D; d++)
-        {
-            int e = I[d] - cbit<D>(A, d);
-            ok = ok && e >= 0 && e < g.r;
-        }
-        if (ok)
-        {
-            int sd[D];  // signed stride of canonical axis a
-#pragma unroll
-            for (int a = 0; a < D; a++)
-            {
-                const int d = kAxes[K][a];
-                sd[a] = cbit<D>(A, d) ? -st[d] : st[d];
-            }
-            Real x[16], y[16];
-#pragma unroll
-            for (int cc = 0; cc < 16; cc++)
-            {
-                int jj = (int)iu;
-#pragma unroll
-                for (int a = 0; a < D; a++)
-                    if (cbit<D>(cc, a)) jj += sd[a];
-                Real2<Real> p = ld2(xy, (int64_t)(uint32_t)jj);
-                x[cc] = p.x;
-                y[cc] = p.y;
-            }
-            component_fit<D, 0, Real>(x, y, 0, v);
-        }
-    }
-    else
-    {
-        for (int o = lane; o < S; o += 32)
-        {
-            int off[D];
-            stencil_offset<D>(o, off);
-            bool in = true;
-            int jj = (int)iu;
-#pragma unroll
-            for (int d = 0; d < D; d++)
-            {
-                int q = I[d] + off[d];
-                in = in && q >= 0 && q <= g.r;
-                jj += off[d] * st[d];
-            }
-            if (!in) continue;
-            const Real a = L.A[(int64_t)o * L.N + iu];
-            const Real b = L.B[(int64_t)o * L.N + iu];
-            const Real2<Real> p = ld2(xy, (int64_t)(uint32_t)jj);
-            v[5] += a * p.x;
-            v[6] += a * p.y;
-            if (o == Dims<D>::CENTER) v[9] = a;
-            else { v[7] += b * p.x; v[8] += b * p.y; }
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < 10; k++)
-    {
-        Real r = v[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-        if (lane == 0) part[warp][k] = r;
-    }
-    __syncthreads();
-    if (t != 0) return;
-    Real h[10];
-#pragma unroll
-    for (int k = 0; k < 10; k++) h[k] = ((part[0][k] + part[1][k]) + part[2][k]) + part[3][k];
-    const Real sc = (Real)wedge_scale<D>(g.r);
-    Real q[5];
-    q[0] = h[0] * sc + h[9];
-    q[1] = h[1] * sc + h[9];
-    q[2] = (Real)2 * h[2] * sc;
-    q[3] = (Real)2 * h[3] * sc + (Real)2 * h[5] - (Real)2 * h[8];
-    q[4] = (Real)2 * h[4] * sc + (Real)2 * h[6] + (Real)2 * h[7];
-    Real p0, p1;
-    if (node_step<Real>(q, separate, p0, p1))
-    {
-        Real2<Real> cur = ld2(xy, (int64_t)iu);
-        cur.x += p0;
-        cur.y += p1;
-        if (!isfinite((double)cur.x) || !isfinite((double)cur.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
-        reinterpret_cast<Real2<Real> *>(L.xy)[iu] = cur;
-    }
-}
-
 // All sweeps of a small level in one thread block: the colours follow each other behind a block
 // barrier, which also makes each colour's writes visible to the next.  Used for the coarse levels
 // of the cascadic schedule, whose thousands of tiny sweeps would otherwise be bound by launch
@@ -963,8 +842,7 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n)
 
 inline unsigned int blocks_for(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
 
-int g_gs_variant = 1;  // 0: one thread per node, 1: 2^D lanes per node (row grid; 4D: a block per node),
-                       // 2: 2^D lanes per node (flat grid; 4D: a block per node), 3: 2^D lanes per node (row grid, 4D too)
+int g_gs_variant = 1;  // 0: one thread per node, 1: 2^D lanes per node (row grid), 2: 2^D lanes per node (flat grid)
 
 }  // namespace
 
@@ -1008,12 +886,6 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
     Grid<D> g(L.level);
     Colour<D> col(g, colour);
     if (col.n == 0) return;
-    if constexpr (D == 4)
-        if (g_gs_variant != 0 && g_gs_variant != 3)
-        {
-            gs_colour_node4_kernel<Real><<<(unsigned)col.n, 128, 0, s>>>(L, col, err, separate);
-            return;
-        }
     if (g_gs_variant == 0) gs_colour_kernel<D, Real><<<blocks_for(col.n), kThreads, 0, s>>>(L, col, err, separate);
     else if (g_gs_variant == 2)
         gs_colour_flat_kernel<D, Real><<<blocks_for(col.n << D), kThreads, 0, s>>>(L, col, err, separate);
