@@ -291,10 +291,9 @@ bool Context::relax_levels(int minD, int maxD, bool useGraph)
     for (int l = minD; ok && l <= maxD; l++)
     {
         int iters = (int)std::ceil(std::pow(P.i_mult, depth - l) * P.gs_iters);
-        // the captured sequence launches one kernel per colour from level 2 on; a direct run keeps
-        // the single-block kernel up to 729 nodes (fewer host launches).  Both compute every node
-        // update with the same arithmetic, so the results are identical.
-        ok = gs(l, iters, capture ? graphPersistentMax : kPersistentMaxNodes);
+        // the same launch configuration whether captured or not (one kernel per colour from level 2
+        // on), so that every solve of a context runs the same kernels and gives the same bits
+        ok = gs(l, iters, useGraph ? graphPersistentMax : kPersistentMaxNodes);
         if (ok && l < maxD) ok = prolong_add(l);
     }
     if (!capture) return ok;

@@ -158,3 +158,19 @@ def test_solver_variants(name):
     for l in range(depth + 1):
         assert rel(xs[l], g[f"solx_d{l}"]) < 1e-9
         assert rel(ys[l], g[f"soly_d{l}"]) < 1e-9
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_repeated_solves_are_identical(precision):
+    """The first solve of a context launches directly, the second captures the relaxation sequence
+    into a CUDA graph and later ones replay it: all give bitwise the same solution."""
+    g = load_golden("link3_d4")
+    r = epr.Reconstructor(3, int(g["depth"]), g["pos"], g["skew"], precision=precision)
+    sols = []
+    for _ in range(3):
+        st = r.solve()
+        xs, ys = r.solution()
+        sols.append((np.concatenate(xs), np.concatenate(ys), st["fit_energy"], st["reg_energy"]))
+    for s in sols[1:]:
+        assert np.array_equal(s[0], sols[0][0]) and np.array_equal(s[1], sols[0][1])
+        assert s[2] == sols[0][2] and s[3] == sols[0][3]
