@@ -91,13 +91,37 @@ bool Context::ensure_level(int l)
 
 bool Context::lvl32(int l) const { return P.precision == EPR_FP32 && l >= P.fp64_levels; }
 
+// refreshes the derived copies of a level's system: the float stencils (float levels) and the
+// colour-blocked stencils of the levels that are relaxed by one kernel per colour
 bool Context::sync_system32(int l)
 {
-    if (!lvl32(l)) return true;
     Level &L = levels[l];
     size_t S = (size_t)stencil();
-    launch_convert_d2f(L.A64, L.A32, (int64_t)S * L.N, stream);
-    launch_convert_d2f(L.B64, L.B32, (int64_t)S * L.N, stream);
+    if (lvl32(l))
+    {
+        launch_convert_d2f(L.A64, L.A32, (int64_t)S * L.N, stream);
+        launch_convert_d2f(L.B64, L.B32, (int64_t)S * L.N, stream);
+    }
+    if (L.N > (dim == 3 ? 27 : 81))
+    {
+        const size_t bytes = S * L.N * (lvl32(l) ? sizeof(float) : sizeof(double));
+        if (!L.Acb && (!alloc(&L.Acb, bytes, "alloc colour blocks") || !alloc(&L.Bcb, bytes, "alloc colour blocks"))) return false;
+        auto blocks = [&](auto dd) {
+            constexpr int D = decltype(dd)::value;
+            if (lvl32(l))
+            {
+                launch_to_colour_blocks<D, float>(l, L.A64, (float *)L.Acb, stream);
+                launch_to_colour_blocks<D, float>(l, L.B64, (float *)L.Bcb, stream);
+            }
+            else
+            {
+                launch_to_colour_blocks<D, double>(l, L.A64, (double *)L.Acb, stream);
+                launch_to_colour_blocks<D, double>(l, L.B64, (double *)L.Bcb, stream);
+            }
+        };
+        if (dim == 3) blocks(std::integral_constant<int, 3>{});
+        else blocks(std::integral_constant<int, 4>{});
+    }
     return launch_ok("convert system");
 }
 
@@ -122,7 +146,7 @@ Context::~Context()
         for (Level &L : levels)
         {
             release(L.xy64); release(L.xy32); release(L.A64); release(L.B64); release(L.A32); release(L.B32);
-            release(L.tmp64); release(L.tmp32);
+            release(L.tmp64); release(L.tmp32); release(L.Acb); release(L.Bcb);
         }
         release(red.partial); release(red.out); release(d_err); release(d_fit);
         setup.release(*this);
@@ -154,6 +178,11 @@ LevelPtrs<Real> level_ptrs(Context *c, int l)
     p.N = L.N;
     if constexpr (std::is_same<Real, double>::value) { p.xy = L.xy64; p.A = L.A64; p.B = L.B64; }
     else { p.xy = L.xy32; p.A = L.A32; p.B = L.B32; }
+    if (L.Acb && c->lvl32(l) == std::is_same<Real, float>::value)
+    {
+        p.Acb = (const Real *)L.Acb;
+        p.Bcb = (const Real *)L.Bcb;
+    }
     return p;
 }
 

@@ -125,6 +125,18 @@ struct Colour
     }
 };
 
+// Colour-blocked stencil layout: the nodes of colour c (in Colour::node order) form one block; the
+// block of colour c starts after the blocks of colours 0..c-1, and coefficient o of the colour's
+// j-th node sits at block + o * n_c + j.  One colour sweep then streams its coefficients
+// contiguously instead of every other element of each sector.
+template <int D>
+__host__ __device__ inline int64_t colour_block_base(const Grid<D> &g, int colour)
+{
+    int64_t at = 0;
+    for (int c = 0; c < colour; c++) at += Colour<D>(g, c).n * ipow(3, D);
+    return at;
+}
+
 // Error flags written by kernels and read by the host after a step
 enum ErrorBits : unsigned int
 {

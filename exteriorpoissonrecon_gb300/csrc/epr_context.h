@@ -26,6 +26,8 @@ struct Level
     float *A32 = nullptr;
     float *B32 = nullptr;
     float *tmp32 = nullptr;
+    void *Acb = nullptr;      // colour-blocked A and B in the level's precision (levels relaxed
+    void *Bcb = nullptr;      // by one kernel per colour)
 };
 
 // Sample-side state of the build (ordered sampling, estimator, splats).  Defined in epr_setup.cu.

@@ -16,6 +16,8 @@ struct LevelPtrs
     Real *xy = nullptr;       // 2N interleaved (x, y)
     const Real *A = nullptr;  // 3^Dim * N column stencil of R + dWeight K (offset-major)
     const Real *B = nullptr;  // 3^Dim * N column stencil of the frame constraint
+    const Real *Acb = nullptr;  // optional colour-blocked copies of A and B (colour_block_base)
+    const Real *Bcb = nullptr;
 };
 
 // Scratch for deterministic two-pass reductions
@@ -62,6 +64,10 @@ void launch_restrict(int coarseLevel, const Real *fine, Real *coarse, cudaStream
 // coarse = P^T fine P of a column stencil (offset-major, double), fine level -> fineLevel - 1
 template <int D>
 void launch_galerkin(int fineLevel, const double *Mf, double *Mc, cudaStream_t s);
+
+// colour-blocked copy (Real) of a natural offset-major double stencil of `level`
+template <int D, typename Real>
+void launch_to_colour_blocks(int level, const double *M, Real *out, cudaStream_t s);
 
 // elementwise helpers
 template <typename Real>

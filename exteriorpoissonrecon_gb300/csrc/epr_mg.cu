@@ -645,6 +645,17 @@ __global__ void biquad_finish_kernel(const double *partial, int nblocks, double 
 
 }  // namespace
 
+template <int D, typename Real>
+void launch_to_colour_blocks(int level, const double *M, Real *out, cudaStream_t s)
+{
+    ColourBlocks<D> cb = colour_blocks<D>(level);
+    to_colour_blocks_kernel<D, Real><<<dim3(blocks(cb.count[0]), 1 << D), kThreads, 0, s>>>(level, M, cb, out);
+}
+template void launch_to_colour_blocks<3, float>(int, const double *, float *, cudaStream_t);
+template void launch_to_colour_blocks<3, double>(int, const double *, double *, cudaStream_t);
+template void launch_to_colour_blocks<4, float>(int, const double *, float *, cudaStream_t);
+template void launch_to_colour_blocks<4, double>(int, const double *, double *, cudaStream_t);
+
 // =============================================================================================
 // Host side
 // =============================================================================================

@@ -408,9 +408,12 @@ __device__ __forceinline__ double group_sum(double v)
     return v;
 }
 
+// Ac, Bc (optional): the colour's block of the colour-blocked stencils, the node being the colour's
+// jc-th of nc; otherwise the natural stencils L.A, L.B are read.
 template <int D, typename Real>
 __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Real *xy, const Grid<D> &g, const int *I, bool active,
-                                                   int A, unsigned int *err, int separate = 0)
+                                                   int A, unsigned int *err, int separate = 0, const Real *Ac = nullptr,
+                                                   const Real *Bc = nullptr, int64_t jc = 0, int64_t nc = 0)
 {
     constexpr int C = 1 << D, S = Dims<D>::S;
     int64_t i = 0;
@@ -465,8 +468,17 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
                 jj += off[d] * st[d];
             }
             if (!in) continue;
-            Real a = L.A[(int64_t)o * L.N + i];
-            Real b = L.B[(int64_t)o * L.N + i];
+            Real a, b;
+            if (Ac)
+            {
+                a = Ac[(int64_t)o * nc + jc];
+                b = Bc[(int64_t)o * nc + jc];
+            }
+            else
+            {
+                a = L.A[(int64_t)o * L.N + i];
+                b = L.B[(int64_t)o * L.N + i];
+            }
             Real2<Real> v = ld2(xy, (int64_t)(uint32_t)jj);
             ax += a * v.x;
             ay += a * v.y;
@@ -618,7 +630,8 @@ constexpr int lanes_min_blocks() { return (D == 3 && sizeof(Real) == 4) ? 10 : 1
 
 template <int D, typename Real>
 __global__ void __launch_bounds__(kThreads, lanes_min_blocks<D, Real>()) gs_colour_lanes_kernel(LevelPtrs<Real> L, Colour<D> col,
-                                                                                                unsigned int *err, int separate)
+                                                                                                int64_t cbBase, unsigned int *err,
+                                                                                                int separate)
 {
     Grid<D> g(L.level);
     constexpr int NPB = kThreads >> D;
@@ -634,7 +647,10 @@ __global__ void __launch_bounds__(kThreads, lanes_min_blocks<D, Real>()) gs_colo
         I[1] = 2 * (z % col.cnt[1]) + col.par[1];
         I[0] = 2 * (z / col.cnt[1]) + col.par[0];
     }
-    gs_update_lanes_at<D, Real>(L, L.xy, g, I, tl < col.cnt[D - 1], A, err, separate);
+    // index of the node in the colour (axis 0 slowest)
+    const int64_t jc = ((int64_t)blockIdx.z * col.cnt[D - 2] + blockIdx.y) * col.cnt[D - 1] + tl;
+    const Real *Ac = L.Acb ? L.Acb + cbBase : nullptr, *Bc = L.Bcb ? L.Bcb + cbBase : nullptr;
+    gs_update_lanes_at<D, Real>(L, L.xy, g, I, tl < col.cnt[D - 1], A, err, separate, Ac, Bc, jc, col.n);
 }
 
 // Flat variant: consecutive groups of 2^D threads take consecutive nodes of the colour (32-bit
@@ -894,7 +910,7 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
         constexpr int NPB = kThreads >> D;
         dim3 grid((unsigned)((col.cnt[D - 1] + NPB - 1) / NPB), (unsigned)col.cnt[D - 2],
                   (unsigned)(D == 3 ? col.cnt[0] : col.cnt[0] * col.cnt[1]));
-        gs_colour_lanes_kernel<D, Real><<<grid, kThreads, 0, s>>>(L, col, err, separate);
+        gs_colour_lanes_kernel<D, Real><<<grid, kThreads, 0, s>>>(L, col, colour_block_base<D>(g, colour), err, separate);
     }
 }
 
