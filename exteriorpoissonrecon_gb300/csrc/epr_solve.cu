@@ -514,13 +514,6 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
 // same code: the element is mirrored so that the node is its corner 0 and its axes are permuted so
 // that component K's axes (P, Q) and the remaining axis become component 0's (1, 0) and 2; the
 // integrals are invariant under both maps (each term carries one P- and one Q-derivative).
-template <typename Real>
-__device__ __forceinline__ Real warp_sum_all(Real v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 
 template <typename Real>
 __device__ __forceinline__ void gs_update_warp3(const LevelPtrs<Real> &L, Real *xy, const Grid<3> &g, const int *I, bool active,
@@ -528,19 +521,18 @@ __device__ __forceinline__ void gs_update_warp3(const LevelPtrs<Real> &L, Real *
 {
     constexpr int S = 27;
     const int lane = threadIdx.x & 31;
-    Real h[5] = {0, 0, 0, 0, 0};
-    Real ax = 0, ay = 0, bx = 0, by = 0, acen = 0;
-    int64_t i = 0;
+    // v[0..4]: wedge integrals h0..h4 on lanes 0-23; stencil sums ax, ay, bx, by, acen on lanes 24-31
+    Real v[5] = {0, 0, 0, 0, 0};
+    const int s1 = g.r + 1, s0 = s1 * s1;
+    const int i = I[0] * s0 + I[1] * s1 + I[2];
     if (active)
     {
-        const int64_t st[3] = {(int64_t)(g.r + 1) * (g.r + 1), (int64_t)(g.r + 1), 1};
-        i = I[0] * st[0] + I[1] * st[1] + I[2];
+        const int st[3] = {s0, s1, 1};
         if (lane < 24)
         {
             const int A = lane / 3, K = lane - 3 * (lane / 3);
             // physical axis of canonical axes 0, 1, 2 (= Q, P, R of component K)
-            const int p0 = (K == 2) ? 1 : 0, p1 = (K == 0) ? 1 : 2, p2 = (K == 0) ? 2 : (K == 1 ? 1 : 0);
-            const int pax[3] = {p0, p1, p2};
+            const int pax[3] = {(K == 2) ? 1 : 0, (K == 0) ? 1 : 2, (K == 0) ? 2 : (K == 1 ? 1 : 0)};
             bool ok = true;
 #pragma unroll
             for (int d = 0; d < 3; d++)
@@ -550,22 +542,22 @@ __device__ __forceinline__ void gs_update_warp3(const LevelPtrs<Real> &L, Real *
             }
             if (ok)
             {
+                int sd[3];
+#pragma unroll
+                for (int a = 0; a < 3; a++) sd[a] = cbit<3>(A, pax[a]) ? -st[pax[a]] : st[pax[a]];
                 Real x[8], y[8];
 #pragma unroll
                 for (int cc = 0; cc < 8; cc++)
                 {
-                    int64_t jj = i;
+                    int jj = i;
 #pragma unroll
                     for (int a = 0; a < 3; a++)
-                    {
-                        const int d = pax[a], b = cbit<3>(cc, a);
-                        jj += (cbit<3>(A, d) ? -b : b) * st[d];
-                    }
-                    Real2<Real> v = ld2(xy, jj);
-                    x[cc] = v.x;
-                    y[cc] = v.y;
+                        if (cbit<3>(cc, a)) jj += sd[a];
+                    Real2<Real> p = ld2(xy, jj);
+                    x[cc] = p.x;
+                    y[cc] = p.y;
                 }
-                component_fit<3, 0, Real>(x, y, 0, h);
+                component_fit<3, 0, Real>(x, y, 0, v);
             }
         }
         else
@@ -577,21 +569,33 @@ __device__ __forceinline__ void gs_update_warp3(const LevelPtrs<Real> &L, Real *
 #pragma unroll
                 for (int d = 0; d < 3; d++) { int t = I[d] + off[d]; in = in && t >= 0 && t <= g.r; }
                 if (!in) continue;
-                const int64_t jj = i + off[0] * st[0] + off[1] * st[1] + off[2];
+                const int jj = i + off[0] * s0 + off[1] * s1 + off[2];
                 Real a = L.A[(int64_t)o * L.N + i];
                 Real b = L.B[(int64_t)o * L.N + i];
-                Real2<Real> v = ld2(xy, jj);
-                ax += a * v.x;
-                ay += a * v.y;
-                if (o == 13) acen = a;
-                else { bx += b * v.x; by += b * v.y; }
+                Real2<Real> p = ld2(xy, jj);
+                v[0] += a * p.x;
+                v[1] += a * p.y;
+                if (o == 13) v[4] = a;
+                else { v[2] += b * p.x; v[3] += b * p.y; }
             }
         }
     }
+    // sums within the four 8-lane groups (the wedge groups 0-2 and the stencil group 3), then lane 0
+    // adds the three wedge groups in order and takes the stencil group's sums
 #pragma unroll
-    for (int k = 0; k < 5; k++) h[k] = warp_sum_all(h[k]);
-    ax = warp_sum_all(ax); ay = warp_sum_all(ay); bx = warp_sum_all(bx); by = warp_sum_all(by); acen = warp_sum_all(acen);
+    for (int k = 0; k < 5; k++)
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    Real h[5], st5[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++)
+    {
+        const Real g1 = __shfl_sync(0xffffffffu, v[k], 8), g2 = __shfl_sync(0xffffffffu, v[k], 16);
+        st5[k] = __shfl_sync(0xffffffffu, v[k], 24);
+        h[k] = (v[k] + g1) + g2;
+    }
     if (!active || lane != 0) return;
+    const Real ax = st5[0], ay = st5[1], bx = st5[2], by = st5[3], acen = st5[4];
     const Real sc = (Real)wedge_scale<3>(g.r);
     Real q[5];
     q[0] = h[0] * sc + acen;
@@ -602,11 +606,11 @@ __device__ __forceinline__ void gs_update_warp3(const LevelPtrs<Real> &L, Real *
     Real p0, p1;
     if (node_step<Real>(q, separate, p0, p1))
     {
-        Real2<Real> v = ld2(xy, i);
-        v.x += p0;
-        v.y += p1;
-        if (!isfinite((double)v.x) || !isfinite((double)v.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
-        reinterpret_cast<Real2<Real> *>(xy)[i] = v;
+        Real2<Real> cur = ld2(xy, i);
+        cur.x += p0;
+        cur.y += p1;
+        if (!isfinite((double)cur.x) || !isfinite((double)cur.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
+        reinterpret_cast<Real2<Real> *>(xy)[i] = cur;
     }
 }
 
