@@ -423,14 +423,19 @@ __global__ void skew_frame_kernel(const double *skew, const double *measure, con
     for (int k = 0; k < W; k++) frame[j * W + k] = sk[k] / nrm * m * sc;
 }
 
-// one warp per chunk
+// One warp per chunk.  The vertex's window cells are taken 32 at a time: each lane looks up one
+// cell's item range, a warp scan places the cells' items end to end, and the warp then walks the
+// part of those items that falls into the chunk 32 items at a time, every lane finding the cell of
+// its item by a binary search over the scanned offsets (shuffles).  Lanes stay busy however the
+// items spread over the cells, and every lane's order of accumulation is fixed by the item index.
 template <int D, bool Samples, class Item>
 __global__ void chunk_gather_kernel(SplatArgs a, Item item, const int *chunkStart, int64_t NV, int64_t nchunks, double *partial)
 {
     constexpr int W = Item::W;
+    const unsigned full = 0xffffffffu;
     int64_t chunk = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
-    if (chunk >= nchunks) return;
+    if (chunk >= nchunks) return;  // whole warps
     // vertex owning the chunk: last vi with chunkStart[vi] <= chunk
     int64_t lo = 0, hi = NV;
     while (hi - lo > 1)
@@ -441,21 +446,63 @@ __global__ void chunk_gather_kernel(SplatArgs a, Item item, const int *chunkStar
     const int64_t vi = lo;
     const int64_t first = (chunk - chunkStart[vi]) * kChunk, last = first + kChunk;
     int res = 1 << (a.t - 1), nv = res + 1;
-    int v[D], clo[D], chi[D], C[D];
+    int v[D], clo[D], wd[D];
     vertex_of<D>(vi, nv, v);
-    for (int d = 0; d < D; d++) { clo[d] = max(0, v[d] - a.KR - 1); chi[d] = min(res - 1, v[d] + a.KR); C[d] = clo[d]; }
+    int ncell = 1;
+    for (int d = 0; d < D; d++)
+    {
+        clo[d] = max(0, v[d] - a.KR - 1);
+        wd[d] = min(res - 1, v[d] + a.KR) - clo[d] + 1;
+        ncell *= wd[d];
+    }
     double acc[W];
     for (int w = 0; w < W; w++) acc[w] = 0;
-    int64_t base = 0;
-    do
+    int64_t base = 0;  // items of the window cells before the current batch
+    for (int kb = 0; kb < ncell && base < last; kb += 32)
     {
-        int ilo, ihi;
-        item_range<D, Samples>(a, C, ilo, ihi);
-        int64_t sz = ihi - ilo;
-        int64_t b0 = max(base, first), b1 = min(base + sz, last);
-        for (int64_t o = b0 + lane; o < b1; o += 32) item(a, (int)(ilo + (o - base)), v, C, acc);
-        base += sz;
-    } while (base < last && window_next<D>(C, clo, chi));
+        // this lane's cell (window order: last axis fastest) and its items
+        const int k = kb + lane;
+        int C[D], ilo = 0, cnt = 0;
+        {
+            int t = k < ncell ? k : 0;
+            for (int d = D - 1; d >= 0; d--) { C[d] = clo[d] + t % wd[d]; t /= wd[d]; }
+        }
+        if (k < ncell)
+        {
+            int ihi;
+            item_range<D, Samples>(a, C, ilo, ihi);
+            cnt = ihi - ilo;
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            int n = __shfl_up_sync(full, incl, o);
+            if (lane >= o) incl += n;
+        }
+        const int excl = incl - cnt;
+        const int total = __shfl_sync(full, incl, 31);
+        const int64_t b0 = max(base, first), b1 = min(base + (int64_t)total, last);
+        for (int64_t t0 = b0; t0 < b1; t0 += 32)
+        {
+            const int64_t t = t0 + lane;
+            const int r = (int)(t - base);  // position among this batch's items
+            int own = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+            {
+                const int cand = own + step;
+                const int e = __shfl_sync(full, excl, cand & 31);
+                if (cand < 32 && e <= r) own = cand;
+            }
+            const int olo = __shfl_sync(full, ilo, own), oex = __shfl_sync(full, excl, own);
+            int Co[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) Co[d] = __shfl_sync(full, C[d], own);
+            if (t < b1) item(a, olo + (r - oex), v, Co, acc);
+        }
+        base += total;
+    }
     for (int w = 0; w < W; w++)
     {
         double sum = warp_sum(acc[w]);
