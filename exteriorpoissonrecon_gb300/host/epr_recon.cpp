@@ -31,8 +31,9 @@ struct Args
     double nSigma = 0.25, scale = 1.1, sWeight = 100., dWeight = 0.00625, iMult = 2., jitter = 0.;
     int depth = 5, seed = 0, tRadius = 1, dRadius = 1, aRadius = -1, minSolveDepth = 0, gsIters = 10, maxSolveDepth = -1;
     bool singleLevel = false, separate = false, verbose = false, project = false;
-    std::string precision = "fp64";
-    int device = 0;
+    std::string precision = "fp64", solver = "cascadic";
+    int device = 0, fp64Levels = 0, maxCycles = 200;
+    double tolerance = 1e-6;
 };
 
 [[noreturn]] void Fail(const std::string &msg, int code = 1)
@@ -62,6 +63,10 @@ void Usage(const char *ex)
     printf("\t[--scale <bounding box scale>=1.1]\n");
     printf("\t[--iMult <iteration multiplier>=2]\n");
     printf("\t[--precision fp64|fp32]\n");
+    printf("\t[--fp64Levels <levels below this one relax in double with --precision fp32>=0]\n");
+    printf("\t[--solver cascadic|multigrid]\n");
+    printf("\t[--tolerance <multigrid: relative gradient per level>=1e-6]\n");
+    printf("\t[--maxCycles <multigrid: alternating rounds per level>=200]\n");
     printf("\t[--device <CUDA device>=0]\n");
     printf("\t[--separate]\n\t[--singleLevel]\n\t[--verbose]\n");
 }
@@ -69,12 +74,15 @@ void Usage(const char *ex)
 Args Parse(int argc, char **argv)
 {
     Args a;
-    std::map<std::string, std::string *> strs = {{"in", &a.in}, {"out", &a.out}, {"grid", &a.grid}, {"precision", &a.precision}};
+    std::map<std::string, std::string *> strs = {{"in", &a.in}, {"out", &a.out}, {"grid", &a.grid}, {"precision", &a.precision},
+                                                 {"solver", &a.solver}};
     std::map<std::string, double *> dbls = {{"nSigma", &a.nSigma}, {"scale", &a.scale}, {"sWeight", &a.sWeight},
-                                            {"dWeight", &a.dWeight}, {"iMult", &a.iMult}, {"jitter", &a.jitter}};
+                                            {"dWeight", &a.dWeight}, {"iMult", &a.iMult}, {"jitter", &a.jitter},
+                                            {"tolerance", &a.tolerance}};
     std::map<std::string, int *> ints = {{"depth", &a.depth}, {"seed", &a.seed}, {"tRadius", &a.tRadius},
                                          {"dRadius", &a.dRadius}, {"aRadius", &a.aRadius}, {"minSolveDepth", &a.minSolveDepth},
-                                         {"gsIters", &a.gsIters}, {"maxSolveDepth", &a.maxSolveDepth}, {"device", &a.device}};
+                                         {"gsIters", &a.gsIters}, {"maxSolveDepth", &a.maxSolveDepth}, {"device", &a.device},
+                                         {"fp64Levels", &a.fp64Levels}, {"maxCycles", &a.maxCycles}};
     std::map<std::string, bool *> flags = {{"singleLevel", &a.singleLevel}, {"separate", &a.separate},
                                            {"verbose", &a.verbose}, {"project", &a.project}};
     for (int i = 1; i < argc; i++)
@@ -280,6 +288,8 @@ int main(int argc, char **argv)
     if (a.in.empty()) { Usage(argv[0]); return EXIT_SUCCESS; }
     if (a.aRadius != -1) Fail("only the regular grid (--aRadius -1) is implemented; the adaptive indexer is not", 2);
     if (a.project) Fail("--project is not supported", 2);
+    if (a.precision != "fp32" && a.precision != "fp64") Fail("--precision must be fp64 or fp32", 2);
+    if (a.solver != "cascadic" && a.solver != "multigrid") Fail("--solver must be cascadic or multigrid", 2);
     if (a.depth < 1) Fail("depth must be at least 1", 2);
     std::string ext = a.in.substr(a.in.find_last_of('.') + 1);
     if (ext != "ply") Fail("Only .ply files supported", 2);
@@ -342,6 +352,10 @@ int main(int argc, char **argv)
     p.max_solve_depth = a.maxSolveDepth < 0 ? -1 : std::min(a.maxSolveDepth, a.depth);
     p.seed = (unsigned)a.seed;
     p.precision = a.precision == "fp32" ? EPR_FP32 : EPR_FP64;
+    p.fp64_levels = a.fp64Levels;
+    p.solver = a.solver == "multigrid" ? EPR_SOLVER_MULTIGRID : EPR_SOLVER_CASCADIC;
+    p.tolerance = a.tolerance;
+    p.max_cycles = a.maxCycles;
     p.verbose = a.verbose ? 1 : 0;
     p.device = a.device;
     p.single_level = a.singleLevel ? 1 : 0;
