@@ -309,6 +309,18 @@ def main():
         line["error_vs_fp64"] = {"energy_fp64": e64, "energy_rel_diff": (e32 - e64) / e64,
                                  "finest_x_rel_l2": float(np.linalg.norm(xs32 - xs64) / np.linalg.norm(xs64)),
                                  "fp64_solve_s": st64["solve_ms"] / 1e3}
+        # the same float schedule with the coarse levels 0-3 in double: the cascadic solve leaves the
+        # zero stationary point there, and double keeps the double run's local minimum
+        rm = epr.Reconstructor(dim, depth, pu, sk, precision="fp32", fp64_levels=4, solver=args.solver, device=local)
+        for _ in range(3):
+            stm = rm.solve()
+        em = stm["fit_energy"] + stm["reg_energy"]
+        xsm = rm.coefficients(depth)[0]
+        line["fp32_with_fp64_coarse_levels"] = {
+            "fp64_levels": 4, "solve_s": stm["solve_ms"] / 1e3, "energy": em, "energy_rel_diff_vs_fp64": (em - e64) / e64,
+            "finest_x_rel_l2_vs_fp64": float(np.linalg.norm(xsm - xs64) / np.linalg.norm(xs64)),
+            "speedup_vs_fp64_solve": st64["solve_ms"] / stm["solve_ms"]}
+        rm.close()
         r64.close()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference(pu, sk, depth, cpu_depth, 2, 1, dim)
