@@ -285,6 +285,40 @@ __device__ __forceinline__ void component_fit(const Real *x, const Real *y, int 
     }
 }
 
+// Component 0 of a 3D element in the canonical orientation (corner 0), restricted to the Gauss
+// points with the given (gp, gq): the share of one of four threads that split a component's
+// integral (the values of the points are those of component_fit).
+template <typename Real>
+__device__ __forceinline__ void component_fit_pq3(const Real *x, const Real *y, int gp, int gq, Real *h)
+{
+    Real txP[2][2], txQ[2][2], tyP[2][2], tyQ[2][2];
+    derivative_partial<3, 0, true>(x, txP);
+    derivative_partial<3, 0, false>(x, txQ);
+    derivative_partial<3, 0, true>(y, tyP);
+    derivative_partial<3, 0, false>(y, tyQ);
+    const Real w2 = (Real)(Gauss::W2(gp) * Gauss::W2(gq));
+    const Real hq = hat2<Real>(0, gq), hp = hat2<Real>(0, gp);
+#pragma unroll
+    for (int go = 0; go < 3; go++)
+    {
+        const Real lo = hat3<Real>(0, go);
+        const Real w = w2 * (Real)other_weight<1>(go);
+        const Real phP = (Real)-1 * hq * lo;
+        const Real phQ = (Real)-1 * hp * lo;
+        const Real xp = derivative_at<1, Real>(txP[gq], go), xq = derivative_at<1, Real>(txQ[gp], go);
+        const Real yp = derivative_at<1, Real>(tyP[gq], go), yq = derivative_at<1, Real>(tyQ[gp], go);
+        const Real W = yp * xq - xp * yq;
+        const Real U = yp * phQ - phP * yq;
+        const Real V = phP * xq - xp * phQ;
+        const Real wU = w * U, wV = w * V;
+        h[0] += wU * U;
+        h[1] += wV * V;
+        h[2] += wU * V;
+        h[3] += wU * W;
+        h[4] += wV * W;
+    }
+}
+
 template <int D, typename Real>
 __device__ __forceinline__ void element_fit(const Real *x, const Real *y, int A, Real *h)
 {

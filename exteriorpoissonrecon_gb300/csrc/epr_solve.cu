@@ -614,6 +614,139 @@ __device__ __forceinline__ void gs_update_warp3(const LevelPtrs<Real> &L, Real *
     }
 }
 
+// Point-split variant for the latency-bound small 3D levels: 128 threads per node.  Warp p takes
+// the Gauss points with (gp, gq) = (p >> 1, p & 1) of every (element A, component K) pair (lane
+// 3 A + K < 24, canonical orientation and axis permutation as above) and the stencil offsets
+// 8 p + lane - 24 < 27 (lanes 24-31).  Each warp sums its 8-lane groups, the node's four warps
+// meet in shared memory (part: 4 x 10 values per node) and the node's first thread adds them in a
+// fixed order and applies the step.  Every thread of the block must call this (block barriers).
+template <typename Real>
+__device__ __forceinline__ void gs_update_split3(const LevelPtrs<Real> &L, Real *xy, const Grid<3> &g, const int *I, bool active,
+                                                 unsigned int *err, int separate, const Real *Ac, const Real *Bc, int64_t jc,
+                                                 int64_t nc, Real (*part)[10])
+{
+    const int t = threadIdx.x & 127, p = t >> 5, lane = t & 31;
+    Real v[5] = {0, 0, 0, 0, 0};
+    const int s1 = g.r + 1, s0 = s1 * s1;
+    const int i = I[0] * s0 + I[1] * s1 + I[2];
+    if (active)
+    {
+        const int st[3] = {s0, s1, 1};
+        if (lane < 24)
+        {
+            const int A = lane / 3, K = lane - 3 * (lane / 3);
+            const int pax[3] = {(K == 2) ? 1 : 0, (K == 0) ? 1 : 2, (K == 0) ? 2 : (K == 1 ? 1 : 0)};
+            bool ok = true;
+#pragma unroll
+            for (int d = 0; d < 3; d++)
+            {
+                int e = I[d] - cbit<3>(A, d);
+                ok = ok && e >= 0 && e < g.r;
+            }
+            if (ok)
+            {
+                int sd[3];
+#pragma unroll
+                for (int a = 0; a < 3; a++) sd[a] = cbit<3>(A, pax[a]) ? -st[pax[a]] : st[pax[a]];
+                Real x[8], y[8];
+#pragma unroll
+                for (int cc = 0; cc < 8; cc++)
+                {
+                    int jj = i;
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+                        if (cbit<3>(cc, a)) jj += sd[a];
+                    Real2<Real> q = ld2(xy, jj);
+                    x[cc] = q.x;
+                    y[cc] = q.y;
+                }
+                component_fit_pq3<Real>(x, y, p >> 1, p & 1, v);
+            }
+        }
+        else
+        {
+            const int o = 8 * p + lane - 24;
+            if (o < 27)
+            {
+                const int off[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+                bool in = true;
+#pragma unroll
+                for (int d = 0; d < 3; d++) { int q = I[d] + off[d]; in = in && q >= 0 && q <= g.r; }
+                if (in)
+                {
+                    const int jj = i + off[0] * s0 + off[1] * s1 + off[2];
+                    const Real a = Ac ? Ac[(int64_t)o * nc + jc] : L.A[(int64_t)o * L.N + i];
+                    const Real b = Bc ? Bc[(int64_t)o * nc + jc] : L.B[(int64_t)o * L.N + i];
+                    const Real2<Real> q = ld2(xy, jj);
+                    v[0] = a * q.x;
+                    v[1] = a * q.y;
+                    if (o == 13) v[4] = a;
+                    else { v[2] = b * q.x; v[3] = b * q.y; }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++)
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+#pragma unroll
+    for (int k = 0; k < 5; k++)
+    {
+        const Real g1 = __shfl_sync(0xffffffffu, v[k], 8), g2 = __shfl_sync(0xffffffffu, v[k], 16);
+        const Real g3 = __shfl_sync(0xffffffffu, v[k], 24);
+        if (lane == 0)
+        {
+            part[p][k] = (v[k] + g1) + g2;
+            part[p][5 + k] = g3;
+        }
+    }
+    __syncthreads();
+    if (active && t == 0)
+    {
+        Real h[10];
+#pragma unroll
+        for (int k = 0; k < 10; k++) h[k] = ((part[0][k] + part[1][k]) + part[2][k]) + part[3][k];
+        const Real ax = h[5], ay = h[6], bx = h[7], by = h[8], acen = h[9];
+        const Real sc = (Real)wedge_scale<3>(g.r);
+        Real q[5];
+        q[0] = h[0] * sc + acen;
+        q[1] = h[1] * sc + acen;
+        q[2] = (Real)2 * h[2] * sc;
+        q[3] = (Real)2 * h[3] * sc + (Real)2 * ax - (Real)2 * by;
+        q[4] = (Real)2 * h[4] * sc + (Real)2 * ay + (Real)2 * bx;
+        Real p0, p1;
+        if (node_step<Real>(q, separate, p0, p1))
+        {
+            Real2<Real> cur = ld2(xy, i);
+            cur.x += p0;
+            cur.y += p1;
+            if (!isfinite((double)cur.x) || !isfinite((double)cur.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
+            reinterpret_cast<Real2<Real> *>(xy)[i] = cur;
+        }
+    }
+    __syncthreads();
+}
+
+// one colour of a small 3D level, point-split: 128 threads per node, kSplitNodes nodes per block;
+// used for colours of at most kSplitMaxColourNodes nodes (3D levels up to 3), whose launches are
+// latency-bound
+constexpr int kSplitNodes = 2;
+constexpr int64_t kSplitMaxColourNodes = 125;
+template <typename Real>
+__global__ void __launch_bounds__(128 * kSplitNodes) gs_colour_split3_kernel(LevelPtrs<Real> L, Colour<3> col, int64_t cbBase,
+                                                                              unsigned int *err, int separate)
+{
+    __shared__ Real part[kSplitNodes][4][10];
+    Grid<3> g(L.level);
+    const int64_t j = (int64_t)blockIdx.x * kSplitNodes + (threadIdx.x >> 7);
+    const bool active = j < col.n;
+    int I[3] = {0, 0, 0};
+    if (active) col.node(j, I);
+    const Real *Ac = L.Acb ? L.Acb + cbBase : nullptr, *Bc = L.Bcb ? L.Bcb + cbBase : nullptr;
+    gs_update_split3<Real>(L, L.xy, g, I, active, err, separate, Ac, Bc, j, col.n, part[threadIdx.x >> 7]);
+}
+
 template <int D, typename Real>
 __device__ __forceinline__ void gs_update_lanes(const LevelPtrs<Real> &L, const Grid<D> &g, const Colour<D> &col, int64_t j,
                                                 bool active, int A, unsigned int *err)
@@ -681,7 +814,7 @@ __global__ void __launch_bounds__(kThreads) gs_colour_flat_kernel(LevelPtrs<Real
 // registers: 3D float) so that a colour takes as few passes as possible.
 template <int D, typename Real>
 constexpr int persistent_threads() { return (D == 3 && sizeof(Real) == 4) ? 1024 : 256; }
-template <int D, typename Real, bool SmemStencil, int MaxThreads, bool WarpPerNode>
+template <int D, typename Real, bool SmemStencil, int MaxThreads, int Mode>
 __global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L, int iters, unsigned int *err, int separate)
 {
     Grid<D> g(L.level);
@@ -702,7 +835,17 @@ __global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L,
         for (int c = 0; c < (1 << D); c++)
         {
             Colour<D> col(g, c);
-            if constexpr (WarpPerNode && D == 3)
+            if constexpr (Mode == 2 && D == 3)
+            {
+                // 128 threads per node, the block holds every node of the largest colour
+                __shared__ Real part[8][4][10];
+                const int64_t j = threadIdx.x >> 7;
+                const bool active = j < col.n;
+                int I[3] = {0, 0, 0};
+                if (active) col.node(j, I);
+                gs_update_split3<Real>(Ls, xy, g, I, active, err, separate, nullptr, nullptr, 0, 0, part[threadIdx.x >> 7]);
+            }
+            else if constexpr (Mode == 1 && D == 3)
             {
                 // one warp per node; the block holds a warp for every node of the largest colour
                 const int64_t j = threadIdx.x >> 5;
@@ -906,6 +1049,14 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
     Grid<D> g(L.level);
     Colour<D> col(g, colour);
     if (col.n == 0) return;
+    if constexpr (D == 3)
+        if (g_gs_variant != 0 && col.n <= kSplitMaxColourNodes)
+        {
+            // small levels: point-split update, 128 threads per node
+            gs_colour_split3_kernel<Real><<<(unsigned)((col.n + kSplitNodes - 1) / kSplitNodes), 128 * kSplitNodes, 0, s>>>(
+                L, col, colour_block_base<D>(g, colour), err, separate);
+            return;
+        }
     if (g_gs_variant == 0) gs_colour_kernel<D, Real><<<blocks_for(col.n), kThreads, 0, s>>>(L, col, err, separate);
     else if (g_gs_variant == 2)
         gs_colour_flat_kernel<D, Real><<<blocks_for(col.n << D), kThreads, 0, s>>>(L, col, err, separate);
@@ -923,12 +1074,17 @@ void set_gs_variant(int v) { g_gs_variant = v; }
 // shared-memory carve-out of the single-block level kernels whose stencils live in shared memory
 constexpr size_t kLevelSmemLimit = 200 * 1024;
 
+// the point-split level kernel holds 128 threads per node, up to 8 nodes
+constexpr int kSplitThreads = 1024;
+
 template <int D, typename Real>
 static void prepare_level_kernels()
 {
     constexpr int MT = persistent_threads<D, Real>();
-    cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLevelSmemLimit);
-    cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLevelSmemLimit);
+    cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLevelSmemLimit);
+    if constexpr (D == 3)
+        cudaFuncSetAttribute(gs_level_kernel<D, Real, true, kSplitThreads, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kLevelSmemLimit);
 }
 
 void prepare_gs_kernels()
@@ -951,18 +1107,19 @@ int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cud
         const size_t xyBytes = 2 * g.N * sizeof(Real), stBytes = 2 * (size_t)Dims<D>::S * g.N * sizeof(Real);
         const bool smemStencil = xyBytes + stBytes <= kLevelSmemLimit;
         const size_t smem = xyBytes + (smemStencil ? stBytes : 0);
-        if (D == 3 && colour0 <= 8 && colour0 * 32 <= MT)
-        {
-            // a warp per node: the tiny levels, where the update latency sets the pace
-            const int threads = (int)colour0 * 32;
-            if (smemStencil) gs_level_kernel<D, Real, true, MT, true><<<1, threads, smem, s>>>(L, iters, err, separate);
-            else gs_level_kernel<D, Real, false, MT, true><<<1, threads, smem, s>>>(L, iters, err, separate);
-            return 1;
-        }
+        if constexpr (D == 3)
+            if (colour0 * 128 <= kSplitThreads)
+            {
+                // 128 threads per node: the tiny levels, where the update latency sets the pace
+                const int threads = (int)colour0 * 128;
+                if (smemStencil) gs_level_kernel<D, Real, true, kSplitThreads, 2><<<1, threads, smem, s>>>(L, iters, err, separate);
+                else gs_level_kernel<D, Real, false, kSplitThreads, 2><<<1, threads, smem, s>>>(L, iters, err, separate);
+                return 1;
+            }
         // lanes per node: one pass per colour where the block allows it, whole warps
         const int threads = (int)std::min<int64_t>(MT, ((colour0 << D) + 31) / 32 * 32);
-        if (smemStencil) gs_level_kernel<D, Real, true, MT, false><<<1, threads, smem, s>>>(L, iters, err, separate);
-        else gs_level_kernel<D, Real, false, MT, false><<<1, threads, smem, s>>>(L, iters, err, separate);
+        if (smemStencil) gs_level_kernel<D, Real, true, MT, 0><<<1, threads, smem, s>>>(L, iters, err, separate);
+        else gs_level_kernel<D, Real, false, MT, 0><<<1, threads, smem, s>>>(L, iters, err, separate);
         return 1;
     }
     int n = 0;
