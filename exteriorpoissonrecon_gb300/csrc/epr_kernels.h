@@ -40,7 +40,8 @@ void launch_quadfit(const LevelPtrs<Real> &L, const Real *xy, double *out, cudaS
 template <int D, typename Real>
 void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, cudaStream_t s, int separate = 0);
 // selects the colour-kernel variant (0: one thread per node, 1: 2^D lanes per node on a row grid,
-// 2: 2^D lanes per node on a flat grid; 1 is the default, 0.69 ms against 0.70 ms at depth 8)
+// 2: 2^D lanes per node on a flat grid; 1 is the default, 0.69 ms against 0.70 ms at depth 8;
+// 4: as 1 without the point-split update of the small 3D levels)
 void set_gs_variant(int v);
 // iters full sweeps (all 2^D colours in order); levels of at most persistentMaxNodes nodes run all
 // sweeps inside one thread block, larger ones launch one kernel per colour.  Returns the number of

@@ -1005,7 +1005,8 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n)
 
 inline unsigned int blocks_for(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
 
-int g_gs_variant = 1;  // 0: one thread per node, 1: 2^D lanes per node (row grid), 2: 2^D lanes per node (flat grid)
+int g_gs_variant = 1;  // 0: one thread per node, 1: 2^D lanes per node (row grid), 2: 2^D lanes per node (flat grid),
+                       // 4: as 1 without the point-split update of the small 3D levels
 
 }  // namespace
 
@@ -1050,7 +1051,7 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
     Colour<D> col(g, colour);
     if (col.n == 0) return;
     if constexpr (D == 3)
-        if (g_gs_variant != 0 && col.n <= kSplitMaxColourNodes)
+        if (g_gs_variant != 0 && g_gs_variant != 4 && col.n <= kSplitMaxColourNodes)
         {
             // small levels: point-split update, 128 threads per node
             gs_colour_split3_kernel<Real><<<(unsigned)((col.n + kSplitNodes - 1) / kSplitNodes), 128 * kSplitNodes, 0, s>>>(
@@ -1074,7 +1075,7 @@ void set_gs_variant(int v) { g_gs_variant = v; }
 // shared-memory carve-out of the single-block level kernels whose stencils live in shared memory
 constexpr size_t kLevelSmemLimit = 200 * 1024;
 
-// the point-split level kernel holds 128 threads per node, up to 8 nodes
+// block size bound of the point-split level kernel (128 threads per node)
 constexpr int kSplitThreads = 1024;
 
 template <int D, typename Real>
@@ -1083,8 +1084,11 @@ static void prepare_level_kernels()
     constexpr int MT = persistent_threads<D, Real>();
     cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLevelSmemLimit);
     if constexpr (D == 3)
+    {
+        cudaFuncSetAttribute(gs_level_kernel<D, Real, true, MT, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLevelSmemLimit);
         cudaFuncSetAttribute(gs_level_kernel<D, Real, true, kSplitThreads, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kLevelSmemLimit);
+    }
 }
 
 void prepare_gs_kernels()
@@ -1107,13 +1111,24 @@ int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cud
         const size_t xyBytes = 2 * g.N * sizeof(Real), stBytes = 2 * (size_t)Dims<D>::S * g.N * sizeof(Real);
         const bool smemStencil = xyBytes + stBytes <= kLevelSmemLimit;
         const size_t smem = xyBytes + (smemStencil ? stBytes : 0);
+        // the single node of a colour at resolution 1 is split over four warps (21 against 24 ms
+        // float, 176 against 234 ms double for the level's 2560 sweeps at depth 8); resolution 2
+        // takes a warp per node (13 against 22 ms float, 145 against 265 ms double)
         if constexpr (D == 3)
-            if (colour0 * 128 <= kSplitThreads)
+            if (g_gs_variant != 4 && colour0 == 1)
             {
                 // 128 threads per node: the tiny levels, where the update latency sets the pace
                 const int threads = (int)colour0 * 128;
                 if (smemStencil) gs_level_kernel<D, Real, true, kSplitThreads, 2><<<1, threads, smem, s>>>(L, iters, err, separate);
                 else gs_level_kernel<D, Real, false, kSplitThreads, 2><<<1, threads, smem, s>>>(L, iters, err, separate);
+                return 1;
+            }
+        if constexpr (D == 3)
+            if (colour0 <= 8 && colour0 * 32 <= MT)
+            {
+                const int threads = (int)colour0 * 32;
+                if (smemStencil) gs_level_kernel<D, Real, true, MT, 1><<<1, threads, smem, s>>>(L, iters, err, separate);
+                else gs_level_kernel<D, Real, false, MT, 1><<<1, threads, smem, s>>>(L, iters, err, separate);
                 return 1;
             }
         // lanes per node: one pass per colour where the block allows it, whole warps
