@@ -614,27 +614,31 @@ __device__ __forceinline__ void gs_update_warp3(const LevelPtrs<Real> &L, Real *
     }
 }
 
-// Point-split variant for the latency-bound small 3D levels: 128 threads per node.  Warp p takes
-// the Gauss points with (gp, gq) = (p >> 1, p & 1) of every (element A, component K) pair (lane
-// 3 A + K < 24, canonical orientation and axis permutation as above) and the stencil offsets
-// 8 p + lane - 24 < 27 (lanes 24-31).  Each warp sums its 8-lane groups, the node's four warps
-// meet in shared memory (part: 4 x 10 values per node) and the node's first thread adds them in a
-// fixed order and applies the step.  Every thread of the block must call this (block barriers).
+// Point-split variant for the latency-bound small 3D levels: 128 threads per node.  Thread
+// u < 96 takes the Gauss points with (gp, gq) = (u & 3) >> 1, u & 1 of component K of element A,
+// 3 A + K = u >> 2 (canonical orientation and axis permutation as above), so that the work of the
+// existing elements is packed into as few warps as possible (the FP64 pipe is charged per warp
+// instruction, whatever the number of active lanes); threads 96-122 take one stencil offset each.
+// Each warp sums its lanes, the node's four warps meet in shared memory (part: 4 x 5 values per
+// node: warps 0-2 the wedge integrals, warp 3 the stencil sums) and the node's first thread adds
+// them in a fixed order and applies the step.  Every thread of the block must call this (block
+// barriers).
 template <typename Real>
 __device__ __forceinline__ void gs_update_split3(const LevelPtrs<Real> &L, Real *xy, const Grid<3> &g, const int *I, bool active,
                                                  unsigned int *err, int separate, const Real *Ac, const Real *Bc, int64_t jc,
-                                                 int64_t nc, Real (*part)[10])
+                                                 int64_t nc, Real (*part)[5])
 {
-    const int t = threadIdx.x & 127, p = t >> 5, lane = t & 31;
+    const int t = threadIdx.x & 127, wp = t >> 5, lane = t & 31;
     Real v[5] = {0, 0, 0, 0, 0};
     const int s1 = g.r + 1, s0 = s1 * s1;
     const int i = I[0] * s0 + I[1] * s1 + I[2];
     if (active)
     {
         const int st[3] = {s0, s1, 1};
-        if (lane < 24)
+        if (t < 96)
         {
-            const int A = lane / 3, K = lane - 3 * (lane / 3);
+            const int ak = t >> 2, pq = t & 3;
+            const int A = ak / 3, K = ak - 3 * (ak / 3);
             const int pax[3] = {(K == 2) ? 1 : 0, (K == 0) ? 1 : 2, (K == 0) ? 2 : (K == 1 ? 1 : 0)};
             bool ok = true;
 #pragma unroll
@@ -660,54 +664,43 @@ __device__ __forceinline__ void gs_update_split3(const LevelPtrs<Real> &L, Real 
                     x[cc] = q.x;
                     y[cc] = q.y;
                 }
-                component_fit_pq3<Real>(x, y, p >> 1, p & 1, v);
+                component_fit_pq3<Real>(x, y, pq >> 1, pq & 1, v);
             }
         }
-        else
+        else if (t < 96 + 27)
         {
-            const int o = 8 * p + lane - 24;
-            if (o < 27)
-            {
-                const int off[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
-                bool in = true;
+            const int o = t - 96;
+            const int off[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+            bool in = true;
 #pragma unroll
-                for (int d = 0; d < 3; d++) { int q = I[d] + off[d]; in = in && q >= 0 && q <= g.r; }
-                if (in)
-                {
-                    const int jj = i + off[0] * s0 + off[1] * s1 + off[2];
-                    const Real a = Ac ? Ac[(int64_t)o * nc + jc] : L.A[(int64_t)o * L.N + i];
-                    const Real b = Bc ? Bc[(int64_t)o * nc + jc] : L.B[(int64_t)o * L.N + i];
-                    const Real2<Real> q = ld2(xy, jj);
-                    v[0] = a * q.x;
-                    v[1] = a * q.y;
-                    if (o == 13) v[4] = a;
-                    else { v[2] = b * q.x; v[3] = b * q.y; }
-                }
+            for (int d = 0; d < 3; d++) { int q = I[d] + off[d]; in = in && q >= 0 && q <= g.r; }
+            if (in)
+            {
+                const int jj = i + off[0] * s0 + off[1] * s1 + off[2];
+                const Real a = Ac ? Ac[(int64_t)o * nc + jc] : L.A[(int64_t)o * L.N + i];
+                const Real b = Bc ? Bc[(int64_t)o * nc + jc] : L.B[(int64_t)o * L.N + i];
+                const Real2<Real> q = ld2(xy, jj);
+                v[0] = a * q.x;
+                v[1] = a * q.y;
+                if (o == 13) v[4] = a;
+                else { v[2] = b * q.x; v[3] = b * q.y; }
             }
         }
     }
 #pragma unroll
     for (int k = 0; k < 5; k++)
-#pragma unroll
-        for (int o = 4; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-#pragma unroll
-    for (int k = 0; k < 5; k++)
     {
-        const Real g1 = __shfl_sync(0xffffffffu, v[k], 8), g2 = __shfl_sync(0xffffffffu, v[k], 16);
-        const Real g3 = __shfl_sync(0xffffffffu, v[k], 24);
-        if (lane == 0)
-        {
-            part[p][k] = (v[k] + g1) + g2;
-            part[p][5 + k] = g3;
-        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+        if (lane == 0) part[wp][k] = v[k];
     }
     __syncthreads();
     if (active && t == 0)
     {
-        Real h[10];
+        Real h[5];
 #pragma unroll
-        for (int k = 0; k < 10; k++) h[k] = ((part[0][k] + part[1][k]) + part[2][k]) + part[3][k];
-        const Real ax = h[5], ay = h[6], bx = h[7], by = h[8], acen = h[9];
+        for (int k = 0; k < 5; k++) h[k] = (part[0][k] + part[1][k]) + part[2][k];
+        const Real ax = part[3][0], ay = part[3][1], bx = part[3][2], by = part[3][3], acen = part[3][4];
         const Real sc = (Real)wedge_scale<3>(g.r);
         Real q[5];
         q[0] = h[0] * sc + acen;
@@ -737,7 +730,7 @@ template <typename Real>
 __global__ void __launch_bounds__(128 * kSplitNodes) gs_colour_split3_kernel(LevelPtrs<Real> L, Colour<3> col, int64_t cbBase,
                                                                               unsigned int *err, int separate)
 {
-    __shared__ Real part[kSplitNodes][4][10];
+    __shared__ Real part[kSplitNodes][4][5];
     Grid<3> g(L.level);
     const int64_t j = (int64_t)blockIdx.x * kSplitNodes + (threadIdx.x >> 7);
     const bool active = j < col.n;
@@ -838,7 +831,7 @@ __global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L,
             if constexpr (Mode == 2 && D == 3)
             {
                 // 128 threads per node, the block holds every node of the largest colour
-                __shared__ Real part[8][4][10];
+                __shared__ Real part[8][4][5];
                 const int64_t j = threadIdx.x >> 7;
                 const bool active = j < col.n;
                 int I[3] = {0, 0, 0};
