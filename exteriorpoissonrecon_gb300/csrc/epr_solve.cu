@@ -1104,9 +1104,9 @@ int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cud
         const size_t xyBytes = 2 * g.N * sizeof(Real), stBytes = 2 * (size_t)Dims<D>::S * g.N * sizeof(Real);
         const bool smemStencil = xyBytes + stBytes <= kLevelSmemLimit;
         const size_t smem = xyBytes + (smemStencil ? stBytes : 0);
-        // the single node of a colour at resolution 1 is split over four warps (21 against 24 ms
-        // float, 176 against 234 ms double for the level's 2560 sweeps at depth 8); resolution 2
-        // takes a warp per node (13 against 22 ms float, 145 against 265 ms double)
+        // the single node of a colour at resolution 1 is point-split (17 against 24 ms float, 146
+        // against 234 ms double for the level's 2560 sweeps at depth 8); resolution 2 takes a warp
+        // per node (13 against 16 ms float, 145 against 182 ms double)
         if constexpr (D == 3)
             if (g_gs_variant != 4 && colour0 == 1)
             {
