@@ -8,7 +8,11 @@ one in the xz-plane centred at (1,0,0)), 1M samples uniform in arc length, Gauss
 noise sigma 0.005 (unit-cube units), 5 degree angular noise, plus 10% uniform spot outliers with
 random frames; 3D, depth 8 (257^3 nodes x 2 channels = 33.9M unknowns), code-default parameters.
 
-One step = one full solve from the built system (fresh initial guess each time).  `value` is the
+One step = one full solve from the built system (fresh initial guess each time): the reference's
+cascadic paired Gauss-Seidel schedule with FP32 smoothing on levels >= 4 and FP64 on levels 0-3
+(the named configuration's FP64 coarse solve; it keeps the double run's local minimum), FP64
+energies and reductions.  The line also reports the all-double and the all-float runs of the
+same schedule.  `value` is the
 device time per solve with the system resident in HBM; `e2e` repeats the whole public-API
 pipeline per step from host buffers (samples host->device, build, solve, solution device->host).
 Every array of a level exceeds the 129 MB L2 (coefficients 137 MB in FP32, stencils 3.7 GB), so no
@@ -55,6 +59,9 @@ def parse():
     ap.add_argument("--depth", type=int, default=None)
     ap.add_argument("--samples", type=int, default=1_000_000)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--fp64-levels", type=int, default=4,
+                    help="with fp32: levels below this one relax in double (the named configuration's FP64 "
+                         "coarse solve; 4 keeps the double run's local minimum)")
     ap.add_argument("--solver", default="cascadic", choices=["cascadic", "multigrid"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -193,7 +200,9 @@ def main():
     name = f"link-1M+10%spot-3D-depth{depth}" if dim == 3 else f"clifford-torus-1M-4D-depth{depth}"
     config = {"workload": name, "samples": int(len(pu)), "depth": depth,
               "dim": dim, "nodes": (2 ** depth + 1) ** dim, "unknowns": 2 * (2 ** depth + 1) ** dim,
-              "solver": args.solver, "precision": args.precision, "l2": "inputs larger than L2 (no flush)",
+              "solver": args.solver, "precision": args.precision,
+              "fp64_levels": args.fp64_levels if args.precision == "fp32" else None,
+              "l2": "inputs larger than L2 (no flush)",
               "parallelism": f"replicas{ws}"}
 
     if args.impl == "reference":
@@ -209,7 +218,8 @@ def main():
         return
 
     import exteriorpoissonrecon_gb300 as epr
-    r = epr.Reconstructor(dim, depth, pu, sk, precision=args.precision, solver=args.solver, device=local)
+    mixed = dict(fp64_levels=args.fp64_levels) if args.precision == "fp32" else {}
+    r = epr.Reconstructor(dim, depth, pu, sk, precision=args.precision, solver=args.solver, device=local, **mixed)
     for _ in range(args.warmup):
         r.solve()
     build_ms = r.stats.build_ms  # device time of epr_build (filled in by the first solve's stats copy)
@@ -252,7 +262,10 @@ def main():
     roofline = {"bound": "hbm", "kernel": "gs_colour_lanes_kernel", "achieved": achieved, "peak": hbm_peak,
                 "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_kind, "traffic": gs_traffic,
                 "launch_ms": gs_ms, "algorithmic_bytes_per_launch": gs_bytes,
-                "note": "FMA-bound quartic relaxation; bytes = coefficient read + stencil columns + update writes",
+                "note": ("FMA-bound quartic relaxation; bytes = coefficient read + stencil columns + update writes; "
+                         "the finest level's colour launches take share_of_step of the step, the rest is the "
+                         "coarser levels (levels below fp64_levels in double: single-block, FP64-latency-bound)"),
+                "share_of_step": 10 * (2 ** dim) * gs_ms / (per_step_s * 1e3),
                 "compute": {"algorithmic_flops_per_launch": gs_flops, "achieved_tflops": gs_flops / (gs_ms * 1e-3) / 1e12,
                             "peak_tflops": fp32_peak if args.precision == "fp32" else None,
                             "peak_source": "nominal FP32 at the sampled SM clock",
@@ -277,7 +290,7 @@ def main():
     e2e_parts = []
     for _ in range(args.e2e_steps):
         t0 = time.perf_counter()
-        r2 = epr.Reconstructor(dim, depth, pu, sk, precision=args.precision, solver=args.solver, device=local)
+        r2 = epr.Reconstructor(dim, depth, pu, sk, precision=args.precision, solver=args.solver, device=local, **mixed)
         t1 = time.perf_counter()
         r2.solve()
         t2 = time.perf_counter()
@@ -309,17 +322,19 @@ def main():
         line["error_vs_fp64"] = {"energy_fp64": e64, "energy_rel_diff": (e32 - e64) / e64,
                                  "finest_x_rel_l2": float(np.linalg.norm(xs32 - xs64) / np.linalg.norm(xs64)),
                                  "fp64_solve_s": st64["solve_ms"] / 1e3}
-        # the same float schedule with the coarse levels 0-3 in double: the cascadic solve leaves the
-        # zero stationary point there, and double keeps the double run's local minimum
-        rm = epr.Reconstructor(dim, depth, pu, sk, precision="fp32", fp64_levels=4, solver=args.solver, device=local)
+        # the same schedule with every level in float: faster, but the cascadic solve leaves the zero
+        # stationary point at levels 3-4 from components that rounding decides, so it ends in another
+        # local minimum
+        rm = epr.Reconstructor(dim, depth, pu, sk, precision="fp32", fp64_levels=0, solver=args.solver, device=local)
         for _ in range(3):
             stm = rm.solve()
         em = stm["fit_energy"] + stm["reg_energy"]
         xsm = rm.coefficients(depth)[0]
-        line["fp32_with_fp64_coarse_levels"] = {
-            "fp64_levels": 4, "solve_s": stm["solve_ms"] / 1e3, "energy": em, "energy_rel_diff_vs_fp64": (em - e64) / e64,
+        line["all_levels_fp32"] = {
+            "fp64_levels": 0, "solve_s": stm["solve_ms"] / 1e3, "energy": em, "energy_rel_diff_vs_fp64": (em - e64) / e64,
             "finest_x_rel_l2_vs_fp64": float(np.linalg.norm(xsm - xs64) / np.linalg.norm(xs64)),
             "speedup_vs_fp64_solve": st64["solve_ms"] / stm["solve_ms"]}
+        line["error_vs_fp64"]["speedup_vs_fp64_solve"] = st64["solve_ms"] / (per_step_s * 1e3)
         rm.close()
         r64.close()
     if rank == 0 and not args.no_cpu_baseline:
