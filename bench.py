@@ -59,9 +59,10 @@ def parse():
     ap.add_argument("--depth", type=int, default=None)
     ap.add_argument("--samples", type=int, default=1_000_000)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
-    ap.add_argument("--fp64-levels", type=int, default=4,
-                    help="with fp32: levels below this one relax in double (the named configuration's FP64 "
-                         "coarse solve; 4 keeps the double run's local minimum)")
+    ap.add_argument("--fp64-levels", type=int, default=None,
+                    help="with fp32: levels below this one relax in double (default 4 in 3D: the named "
+                         "configuration's FP64 coarse solve, which keeps the double run's local minimum; "
+                         "0 in 4D, where the all-float solve already has the double energy to 1e-9)")
     ap.add_argument("--solver", default="cascadic", choices=["cascadic", "multigrid"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -194,6 +195,8 @@ def main():
     args = parse()
     ws, rank, local, pg = dist_setup(args)
     depth = args.depth if args.depth is not None else (8 if args.dim == 3 else 6)
+    if args.fp64_levels is None:
+        args.fp64_levels = 4 if args.dim == 3 else 0
     cpu_depth = args.cpu_depth if args.dim == 3 else min(args.cpu_depth, 4)
     dim = args.dim
     pu, sk = workload(args.samples, dim)
