@@ -9,9 +9,9 @@ noise sigma 0.005 (unit-cube units), 5 degree angular noise, plus 10% uniform sp
 random frames; 3D, depth 8 (257^3 nodes x 2 channels = 33.9M unknowns), code-default parameters.
 
 One step = one full solve from the built system (fresh initial guess each time): the reference's
-cascadic paired Gauss-Seidel schedule with FP32 smoothing on levels >= 4 and FP64 on levels 0-3
-(the named configuration's FP64 coarse solve; it keeps the double run's local minimum), FP64
-energies and reductions.  The line also reports the all-double and the all-float runs of the
+cascadic paired Gauss-Seidel schedule with FP32 smoothing except on levels 2-3, which run in FP64
+(the named configuration's FP64 coarse solve: the cascadic solve leaves the zero stationary point
+there, and double keeps the double run's local minimum), FP64 energies and reductions.  The line also reports the all-double and the all-float runs of the
 same schedule.  `value` is the
 device time per solve with the system resident in HBM; `e2e` repeats the whole public-API
 pipeline per step from host buffers (samples host->device, build, solve, solution device->host).
@@ -60,9 +60,11 @@ def parse():
     ap.add_argument("--samples", type=int, default=1_000_000)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--fp64-levels", type=int, default=None,
-                    help="with fp32: levels below this one relax in double (default 4 in 3D: the named "
-                         "configuration's FP64 coarse solve, which keeps the double run's local minimum; "
-                         "0 in 4D, where the all-float solve already has the double energy to 1e-9)")
+                    help="with fp32: levels fp64-from .. fp64-levels-1 relax in double (default 2..3 in 3D: the "
+                         "named configuration's FP64 coarse solve, where the cascadic solve leaves the zero "
+                         "stationary point, which keeps the double run's local minimum; none in 4D, where the "
+                         "all-float solve already has the double energy to 1e-9)")
+    ap.add_argument("--fp64-from", type=int, default=None)
     ap.add_argument("--solver", default="cascadic", choices=["cascadic", "multigrid"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -197,6 +199,8 @@ def main():
     depth = args.depth if args.depth is not None else (8 if args.dim == 3 else 6)
     if args.fp64_levels is None:
         args.fp64_levels = 4 if args.dim == 3 else 0
+    if args.fp64_from is None:
+        args.fp64_from = 2 if args.dim == 3 else 0
     cpu_depth = args.cpu_depth if args.dim == 3 else min(args.cpu_depth, 4)
     dim = args.dim
     pu, sk = workload(args.samples, dim)
@@ -204,7 +208,7 @@ def main():
     config = {"workload": name, "samples": int(len(pu)), "depth": depth,
               "dim": dim, "nodes": (2 ** depth + 1) ** dim, "unknowns": 2 * (2 ** depth + 1) ** dim,
               "solver": args.solver, "precision": args.precision,
-              "fp64_levels": args.fp64_levels if args.precision == "fp32" else None,
+              "fp64_levels": [args.fp64_from, args.fp64_levels] if args.precision == "fp32" else None,
               "l2": "inputs larger than L2 (no flush)",
               "parallelism": f"replicas{ws}"}
 
@@ -221,7 +225,7 @@ def main():
         return
 
     import exteriorpoissonrecon_gb300 as epr
-    mixed = dict(fp64_levels=args.fp64_levels) if args.precision == "fp32" else {}
+    mixed = dict(fp64_levels=args.fp64_levels, fp64_from=args.fp64_from) if args.precision == "fp32" else {}
     r = epr.Reconstructor(dim, depth, pu, sk, precision=args.precision, solver=args.solver, device=local, **mixed)
     for _ in range(args.warmup):
         r.solve()
@@ -267,7 +271,7 @@ def main():
                 "launch_ms": gs_ms, "algorithmic_bytes_per_launch": gs_bytes,
                 "note": ("FMA-bound quartic relaxation; bytes = coefficient read + stencil columns + update writes; "
                          "the finest level's colour launches take share_of_step of the step, the rest is the "
-                         "coarser levels (levels below fp64_levels in double: single-block, FP64-latency-bound)"),
+                         "coarser levels (the double band latency-bound on the FP64 pipe)"),
                 "share_of_step": 10 * (2 ** dim) * gs_ms / (per_step_s * 1e3),
                 "compute": {"algorithmic_flops_per_launch": gs_flops, "achieved_tflops": gs_flops / (gs_ms * 1e-3) / 1e12,
                             "peak_tflops": fp32_peak if args.precision == "fp32" else None,

@@ -56,6 +56,7 @@ class Params(ctypes.Structure):
         ("fp64_levels", ctypes.c_int),
         ("single_level", ctypes.c_int),
         ("separate", ctypes.c_int),
+        ("fp64_from", ctypes.c_int),
     ]
 
 

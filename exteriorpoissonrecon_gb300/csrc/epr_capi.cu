@@ -89,7 +89,7 @@ bool Context::ensure_level(int l)
     return true;
 }
 
-bool Context::lvl32(int l) const { return P.precision == EPR_FP32 && l >= P.fp64_levels; }
+bool Context::lvl32(int l) const { return P.precision == EPR_FP32 && !(l >= P.fp64_from && l < P.fp64_levels); }
 
 // refreshes the derived copies of a level's system: the float stencils (float levels) and the
 // colour-blocked stencils of the levels that are relaxed by one kernel per colour
@@ -233,6 +233,14 @@ bool Context::prolong_add(int l)
     with_dim(this, [&](auto dd) {
         constexpr int D = decltype(dd)::value;
         if (c32 && f32) launch_prolong<D, float>(l, levels[l].xy32, levels[l + 1].xy32, 1, stream);
+        else if (c32 && !f32)
+        {
+            // a float coarse level feeding a double fine level: refresh the coarse level's double
+            // copy, then prolong in double
+            launch_convert_f2d(levels[l].xy32, levels[l].xy64, 2 * levels[l].N, stream);
+            launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 1, stream);
+            launches++;
+        }
         else
         {
             // a double coarse level feeding a float fine level: prolong in double, then refresh
@@ -482,6 +490,7 @@ void epr_default_params(epr_params *p)
     p->verbose = 0;
     p->device = 0;
     p->fp64_levels = 0;
+    p->fp64_from = 0;
     p->single_level = 0;
     p->separate = 0;
 }
@@ -500,6 +509,7 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
     if (p.t_radius < 0 || p.t_radius > 4 || p.d_radius < 0 || p.d_radius > 4) { g_error = "kernel radius must be in [0,4]"; return nullptr; }
     if (p.precision != EPR_FP64 && p.precision != EPR_FP32) { g_error = "unknown precision"; return nullptr; }
     if (p.solver != EPR_SOLVER_CASCADIC && p.solver != EPR_SOLVER_MULTIGRID) { g_error = "unknown solver"; return nullptr; }
+    if (p.fp64_from < 0 || p.fp64_levels < 0) { g_error = "fp64_from and fp64_levels must not be negative"; return nullptr; }
     if (p.solver == EPR_SOLVER_MULTIGRID && (p.max_cycles < 0 || !(p.tolerance >= 0))) { g_error = "bad multigrid cycle cap or tolerance"; return nullptr; }
     if (cudaSetDevice(p.device) != cudaSuccess)
     {

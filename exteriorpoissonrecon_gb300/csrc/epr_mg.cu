@@ -678,7 +678,7 @@ struct MGLevel
 struct MGHierarchy
 {
     int top = -1;
-    int mode = -1;  // precision and fp64_levels the levels were allocated for
+    int mode = -1;  // precision and double band the levels were allocated for
     std::vector<MGLevel> L;
     double *x64 = nullptr, *b64 = nullptr;  // finest-level double vectors (solution, right-hand side)
 };
@@ -699,7 +699,7 @@ void release_mg(Context &c)
 // (re)allocates the hierarchy for levels 0..top
 static bool mg_prepare(Context &c, int top)
 {
-    const int mode = c.P.precision * 1024 + c.P.fp64_levels;
+    const int mode = (c.P.precision * 1024 + c.P.fp64_levels) * 1024 + c.P.fp64_from;
     if (c.mg && c.mg->top >= top && c.mg->mode == mode) return true;
     release_mg(c);
     c.mg = new MGHierarchy;
@@ -712,7 +712,7 @@ static bool mg_prepare(Context &c, int top)
     {
         MGLevel &m = h.L[l];
         m.N = c.nodes(l);
-        m.f32 = c.P.precision == EPR_FP32 && m.N >= kFloatMinNodes && l >= c.P.fp64_levels;
+        m.f32 = c.lvl32(l) && m.N >= kFloatMinNodes;
         const size_t rs = m.f32 ? sizeof(float) : sizeof(double);
         if (!c.alloc((void **)&m.M64, sizeof(double) * S * m.N, "alloc mg stencil") ||
             !c.alloc(&m.Mcb, rs * S * m.N, "alloc mg stencil") || !c.alloc(&m.x, rs * m.N, "alloc mg x") ||

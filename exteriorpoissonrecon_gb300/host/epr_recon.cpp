@@ -32,7 +32,7 @@ struct Args
     int depth = 5, seed = 0, tRadius = 1, dRadius = 1, aRadius = -1, minSolveDepth = 0, gsIters = 10, maxSolveDepth = -1;
     bool singleLevel = false, separate = false, verbose = false, project = false;
     std::string precision = "fp64", solver = "cascadic";
-    int device = 0, fp64Levels = 0, maxCycles = 200;
+    int device = 0, fp64Levels = 0, fp64From = 0, maxCycles = 200;
     double tolerance = 1e-6;
 };
 
@@ -63,7 +63,8 @@ void Usage(const char *ex)
     printf("\t[--scale <bounding box scale>=1.1]\n");
     printf("\t[--iMult <iteration multiplier>=2]\n");
     printf("\t[--precision fp64|fp32]\n");
-    printf("\t[--fp64Levels <levels below this one relax in double with --precision fp32>=0]\n");
+    printf("\t[--fp64From <first level of the double band with --precision fp32>=0]\n");
+    printf("\t[--fp64Levels <levels from --fp64From below this one relax in double with --precision fp32>=0]\n");
     printf("\t[--solver cascadic|multigrid]\n");
     printf("\t[--tolerance <multigrid: relative gradient per level>=1e-6]\n");
     printf("\t[--maxCycles <multigrid: alternating rounds per level>=200]\n");
@@ -82,7 +83,7 @@ Args Parse(int argc, char **argv)
     std::map<std::string, int *> ints = {{"depth", &a.depth}, {"seed", &a.seed}, {"tRadius", &a.tRadius},
                                          {"dRadius", &a.dRadius}, {"aRadius", &a.aRadius}, {"minSolveDepth", &a.minSolveDepth},
                                          {"gsIters", &a.gsIters}, {"maxSolveDepth", &a.maxSolveDepth}, {"device", &a.device},
-                                         {"fp64Levels", &a.fp64Levels}, {"maxCycles", &a.maxCycles}};
+                                         {"fp64Levels", &a.fp64Levels}, {"fp64From", &a.fp64From}, {"maxCycles", &a.maxCycles}};
     std::map<std::string, bool *> flags = {{"singleLevel", &a.singleLevel}, {"separate", &a.separate},
                                            {"verbose", &a.verbose}, {"project", &a.project}};
     for (int i = 1; i < argc; i++)
@@ -353,6 +354,7 @@ int main(int argc, char **argv)
     p.seed = (unsigned)a.seed;
     p.precision = a.precision == "fp32" ? EPR_FP32 : EPR_FP64;
     p.fp64_levels = a.fp64Levels;
+    p.fp64_from = a.fp64From;
     p.solver = a.solver == "multigrid" ? EPR_SOLVER_MULTIGRID : EPR_SOLVER_CASCADIC;
     p.tolerance = a.tolerance;
     p.max_cycles = a.maxCycles;

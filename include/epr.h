@@ -88,9 +88,10 @@ typedef struct epr_params {
     int max_cycles;       /* multigrid: cycle cap (200) */
     int verbose;          /* print the reference's per-level "Error[...]" lines */
     int device;           /* CUDA device ordinal the context runs on (0) */
-    int fp64_levels;      /* EPR_FP32 only: levels below this one still run in double (0) */
+    int fp64_levels;      /* EPR_FP32 only: levels fp64_from .. fp64_levels-1 still run in double (0) */
     int single_level;     /* --singleLevel: prolong the initial guess and relax only the finest solve level */
     int separate;         /* --separate: update x then y per node instead of the paired 2x2 step */
+    int fp64_from;        /* EPR_FP32 only: first level of the double band (0) */
 } epr_params;
 
 typedef struct epr_stats {
