@@ -174,3 +174,19 @@ def test_repeated_solves_are_identical(precision):
     for s in sols[1:]:
         assert np.array_equal(s[0], sols[0][0]) and np.array_equal(s[1], sols[0][1])
         assert s[2] == sols[0][2] and s[3] == sols[0][3]
+
+
+def test_double_band_keeps_the_double_minimum():
+    """Float relaxation with levels 2-3 in double reaches the double run's energy (the cascadic
+    solve leaves the zero stationary point on those levels, where float rounding would pick another
+    local minimum)."""
+    pos, fr = epr.samples.make_workload("link", 100000, seed=1)
+    pu, _ = epr.unit_cube(pos)
+    sk = epr.pack_skew(fr)
+    e = {}
+    for name, kw in [("fp64", dict(precision="fp64")), ("band", dict(precision="fp32", fp64_from=2, fp64_levels=4))]:
+        r = epr.Reconstructor(3, 6, pu, sk, **kw)
+        st = r.solve()
+        e[name] = st["fit_energy"] + st["reg_energy"]
+        r.close()
+    assert abs(e["band"] - e["fp64"]) < 1e-6 * e["fp64"]
