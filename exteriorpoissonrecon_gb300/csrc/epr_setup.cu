@@ -1093,34 +1093,6 @@ bool chunked_level(Context &c, const SplatArgs &a, const Item &item, double scal
     return c.launch_ok("chunked gather");
 }
 
-// levels with at most this many vertices use the chunked gather (all levels: the item counts of
-// the vertices near the samples vary too much for one thread or warp per vertex)
-constexpr int64_t kChunkedMaxVertices = (int64_t)1 << 40;
-
-// Fine levels: one thread per vertex (most windows hold no or few items), fixed window order.
-template <int D, bool Samples, class Item>
-__global__ void vertex_gather_kernel(SplatArgs a, Item item, double scale, double *grid)
-{
-    constexpr int W = Item::W;
-    int res = 1 << (a.t - 1), nv = res + 1;
-    int64_t NV = 1;
-    for (int d = 0; d < D; d++) NV *= nv;
-    int64_t vi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (vi >= NV) return;
-    int v[D], clo[D], chi[D], C[D];
-    vertex_of<D>(vi, nv, v);
-    for (int d = 0; d < D; d++) { clo[d] = max(0, v[d] - a.KR - 1); chi[d] = min(res - 1, v[d] + a.KR); C[d] = clo[d]; }
-    double acc[W];
-    for (int w = 0; w < W; w++) acc[w] = 0;
-    do
-    {
-        int lo, hi;
-        item_range<D, Samples>(a, C, lo, hi);
-        for (int it = lo; it < hi; it++) item(a, it, v, C, acc);
-    } while (window_next<D>(C, clo, chi));
-    for (int w = 0; w < W; w++) grid[vi * W + w] = acc[w] * scale;
-}
-
 template <int D>
 bool build_impl(Context &c, Setup &st)
 {
@@ -1245,12 +1217,7 @@ bool build_impl(Context &c, Setup &st)
             double dw = scale / std::pow(std::pow(0.5, t - 1), D - 2);
             item_bspline_kernel<D><<<nblocks(nc, 256), 256, 0, s>>>(mean, nullptr, nc, t, 2 * KR + 1, nullptr, bs);
             DensityItem<D> item{bs, datum, dw};
-            if (gl.N <= kChunkedMaxVertices)
-            {
-                if (!chunked_level<D, false>(c, a, item, 1.0, st.density[t - 1])) return false;
-            }
-            else
-                vertex_gather_kernel<D, false><<<nblocks(gl.N, 128), 128, 0, s>>>(a, item, 1.0, st.density[t - 1]);
+            if (!chunked_level<D, false>(c, a, item, 1.0, st.density[t - 1])) return false;
         }
         c.release(bs);
     }
@@ -1284,13 +1251,7 @@ bool build_impl(Context &c, Setup &st)
             skew_level_kernel<<<nblocks(n, 256), 256, 0, s>>>(st.sdepth, st.order, n, t, depth, D, lw);
             item_bspline_kernel<D><<<nblocks(n, 256), 256, 0, s>>>(st.pos, st.order, n, t, 2 * TR + 1, lw, bs);
             SkewItem<D> item{bs, lw, frame};
-            if (gl.N <= kChunkedMaxVertices)
-            {
-                if (!chunked_level<D, true>(c, a, item, std::pow(std::pow(0.5, depth), 1.5 * 2), st.skewGrid[t - 1])) return false;
-            }
-            else
-                vertex_gather_kernel<D, true><<<nblocks(gl.N, 128), 128, 0, s>>>(a, item, std::pow(std::pow(0.5, depth), 1.5 * 2),
-                                                                               st.skewGrid[t - 1]);
+            if (!chunked_level<D, true>(c, a, item, std::pow(std::pow(0.5, depth), 1.5 * 2), st.skewGrid[t - 1])) return false;
         }
         c.release(bs); c.release(lw); c.release(frame);
     }
