@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -125,7 +126,16 @@ __device__ __forceinline__ uint32_t colour_node(const Colour<D> &col, const uint
 
 // sum_o M[o] x[i + off(o)] over the stencil of node i: interior nodes take the unrolled path with
 // compile-time offsets, boundary nodes check every neighbour.
-template <int D, typename Real>
+// coefficient load: read-only path, or streaming (evict-first: the coefficients are read once per
+// sweep, the x vector is what should stay cached)
+template <bool Streaming, typename Real>
+__device__ __forceinline__ Real coef_load(const Real *p)
+{
+    if constexpr (Streaming) return __ldcs(p);
+    else return __ldg(p);
+}
+
+template <int D, typename Real, bool Streaming = false>
 __device__ __forceinline__ Real stencil_dot(const Real *__restrict__ Mc, int64_t n, int64_t j, const Real *x, uint32_t i,
                                             const int *I, const uint32_t *st, int r)
 {
@@ -142,7 +152,7 @@ __device__ __forceinline__ Real stencil_dot(const Real *__restrict__ Mc, int64_t
             int64_t k = (int64_t)i;
 #pragma unroll
             for (int d = 0; d < D; d++) k += (int64_t)offset_of<D>(o, d) * (int64_t)st[d];
-            s += __ldg(Mc + (int64_t)o * n + j) * x[k];
+            s += coef_load<Streaming>(Mc + (int64_t)o * n + j) * x[k];
         }
     }
     else
@@ -159,7 +169,7 @@ __device__ __forceinline__ Real stencil_dot(const Real *__restrict__ Mc, int64_t
                 ok = ok && q >= 0 && q <= r;
                 k += (int64_t)off * (int64_t)st[d];
             }
-            if (ok) s += __ldg(Mc + (int64_t)o * n + j) * x[k];
+            if (ok) s += coef_load<Streaming>(Mc + (int64_t)o * n + j) * x[k];
         }
     }
     return s;
@@ -175,9 +185,9 @@ __device__ __forceinline__ void node_strides(int r, uint32_t *st)
 
 // x_i += (b_i - sum_j M(j, i) x_j) / M(i, i) for the nodes of one colour (the GSRelaxer update,
 // which reads column i of M; M is symmetric)
-template <int D, typename Real>
-__global__ void __launch_bounds__(kThreads) linear_gs_colour_kernel(int level, int colour, const Real *__restrict__ Mc, int64_t n,
-                                                                     const Real *__restrict__ b, Real *x)
+template <int D, typename Real, int MinBlocks = 1, bool Streaming = false>
+__global__ void __launch_bounds__(kThreads, MinBlocks) linear_gs_colour_kernel(int level, int colour, const Real *__restrict__ Mc,
+                                                                                int64_t n, const Real *__restrict__ b, Real *x)
 {
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= n) return;
@@ -188,8 +198,8 @@ __global__ void __launch_bounds__(kThreads) linear_gs_colour_kernel(int level, i
     node_strides<D>(r, st);
     int I[D];
     const uint32_t i = colour_node<D>(col, st, (uint32_t)j, I);
-    const Real s = stencil_dot<D, Real>(Mc, n, j, x, i, I, st, r);
-    x[i] += (__ldg(b + i) - s) / __ldg(Mc + (int64_t)Dims<D>::CENTER * n + j);
+    const Real s = stencil_dot<D, Real, Streaming>(Mc, n, j, x, i, I, st, r);
+    x[i] += (__ldg(b + i) - s) / coef_load<Streaming>(Mc + (int64_t)Dims<D>::CENTER * n + j);
 }
 
 // r = b - M x over every node, colour-blocked coefficients; grid.y = colour
@@ -763,6 +773,36 @@ static bool mg_build(Context &c, int top, int lo)
     return c.launch_ok("mg hierarchy");
 }
 
+// variant of the linear GS colour kernel (EPR_LGS_VARIANT): 0 default (float: at most 51 registers,
+// read-only loads; double: 32 registers, streaming coefficient loads), 1 32 registers + streaming,
+// 2 no register cap, 3 32 registers + read-only loads
+static int g_lgs_variant = -1;
+static int lgs_variant()
+{
+    if (g_lgs_variant < 0)
+    {
+        const char *v = getenv("EPR_LGS_VARIANT");
+        g_lgs_variant = v ? atoi(v) : 0;
+    }
+    return g_lgs_variant;
+}
+
+template <int D, typename Real>
+static void launch_lgs_colour(int l, int col, const Real *Mc, int64_t n, const Real *b, Real *x, cudaStream_t s)
+{
+    const int v = lgs_variant();
+    if (v == 1)
+        linear_gs_colour_kernel<D, Real, 8, true><<<blocks(n), kThreads, 0, s>>>(l, col, Mc, n, b, x);
+    else if (v == 2)
+        linear_gs_colour_kernel<D, Real, 1, false><<<blocks(n), kThreads, 0, s>>>(l, col, Mc, n, b, x);
+    else if (v == 3)
+        linear_gs_colour_kernel<D, Real, 8, false><<<blocks(n), kThreads, 0, s>>>(l, col, Mc, n, b, x);
+    else if constexpr (sizeof(Real) == 4)
+        linear_gs_colour_kernel<D, Real, 5, false><<<blocks(n), kThreads, 0, s>>>(l, col, Mc, n, b, x);
+    else
+        linear_gs_colour_kernel<D, Real, 8, true><<<blocks(n), kThreads, 0, s>>>(l, col, Mc, n, b, x);
+}
+
 template <int D, typename Real>
 static void mg_sweeps(Context &c, int l, const Real *b, Real *x, int iters)
 {
@@ -771,8 +811,7 @@ static void mg_sweeps(Context &c, int l, const Real *b, Real *x, int iters)
     for (int it = 0; it < iters; it++)
         for (int col = 0; col < (1 << D); col++)
         {
-            linear_gs_colour_kernel<D, Real><<<blocks(cb.count[col]), kThreads, 0, c.stream>>>(
-                l, col, (const Real *)m.Mcb + cb.base[col], cb.count[col], b, x);
+            launch_lgs_colour<D, Real>(l, col, (const Real *)m.Mcb + cb.base[col], cb.count[col], b, x, c.stream);
             c.launches++;
         }
 }
@@ -1044,11 +1083,10 @@ bool time_mg_kernel(Context &c, const char *kernel, int level, int reps, double 
             if (k == "lgs")
             {
                 if (m.f32)
-                    linear_gs_colour_kernel<D, float><<<blocks(cb.count[0]), kThreads, 0, c.stream>>>(
-                        level, 0, (const float *)m.Mcb, cb.count[0], (const float *)m.b, (float *)m.x);
+                    launch_lgs_colour<D, float>(level, 0, (const float *)m.Mcb, cb.count[0], (const float *)m.b, (float *)m.x, c.stream);
                 else
-                    linear_gs_colour_kernel<D, double><<<blocks(cb.count[0]), kThreads, 0, c.stream>>>(
-                        level, 0, (const double *)m.Mcb, cb.count[0], (const double *)m.b, (double *)m.x);
+                    launch_lgs_colour<D, double>(level, 0, (const double *)m.Mcb, cb.count[0], (const double *)m.b, (double *)m.x,
+                                                 c.stream);
             }
             else if (k == "residual")
             {
