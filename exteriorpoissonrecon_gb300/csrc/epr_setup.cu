@@ -532,11 +532,13 @@ struct DensityGrids
     int depth;
 };
 
-template <int D>
+// Interpolated splat data at p from tree depth t; only the first NW of the W components (the
+// sample count alone for the depth search), each summed exactly as in the full interpolation.
+template <int D, int NW = 1 + D + D * D>
 __device__ void density_interp(const DensityGrids<D> &G, int t, const double *p, double *out)
 {
     constexpr int W = 1 + D + D * D;
-    for (int w = 0; w < W; w++) out[w] = 0;
+    for (int w = 0; w < NW; w++) out[w] = 0;
     if (t < 1) return;  // the root carries no data
     int res = 1 << (t - 1), nv = res + 1;
     int e[D];
@@ -565,17 +567,16 @@ __device__ void density_interp(const DensityGrids<D> &G, int t, const double *p,
             vi = vi * nv + o;
         }
         if (!in) continue;
-        for (int w = 0; w < W; w++) out[w] += g[vi * W + w] * s;
+        for (int w = 0; w < NW; w++) out[w] += g[vi * W + w] * s;
     }
 }
 
 template <int D>
 __device__ double samples_per_cell(const DensityGrids<D> &G, int t, const double *p)
 {
-    constexpr int W = 1 + D + D * D;
-    double info[W];
-    density_interp<D>(G, t, p, info);
-    return info[0] / (double)(1u << ((t - 1) * (D - 2)));
+    double count;
+    density_interp<D, 1>(G, t, p, &count);
+    return count / (double)(1u << ((t - 1) * (D - 2)));
 }
 
 template <int D>
@@ -583,14 +584,23 @@ __device__ double est_depth_raw(const DensityGrids<D> &G, int maxT, const double
 {
     const double tg = (double)(1 << (D - 2));
     int d1 = maxT, d2 = maxT + 1;
-    while (d2 > 1 && samples_per_cell<D>(G, d1, p) < tg) d1--, d2--;
+    // s1: samples per cell at depth d1 (computed by the search), s2 at d2 = d1 + 1 (the previous s1)
+    double s1 = samples_per_cell<D>(G, d1, p), s2 = 0;
+    bool have2 = false;
+    while (d2 > 1 && s1 < tg)
+    {
+        d1--, d2--;
+        s2 = s1;
+        have2 = true;
+        s1 = d1 >= 1 ? samples_per_cell<D>(G, d1, p) : 0;
+    }
     if (d2 == 1 || d2 == maxT + 1)
     {
         int d = (d2 == 1) ? 1 : maxT;
-        double spc = samples_per_cell<D>(G, d, p);
+        double spc = (d2 == 1) ? s2 : s1;
         return d + log(spc / tg) / log(2.);
     }
-    double s1 = samples_per_cell<D>(G, d1, p), s2 = samples_per_cell<D>(G, d2, p);
+    if (!have2) s2 = samples_per_cell<D>(G, d2, p);
     if (!s2) return d1;
     return d1 + log(tg / s1) / log(s2 / s1);
 }
@@ -684,10 +694,7 @@ __global__ void element_frame_kernel(SkewGrids<D> G, double *S, int *leaf)
     int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= NE) return;
     int E[D];
-    {
-        int64_t t = e;
-        for (int d = D - 1; d >= 0; d--) { E[d] = (int)(t % r); t /= r; }
-    }
+    Grid<D>(G.depth).elem(e, E);
     double p[D];
     for (int d = 0; d < D; d++) p[d] = (E[d] + 0.5) / r;
     int L = 1;

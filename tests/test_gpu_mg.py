@@ -186,3 +186,19 @@ def test_float_levels_track_double(link6):
         sol[prec] = r.solution()[0][depth]
     assert abs(e["fp32"] - e["fp64"]) < 1e-5 * e["fp64"]
     assert np.linalg.norm(sol["fp32"] - sol["fp64"]) < 1e-3 * np.linalg.norm(sol["fp64"])
+
+
+def test_multigrid_solver_4d_matches_oracle():
+    g = load_golden("cliff4_d3")
+    depth = int(g["depth"])
+    r = epr.Reconstructor(4, depth, g["pos"], g["skew"], solver="multigrid", tolerance=0.0, max_cycles=2, gsIters=2)
+    st = r.solve()
+    assert st["cycles"] == 2 * (depth + 1)
+    xs, ys = r.solution()
+    o = O.Oracle(4, depth, alt_rounds=2, gs_iters=2)
+    o.set_samples(g["pos"], g["skew"])
+    o.build()
+    xo, yo, eo = o.solve()
+    for l in range(depth + 1):
+        assert rel(xs[l], xo[l]) < 1e-8, l
+        assert rel(ys[l], yo[l]) < 1e-8, l
