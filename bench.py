@@ -70,6 +70,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true")
     ap.add_argument("--cpu-depth", type=int, default=6)
+    ap.add_argument("--workload", default="single", choices=["single", "batch"],
+                    help="single: the one large reconstruction above; batch: many small reconstructions "
+                         "solved concurrently (torus knots + helices, depths 5-7)")
+    ap.add_argument("--batch", type=int, default=64, help="reconstructions per batch")
+    ap.add_argument("--batch-threads", type=int, default=0, help="host workers of the batch (0: 32)")
     return ap.parse_args()
 
 
@@ -193,10 +198,218 @@ def cpu_reference(pu, sk, depth, cpu_depth, steps, warmup, dim=3):
                        f"({schedule_node_updates(dim, depth)} node updates); build took {build_s:.1f} s")}
 
 
+def kernel_rooflines(r, dim, depth, precision, clk):
+    """Roofline objects of the two relaxation kernels on the finest level of reconstruction r: one
+    parity colour of the paired Gauss-Seidel sweep (the solve's dominant kernel) and one colour of
+    the stored-stencil linear Gauss-Seidel sweep."""
+    hbm_peak, peak_kind = measured_peaks()
+    gs_ms = r.time_kernel("gs", depth, reps=20)
+    N = (2 ** depth + 1) ** dim
+    S = 3 ** dim
+    rs = 4 if precision == "fp32" else 8
+    colour_nodes = (2 ** (depth - 1) + 1) ** dim
+    gs_bytes = 2 * rs * N + colour_nodes * (2 * S * rs + 2 * rs)
+    achieved = gs_bytes / (gs_ms * 1e-3) / 1e9
+    fp32 = precision == "fp32" and dim == 3  # the captures are of the 3D float kernels
+    # the quartic relaxation is bound by FP32/FP64 issue, not by HBM: its algorithmic FLOPs per node
+    # update (this formulation: per incident element and wedge component 4 derivative tables of
+    # ~34 flops and 2 x 2 x 3^(D-2) Gauss points of ~21 flops; plus the 3^D-point stencil column)
+    # against the nominal FP32 rate of 152 SMs x 128 lanes x 2 flops at the sampled SM clock
+    K = dim * (dim - 1) // 2
+    node_flops = (2 ** dim) * K * (4 * 34 + 4 * 3 ** (dim - 2) * 21) + 8 * S + 30
+    gs_flops = node_flops * colour_nodes
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    gs_traffic = GS_DRAM_BYTES_PER_COLOUR_NODE_FP32 * colour_nodes if fp32 else None
+    roofline = {"bound": "hbm", "kernel": "gs_colour_lanes_kernel", "achieved": achieved, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_kind, "traffic": gs_traffic,
+                "launch_ms": gs_ms, "algorithmic_bytes_per_launch": gs_bytes,
+                "note": ("FMA-bound quartic relaxation; bytes = coefficient read + stencil columns + update writes; "
+                         "the finest level's colour launches take share_of_step of the step, the rest is the "
+                         "coarser levels (the double band latency-bound on the FP64 pipe)"),
+                "compute": {"algorithmic_flops_per_launch": gs_flops, "achieved_tflops": gs_flops / (gs_ms * 1e-3) / 1e12,
+                            "peak_tflops": fp32_peak if precision == "fp32" else None,
+                            "peak_source": "nominal FP32 at the sampled SM clock",
+                            "frac": (gs_flops / (gs_ms * 1e-3) / 1e12 / fp32_peak) if precision == "fp32" else None}}
+
+    # stored-stencil relaxation (the smoother of the linear multigrid, MG.h GSRelaxer): one colour of
+    # the linear Gauss-Seidel sweep on the alternating y-system of the finest level, colour-blocked
+    # 27-point stencil; bytes = the colour's coefficients, right-hand side and update plus one read
+    # of the whole x vector (every node neighbours the colour)
+    lgs_ms = r.time_kernel("lgs", depth, reps=20)
+    lgs_bytes = colour_nodes * (S + 2) * rs + N * rs
+    lgs_achieved = lgs_bytes / (lgs_ms * 1e-3) / 1e9
+    stencil_roofline = {"bound": "hbm", "kernel": "linear_gs_colour_kernel", "achieved": lgs_achieved, "peak": hbm_peak,
+                        "unit": "GB/s", "frac": lgs_achieved / hbm_peak, "peak_source": peak_kind,
+                        "traffic": LGS_DRAM_BYTES_PER_COLOUR_NODE_FP32 * colour_nodes if fp32 else None,
+                        "launch_ms": lgs_ms, "algorithmic_bytes_per_launch": lgs_bytes}
+    return roofline, stencil_roofline
+
+
+BATCH_METRIC = "Batched reconstructions per second (3D torus knots + helices, depths 5-7, FP32 smoothing, FP64 levels 0-3)"
+
+
+def batch_inputs(count, seed=0):
+    from exteriorpoissonrecon_gb300 import samples, unit_cube, pack_skew
+    out = []
+    for w in samples.batch_workloads(count, seed=seed):
+        pu, _ = unit_cube(w["pos"])
+        out.append((w["depth"], pu, pack_skew(w["frames"])))
+    return out
+
+
+def cpu_batch_reference(inputs):
+    """CPU restatement (oracle) of the reference's build + cascadic solve, all host threads, on a
+    bounded sample of the batch: the smallest member of each depth up to 6 is reconstructed in full,
+    and the per-node-update time of those runs (build included) is scaled to the whole batch's
+    schedules."""
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    picked = {}
+    for k, (d, pu, sk) in enumerate(inputs):
+        if d <= 6 and (d not in picked or len(pu) < len(inputs[picked[d]][1])):
+            picked[d] = k
+    t_sum = u_sum = 0.0
+    for d, k in sorted(picked.items()):
+        _, pu, sk = inputs[k]
+        t0 = time.perf_counter()
+        o = O.Oracle(3, d, threads=cores)
+        o.set_samples(pu, sk)
+        o.build()
+        o.solve()
+        t_sum += time.perf_counter() - t0
+        u_sum += schedule_node_updates(3, d)
+        del o
+    total_updates = sum(schedule_node_updates(3, d) for d, _, _ in inputs)
+    total_s = t_sum / u_sum * total_updates
+    return {"value": len(inputs) / total_s, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": (f"oracle build + cascadic solve of {len(picked)} members (depths "
+                       f"{sorted(picked)}, {int(u_sum)} node updates, {t_sum:.1f} s, FP64); the time per node "
+                       f"update scaled to the batch's {total_updates} node updates ({total_s:.1f} s for "
+                       f"{len(inputs)} reconstructions)")}
+
+
+def bench_batch(args, ws, rank, local, pg):
+    """Many small reconstructions at once (epr_batch_solve): one step = solving every reconstruction
+    of the batch once from its built system; value = reconstructions per second over all replicas.
+    Levels 0-3 relax in double (the coarse solve; in float, rounding on the two coarsest levels moves
+    a few reconstructions of the mix by up to 1.6e-5 in energy), the others in float.  32 host
+    workers keep 32 reconstructions in flight, on 32 hardware work queues."""
+    # read by the CUDA runtime when it starts: one hardware work queue per worker stream
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+    if args.fp64_from is None:
+        args.fp64_from = 0
+    if args.fp64_levels is None:
+        args.fp64_levels = 4
+    if args.batch_threads <= 0:
+        args.batch_threads = 32
+    inputs = batch_inputs(args.batch)
+    depths = [d for d, _, _ in inputs]
+    config = {"workload": f"batch-{len(inputs)}-knots+helices-3D-depths5-7", "reconstructions": len(inputs),
+              "samples_total": int(sum(len(pu) for _, pu, _ in inputs)),
+              "depth_counts": {str(d): depths.count(d) for d in sorted(set(depths))},
+              "precision": args.precision,
+              "fp64_levels": [args.fp64_from, args.fp64_levels] if args.precision == "fp32" else None,
+              "threads": args.batch_threads,
+              "l2": "working set (tens of GB of stencils) far larger than L2 (no flush)",
+              "parallelism": f"replicas{ws}"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_batch_reference(inputs)
+        line = {"metric": BATCH_METRIC, "value": cb["value"], "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": len(inputs) / cb["value"] * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "impl": "reference", "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    import exteriorpoissonrecon_gb300 as epr
+    mixed = dict(fp64_levels=args.fp64_levels, fp64_from=args.fp64_from) if args.precision == "fp32" else {}
+    make = lambda prec, kw: [epr.Reconstructor(3, d, pu, sk, build=False, precision=prec, device=local, **kw)
+                             for d, pu, sk in inputs]
+    recons = make(args.precision, mixed)
+    # the first batch builds and launches directly; the second captures each context's CUDA graph
+    for i in range(max(args.warmup, 2)):
+        epr.batch_solve(recons, build=(i == 0), threads=args.batch_threads)
+    build_ms = sum(r.stats.build_ms for r in recons)
+    barrier(pg)
+    clocks = ClockSampler(local)
+    clocks.start()
+    times, launches = [], 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        st = epr.batch_solve(recons, build=False, threads=args.batch_threads)
+        times.append(time.perf_counter() - t0)
+        launches += sum(x["kernel_launches"] for x in st)
+    clk = clocks.stop()
+    barrier(pg)
+    per_step_s = allmax(pg, statistics.mean(times))
+    value = ws * len(inputs) / per_step_s
+    big = max(range(len(inputs)), key=lambda k: (inputs[k][0], len(inputs[k][1])))
+    roofline, stencil_roofline = kernel_rooflines(recons[big], 3, inputs[big][0], args.precision, clk)
+    energies = [x["fit_energy"] + x["reg_energy"] for x in st]
+
+    # end to end: contexts created, samples host->device, build + solve, every level's solution back
+    e2e_s = []
+    h2d = sum(pu.nbytes + sk.nbytes for _, pu, sk in inputs)
+    d2h = sum(2 * 8 * (2 ** l + 1) ** 3 for d in depths for l in range(d + 1))
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        rs = [epr.Reconstructor(3, d, pu, sk, build=False, precision=args.precision, device=local, **mixed)
+              for d, pu, sk in inputs]
+        epr.batch_solve(rs, build=True, threads=args.batch_threads)
+        for r in rs:
+            r.solution()
+        e2e_s.append(time.perf_counter() - t0)
+        for r in rs:
+            r.close()
+    e2e_v = ws * len(inputs) / allmax(pg, statistics.mean(e2e_s)) if e2e_s else None
+
+    line = {"metric": BATCH_METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 2), "ms_per_step": per_step_s * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
+            "data": "synthetic", "config": config, "clocks": clk, "gpu_launches": int(launches),
+            "roofline": roofline, "stencil_roofline": stencil_roofline,
+            "e2e": {"value": e2e_v, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "build_ms_sum": build_ms,
+            "unknown_sweeps_per_s": ws * 2 * sum(schedule_node_updates(3, d) for d in depths) / per_step_s}
+    # one at a time: the same batch solved by one host worker
+    t0 = time.perf_counter()
+    epr.batch_solve(recons, build=False, threads=1)
+    line["sequential_solves_per_s"] = len(inputs) / (time.perf_counter() - t0)
+    # error of every result against the double-precision run of the same schedule
+    if args.precision == "fp32" and not args.no_fp64_check:
+        for r in recons:
+            r.close()
+        r64 = make("fp64", {})
+        epr.batch_solve(r64, build=True, threads=args.batch_threads)
+        t0 = time.perf_counter()
+        st64 = epr.batch_solve(r64, build=False, threads=args.batch_threads)
+        t64 = time.perf_counter() - t0
+        e64 = [x["fit_energy"] + x["reg_energy"] for x in st64]
+        rel = [abs(a - b) / b for a, b in zip(energies, e64)]
+        line["error_vs_fp64"] = {"max_energy_rel_diff": max(rel), "median_energy_rel_diff": statistics.median(rel),
+                                 "within_1e-6": sum(x <= 1e-6 for x in rel),
+                                 "above_1e-6": [[k, depths[k], len(inputs[k][1]), rel[k]] for k in range(len(rel))
+                                                if rel[k] > 1e-6],
+                                 "fp64_solves_per_s": len(inputs) / t64, "speedup_vs_fp64": value / ws / (len(inputs) / t64)}
+        for r in r64:
+            r.close()
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_batch_reference(inputs)
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     args = parse()
     ws, rank, local, pg = dist_setup(args)
     depth = args.depth if args.depth is not None else (8 if args.dim == 3 else 6)
+    if args.workload == "batch":
+        if args.dim != 3:
+            raise SystemExit("the batched workload is 3D")
+        return bench_batch(args, ws, rank, local, pg)
     if args.fp64_levels is None:
         args.fp64_levels = 4 if args.dim == 3 else 0
     if args.fp64_from is None:
@@ -246,49 +459,8 @@ def main():
     total_ms = allmax(pg, sum(dev_ms))
     per_step_s = total_ms / 1e3 / args.steps
 
-    # kernel roofline: one parity colour of the paired Gauss-Seidel sweep at the finest level
-    hbm_peak, peak_kind = measured_peaks()
-    gs_ms = r.time_kernel("gs", depth, reps=20)
-    N = (2 ** depth + 1) ** dim
-    S = 3 ** dim
-    rs = 4 if args.precision == "fp32" else 8
-    colour_nodes = (2 ** (depth - 1) + 1) ** dim
-    gs_bytes = 2 * rs * N + colour_nodes * (2 * S * rs + 2 * rs)
-    achieved = gs_bytes / (gs_ms * 1e-3) / 1e9
-    fp32 = args.precision == "fp32" and dim == 3  # the captures are of the 3D float kernels
-    # the quartic relaxation is bound by FP32/FP64 issue, not by HBM: its algorithmic FLOPs per node
-    # update (this formulation: per incident element and wedge component 4 derivative tables of
-    # ~34 flops and 2 x 2 x 3^(D-2) Gauss points of ~21 flops; plus the 3^D-point stencil column)
-    # against the nominal FP32 rate of 152 SMs x 128 lanes x 2 flops at the sampled SM clock
-    K = dim * (dim - 1) // 2
-    node_flops = (2 ** dim) * K * (4 * 34 + 4 * 3 ** (dim - 2) * 21) + 8 * S + 30
-    gs_flops = node_flops * colour_nodes
-    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    gs_traffic = GS_DRAM_BYTES_PER_COLOUR_NODE_FP32 * colour_nodes if fp32 else None
-    roofline = {"bound": "hbm", "kernel": "gs_colour_lanes_kernel", "achieved": achieved, "peak": hbm_peak,
-                "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_kind, "traffic": gs_traffic,
-                "launch_ms": gs_ms, "algorithmic_bytes_per_launch": gs_bytes,
-                "note": ("FMA-bound quartic relaxation; bytes = coefficient read + stencil columns + update writes; "
-                         "the finest level's colour launches take share_of_step of the step, the rest is the "
-                         "coarser levels (the double band latency-bound on the FP64 pipe)"),
-                "share_of_step": 10 * (2 ** dim) * gs_ms / (per_step_s * 1e3),
-                "compute": {"algorithmic_flops_per_launch": gs_flops, "achieved_tflops": gs_flops / (gs_ms * 1e-3) / 1e12,
-                            "peak_tflops": fp32_peak if args.precision == "fp32" else None,
-                            "peak_source": "nominal FP32 at the sampled SM clock",
-                            "frac": (gs_flops / (gs_ms * 1e-3) / 1e12 / fp32_peak) if args.precision == "fp32" else None}}
-
-    # stored-stencil relaxation (the smoother of the linear multigrid, MG.h GSRelaxer): one colour of
-    # the linear Gauss-Seidel sweep on the alternating y-system of the finest level, colour-blocked
-    # 27-point stencil; bytes = the colour's coefficients, right-hand side and update plus one read
-    # of the whole x vector (every node neighbours the colour)
-    lgs_ms = r.time_kernel("lgs", depth, reps=20)
-    lgs_bytes = colour_nodes * (S + 2) * rs + N * rs
-    lgs_achieved = lgs_bytes / (lgs_ms * 1e-3) / 1e9
-    stencil_roofline = {"bound": "hbm", "kernel": "linear_gs_colour_kernel", "achieved": lgs_achieved, "peak": hbm_peak,
-                        "unit": "GB/s", "frac": lgs_achieved / hbm_peak, "peak_source": peak_kind,
-                        "traffic": LGS_DRAM_BYTES_PER_COLOUR_NODE_FP32 * colour_nodes if fp32 else None,
-                        "launch_ms": lgs_ms, "algorithmic_bytes_per_launch": lgs_bytes}
+    roofline, stencil_roofline = kernel_rooflines(r, dim, depth, args.precision, clk)
+    roofline["share_of_step"] = 10 * (2 ** dim) * roofline["launch_ms"] / (per_step_s * 1e3)
 
     # end to end through the public API from host buffers
     e2e_s = []

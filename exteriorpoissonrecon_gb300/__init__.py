@@ -124,6 +124,8 @@ def load():
     L.epr_prolong.argtypes = [vp, ctypes.c_int]
     L.epr_gn_matvec.argtypes = [vp, ctypes.c_int, P, P, P, P]
     L.epr_solve.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.epr_batch_solve.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.POINTER(Stats), ctypes.POINTER(ctypes.c_int)]
     L.epr_get_solution.argtypes = [vp, ctypes.c_int, P, P]
     L.epr_get_array.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, P, ctypes.c_size_t,
                                 ctypes.POINTER(ctypes.c_size_t)]
@@ -372,3 +374,23 @@ class Reconstructor:
             xs.append(x)
             ys.append(y)
         return xs, ys
+
+
+def batch_solve(recons, build: bool = True, threads: int = 0):
+    """Builds (when `build`) and solves several Reconstructors at once on one GPU
+    (epr_batch_solve): host workers drive whole reconstructions on their own streams, so the
+    kernels of small reconstructions overlap.  Each result is the one its Reconstructor gives
+    alone.  Returns the per-reconstruction stats dicts; raises EprError naming the first failure."""
+    recons = list(recons)
+    n = len(recons)
+    L = load()
+    handles = (ctypes.c_void_p * max(n, 1))(*[r._h for r in recons])
+    stats = (Stats * max(n, 1))()
+    status = (ctypes.c_int * max(n, 1))()
+    rc = L.epr_batch_solve(handles, n, int(bool(build)), int(threads), stats, status)
+    for i, r in enumerate(recons):
+        if status[i] == EPR_OK:
+            ctypes.memmove(ctypes.byref(r.stats), ctypes.byref(stats[i]), ctypes.sizeof(Stats))
+    if rc != EPR_OK:
+        raise EprError(f"[{rc}] " + L.epr_global_error().decode())
+    return [stats[i].as_dict() for i in range(n)]

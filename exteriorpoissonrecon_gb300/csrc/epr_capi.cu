@@ -1,13 +1,18 @@
 // The C ABI of libepr_cuda (declared in include/epr.h): context management, host <-> device
 // transfers and the solver drivers.  All arithmetic runs in the kernels of epr_solve.cu and
 // epr_setup.cu; this file only sequences them on the context's stream.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "../../include/epr.h"
@@ -21,6 +26,13 @@
 namespace {
 
 thread_local std::string g_error;
+
+// host workers of epr_batch_solve when the caller does not choose: each drives one stream, and
+// eight streams fill the device's default number of hardware work queues
+// (CUDA_DEVICE_MAX_CONNECTIONS, 8 unless the process raises it before CUDA starts)
+constexpr int kBatchThreads = 8;
+
+std::mutex g_create_mutex;
 
 }  // namespace
 
@@ -260,16 +272,38 @@ bool Context::prolong_add(int l)
     return launch_ok("prolong");
 }
 
-// Random<double> (Misha/Geometry.inl:430-438) on the C library generator
-static double RandomDouble()
+// Random<double> (Misha/Geometry.inl:430-438) on the C library generator seeded by srand(seed).
+// glibc's rand() is random() on a 128-byte additive-feedback state; random_r runs the same
+// generator on a state of the context's own, so the sequence is the one srand(seed) + rand() give,
+// and reconstructions solved concurrently on several host threads neither share nor disturb the
+// process's rand() state.
+class CRandom
 {
-    const unsigned long long ULL_RAND_MAX = (unsigned long long)(RAND_MAX) + 1;
-    const double RAND_MAX_SQUARED = double(ULL_RAND_MAX * ULL_RAND_MAX - 1);
-    unsigned long long r1 = rand();
-    unsigned long long r2 = rand();
-    long long v = (long long)(r1 * ULL_RAND_MAX + r2);
-    return double(v) / RAND_MAX_SQUARED;
-}
+  public:
+    explicit CRandom(unsigned int seed)
+    {
+        std::memset(&data_, 0, sizeof(data_));
+        initstate_r(seed, state_, sizeof(state_), &data_);
+    }
+    double next_double()
+    {
+        const unsigned long long ULL_RAND_MAX = (unsigned long long)(RAND_MAX) + 1;
+        const double RAND_MAX_SQUARED = double(ULL_RAND_MAX * ULL_RAND_MAX - 1);
+        unsigned long long r1 = next(), r2 = next();
+        long long v = (long long)(r1 * ULL_RAND_MAX + r2);
+        return double(v) / RAND_MAX_SQUARED;
+    }
+
+  private:
+    unsigned long long next()
+    {
+        int32_t r = 0;
+        random_r(&data_, &r);
+        return (unsigned long long)r;
+    }
+    alignas(8) char state_[128];
+    random_data data_;
+};
 
 // host planar arrays <-> device pairs: the two arrays travel as they are and the (de)interleaving
 // runs on the device
@@ -360,10 +394,10 @@ bool Context::solve_cascadic()
     }
     // random initial guess at the coarsest solve level, scaled to the target's magnitude
     {
-        srand(P.seed);
+        CRandom rng((unsigned int)P.seed);
         int64_t N = levels[minD].N;
         std::vector<double> x(N), y(N);
-        for (int64_t i = 0; i < N; i++) { x[i] = RandomDouble(); y[i] = RandomDouble(); }
+        for (int64_t i = 0; i < N; i++) { x[i] = rng.next_double(); y[i] = rng.next_double(); }
         if (!upload_xy(minD, x.data(), y.data())) return false;
         double e[3];
         if (!energy(minD, e)) return false;
@@ -516,12 +550,15 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
         g_error = std::string("cannot select CUDA device: ") + cudaGetErrorString(cudaGetLastError());
         return nullptr;
     }
-    if (const char *v = getenv("EPR_GS_VARIANT")) epr::set_gs_variant(atoi(v));
-    static uint64_t prepared = 0;  // devices whose kernel attributes are set
-    if (p.device >= 0 && p.device < 64 && !(prepared & (1ull << p.device)))
     {
-        epr::prepare_gs_kernels();
-        prepared |= 1ull << p.device;
+        std::lock_guard<std::mutex> lock(g_create_mutex);
+        if (const char *v = getenv("EPR_GS_VARIANT")) epr::set_gs_variant(atoi(v));
+        static uint64_t prepared = 0;  // devices whose kernel attributes are set
+        if (p.device >= 0 && p.device < 64 && !(prepared & (1ull << p.device)))
+        {
+            epr::prepare_gs_kernels();
+            prepared |= 1ull << p.device;
+        }
     }
     epr_ctx *c = new epr_ctx;
     c->dim = dim;
@@ -721,6 +758,91 @@ int epr_solve(epr_ctx *ctx, epr_stats *stats)
     bool ok = ctx->solve_cascadic();
     if (ok && stats) *stats = ctx->stats;
     EPR_RETURN(ctx, ok);
+}
+
+// Many independent reconstructions on one GPU.  A reconstruction at depth 5-7 keeps only a part of
+// the 152 SMs busy (a colour of a 33^3 grid is 4.5K nodes) and spends much of its time in launch
+// latency, so several run at once: host workers each take whole reconstructions, largest first,
+// and drive them on the contexts' own non-blocking streams, where the device overlaps their
+// kernels.  Every context computes exactly what it computes alone (same kernels, same launch
+// configurations, its own stream and memory), so the results do not depend on the schedule.
+int epr_batch_solve(epr_ctx *const *ctxs, int n, int build, int threads, epr_stats *stats, int *status)
+{
+    if (n < 0 || (n > 0 && !ctxs)) { g_error = "bad batch"; return EPR_ERR_ARG; }
+    for (int i = 0; i < n; i++)
+    {
+        if (!ctxs[i]) { g_error = "null context in batch"; return EPR_ERR_ARG; }
+        for (int j = 0; j < i; j++)
+            if (ctxs[j] == ctxs[i]) { g_error = "a context appears twice in the batch"; return EPR_ERR_ARG; }
+    }
+    for (int i = 1; i < n; i++)
+        if (ctxs[i]->P.device != ctxs[0]->P.device) { g_error = "the batch's contexts are on different devices"; return EPR_ERR_ARG; }
+    if (n == 0) return EPR_OK;
+    // largest reconstruction first (finest-level nodes, then samples): the long ones start early
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    auto cost = [&](int i) {
+        const epr::Context *c = ctxs[i];
+        return std::make_pair(c->levels[c->depth].N, (int64_t)c->setup.n);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
+    std::vector<int> rc(n, EPR_OK);
+    std::atomic<int> next{0};
+    if (threads <= 0) threads = kBatchThreads;
+    threads = std::min(threads, n);
+    // One stream per worker, created together: the device spreads streams over its hardware work
+    // queues in creation order, so the workers' streams do not share a queue (the contexts' own
+    // streams, created one per context, would put concurrently running contexts on the same queue
+    // and serialise them).  A context runs on its worker's stream while the worker holds it; every
+    // build and solve ends with a stream synchronisation, so nothing is in flight when the
+    // context's own stream comes back.
+    std::vector<cudaStream_t> streams(threads, nullptr);
+    cudaSetDevice(ctxs[0]->P.device);
+    for (int t = 0; t < threads; t++)
+        if (cudaStreamCreateWithFlags(&streams[t], cudaStreamNonBlocking) != cudaSuccess)
+        {
+            streams[t] = nullptr;  // the worker then uses the contexts' own streams
+            cudaGetLastError();
+        }
+    auto worker = [&](int t) {
+        for (int k; (k = next.fetch_add(1)) < n;)
+        {
+            const int i = order[k];
+            epr_ctx *c = ctxs[i];
+            cudaStream_t own = c->stream;
+            const bool swap = streams[t] != nullptr;
+            if (swap)
+            {
+                cudaStreamSynchronize(own);  // work the context queued before the batch
+                c->stream = streams[t];
+            }
+            int r = build ? epr_build(c) : EPR_OK;
+            if (r == EPR_OK) r = epr_solve(c, stats ? &stats[i] : nullptr);
+            if (swap)
+            {
+                cudaStreamSynchronize(c->stream);
+                c->stream = own;
+            }
+            rc[i] = r;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < threads; t++) pool.emplace_back(worker, t);
+    worker(0);
+    for (std::thread &t : pool) t.join();
+    for (cudaStream_t st : streams)
+        if (st) cudaStreamDestroy(st);
+    int first = EPR_OK;
+    for (int i = 0; i < n; i++)
+    {
+        if (status) status[i] = rc[i];
+        if (first == EPR_OK && rc[i] != EPR_OK)
+        {
+            first = rc[i];
+            g_error = "context " + std::to_string(i) + ": " + ctxs[i]->err;
+        }
+    }
+    return first;
 }
 
 int epr_get_solution(epr_ctx *ctx, int level, double *x, double *y)

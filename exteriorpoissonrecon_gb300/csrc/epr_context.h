@@ -50,6 +50,7 @@ struct Setup
     bool set_samples(Context &c, size_t n, const double *pos, const double *skew);
     bool build(Context &c);
     bool get(Context &c, const std::string &name, double *out, size_t cap, size_t *count);
+    void release_built(Context &c);
     void release(Context &c);
 };
 

@@ -776,15 +776,13 @@ static bool mg_build(Context &c, int top, int lo)
 // variant of the linear GS colour kernel (EPR_LGS_VARIANT): 0 default (float: at most 51 registers,
 // read-only loads; double: 32 registers, streaming coefficient loads), 1 32 registers + streaming,
 // 2 no register cap, 3 32 registers + read-only loads
-static int g_lgs_variant = -1;
 static int lgs_variant()
 {
-    if (g_lgs_variant < 0)
-    {
-        const char *v = getenv("EPR_LGS_VARIANT");
-        g_lgs_variant = v ? atoi(v) : 0;
-    }
-    return g_lgs_variant;
+    static const int v = [] {
+        const char *e = getenv("EPR_LGS_VARIANT");
+        return e ? atoi(e) : 0;
+    }();
+    return v;
 }
 
 template <int D, typename Real>

@@ -1108,6 +1108,7 @@ bool build_impl(Context &c, Setup &st)
     const int depth = c.depth;
     const int64_t n = (int64_t)st.n;
     cudaStream_t s = c.stream;
+    st.release_built(c);
     cudaEventRecord(c.ev0, s);
 
     // ---- ordered sampling: Morton keys of the finest cells, stable radix sort ----
@@ -1401,20 +1402,28 @@ void launch_galerkin(int fineLevel, const double *Mf, double *Mc, cudaStream_t s
 template void launch_galerkin<3>(int, const double *, double *, cudaStream_t);
 template void launch_galerkin<4>(int, const double *, double *, cudaStream_t);
 
-void Setup::release(Context &c)
+// the products of a build (everything but the samples), so that a context can be built again
+void Setup::release_built(Context &c)
 {
-    c.release(pos); c.release(skew); c.release(order); c.release(cellKey); c.release(cellStart); c.release(cellOfFinest);
+    c.release(order); c.release(cellKey); c.release(cellStart); c.release(cellOfFinest);
     c.release(measure); c.release(noise); c.release(sdepth); c.release(S); c.release(leaf);
     for (double *p : density) c.release(p);
     for (double *p : skewGrid) c.release(p);
     for (uint8_t *p : refinedD) c.release(p);
     for (uint8_t *p : refinedS) c.release(p);
     density.clear(); skewGrid.clear(); refinedD.clear(); refinedS.clear();
-    pos = skew = measure = noise = sdepth = S = nullptr;
+    measure = noise = sdepth = S = nullptr;
     order = cellStart = cellOfFinest = leaf = nullptr;
     cellKey = nullptr;
-    n = 0;
     ncells = 0;
+}
+
+void Setup::release(Context &c)
+{
+    release_built(c);
+    c.release(pos); c.release(skew);
+    pos = skew = nullptr;
+    n = 0;
 }
 
 }  // namespace epr

@@ -172,6 +172,36 @@ def make_workload(name: str, n: int | None = None, seed: int = 0):
     raise ValueError(f"unknown workload {name!r}")
 
 
+def batch_workloads(count: int = 64, seed: int = 0, n_range=(2048, 262144), depths=(5, 6, 7)):
+    """The batched-reconstruction mix: the first half torus knots with seed-drawn coprime (p, q) in
+    [2, 7] (t uniform), the second half helices of radius 0.3 along z over height 1 with a rotation
+    count uniform in [1, 8]; sample counts log-uniform in `n_range`, depths uniform in `depths`,
+    positional sigma uniform in [0, 0.01] (unit-cube units) and angular noise uniform in [0, 10]
+    degrees.  Returns a list of dicts with name, depth, pos (world) and frames."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1])))))
+        depth = int(rng.choice(depths))
+        sigma = float(rng.uniform(0.0, 0.01))
+        ang = float(rng.uniform(0.0, 10.0))
+        if k < count // 2:
+            while True:
+                p, q = (int(v) for v in rng.integers(2, 8, 2))
+                if math.gcd(p, q) == 1:
+                    break
+            pos, fr = torus_knot(n, p, q, regular=False, rng=rng)
+            name = f"knot_{p}_{q}"
+        else:
+            turns = float(rng.uniform(1.0, 8.0))
+            pos, fr = helix(n, turns, rng)
+            name = f"helix_{turns:.2f}"
+        pos, fr = add_noise(pos, fr, rng, sigma, ang, 0.0)
+        out.append({"name": name, "depth": depth, "pos": pos, "frames": fr, "n": n,
+                    "sigma": sigma, "angle_deg": ang})
+    return out
+
+
 # ---------------------------------------------------------------------------------------------
 # PLY
 # ---------------------------------------------------------------------------------------------

@@ -41,6 +41,9 @@
  *       SystemEnergy::biQuadraticFit                        Include/SystemEnergy.h:78,499-540
  *   epr_step_size / epr_newton_update
  *       SystemEnergy::stepSize / newtonUpdate               Include/SystemEnergy.h:66-69,256-303
+ *   epr_batch_solve
+ *       no reference counterpart: the reference reconstructs one input per process; this runs
+ *       Reconstructor::Reconstructor + solve (ExteriorPoisson.h:59-81) for many inputs at once
  *   epr_get_array
  *       read-only views of the reference's internal state (TreeEstimator::measure/noise/depth
  *       GridSamples.inl:838-862, S(E) ExteriorPoisson.h:290-307, _R/_B SystemEnergy.h:172-175)
@@ -149,6 +152,16 @@ int epr_gn_matvec(epr_ctx *ctx, int level, const double *dx, const double *dy, d
 
 /* Runs the configured solver; stats may be NULL. */
 int epr_solve(epr_ctx *ctx, epr_stats *stats);
+/* Builds (build != 0) and solves n independent reconstructions concurrently on one GPU: `threads`
+ * host threads (<= 0: 8) each take whole reconstructions, largest first, and drive them on the
+ * contexts' own streams, so their kernels overlap on the device.  The contexts must be distinct and
+ * on the same device; they may differ in dim, depth, samples and parameters, and each computes
+ * exactly what epr_build + epr_solve compute for it alone.  stats[i] and status[i] (either may be
+ * NULL) receive context i's statistics and return code.  Returns EPR_OK, or the code of the first
+ * failing context in index order (epr_global_error() names it).  The contexts must not be used by
+ * other threads meanwhile. */
+int epr_batch_solve(epr_ctx *const *ctxs, int n, int build, int threads, epr_stats *stats, int *status);
+
 /* Hierarchical solution coefficients of one level after epr_solve (what the reference writes to
  * its .tree file: level 0 regular, level d > 0 the residual x[d] - P x[d-1]). */
 int epr_get_solution(epr_ctx *ctx, int level, double *x, double *y);

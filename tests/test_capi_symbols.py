@@ -45,3 +45,17 @@ def test_line_searches_host_only():
     q = np.zeros((3, 3))
     q[2, 0], q[0, 2] = 1.0, 1.0
     assert epr.step_size(q) == 0.0
+
+
+def test_batch_argument_checks_host_only():
+    """epr_batch_solve validates its arguments before touching a context or the GPU."""
+    import ctypes
+    lib = epr.load()
+    st = (epr.Stats * 2)()
+    status = (ctypes.c_int * 2)()
+    assert lib.epr_batch_solve(None, 0, 1, 0, st, status) == epr.EPR_OK
+    assert lib.epr_batch_solve(None, 2, 1, 0, st, status) == -1
+    assert lib.epr_batch_solve(None, -1, 1, 0, st, status) == -1
+    handles = (ctypes.c_void_p * 2)(None, None)
+    assert lib.epr_batch_solve(handles, 2, 1, 0, st, status) == -1
+    assert b"null context" in lib.epr_global_error()
