@@ -65,6 +65,9 @@ def parse():
                          "stationary point, which keeps the double run's local minimum; none in 4D, where the "
                          "all-float solve already has the double energy to 1e-9)")
     ap.add_argument("--fp64-from", type=int, default=None)
+    ap.add_argument("--band-precision", default="df", choices=["df", "fp64"],
+                    help="arithmetic of the band's 3D levels up to 3: df = double-float on the FP32 pipe with a "
+                         "power-of-two exponent per level (default), fp64 = double")
     ap.add_argument("--solver", default="cascadic", choices=["cascadic", "multigrid"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -292,8 +295,8 @@ def cpu_batch_reference(inputs):
 def bench_batch(args, ws, rank, local, pg):
     """Many small reconstructions at once (epr_batch_solve): one step = solving every reconstruction
     of the batch once from its built system; value = reconstructions per second over all replicas.
-    Levels 0-3 relax in double (the coarse solve; in float, rounding on the two coarsest levels moves
-    a few reconstructions of the mix by up to 1.6e-5 in energy), the others in float.  32 host
+    Levels 0-3 relax in double-float (the coarse solve; in float, rounding on the two coarsest levels
+    moves a few reconstructions of the mix by up to 1.6e-5 in energy), the others in float.  32 host
     workers keep 32 reconstructions in flight, on 32 hardware work queues."""
     # read by the CUDA runtime when it starts: one hardware work queue per worker stream
     os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
@@ -310,6 +313,7 @@ def bench_batch(args, ws, rank, local, pg):
               "depth_counts": {str(d): depths.count(d) for d in sorted(set(depths))},
               "precision": args.precision,
               "fp64_levels": [args.fp64_from, args.fp64_levels] if args.precision == "fp32" else None,
+              "band_precision": args.band_precision if args.precision == "fp32" else None,
               "threads": args.batch_threads,
               "l2": "working set (tens of GB of stencils) far larger than L2 (no flush)",
               "parallelism": f"replicas{ws}"}
@@ -325,7 +329,8 @@ def bench_batch(args, ws, rank, local, pg):
         print(json.dumps(line))
         return
     import exteriorpoissonrecon_gb300 as epr
-    mixed = dict(fp64_levels=args.fp64_levels, fp64_from=args.fp64_from) if args.precision == "fp32" else {}
+    mixed = (dict(fp64_levels=args.fp64_levels, fp64_from=args.fp64_from, band_precision=args.band_precision)
+             if args.precision == "fp32" else {})
     make = lambda prec, kw: [epr.Reconstructor(3, d, pu, sk, build=False, precision=prec, device=local, **kw)
                              for d, pu, sk in inputs]
     recons = make(args.precision, mixed)
@@ -422,6 +427,7 @@ def main():
               "dim": dim, "nodes": (2 ** depth + 1) ** dim, "unknowns": 2 * (2 ** depth + 1) ** dim,
               "solver": args.solver, "precision": args.precision,
               "fp64_levels": [args.fp64_from, args.fp64_levels] if args.precision == "fp32" else None,
+              "band_precision": args.band_precision if args.precision == "fp32" else None,
               "l2": "inputs larger than L2 (no flush)",
               "parallelism": f"replicas{ws}"}
 
@@ -438,7 +444,8 @@ def main():
         return
 
     import exteriorpoissonrecon_gb300 as epr
-    mixed = dict(fp64_levels=args.fp64_levels, fp64_from=args.fp64_from) if args.precision == "fp32" else {}
+    mixed = (dict(fp64_levels=args.fp64_levels, fp64_from=args.fp64_from, band_precision=args.band_precision)
+             if args.precision == "fp32" else {})
     r = epr.Reconstructor(dim, depth, pu, sk, precision=args.precision, solver=args.solver, device=local, **mixed)
     for _ in range(args.warmup):
         r.solve()
@@ -515,6 +522,18 @@ def main():
             "speedup_vs_fp64_solve": st64["solve_ms"] / stm["solve_ms"]}
         line["error_vs_fp64"]["speedup_vs_fp64_solve"] = st64["solve_ms"] / (per_step_s * 1e3)
         rm.close()
+        if args.fp64_levels > args.fp64_from:
+            # the same band in the other arithmetic (double against double-float)
+            other = "fp64" if args.band_precision == "df" else "df"
+            rb = epr.Reconstructor(dim, depth, pu, sk, precision="fp32", fp64_levels=args.fp64_levels,
+                                   fp64_from=args.fp64_from, band_precision=other, solver=args.solver, device=local)
+            for _ in range(3):
+                stb = rb.solve()
+            eb = stb["fit_energy"] + stb["reg_energy"]
+            line[f"band_{other}"] = {"solve_s": stb["solve_ms"] / 1e3, "energy": eb,
+                                     "energy_rel_diff_vs_fp64": (eb - e64) / e64,
+                                     "speedup_vs_fp64_solve": st64["solve_ms"] / stb["solve_ms"]}
+            rb.close()
         r64.close()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference(pu, sk, depth, cpu_depth, 2, 1, dim)

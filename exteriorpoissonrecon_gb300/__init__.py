@@ -27,6 +27,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "epr.h")
 EPR_OK = 0
 EPR_FP64, EPR_FP32 = 0, 1
 EPR_SOLVER_CASCADIC, EPR_SOLVER_MULTIGRID = 0, 1
+EPR_BAND_FP64, EPR_BAND_DF = 0, 1
 
 _lib = None
 
@@ -57,6 +58,7 @@ class Params(ctypes.Structure):
         ("single_level", ctypes.c_int),
         ("separate", ctypes.c_int),
         ("fp64_from", ctypes.c_int),
+        ("band_precision", ctypes.c_int),
     ]
 
 
@@ -175,6 +177,8 @@ def default_params(**kw) -> Params:
         k = _FLAG_NAMES.get(k, k)
         if k == "precision" and isinstance(v, str):
             v = {"fp64": EPR_FP64, "fp32": EPR_FP32}[v.lower()]
+        if k == "band_precision" and isinstance(v, str):
+            v = {"fp64": EPR_BAND_FP64, "df": EPR_BAND_DF}[v.lower()]
         if k == "solver" and isinstance(v, str):
             v = {"cascadic": EPR_SOLVER_CASCADIC, "multigrid": EPR_SOLVER_MULTIGRID}[v.lower()]
         setattr(p, k, v)

@@ -98,10 +98,26 @@ bool Context::ensure_level(int l)
         if (!alloc((void **)&L.B32, sizeof(float) * S * L.N, "alloc B32")) return false;
         if (!cuda_ok(cudaMemsetAsync(L.xy32, 0, sizeof(float) * 2 * L.N, stream), "memset xy32")) return false;
     }
+    if (lvlDF(l))
+    {
+        if (!alloc((void **)&L.xyd, sizeof(df) * 2 * L.N, "alloc xy df")) return false;
+        if (!alloc((void **)&L.Ad, sizeof(df) * S * L.N, "alloc A df")) return false;
+        if (!alloc((void **)&L.Bd, sizeof(df) * S * L.N, "alloc B df")) return false;
+        if (!cuda_ok(cudaMemsetAsync(L.xyd, 0, sizeof(df) * 2 * L.N, stream), "memset xy df")) return false;
+    }
     return true;
 }
 
 bool Context::lvl32(int l) const { return P.precision == EPR_FP32 && !(l >= P.fp64_from && l < P.fp64_levels); }
+
+// the coarsest 3D levels of a float solve's band, in double-float when asked (their kernels are the
+// point-split and single-block ones, which take the pair type)
+constexpr int kMaxDFLevel = 3;
+bool Context::lvlDF(int l) const
+{
+    return P.precision == EPR_FP32 && P.band_precision == EPR_BAND_DF && P.solver == EPR_SOLVER_CASCADIC && dim == 3 &&
+           l <= kMaxDFLevel && l >= P.fp64_from && l < P.fp64_levels;
+}
 
 // refreshes the derived copies of a level's system: the float stencils (float levels) and the
 // colour-blocked stencils of the levels that are relaxed by one kernel per colour
@@ -113,6 +129,13 @@ bool Context::sync_system32(int l)
     {
         launch_convert_d2f(L.A64, L.A32, (int64_t)S * L.N, stream);
         launch_convert_d2f(L.B64, L.B32, (int64_t)S * L.N, stream);
+    }
+    if (lvlDF(l))
+    {
+        // the point-split kernels of these levels read the stencils in natural order
+        launch_d2df(L.A64, L.Ad, (int64_t)S * L.N, stream);
+        launch_d2df(L.B64, L.Bd, (int64_t)S * L.N, stream);
+        return launch_ok("convert system");
     }
     if (L.N > (dim == 3 ? 27 : 81))
     {
@@ -140,12 +163,22 @@ bool Context::sync_system32(int l)
 // device coefficients <-> the precision the solve works in
 bool Context::push_xy(int l)
 {
+    if (lvlDF(l))
+    {
+        launch_df_push(levels[l].xy64, levels[l].xyd, 2 * levels[l].N, d_kexp, l, stream);
+        return launch_ok("convert xy");
+    }
     if (!lvl32(l)) return true;
     launch_convert_d2f(levels[l].xy64, levels[l].xy32, 2 * levels[l].N, stream);
     return launch_ok("convert xy");
 }
 bool Context::pull_xy(int l)
 {
+    if (lvlDF(l))
+    {
+        launch_df_pull(levels[l].xyd, levels[l].xy64, 2 * levels[l].N, d_kexp, l, stream);
+        return launch_ok("convert xy");
+    }
     if (!lvl32(l)) return true;
     launch_convert_f2d(levels[l].xy32, levels[l].xy64, 2 * levels[l].N, stream);
     return launch_ok("convert xy");
@@ -159,8 +192,9 @@ Context::~Context()
         {
             release(L.xy64); release(L.xy32); release(L.A64); release(L.B64); release(L.A32); release(L.B32);
             release(L.tmp64); release(L.tmp32); release(L.Acb); release(L.Bcb);
+            release(L.xyd); release(L.Ad); release(L.Bd);
         }
-        release(red.partial); release(red.out); release(d_err); release(d_fit);
+        release(red.partial); release(red.out); release(d_err); release(d_fit); release(d_kexp);
         setup.release(*this);
         release_mg(*this);
         if (solve_graph) cudaGraphExecDestroy(solve_graph);
@@ -189,6 +223,7 @@ LevelPtrs<Real> level_ptrs(Context *c, int l)
     p.level = l;
     p.N = L.N;
     if constexpr (std::is_same<Real, double>::value) { p.xy = L.xy64; p.A = L.A64; p.B = L.B64; }
+    else if constexpr (std::is_same<Real, df>::value) { p.xy = L.xyd; p.A = L.Ad; p.B = L.Bd; return p; }
     else { p.xy = L.xy32; p.A = L.A32; p.B = L.B32; }
     if (L.Acb && c->lvl32(l) == std::is_same<Real, float>::value)
     {
@@ -201,6 +236,7 @@ LevelPtrs<Real> level_ptrs(Context *c, int l)
 bool Context::energy(int l, double *out3)
 {
     bool fp32 = lvl32(l);
+    if (lvlDF(l) && !pull_xy(l)) return false;  // evaluated in double
     with_dim(this, [&](auto dd) {
         constexpr int D = decltype(dd)::value;
         if (fp32) launch_energy<D, float>(level_ptrs<float>(this, l), levels[l].xy32, red, stream);
@@ -221,6 +257,12 @@ bool Context::energy(int l, double *out3)
 bool Context::gs(int l, int iters, int64_t persistentMaxNodes)
 {
     bool fp32 = lvl32(l);
+    if (lvlDF(l))
+    {
+        launches += launch_gs_sweeps_df(level_ptrs<df>(this, l), iters, d_err, stream, P.separate, persistentMaxNodes, d_kexp);
+        stats.node_updates += (int64_t)iters * levels[l].N;
+        return launch_ok("gs");
+    }
     launches += with_dim(this, [&](auto dd) {
         constexpr int D = decltype(dd)::value;
         if (fp32) return launch_gs_sweeps<D, float>(level_ptrs<float>(this, l), iters, d_err, stream, P.separate, persistentMaxNodes);
@@ -241,35 +283,28 @@ bool Context::check_errors()
 
 bool Context::prolong_add(int l)
 {
-    bool c32 = lvl32(l), f32 = lvl32(l + 1);
+    const bool c32 = lvl32(l), f32 = lvl32(l + 1), cdf = lvlDF(l), fdf = lvlDF(l + 1);
+    bool ok = true;
     with_dim(this, [&](auto dd) {
         constexpr int D = decltype(dd)::value;
-        if (c32 && f32) launch_prolong<D, float>(l, levels[l].xy32, levels[l + 1].xy32, 1, stream);
-        else if (c32 && !f32)
+        if (c32 && f32)
         {
-            // a float coarse level feeding a double fine level: refresh the coarse level's double
-            // copy, then prolong in double
-            launch_convert_f2d(levels[l].xy32, levels[l].xy64, 2 * levels[l].N, stream);
-            launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 1, stream);
-            launches++;
+            launch_prolong<D, float>(l, levels[l].xy32, levels[l + 1].xy32, 1, stream);
+            return 0;
         }
-        else
-        {
-            // a double coarse level feeding a float fine level: prolong in double, then refresh
-            // the float copy of the fine level
-            if (!f32) launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 1, stream);
-            else
-            {
-                launch_convert_f2d(levels[l + 1].xy32, levels[l + 1].xy64, 2 * levels[l + 1].N, stream);
-                launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 1, stream);
-                launch_convert_d2f(levels[l + 1].xy64, levels[l + 1].xy32, 2 * levels[l + 1].N, stream);
-                launches += 2;
-            }
-        }
+        // otherwise in double: refresh the double copies of a float or double-float coarse level
+        // and fine level, prolong, and refresh the fine level's working copy
+        if (c32) { launch_convert_f2d(levels[l].xy32, levels[l].xy64, 2 * levels[l].N, stream); launches++; }
+        if (cdf) { ok = ok && pull_xy(l); launches++; }
+        if (f32) { launch_convert_f2d(levels[l + 1].xy32, levels[l + 1].xy64, 2 * levels[l + 1].N, stream); launches++; }
+        if (fdf) { ok = ok && pull_xy(l + 1); launches++; }
+        launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 1, stream);
+        if (f32) { launch_convert_d2f(levels[l + 1].xy64, levels[l + 1].xy32, 2 * levels[l + 1].N, stream); launches++; }
+        if (fdf) { ok = ok && push_xy(l + 1); launches++; }
         return 0;
     });
     launches++;
-    return launch_ok("prolong");
+    return ok && launch_ok("prolong");
 }
 
 // Random<double> (Misha/Geometry.inl:430-438) on the C library generator seeded by srand(seed).
@@ -391,7 +426,9 @@ bool Context::solve_cascadic()
     {
         if (!cuda_ok(cudaMemsetAsync(levels[l].xy64, 0, sizeof(double) * 2 * levels[l].N, stream), "clear")) return false;
         if (fp32 && !cuda_ok(cudaMemsetAsync(levels[l].xy32, 0, sizeof(float) * 2 * levels[l].N, stream), "clear")) return false;
+        if (levels[l].xyd && !cuda_ok(cudaMemsetAsync(levels[l].xyd, 0, sizeof(df) * 2 * levels[l].N, stream), "clear")) return false;
     }
+    if (!cuda_ok(cudaMemsetAsync(d_kexp, 0, sizeof(int) * (depth + 1), stream), "clear")) return false;
     // random initial guess at the coarsest solve level, scaled to the target's magnitude
     {
         CRandom rng((unsigned int)P.seed);
@@ -525,6 +562,7 @@ void epr_default_params(epr_params *p)
     p->device = 0;
     p->fp64_levels = 0;
     p->fp64_from = 0;
+    p->band_precision = EPR_BAND_FP64;
     p->single_level = 0;
     p->separate = 0;
 }
@@ -544,6 +582,7 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
     if (p.precision != EPR_FP64 && p.precision != EPR_FP32) { g_error = "unknown precision"; return nullptr; }
     if (p.solver != EPR_SOLVER_CASCADIC && p.solver != EPR_SOLVER_MULTIGRID) { g_error = "unknown solver"; return nullptr; }
     if (p.fp64_from < 0 || p.fp64_levels < 0) { g_error = "fp64_from and fp64_levels must not be negative"; return nullptr; }
+    if (p.band_precision != EPR_BAND_FP64 && p.band_precision != EPR_BAND_DF) { g_error = "unknown band precision"; return nullptr; }
     if (p.solver == EPR_SOLVER_MULTIGRID && (p.max_cycles < 0 || !(p.tolerance >= 0))) { g_error = "bad multigrid cycle cap or tolerance"; return nullptr; }
     if (cudaSetDevice(p.device) != cudaSuccess)
     {
@@ -553,6 +592,7 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
     {
         std::lock_guard<std::mutex> lock(g_create_mutex);
         if (const char *v = getenv("EPR_GS_VARIANT")) epr::set_gs_variant(atoi(v));
+        if (const char *v = getenv("EPR_LANES_VARIANT")) epr::set_lanes_variant(atoi(v));
         static uint64_t prepared = 0;  // devices whose kernel attributes are set
         if (p.device >= 0 && p.device < 64 && !(prepared & (1ull << p.device)))
         {
@@ -575,7 +615,9 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
     bool ok = c->alloc((void **)&c->red.partial, sizeof(double) * 4 * epr::Reduce::kMaxBlocks, "alloc reduce") &&
               c->alloc((void **)&c->red.out, sizeof(double) * 4, "alloc reduce") &&
               c->alloc((void **)&c->d_err, sizeof(unsigned int), "alloc flag") &&
-              c->cuda_ok(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream), "memset flag");
+              c->cuda_ok(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream), "memset flag") &&
+              c->alloc((void **)&c->d_kexp, sizeof(int) * (depth + 1), "alloc exponents") &&
+              c->cuda_ok(cudaMemsetAsync(c->d_kexp, 0, sizeof(int) * (depth + 1), c->stream), "memset exponents");
     for (int l = 0; ok && l <= depth; l++) ok = c->ensure_level(l);
     if (!ok)
     {
@@ -667,6 +709,7 @@ int epr_quadfit(epr_ctx *ctx, int level, double *out)
     epr::Level &L = ctx->levels[level];
     double *d = nullptr;
     bool ok = ctx->alloc((void **)&d, sizeof(double) * 5 * L.N, "alloc fit");
+    if (ok && ctx->lvlDF(level)) ok = ctx->pull_xy(level);  // a double-float level's fit in double
     if (ok)
     {
         bool fp32 = ctx->lvl32(level);
@@ -722,6 +765,7 @@ int epr_gn_matvec(epr_ctx *ctx, int level, const double *dx, const double *dy, d
     double *d64 = nullptr, *o64 = nullptr;
     float *d32 = nullptr, *o32 = nullptr;
     bool fp32 = ctx->lvl32(level);
+    if (ctx->lvlDF(level) && !ctx->pull_xy(level)) EPR_RETURN(ctx, false);  // evaluated in double
     bool ok = ctx->alloc((void **)&d64, sizeof(double) * 2 * L.N, "alloc") && ctx->alloc((void **)&o64, sizeof(double) * 2 * L.N, "alloc") &&
               ctx->cuda_ok(cudaMemcpyAsync(d64, h.data(), sizeof(double) * 2 * L.N, cudaMemcpyHostToDevice, ctx->stream), "upload");
     if (ok && fp32)

@@ -12,6 +12,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "epr_df.cuh"
+
 namespace epr {
 
 constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1); }
@@ -28,6 +30,7 @@ struct Dims
 template <typename Real> struct Pair;
 template <> struct Pair<double> { using type = double2; };
 template <> struct Pair<float> { using type = float2; };
+template <> struct Pair<df> { using type = df2; };
 template <typename Real> using Real2 = typename Pair<Real>::type;
 
 // 3- and 2-point Gauss-Legendre rules on [0,1]

@@ -28,6 +28,9 @@ struct Level
     float *tmp32 = nullptr;
     void *Acb = nullptr;      // colour-blocked A and B in the level's precision (levels relaxed
     void *Bcb = nullptr;      // by one kernel per colour)
+    df *xyd = nullptr;        // double-float copies of a coarse band level (coefficients stored
+    df *Ad = nullptr;         // as x 2^-k, k = d_kexp[level]; stencils unscaled)
+    df *Bd = nullptr;
 };
 
 // Sample-side state of the build (ordered sampling, estimator, splats).  Defined in epr_setup.cu.
@@ -65,6 +68,7 @@ struct Context
     std::vector<Level> levels;
     Reduce red;
     unsigned int *d_err = nullptr;
+    int *d_kexp = nullptr;  // per level: power-of-two exponent of a double-float level
     double *d_fit = nullptr;
     double c = 0;
     bool have_system = false;
@@ -89,6 +93,7 @@ struct Context
     int stencil() const;
     bool ensure_level(int l);
     bool lvl32(int l) const;  // level l computes in float
+    bool lvlDF(int l) const;  // level l computes in double-float (a 3D coarse band level)
     bool sync_system32(int l);
     bool push_xy(int l);
     bool pull_xy(int l);

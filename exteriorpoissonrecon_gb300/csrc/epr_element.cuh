@@ -334,6 +334,132 @@ __device__ __forceinline__ void element_fit(const Real *x, const Real *y, int A,
 }
 
 // ---------------------------------------------------------------------------------------------
+// Packed float version of element_fit for corner 0 (canonical orientation), on Blackwell's
+// two-wide FP32 instructions (FFMA2 / FMUL2: two lanes of arithmetic per issue slot).  The x and
+// y fields travel together as (x, y) pairs, so every derivative table is one packed table; at a
+// Gauss point, with p = (x_P, y_P), q = (x_Q, y_Q) the P- and Q-derivatives,
+//   T = phP q - phQ p = (V, -U),   W = y_P x_Q - x_P y_Q,
+// and the five integrals accumulate as (h1, h0) += (w T) * T, (h4, -h3) += (w T) * W and
+// h2 += wU V.  The sums are those of element_fit in another association order (float rounding
+// differs in the last bits); the fast float relaxation uses it, the double path keeps the scalar
+// code.
+// ---------------------------------------------------------------------------------------------
+struct PackedFit
+{
+    float2 hv = {0.f, 0.f};  // (h1, h0)
+    float2 hw = {0.f, 0.f};  // (h4, -h3)
+    float h2 = 0.f;
+    __device__ __forceinline__ void add_to(float *h) const
+    {
+        h[0] += hv.y;
+        h[1] += hv.x;
+        h[2] += h2;
+        h[3] -= hw.y;
+        h[4] += hw.x;
+    }
+};
+
+__device__ __forceinline__ float2 splat2(float v) { return make_float2(v, v); }
+
+// derivative_partial on (x, y) pairs (a - b formed as fma(b, -1, a), which rounds once like a - b)
+template <int D, int K, bool AisP>
+__device__ __forceinline__ void derivative_partial_packed(const float2 *f, float2 (&t)[2][1 << (D - 2)])
+{
+    using Cp = Component<D, K>;
+    constexpr int NO = 1 << Cp::M;
+    float2 dif[2][NO];
+#pragma unroll
+    for (int bB = 0; bB < 2; bB++)
+#pragma unroll
+        for (int bo = 0; bo < NO; bo++)
+        {
+            int c1 = AisP ? Cp::corner(1, bB, bo) : Cp::corner(bB, 1, bo);
+            int c0 = AisP ? Cp::corner(0, bB, bo) : Cp::corner(bB, 0, bo);
+            dif[bB][bo] = __ffma2_rn(f[c0], splat2(-1.f), f[c1]);
+        }
+#pragma unroll
+    for (int g = 0; g < 2; g++)
+#pragma unroll
+        for (int bo = 0; bo < NO; bo++)
+            t[g][bo] = __ffma2_rn(splat2(hat2<float>(1, g)), dif[1][bo], __fmul2_rn(splat2(hat2<float>(0, g)), dif[0][bo]));
+}
+
+// ... and its value at the other-axis Gauss point go (derivative_at on pairs)
+template <int M>
+__device__ __forceinline__ float2 derivative_at_packed(const float2 *t, int go)
+{
+    if constexpr (M == 1) return __ffma2_rn(splat2(hat3<float>(1, go)), t[1], __fmul2_rn(splat2(hat3<float>(0, go)), t[0]));
+    else
+    {
+        const int g0 = go / 3, g1 = go % 3;
+        const float2 a0 = splat2(hat3<float>(0, g0)), a1 = splat2(hat3<float>(1, g0));
+        const float2 u0 = __ffma2_rn(a1, t[2], __fmul2_rn(a0, t[0]));
+        const float2 u1 = __ffma2_rn(a1, t[3], __fmul2_rn(a0, t[1]));
+        return __ffma2_rn(splat2(hat3<float>(1, g1)), u1, __fmul2_rn(splat2(hat3<float>(0, g1)), u0));
+    }
+}
+
+template <int D, int K>
+__device__ __forceinline__ void component_fit_packed(const float2 *c, PackedFit &acc)
+{
+    using Cp = Component<D, K>;
+    constexpr int M = Cp::M;
+    constexpr int NG = ipow(3, M);
+    float2 tP[2][1 << M], tQ[2][1 << M];
+    derivative_partial_packed<D, K, true>(c, tP);
+    derivative_partial_packed<D, K, false>(c, tQ);
+#pragma unroll
+    for (int go = 0; go < NG; go++)
+    {
+        // corner 0: every hat factor is the one of bit 0, both signs are -1
+        float lo;
+        if constexpr (M == 1) lo = hat3<float>(0, go);
+        else lo = hat3<float>(0, go / 3) * hat3<float>(0, go % 3);
+        const float wo = (float)other_weight<M>(go);
+        float2 Pg[2], Qg[2];
+#pragma unroll
+        for (int g = 0; g < 2; g++)
+        {
+            Pg[g] = derivative_at_packed<M>(tP[g], go);
+            Qg[g] = derivative_at_packed<M>(tQ[g], go);
+        }
+#pragma unroll
+        for (int gp = 0; gp < 2; gp++)
+#pragma unroll
+            for (int gq = 0; gq < 2; gq++)
+            {
+                const float w = (float)(Gauss::W2(gp) * Gauss::W2(gq)) * wo;
+                const float phP = -hat2<float>(0, gq) * lo;
+                const float phQ = -hat2<float>(0, gp) * lo;
+                const float2 p = Pg[gq], q = Qg[gp];
+                const float W = fmaf(p.y, q.x, -(p.x * q.y));
+                const float2 T = __ffma2_rn(splat2(phP), q, __fmul2_rn(splat2(-phQ), p));
+                const float2 wT = __fmul2_rn(splat2(w), T);
+                acc.hv = __ffma2_rn(wT, T, acc.hv);
+                acc.hw = __ffma2_rn(wT, splat2(W), acc.hw);
+                acc.h2 = fmaf(-wT.y, T.x, acc.h2);
+            }
+    }
+}
+
+// element_fit<D, float>(x, y, 0, h) on interleaved (x, y) corners
+template <int D>
+__device__ __forceinline__ void element_fit_packed(const float2 *c, float *h)
+{
+    PackedFit acc;
+    component_fit_packed<D, 0>(c, acc);
+    component_fit_packed<D, 1>(c, acc);
+    component_fit_packed<D, 2>(c, acc);
+    if constexpr (D == 4)
+    {
+        component_fit_packed<D, 3>(c, acc);
+        component_fit_packed<D, 4>(c, acc);
+        component_fit_packed<D, 5>(c, acc);
+    }
+    acc.add_to(h);
+}
+
+// ---------------------------------------------------------------------------------------------
 // Canonical orientation.  Mirroring an element along axis d (xi_d -> 1 - xi_d) flips the sign of
 // every d-derivative; each component of W, U and V carries exactly one derivative along each of
 // its two axes, so all the products in the fit integrals keep their sign.  Any corner A can

@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "epr_df.cuh"
+
 namespace epr {
 
 // One level of the hierarchy as the solve kernels see it.
@@ -43,6 +45,13 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
 // 2: 2^D lanes per node on a flat grid; 1 is the default, 0.69 ms against 0.70 ms at depth 8;
 // 4: as 1 without the point-split update of the small 3D levels)
 void set_gs_variant(int v);
+void set_lanes_variant(int v);
+// double-float levels: pairs stored as x 2^-k with k = kexp[level] (epr_df.cuh)
+void launch_df_push(const double *in, df *out, int64_t n, int *kexp, int level, cudaStream_t s);
+void launch_df_pull(const df *in, double *out, int64_t n, const int *kexp, int level, cudaStream_t s);
+void launch_d2df(const double *in, df *out, int64_t n, cudaStream_t s);
+int launch_gs_sweeps_df(const LevelPtrs<df> &L, int iters, unsigned int *err, cudaStream_t s, int separate,
+                        int64_t persistentMaxNodes, int *kexp);
 // iters full sweeps (all 2^D colours in order); levels of at most persistentMaxNodes nodes run all
 // sweeps inside one thread block, larger ones launch one kernel per colour.  Returns the number of
 // kernels launched.

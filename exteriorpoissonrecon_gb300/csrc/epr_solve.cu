@@ -9,6 +9,7 @@
 //   prolongation  ScalarFunctions::prolongation                      Hat.scalars.inl:1747-1779
 //   restriction   its transpose (the Galerkin restriction of MG.h:120-127)
 #include <algorithm>
+#include <type_traits>
 
 #include "epr_common.cuh"
 #include "epr_element.cuh"
@@ -407,13 +408,55 @@ __device__ __forceinline__ double group_sum(double v)
     for (int o = (1 << D) / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, 1 << D);
     return v;
 }
+template <int D>
+__device__ __forceinline__ df group_sum(df v)
+{
+#pragma unroll
+    for (int o = (1 << D) / 2; o > 0; o >>= 1) v += shfl_xor_any(v, o, 1 << D);
+    return v;
+}
+
+// Power-of-two shift that brings the largest stored magnitude |hi| of a double-float level into
+// [1, 2), or 0 while it stays within [2^-8, 2^9) (or the level is zero).  The whole block calls it;
+// it ends with a barrier.
+__device__ __forceinline__ int df_rescale_shift(const df *v, int64_t n)
+{
+    __shared__ float wmax[32];
+    __shared__ int shift;
+    float m = 0.f;
+    for (int64_t k = threadIdx.x; k < n; k += blockDim.x) m = fmaxf(m, fabsf(v[k].hi));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        float mm = 0.f;
+        for (int w = 0; w < (int)((blockDim.x + 31) >> 5); w++) mm = fmaxf(mm, wmax[w]);
+        const int e = mm > 0.f ? ilogbf(mm) : 0;
+        shift = (mm > 0.f && (e < -8 || e > 8)) ? -e : 0;
+    }
+    __syncthreads();
+    return shift;
+}
+
+// Factor of the wedge integrals of a level kept in double-float at the exponent k of its level
+// (coefficients stored as x 2^-k): the fit's wedge terms carry two more powers of the coefficients
+// than its stencil terms, so they are multiplied by 2^(2k) (exactly 1 for float and double levels).
+template <typename Real>
+__device__ __forceinline__ Real wedge_mult(const int *kexp, int level)
+{
+    if constexpr (std::is_same<Real, df>::value) return kexp ? ldexp_df(df(1), 2 * kexp[level]) : df(1);
+    else return (Real)1;
+}
 
 // Ac, Bc (optional): the colour's block of the colour-blocked stencils, the node being the colour's
 // jc-th of nc; otherwise the natural stencils L.A, L.B are read.
-template <int D, typename Real>
+template <int D, typename Real, bool Packed = false>
 __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Real *xy, const Grid<D> &g, const int *I, bool active,
                                                    int A, unsigned int *err, int separate = 0, const Real *Ac = nullptr,
-                                                   const Real *Bc = nullptr, int64_t jc = 0, int64_t nc = 0)
+                                                   const Real *Bc = nullptr, int64_t jc = 0, int64_t nc = 0,
+                                                   Real wmul = (Real)1)
 {
     constexpr int C = 1 << D, S = Dims<D>::S;
     int64_t i = 0;
@@ -440,19 +483,37 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
         i = iu;
         if (ok)
         {
-            Real x[C], y[C];
-#pragma unroll
-            for (int cc = 0; cc < C; cc++)
+            if constexpr (std::is_same<Real, float>::value && Packed)
             {
-                int jj = (int)iu;
+                // the (x, y) corner pairs as loaded, on the two-wide FP32 instructions
+                float2 c2[C];
 #pragma unroll
-                for (int d = 0; d < D; d++)
-                    if (cbit<D>(cc, d)) jj += sd[d];
-                Real2<Real> v = ld2(xy, (int64_t)(uint32_t)jj);
-                x[cc] = v.x;
-                y[cc] = v.y;
+                for (int cc = 0; cc < C; cc++)
+                {
+                    int jj = (int)iu;
+#pragma unroll
+                    for (int d = 0; d < D; d++)
+                        if (cbit<D>(cc, d)) jj += sd[d];
+                    c2[cc] = ld2(xy, (int64_t)(uint32_t)jj);
+                }
+                element_fit_packed<D>(c2, h);
             }
-            element_fit<D, Real>(x, y, 0, h);
+            else
+            {
+                Real x[C], y[C];
+#pragma unroll
+                for (int cc = 0; cc < C; cc++)
+                {
+                    int jj = (int)iu;
+#pragma unroll
+                    for (int d = 0; d < D; d++)
+                        if (cbit<D>(cc, d)) jj += sd[d];
+                    Real2<Real> v = ld2(xy, (int64_t)(uint32_t)jj);
+                    x[cc] = v.x;
+                    y[cc] = v.y;
+                }
+                element_fit<D, Real>(x, y, 0, h);
+            }
         }
         for (int o = A; o < S; o += C)
         {
@@ -490,7 +551,7 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
     for (int k = 0; k < 5; k++) h[k] = group_sum<D>(h[k]);
     ax = group_sum<D>(ax); ay = group_sum<D>(ay); bx = group_sum<D>(bx); by = group_sum<D>(by); acen = group_sum<D>(acen);
     if (!active || A != 0) return;
-    const Real sc = (Real)wedge_scale<D>(g.r);
+    const Real sc = (Real)wedge_scale<D>(g.r) * wmul;
     Real q[5];
     q[0] = h[0] * sc + acen;
     q[1] = h[1] * sc + acen;
@@ -517,7 +578,7 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
 
 template <typename Real>
 __device__ __forceinline__ void gs_update_warp3(const LevelPtrs<Real> &L, Real *xy, const Grid<3> &g, const int *I, bool active,
-                                                unsigned int *err, int separate)
+                                                unsigned int *err, int separate, Real wmul = (Real)1)
 {
     constexpr int S = 27;
     const int lane = threadIdx.x & 31;
@@ -585,18 +646,18 @@ __device__ __forceinline__ void gs_update_warp3(const LevelPtrs<Real> &L, Real *
 #pragma unroll
     for (int k = 0; k < 5; k++)
 #pragma unroll
-        for (int o = 4; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+        for (int o = 4; o > 0; o >>= 1) v[k] += shfl_xor_any(v[k], o);
     Real h[5], st5[5];
 #pragma unroll
     for (int k = 0; k < 5; k++)
     {
-        const Real g1 = __shfl_sync(0xffffffffu, v[k], 8), g2 = __shfl_sync(0xffffffffu, v[k], 16);
-        st5[k] = __shfl_sync(0xffffffffu, v[k], 24);
+        const Real g1 = shfl_any(v[k], 8), g2 = shfl_any(v[k], 16);
+        st5[k] = shfl_any(v[k], 24);
         h[k] = (v[k] + g1) + g2;
     }
     if (!active || lane != 0) return;
     const Real ax = st5[0], ay = st5[1], bx = st5[2], by = st5[3], acen = st5[4];
-    const Real sc = (Real)wedge_scale<3>(g.r);
+    const Real sc = (Real)wedge_scale<3>(g.r) * wmul;
     Real q[5];
     q[0] = h[0] * sc + acen;
     q[1] = h[1] * sc + acen;
@@ -626,7 +687,7 @@ __device__ __forceinline__ void gs_update_warp3(const LevelPtrs<Real> &L, Real *
 template <typename Real>
 __device__ __forceinline__ void gs_update_split3(const LevelPtrs<Real> &L, Real *xy, const Grid<3> &g, const int *I, bool active,
                                                  unsigned int *err, int separate, const Real *Ac, const Real *Bc, int64_t jc,
-                                                 int64_t nc, Real (*part)[5])
+                                                 int64_t nc, Real (*part)[5], Real wmul = (Real)1)
 {
     const int t = threadIdx.x & 127, wp = t >> 5, lane = t & 31;
     Real v[5] = {0, 0, 0, 0, 0};
@@ -691,7 +752,7 @@ __device__ __forceinline__ void gs_update_split3(const LevelPtrs<Real> &L, Real 
     for (int k = 0; k < 5; k++)
     {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+        for (int o = 16; o > 0; o >>= 1) v[k] += shfl_xor_any(v[k], o);
         if (lane == 0) part[wp][k] = v[k];
     }
     __syncthreads();
@@ -701,7 +762,7 @@ __device__ __forceinline__ void gs_update_split3(const LevelPtrs<Real> &L, Real 
 #pragma unroll
         for (int k = 0; k < 5; k++) h[k] = (part[0][k] + part[1][k]) + part[2][k];
         const Real ax = part[3][0], ay = part[3][1], bx = part[3][2], by = part[3][3], acen = part[3][4];
-        const Real sc = (Real)wedge_scale<3>(g.r);
+        const Real sc = (Real)wedge_scale<3>(g.r) * wmul;
         Real q[5];
         q[0] = h[0] * sc + acen;
         q[1] = h[1] * sc + acen;
@@ -728,16 +789,18 @@ constexpr int kSplitNodes = 2;
 constexpr int64_t kSplitMaxColourNodes = 125;
 template <typename Real>
 __global__ void __launch_bounds__(128 * kSplitNodes) gs_colour_split3_kernel(LevelPtrs<Real> L, Colour<3> col, int64_t cbBase,
-                                                                              unsigned int *err, int separate)
+                                                                              unsigned int *err, int separate,
+                                                                              const int *kexp = nullptr)
 {
     __shared__ Real part[kSplitNodes][4][5];
+    const Real wmul = wedge_mult<Real>(kexp, L.level);
     Grid<3> g(L.level);
     const int64_t j = (int64_t)blockIdx.x * kSplitNodes + (threadIdx.x >> 7);
     const bool active = j < col.n;
     int I[3] = {0, 0, 0};
     if (active) col.node(j, I);
     const Real *Ac = L.Acb ? L.Acb + cbBase : nullptr, *Bc = L.Bcb ? L.Bcb + cbBase : nullptr;
-    gs_update_split3<Real>(L, L.xy, g, I, active, err, separate, Ac, Bc, j, col.n, part[threadIdx.x >> 7]);
+    gs_update_split3<Real>(L, L.xy, g, I, active, err, separate, Ac, Bc, j, col.n, part[threadIdx.x >> 7], wmul);
 }
 
 template <int D, typename Real>
@@ -758,10 +821,10 @@ __device__ __forceinline__ void gs_update_lanes(const LevelPtrs<Real> &L, const 
 template <int D, typename Real>
 constexpr int lanes_min_blocks() { return (D == 3 && sizeof(Real) == 4) ? 10 : 1; }
 
-template <int D, typename Real>
-__global__ void __launch_bounds__(kThreads, lanes_min_blocks<D, Real>()) gs_colour_lanes_kernel(LevelPtrs<Real> L, Colour<D> col,
-                                                                                                int64_t cbBase, unsigned int *err,
-                                                                                                int separate)
+template <int D, typename Real, int MinBlocks = lanes_min_blocks<D, Real>(), bool Packed = false>
+__global__ void __launch_bounds__(kThreads, MinBlocks) gs_colour_lanes_kernel(LevelPtrs<Real> L, Colour<D> col,
+                                                                              int64_t cbBase, unsigned int *err,
+                                                                              int separate)
 {
     Grid<D> g(L.level);
     constexpr int NPB = kThreads >> D;
@@ -780,7 +843,7 @@ __global__ void __launch_bounds__(kThreads, lanes_min_blocks<D, Real>()) gs_colo
     // index of the node in the colour (axis 0 slowest)
     const int64_t jc = ((int64_t)blockIdx.z * col.cnt[D - 2] + blockIdx.y) * col.cnt[D - 1] + tl;
     const Real *Ac = L.Acb ? L.Acb + cbBase : nullptr, *Bc = L.Bcb ? L.Bcb + cbBase : nullptr;
-    gs_update_lanes_at<D, Real>(L, L.xy, g, I, tl < col.cnt[D - 1], A, err, separate, Ac, Bc, jc, col.n);
+    gs_update_lanes_at<D, Real, Packed>(L, L.xy, g, I, tl < col.cnt[D - 1], A, err, separate, Ac, Bc, jc, col.n);
 }
 
 // Flat variant: consecutive groups of 2^D threads take consecutive nodes of the colour (32-bit
@@ -808,10 +871,13 @@ __global__ void __launch_bounds__(kThreads) gs_colour_flat_kernel(LevelPtrs<Real
 template <int D, typename Real>
 constexpr int persistent_threads() { return (D == 3 && sizeof(Real) == 4) ? 1024 : 256; }
 template <int D, typename Real, bool SmemStencil, int MaxThreads, int Mode>
-__global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L, int iters, unsigned int *err, int separate)
+__global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L, int iters, unsigned int *err, int separate,
+                                                              int *kexp = nullptr)
 {
     Grid<D> g(L.level);
     constexpr int S = Dims<D>::S;
+    constexpr bool kDF = std::is_same<Real, df>::value;
+    Real wmul = wedge_mult<Real>(kexp, L.level);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Real *xy = reinterpret_cast<Real *>(smem_raw);
     for (int64_t k = threadIdx.x; k < 2 * g.N; k += blockDim.x) xy[k] = L.xy[k];
@@ -825,6 +891,7 @@ __global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L,
     }
     __syncthreads();
     for (int it = 0; it < iters; it++)
+    {
         for (int c = 0; c < (1 << D); c++)
         {
             Colour<D> col(g, c);
@@ -836,7 +903,7 @@ __global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L,
                 const bool active = j < col.n;
                 int I[3] = {0, 0, 0};
                 if (active) col.node(j, I);
-                gs_update_split3<Real>(Ls, xy, g, I, active, err, separate, nullptr, nullptr, 0, 0, part[threadIdx.x >> 7]);
+                gs_update_split3<Real>(Ls, xy, g, I, active, err, separate, nullptr, nullptr, 0, 0, part[threadIdx.x >> 7], wmul);
             }
             else if constexpr (Mode == 1 && D == 3)
             {
@@ -845,7 +912,7 @@ __global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L,
                 const bool active = j < col.n;
                 int I[3] = {0, 0, 0};
                 if (active) col.node(j, I);
-                gs_update_warp3<Real>(Ls, xy, g, I, active, err, separate);
+                gs_update_warp3<Real>(Ls, xy, g, I, active, err, separate, wmul);
             }
             else
             {
@@ -859,11 +926,25 @@ __global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L,
                     if (active) col.node(j, I);
                     else
                         for (int d = 0; d < D; d++) I[d] = 0;
-                    gs_update_lanes_at<D, Real>(Ls, xy, g, I, active, A, err, separate);
+                    gs_update_lanes_at<D, Real>(Ls, xy, g, I, active, A, err, separate, nullptr, nullptr, 0, 0, wmul);
                 }
             }
             __syncthreads();
         }
+        if constexpr (kDF)
+            if (kexp)
+            {
+                // keep the stored coefficients near 1: a new power-of-two exponent after every sweep
+                const int shift = df_rescale_shift(xy, 2 * g.N);
+                if (shift)
+                {
+                    for (int64_t k = threadIdx.x; k < 2 * g.N; k += blockDim.x) xy[k] = ldexp_df(xy[k], shift);
+                    if (threadIdx.x == 0) kexp[L.level] -= shift;
+                    __syncthreads();
+                    wmul = wedge_mult<Real>(kexp, L.level);
+                }
+            }
+    }
     for (int64_t k = threadIdx.x; k < 2 * g.N; k += blockDim.x) L.xy[k] = xy[k];
 }
 
@@ -998,6 +1079,7 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n)
 
 inline unsigned int blocks_for(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
 
+int g_lanes_variant = 1;  // 0: scalar float element fit in the lane kernel, 1: packed
 int g_gs_variant = 1;  // 0: one thread per node, 1: 2^D lanes per node (row grid), 2: 2^D lanes per node (flat grid),
                        // 4: as 1 without the point-split update of the small 3D levels
 
@@ -1059,11 +1141,22 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
         constexpr int NPB = kThreads >> D;
         dim3 grid((unsigned)((col.cnt[D - 1] + NPB - 1) / NPB), (unsigned)col.cnt[D - 2],
                   (unsigned)(D == 3 ? col.cnt[0] : col.cnt[0] * col.cnt[1]));
-        gs_colour_lanes_kernel<D, Real><<<grid, kThreads, 0, s>>>(L, col, colour_block_base<D>(g, colour), err, separate);
+        const int64_t cb = colour_block_base<D>(g, colour);
+        // float: the element integrals on the packed two-wide FP32 instructions (3D: 0.614 against
+        // 0.680 ms per depth-8 colour; registers capped at 56, 9 resident blocks, where the
+        // scalar fit ran best at 48); EPR_LANES_VARIANT=0 selects the scalar fit
+        if constexpr (std::is_same<Real, float>::value)
+            if (g_lanes_variant != 0)
+            {
+                gs_colour_lanes_kernel<D, Real, D == 3 ? 9 : 1, true><<<grid, kThreads, 0, s>>>(L, col, cb, err, separate);
+                return;
+            }
+        gs_colour_lanes_kernel<D, Real><<<grid, kThreads, 0, s>>>(L, col, cb, err, separate);
     }
 }
 
 void set_gs_variant(int v) { g_gs_variant = v; }
+void set_lanes_variant(int v) { g_lanes_variant = v; }
 
 // shared-memory carve-out of the single-block level kernels whose stencils live in shared memory
 constexpr size_t kLevelSmemLimit = 200 * 1024;
@@ -1088,6 +1181,7 @@ void prepare_gs_kernels()
 {
     prepare_level_kernels<3, float>();
     prepare_level_kernels<3, double>();
+    prepare_level_kernels<3, df>();
     prepare_level_kernels<4, float>();
     prepare_level_kernels<4, double>();
 }
@@ -1133,6 +1227,115 @@ int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cud
     int n = 0;
     for (int it = 0; it < iters; it++)
         for (int c = 0; c < (1 << D); c++) { launch_gs_colour<D, Real>(L, c, err, s, separate); n++; }
+    return n;
+}
+
+// ---------------------------------------------------------------------------------------------
+// double-float levels (3D levels 0-3 of the float solve's coarse band)
+// ---------------------------------------------------------------------------------------------
+__global__ void df_rescale_kernel(df *xy, int64_t n, int *kexp, int level)
+{
+    const int shift = df_rescale_shift(xy, n);
+    if (!shift) return;
+    for (int64_t k = threadIdx.x; k < n; k += blockDim.x) xy[k] = ldexp_df(xy[k], shift);
+    if (threadIdx.x == 0) kexp[level] -= shift;
+}
+
+// double coefficients -> pairs at the level's new exponent (the largest magnitude in [1, 2))
+__global__ void df_push_kernel(const double *in, df *out, int64_t n, int *kexp, int level)
+{
+    __shared__ double wmax[32];
+    __shared__ int k;
+    double m = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(in[i]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        double mm = 0.0;
+        for (int w = 0; w < (int)((blockDim.x + 31) >> 5); w++) mm = fmax(mm, wmax[w]);
+        k = mm > 0.0 ? ilogb(mm) : 0;
+        kexp[level] = k;
+    }
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) out[i] = df(ldexp(in[i], -k));
+}
+
+__global__ void df_pull_kernel(const df *in, double *out, int64_t n, const int *kexp, int level)
+{
+    const int k = kexp[level];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = ldexp((double)in[i], k);
+}
+
+__global__ void d2df_kernel(const double *in, df *out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) out[i] = df(in[i]);
+}
+
+void launch_df_push(const double *in, df *out, int64_t n, int *kexp, int level, cudaStream_t s)
+{
+    df_push_kernel<<<1, 256, 0, s>>>(in, out, n, kexp, level);
+}
+void launch_df_pull(const df *in, double *out, int64_t n, const int *kexp, int level, cudaStream_t s)
+{
+    df_pull_kernel<<<(unsigned)std::min<int64_t>(blocks_for(n, 256), 1024), 256, 0, s>>>(in, out, n, kexp, level);
+}
+void launch_d2df(const double *in, df *out, int64_t n, cudaStream_t s)
+{
+    if (n) d2df_kernel<<<(unsigned)std::min<int64_t>(blocks_for(n, 256), 1024), 256, 0, s>>>(in, out, n);
+}
+
+// Paired GS sweeps of a 3D double-float level (levels 0-3): the same kernels as a float or double
+// level of that size, with the wedge factor of the level's exponent and a new exponent after every
+// sweep.
+int launch_gs_sweeps_df(const LevelPtrs<df> &L, int iters, unsigned int *err, cudaStream_t s, int separate,
+                        int64_t persistentMaxNodes, int *kexp)
+{
+    Grid<3> g(L.level);
+    if (iters <= 0) return 0;
+    if (g.N <= persistentMaxNodes)
+    {
+        constexpr int MT = persistent_threads<3, df>();
+        const int64_t colour0 = Colour<3>(g, 0).n;
+        const size_t xyBytes = 2 * g.N * sizeof(df), stBytes = 2 * (size_t)Dims<3>::S * g.N * sizeof(df);
+        const bool smemStencil = xyBytes + stBytes <= kLevelSmemLimit;
+        const size_t smem = xyBytes + (smemStencil ? stBytes : 0);
+        if (colour0 == 1)
+        {
+            if (smemStencil) gs_level_kernel<3, df, true, kSplitThreads, 2><<<1, 128, smem, s>>>(L, iters, err, separate, kexp);
+            else gs_level_kernel<3, df, false, kSplitThreads, 2><<<1, 128, smem, s>>>(L, iters, err, separate, kexp);
+            return 1;
+        }
+        if (colour0 <= 8 && colour0 * 32 <= MT)
+        {
+            const int threads = (int)colour0 * 32;
+            if (smemStencil) gs_level_kernel<3, df, true, MT, 1><<<1, threads, smem, s>>>(L, iters, err, separate, kexp);
+            else gs_level_kernel<3, df, false, MT, 1><<<1, threads, smem, s>>>(L, iters, err, separate, kexp);
+            return 1;
+        }
+        const int threads = (int)std::min<int64_t>(MT, ((colour0 << 3) + 31) / 32 * 32);
+        if (smemStencil) gs_level_kernel<3, df, true, MT, 0><<<1, threads, smem, s>>>(L, iters, err, separate, kexp);
+        else gs_level_kernel<3, df, false, MT, 0><<<1, threads, smem, s>>>(L, iters, err, separate, kexp);
+        return 1;
+    }
+    int n = 0;
+    for (int it = 0; it < iters; it++)
+    {
+        for (int c = 0; c < 8; c++)
+        {
+            Colour<3> col(g, c);
+            if (col.n == 0) continue;
+            // colours of levels up to 3 have at most 125 nodes: point-split, 128 threads per node
+            gs_colour_split3_kernel<df><<<(unsigned)((col.n + kSplitNodes - 1) / kSplitNodes), 128 * kSplitNodes, 0, s>>>(
+                L, col, 0, err, separate, kexp);
+            n++;
+        }
+        df_rescale_kernel<<<1, 256, 0, s>>>(L.xy, 2 * g.N, kexp, L.level);
+        n++;
+    }
     return n;
 }
 

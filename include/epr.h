@@ -68,6 +68,8 @@ extern "C" {
 #define EPR_FP64 0  /* all arithmetic in double (parity with the reference to 1e-12) */
 #define EPR_FP32 1  /* smoothing / matvecs in float; energies, norms and the coarse solve in double */
 
+#define EPR_BAND_FP64 0  /* the double band of EPR_FP32 in double */
+#define EPR_BAND_DF 1    /* its 3D levels up to 3 in double-float */
 #define EPR_SOLVER_CASCADIC 0   /* the reference schedule: coarse-to-fine paired Gauss-Seidel */
 #define EPR_SOLVER_MULTIGRID 1  /* cascadic, each level relaxed by the alternating solve with linear
                                    multigrid V-cycles (AlternatingSolve, sType MULTIGRID) */
@@ -95,6 +97,10 @@ typedef struct epr_params {
     int single_level;     /* --singleLevel: prolong the initial guess and relax only the finest solve level */
     int separate;         /* --separate: update x then y per node instead of the paired 2x2 step */
     int fp64_from;        /* EPR_FP32 only: first level of the double band (0) */
+    int band_precision;   /* EPR_FP32 only: EPR_BAND_FP64 (0) runs the band in double; EPR_BAND_DF runs
+                             its 3D levels up to 3 in double-float (pairs of floats, 48 bits, on the
+                             FP32 pipe, with a power-of-two exponent per level) and the rest in double;
+                             cascadic solver only */
 } epr_params;
 
 typedef struct epr_stats {

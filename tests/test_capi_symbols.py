@@ -25,7 +25,9 @@ def test_params_struct_matches_defaults():
     assert p.max_solve_depth == -1 and p.precision == epr.EPR_FP64
     q = epr.default_params(sWeight=50, gsIters=20, precision="fp32")
     assert q.s_weight == 50 and q.gs_iters == 20 and q.precision == epr.EPR_FP32
-    assert ctypes.sizeof(epr.Params) == 104
+    assert p.band_precision == epr.EPR_BAND_FP64
+    assert epr.default_params(band_precision="df").band_precision == epr.EPR_BAND_DF
+    assert ctypes.sizeof(epr.Params) == 104  # band_precision fills the former tail padding
 
 
 def test_line_searches_host_only():
