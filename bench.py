@@ -45,7 +45,7 @@ METRIC = "Depth-8 time-to-1e-6-residual, learned+FP32 vs plain FP64 GPU; stencil
 # depth-7 launch (profiles/gs_colour_lanes_kernel_link_depth7_fp32.txt,
 # profiles/linear_gs_colour_kernel_link_depth7_fp32.txt); a depth-8 launch's traffic is these times
 # its colour nodes (traffic grows in proportion with the nodes).
-GS_DRAM_BYTES_PER_COLOUR_NODE_FP32 = (76.418048e6 + 3.727872e6) / 274625
+GS_DRAM_BYTES_PER_COLOUR_NODE_FP32 = (76.39296e6 + 4.034304e6) / 274625
 LGS_DRAM_BYTES_PER_COLOUR_NODE_FP32 = (40.49792e6 + 1.28e3) / 274625
 
 
