@@ -9,10 +9,13 @@ noise sigma 0.005 (unit-cube units), 5 degree angular noise, plus 10% uniform sp
 random frames; 3D, depth 8 (257^3 nodes x 2 channels = 33.9M unknowns), code-default parameters.
 
 One step = one full solve from the built system (fresh initial guess each time): the reference's
-cascadic paired Gauss-Seidel schedule with FP32 smoothing except on levels 2-3, which run in FP64
-(the named configuration's FP64 coarse solve: the cascadic solve leaves the zero stationary point
-there, and double keeps the double run's local minimum), FP64 energies and reductions.  The line also reports the all-double and the all-float runs of the
-same schedule.  `value` is the
+cascadic paired Gauss-Seidel schedule with FP32 smoothing except on levels 2-3, which run in
+double-float (pairs of floats with a power-of-two exponent per level: the named configuration's
+FP64 coarse solve; the cascadic solve leaves the zero stationary point there, and double precision
+keeps the double run's local minimum), FP64 energies and reductions.  The line also reports the
+all-double run, the same band in double, and the all-float run of the same schedule.
+--workload batch: 64 small reconstructions (torus knots + helices, depths 5-7) solved concurrently,
+in solves/s.  `value` is the
 device time per solve with the system resident in HBM; `e2e` repeats the whole public-API
 pipeline per step from host buffers (samples host->device, build, solve, solution device->host).
 Every array of a level exceeds the 129 MB L2 (coefficients 137 MB in FP32, stencils 3.7 GB), so no
@@ -229,7 +232,7 @@ def kernel_rooflines(r, dim, depth, precision, clk):
                 "launch_ms": gs_ms, "algorithmic_bytes_per_launch": gs_bytes,
                 "note": ("FMA-bound quartic relaxation; bytes = coefficient read + stencil columns + update writes; "
                          "the finest level's colour launches take share_of_step of the step, the rest is the "
-                         "coarser levels (the double band latency-bound on the FP64 pipe)"),
+                         "coarser levels (levels 0-3: thousands of latency-bound launches)"),
                 "compute": {"algorithmic_flops_per_launch": gs_flops, "achieved_tflops": gs_flops / (gs_ms * 1e-3) / 1e12,
                             "peak_tflops": fp32_peak if precision == "fp32" else None,
                             "peak_source": "nominal FP32 at the sampled SM clock",
