@@ -31,7 +31,7 @@ struct Args
     double nSigma = 0.25, scale = 1.1, sWeight = 100., dWeight = 0.00625, iMult = 2., jitter = 0.;
     int depth = 5, seed = 0, tRadius = 1, dRadius = 1, aRadius = -1, minSolveDepth = 0, gsIters = 10, maxSolveDepth = -1;
     bool singleLevel = false, separate = false, verbose = false, project = false;
-    std::string precision = "fp64", solver = "cascadic";
+    std::string precision = "fp64", solver = "cascadic", bandPrecision = "fp64";
     int device = 0, fp64Levels = 0, fp64From = 0, maxCycles = 200;
     double tolerance = 1e-6;
 };
@@ -65,6 +65,7 @@ void Usage(const char *ex)
     printf("\t[--precision fp64|fp32]\n");
     printf("\t[--fp64From <first level of the double band with --precision fp32>=0]\n");
     printf("\t[--fp64Levels <levels from --fp64From below this one relax in double with --precision fp32>=0]\n");
+    printf("\t[--bandPrecision fp64|df <arithmetic of the band's 3D levels up to 3: double or double-float>]\n");
     printf("\t[--solver cascadic|multigrid]\n");
     printf("\t[--tolerance <multigrid: relative gradient per level>=1e-6]\n");
     printf("\t[--maxCycles <multigrid: alternating rounds per level>=200]\n");
@@ -76,7 +77,7 @@ Args Parse(int argc, char **argv)
 {
     Args a;
     std::map<std::string, std::string *> strs = {{"in", &a.in}, {"out", &a.out}, {"grid", &a.grid}, {"precision", &a.precision},
-                                                 {"solver", &a.solver}};
+                                                 {"solver", &a.solver}, {"bandPrecision", &a.bandPrecision}};
     std::map<std::string, double *> dbls = {{"nSigma", &a.nSigma}, {"scale", &a.scale}, {"sWeight", &a.sWeight},
                                             {"dWeight", &a.dWeight}, {"iMult", &a.iMult}, {"jitter", &a.jitter},
                                             {"tolerance", &a.tolerance}};
@@ -291,6 +292,7 @@ int main(int argc, char **argv)
     if (a.project) Fail("--project is not supported", 2);
     if (a.precision != "fp32" && a.precision != "fp64") Fail("--precision must be fp64 or fp32", 2);
     if (a.solver != "cascadic" && a.solver != "multigrid") Fail("--solver must be cascadic or multigrid", 2);
+    if (a.bandPrecision != "fp64" && a.bandPrecision != "df") Fail("--bandPrecision must be fp64 or df", 2);
     if (a.depth < 1) Fail("depth must be at least 1", 2);
     std::string ext = a.in.substr(a.in.find_last_of('.') + 1);
     if (ext != "ply") Fail("Only .ply files supported", 2);
@@ -355,6 +357,7 @@ int main(int argc, char **argv)
     p.precision = a.precision == "fp32" ? EPR_FP32 : EPR_FP64;
     p.fp64_levels = a.fp64Levels;
     p.fp64_from = a.fp64From;
+    p.band_precision = a.bandPrecision == "df" ? EPR_BAND_DF : EPR_BAND_FP64;
     p.solver = a.solver == "multigrid" ? EPR_SOLVER_MULTIGRID : EPR_SOLVER_CASCADIC;
     p.tolerance = a.tolerance;
     p.max_cycles = a.maxCycles;

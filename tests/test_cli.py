@@ -53,6 +53,8 @@ def test_usage_and_argument_errors(cli):
     assert r.returncode == 2 and "precision" in r.stderr
     r = subprocess.run([cli, "--in", "x.ply", "--solver", "newton"], capture_output=True, text=True)
     assert r.returncode == 2 and "solver" in r.stderr
+    r = subprocess.run([cli, "--in", "x.ply", "--bandPrecision", "half"], capture_output=True, text=True)
+    assert r.returncode == 2 and "bandPrecision" in r.stderr
 
 
 def test_tree_parser_reads_reference_output():

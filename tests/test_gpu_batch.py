@@ -21,6 +21,7 @@ def _inputs():
     pu, _ = epr.unit_cube(pos)
     items.append(dict(dim=4, depth=3, pos=pu, skew=epr.pack_skew(fr), kw={}))
     items.append(dict(items[0], kw=dict(precision="fp32", fp64_from=2, fp64_levels=4)))
+    items.append(dict(items[1], kw=dict(precision="fp32", fp64_from=0, fp64_levels=4, band_precision="df")))
     g = load_golden("knot3_d4")
     items.append(dict(dim=3, depth=int(g["depth"]), pos=g["pos"], skew=g["skew"], kw={}))
     return items, g
