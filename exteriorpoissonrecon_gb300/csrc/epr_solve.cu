@@ -9,6 +9,8 @@
 //   prolongation  ScalarFunctions::prolongation                      Hat.scalars.inl:1747-1779
 //   restriction   its transpose (the Galerkin restriction of MG.h:120-127)
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <type_traits>
 
 #include "epr_common.cuh"

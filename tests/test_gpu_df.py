@@ -94,3 +94,4 @@ def test_df_band_is_cascadic_3d_only():
     assert np.isfinite(st["fit_energy"])
     with pytest.raises(epr.EprError):
         epr.Reconstructor(3, 3, band_precision=7)
+
