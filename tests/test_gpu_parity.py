@@ -190,3 +190,27 @@ def test_double_band_keeps_the_double_minimum():
         e[name] = st["fit_energy"] + st["reg_energy"]
         r.close()
     assert abs(e["band"] - e["fp64"]) < 1e-6 * e["fp64"]
+
+
+def test_full_size_mixed_precision_reaches_double_energy():
+    """The benchmark's full size (3D link, 1.1M samples, depth 8, 257^3 nodes): the float solve with
+    levels 2-3 in double-float ends at the all-double solve's energy to 1e-6, and a repeated solve
+    (graph replay) gives the same bits.  Size-independent checks, as the oracle cannot run this size
+    in test time."""
+    pos, fr = epr.samples.make_workload("link", 1_000_000, seed=0)
+    pu, _ = epr.unit_cube(pos)
+    sk = epr.pack_skew(fr)
+    r64 = epr.Reconstructor(3, 8, pu, sk, precision="fp64")
+    s64 = r64.solve()
+    e64 = s64["fit_energy"] + s64["reg_energy"]
+    r64.close()
+    r = epr.Reconstructor(3, 8, pu, sk, precision="fp32", fp64_from=2, fp64_levels=4, band_precision="df")
+    s1 = r.solve()
+    x1 = r.coefficients(8)[0]
+    s2 = r.solve()
+    x2 = r.coefficients(8)[0]
+    e = s2["fit_energy"] + s2["reg_energy"]
+    assert abs(e - e64) < 1e-6 * e64, (e, e64)
+    assert s1["fit_energy"] == s2["fit_energy"] and np.array_equal(x1, x2)
+    assert s2["initial_energy"] == s64["initial_energy"]
+    r.close()
