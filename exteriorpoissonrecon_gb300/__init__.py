@@ -62,6 +62,50 @@ class Params(ctypes.Structure):
     ]
 
 
+class Sampler(ctypes.Structure):
+    """epr_sampler: a shape of the reference's Sample tool with its noise, generated on the GPU."""
+    _fields_ = [
+        ("shape", ctypes.c_int),
+        ("regular", ctypes.c_int),
+        ("a", ctypes.c_double),
+        ("b", ctypes.c_double),
+        ("c", ctypes.c_double),
+        ("pos_sigma", ctypes.c_double),
+        ("angle_deg", ctypes.c_double),
+        ("spot_frac", ctypes.c_double),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
+SHAPES = {"knot": 0, "link": 1, "helix": 2, "clifford": 3}
+
+
+def sampler(shape: str, a: float = 0.0, b: float = 0.0, c: float = 0.0, pos_sigma: float = 0.0,
+            angle_deg: float = 0.0, spot_frac: float = 0.0, seed: int = 0, regular: bool = False) -> Sampler:
+    """knot: a, b = p, q (defaults 2, 3); helix: a turns, radius b (0.3), height c (1)."""
+    if shape == "knot":
+        a, b = a or 2.0, b or 3.0
+    if shape == "helix":
+        b, c = b or 0.3, c or 1.0
+    return Sampler(SHAPES[shape], int(regular), a, b, c, pos_sigma, angle_deg, spot_frac, seed)
+
+
+def generate_samples(sp: Sampler, n: int, device: int = 0):
+    """World positions (total x dim) and packed frames of n generated samples plus the outliers."""
+    L = load()
+    total = ctypes.c_size_t(0)
+    rc = L.epr_generate_samples(device, ctypes.byref(sp), n, None, None, ctypes.byref(total))
+    if rc != EPR_OK:
+        raise EprError(f"[{rc}] " + L.epr_global_error().decode())
+    dim = 4 if sp.shape == SHAPES["clifford"] else 3
+    pos = np.zeros((total.value, dim))
+    skew = np.zeros((total.value, dim * (dim - 1) // 2))
+    rc = L.epr_generate_samples(device, ctypes.byref(sp), n, _p(pos), _p(skew), ctypes.byref(total))
+    if rc != EPR_OK:
+        raise EprError(f"[{rc}] " + L.epr_global_error().decode())
+    return pos, skew
+
+
 class Stats(ctypes.Structure):
     _fields_ = [
         ("initial_energy", ctypes.c_double),
@@ -126,6 +170,9 @@ def load():
     L.epr_prolong.argtypes = [vp, ctypes.c_int]
     L.epr_gn_matvec.argtypes = [vp, ctypes.c_int, P, P, P, P]
     L.epr_solve.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.epr_generate_samples.argtypes = [ctypes.c_int, ctypes.POINTER(Sampler), ctypes.c_size_t, P, P,
+                                       ctypes.POINTER(ctypes.c_size_t)]
+    L.epr_set_generated_samples.argtypes = [vp, ctypes.POINTER(Sampler), ctypes.c_size_t, P]
     L.epr_batch_solve.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                   ctypes.POINTER(Stats), ctypes.POINTER(ctypes.c_int)]
     L.epr_get_solution.argtypes = [vp, ctypes.c_int, P, P]
@@ -250,6 +297,12 @@ class Reconstructor:
 
     def build(self):
         self._check(load().epr_build(self._h))
+
+    def set_generated_samples(self, sp: Sampler, n: int):
+        """Samples generated on the GPU and mapped to the unit cube there; returns the map."""
+        xf = np.zeros((self.dim + 1) * (self.dim + 1))
+        self._check(load().epr_set_generated_samples(self._h, ctypes.byref(sp), n, _p(xf)))
+        return xf.reshape(self.dim + 1, self.dim + 1)
 
     def set_level_system(self, level, R, B, c):
         R = np.ascontiguousarray(R, dtype=np.float64)

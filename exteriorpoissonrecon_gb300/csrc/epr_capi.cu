@@ -38,6 +38,8 @@ std::mutex g_create_mutex;
 
 namespace epr {
 
+void set_global_error(const std::string &msg) { g_error = msg; }
+
 void Context::fail(int code, const char *fmt, ...)
 {
     char buf[1024];
@@ -569,7 +571,6 @@ void epr_default_params(epr_params *p)
 
 const char *epr_global_error(void) { return g_error.c_str(); }
 
-struct epr_ctx : public epr::Context {};
 
 epr_ctx *epr_create(int dim, int depth, const epr_params *params)
 {

@@ -51,6 +51,8 @@ struct Setup
     std::vector<uint8_t *> refinedD, refinedS; // per tree depth
 
     bool set_samples(Context &c, size_t n, const double *pos, const double *skew);
+    // takes device arrays allocated on the context's stream (generated samples) as its own
+    bool set_samples_device(Context &c, size_t n, double *dpos, double *dskew);
     bool build(Context &c);
     bool get(Context &c, const std::string &name, double *out, size_t cap, size_t *count);
     void release_built(Context &c);
@@ -107,9 +109,17 @@ struct Context
     bool solve_cascadic();
 };
 
+// the text epr_global_error() returns (per host thread)
+void set_global_error(const std::string &msg);
+
 // A64[level] += dWeight K (the Dirichlet stiffness of the level, with the reference's
 // resolution-1 stencil table, see epr_setup.cu)
 bool add_dirichlet(Context &c, int level);
 bool add_dirichlet_to(Context &c, int level, double *dst, double w);
 
 }  // namespace epr
+
+// the C ABI's opaque handle is the context itself
+struct epr_ctx : public epr::Context
+{
+};

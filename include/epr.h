@@ -44,6 +44,8 @@
  *   epr_batch_solve
  *       no reference counterpart: the reference reconstructs one input per process; this runs
  *       Reconstructor::Reconstructor + solve (ExteriorPoisson.h:59-81) for many inputs at once
+ *   epr_generate_samples / epr_set_generated_samples
+ *       the Sample tool's shapes and noise              Include/Samples.h, Sample/Sample.cpp:137-199
  *   epr_get_array
  *       read-only views of the reference's internal state (TreeEstimator::measure/noise/depth
  *       GridSamples.inl:838-862, S(E) ExteriorPoisson.h:290-307, _R/_B SystemEnergy.h:172-175)
@@ -167,6 +169,33 @@ int epr_solve(epr_ctx *ctx, epr_stats *stats);
  * failing context in index order (epr_global_error() names it).  The contexts must not be used by
  * other threads meanwhile. */
 int epr_batch_solve(epr_ctx *const *ctxs, int n, int build, int threads, epr_stats *stats, int *status);
+
+/* Synthetic samples generated on the device (the reference's Sample tool: Include/Samples.h shapes,
+ * Sample/Sample.cpp:137-199 noise).  Random numbers: Philox4x32-10 keyed by seed, one counter per
+ * sample, so the output is a function of (parameters, n, seed) alone. */
+#define EPR_SHAPE_TORUS_KNOT 0  /* ((2+cos qt) cos pt, (2+cos qt) sin pt, sin qt); a = p, b = q */
+#define EPR_SHAPE_LINK 1        /* unit circles in xy at the origin and in xz at (1,0,0) */
+#define EPR_SHAPE_HELIX 2       /* a turns of radius b over height c along z */
+#define EPR_SHAPE_CLIFFORD 3    /* 4D: (cos u, sin u, cos v, sin v)/sqrt 2, frame d_u ^ d_v */
+typedef struct epr_sampler {
+    int shape;           /* EPR_SHAPE_* (curves 3D, with frames dual to the tangent) */
+    int regular;         /* torus knot only: parameter t = 2 pi i / n instead of uniform */
+    double a, b, c;      /* shape parameters (above) */
+    double pos_sigma;    /* Gaussian positional noise in unit-cube units (x largest extent x 1.1) */
+    double angle_deg;    /* frames rotated by a N(0, angle) angle in a random 2-plane */
+    double spot_frac;    /* round(n spot_frac) extra samples uniform in the box, frames S - S^T, S in U[-1,1] */
+    uint64_t seed;
+} epr_sampler;
+
+/* n samples (plus the outliers) in world coordinates: pos (total x dim), packed frames
+ * (total x dim(dim-1)/2) copied to host buffers; total receives n + round(n spot_frac).  pos and
+ * skew may both be NULL to query total. */
+int epr_generate_samples(int device, const epr_sampler *sampler, size_t n, double *pos, double *skew, size_t *total);
+
+/* Generates the samples into the context's device memory, maps them to the unit cube there
+ * (ExteriorPoisson::ToUnitCube) and sets them as its samples (what epr_set_samples does with host
+ * arrays), without a host round trip.  xform (may be NULL) receives the (dim+1)^2 map. */
+int epr_set_generated_samples(epr_ctx *ctx, const epr_sampler *sampler, size_t n, double *xform);
 
 /* Hierarchical solution coefficients of one level after epr_solve (what the reference writes to
  * its .tree file: level 0 regular, level d > 0 the residual x[d] - P x[d-1]). */

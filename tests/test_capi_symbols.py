@@ -61,3 +61,21 @@ def test_batch_argument_checks_host_only():
     handles = (ctypes.c_void_p * 2)(None, None)
     assert lib.epr_batch_solve(handles, 2, 1, 0, st, status) == -1
     assert b"null context" in lib.epr_global_error()
+
+
+def test_sampler_arguments_host_only():
+    """epr_generate_samples checks its arguments and reports the output size without the GPU."""
+    import ctypes
+    lib = epr.load()
+    total = ctypes.c_size_t(0)
+    sp = epr.sampler("link", pos_sigma=0.005, spot_frac=0.1)
+    assert lib.epr_generate_samples(0, ctypes.byref(sp), 1000, None, None, ctypes.byref(total)) == epr.EPR_OK
+    assert total.value == 1100
+    assert lib.epr_generate_samples(0, None, 1000, None, None, ctypes.byref(total)) == -1
+    assert lib.epr_generate_samples(0, ctypes.byref(sp), 0, None, None, ctypes.byref(total)) == -1
+    bad = epr.sampler("knot")
+    bad.shape = 9
+    assert lib.epr_generate_samples(0, ctypes.byref(bad), 10, None, None, ctypes.byref(total)) == -1
+    neg = epr.sampler("helix", pos_sigma=-1.0)
+    assert lib.epr_generate_samples(0, ctypes.byref(neg), 10, None, None, ctypes.byref(total)) == -1
+    assert b"non-negative" in lib.epr_global_error()
