@@ -214,3 +214,42 @@ def test_full_size_mixed_precision_reaches_double_energy():
     assert s1["fit_energy"] == s2["fit_energy"] and np.array_equal(x1, x2)
     assert s2["initial_energy"] == s64["initial_energy"]
     r.close()
+
+
+def _edge_case(name):
+    rng = np.random.default_rng(0)
+
+    def frames(n):
+        return epr.pack_skew(epr.samples.curve_frames(rng.normal(size=(n, 3))))
+
+    if name == "one_sample":
+        return np.array([[0.31, 0.52, 0.47]]), frames(1)
+    if name == "two_in_one_cell":
+        return np.array([[0.31, 0.52, 0.47], [0.312, 0.521, 0.471]]), frames(2)
+    # samples on the faces and the far corner of the cube (keys clamped to the last cell)
+    p = rng.uniform(0, 1, (200, 3))
+    p[:20, 0] = 0.0
+    p[20:40, 1] = 1.0
+    p[40:50] = 1.0
+    return p, frames(200)
+
+
+@pytest.mark.parametrize("name", ["one_sample", "two_in_one_cell", "faces"])
+def test_edge_inputs_match_oracle(name):
+    """Inputs at the edges of the reference's sample handling: a single sample, coincident samples
+    in one cell, samples on the cube's faces."""
+    pu, sk = _edge_case(name)
+    depth = 4
+    o = O.Oracle(3, depth)
+    o.set_samples(pu, sk)
+    o.build()
+    r = epr.Reconstructor(3, depth, pu, sk)
+    assert rel(r.get("measure"), o.get("measure")) < 1e-12
+    assert rel(r.get("noise"), o.get("noise")) < 1e-9
+    assert rel(r.get("S"), o.get("S")) < 1e-11
+    for l in (depth, 0):
+        assert rel(r.get("B", l), o.get("B", l)) < 1e-11
+        assert rel(r.get("R", l), o.get("R", l)) < 1e-10
+    st = r.solve()
+    _, _, eo = o.solve()
+    assert abs(st["fit_energy"] - eo[1]) < 1e-9 * eo[1] and abs(st["reg_energy"] - eo[2]) < 1e-9 * eo[2]
