@@ -237,7 +237,11 @@ def _edge_case(name):
 @pytest.mark.parametrize("name", ["one_sample", "two_in_one_cell", "faces"])
 def test_edge_inputs_match_oracle(name):
     """Inputs at the edges of the reference's sample handling: a single sample, coincident samples
-    in one cell, samples on the cube's faces."""
+    in one cell, samples on the cube's faces.  With one or two coincident samples the covariance is
+    rank-deficient and its smallest eigenvalues are rounding noise, so the noise value itself is
+    not reproducible across machines (the oracle gives 2.5 on x86 and -4.7e7 on Arm for the single
+    sample); what the solve uses is the weight exp(-noise^2 / (2 nSigma^2)), which saturates there
+    (0 and 1), and that is compared."""
     pu, sk = _edge_case(name)
     depth = 4
     o = O.Oracle(3, depth)
@@ -245,7 +249,11 @@ def test_edge_inputs_match_oracle(name):
     o.build()
     r = epr.Reconstructor(3, depth, pu, sk)
     assert rel(r.get("measure"), o.get("measure")) < 1e-12
-    assert rel(r.get("noise"), o.get("noise")) < 1e-9
+    weight = lambda v: np.exp(-v * v / (2 * 0.25 * 0.25))
+    if name == "faces":
+        assert rel(r.get("noise"), o.get("noise")) < 1e-9
+    with np.errstate(over="ignore"):
+        assert np.abs(weight(r.get("noise")) - weight(o.get("noise"))).max() < 1e-12
     assert rel(r.get("S"), o.get("S")) < 1e-11
     for l in (depth, 0):
         assert rel(r.get("B", l), o.get("B", l)) < 1e-11
