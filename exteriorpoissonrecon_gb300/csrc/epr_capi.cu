@@ -964,7 +964,14 @@ int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, doubl
         ctx->fail(EPR_ERR_ARG, "unknown kernel '%s'", kernel);
         ok = false;
     }
+    const bool dfLevel = ctx->lvlDF(level) && k == "gs";
     auto run = [&]() {
+        if (dfLevel)
+        {
+            // one colour of a double-float level (its point-split kernel on pairs of floats)
+            epr::launch_gs_colour_df(epr::level_ptrs<epr::df>(ctx, level), 0, ctx->d_err, ctx->stream, ctx->d_kexp);
+            return;
+        }
         epr::with_dim(ctx, [&](auto dd) {
             constexpr int D = decltype(dd)::value;
             if (fp32)

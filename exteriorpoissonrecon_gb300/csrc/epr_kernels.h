@@ -52,6 +52,7 @@ void launch_df_pull(const df *in, double *out, int64_t n, const int *kexp, int l
 void launch_d2df(const double *in, df *out, int64_t n, cudaStream_t s);
 int launch_gs_sweeps_df(const LevelPtrs<df> &L, int iters, unsigned int *err, cudaStream_t s, int separate,
                         int64_t persistentMaxNodes, int *kexp);
+void launch_gs_colour_df(const LevelPtrs<df> &L, int colour, unsigned int *err, cudaStream_t s, int *kexp);
 // iters full sweeps (all 2^D colours in order); levels of at most persistentMaxNodes nodes run all
 // sweeps inside one thread block, larger ones launch one kernel per colour.  Returns the number of
 // kernels launched.

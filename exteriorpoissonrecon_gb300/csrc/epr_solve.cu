@@ -1290,6 +1290,15 @@ void launch_d2df(const double *in, df *out, int64_t n, cudaStream_t s)
     if (n) d2df_kernel<<<(unsigned)std::min<int64_t>(blocks_for(n, 256), 1024), 256, 0, s>>>(in, out, n);
 }
 
+// one colour of a double-float level with the per-colour kernel of the sweeps below (profiling)
+void launch_gs_colour_df(const LevelPtrs<df> &L, int colour, unsigned int *err, cudaStream_t s, int *kexp)
+{
+    Grid<3> g(L.level);
+    Colour<3> col(g, colour);
+    if (col.n == 0) return;
+    gs_colour_split3_kernel<df><<<(unsigned)((col.n + kSplitNodes - 1) / kSplitNodes), 128 * kSplitNodes, 0, s>>>(L, col, 0, err, 0, kexp);
+}
+
 // Paired GS sweeps of a 3D double-float level (levels 0-3): the same kernels as a float or double
 // level of that size, with the wedge factor of the level's exponent and a new exponent after every
 // sweep.

@@ -1,6 +1,7 @@
 """Launches one kernel family of the solve path a few times on a built problem, for profilers.
 
     python -m exteriorpoissonrecon_gb300.profile_kernels --dim 3 --depth 7 --kernel gs --reps 3
+    python -m exteriorpoissonrecon_gb300.profile_kernels --depth 8 --level 3 --band df --kernel gs
 
 Builds the named synthetic workload on the GPU, sets seeded random coefficients on the finest
 level and times `reps` launches of the kernel (plus one warm-up launch) with CUDA events through
@@ -27,11 +28,13 @@ def main():
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--precision", default="fp32")
     ap.add_argument("--level", type=int, default=None)
+    ap.add_argument("--band", default=None, help="with --precision fp32: df or fp64 arithmetic for levels 2-3")
     a = ap.parse_args()
     wl = a.workload or ("link" if a.dim == 3 else "clifford")
     pos, frames = epr.samples.make_workload(wl, a.samples, seed=0)
     pu, _ = epr.unit_cube(pos)
-    r = epr.Reconstructor(a.dim, a.depth, pu, epr.pack_skew(frames), precision=a.precision)
+    band = dict(fp64_from=2, fp64_levels=4, band_precision=a.band) if a.band else {}
+    r = epr.Reconstructor(a.dim, a.depth, pu, epr.pack_skew(frames), precision=a.precision, **band)
     level = a.depth if a.level is None else a.level
     n = r.nodes(level)
     rng = np.random.default_rng(0)
