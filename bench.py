@@ -8,22 +8,27 @@ one in the xz-plane centred at (1,0,0)), 1M samples uniform in arc length, Gauss
 noise sigma 0.005 (unit-cube units), 5 degree angular noise, plus 10% uniform spot outliers with
 random frames; 3D, depth 8 (257^3 nodes x 2 channels = 33.9M unknowns), code-default parameters.
 
-One step = one full solve from the built system (fresh initial guess each time): the reference's
-cascadic paired Gauss-Seidel schedule with FP32 smoothing except on levels 2-3, which run in
-double-float (pairs of floats with a power-of-two exponent per level: the named configuration's
-FP64 coarse solve; the cascadic solve leaves the zero stationary point there, and double precision
-keeps the double run's local minimum), FP64 energies and reductions.  The line also reports the
-all-double run, the same band in double, and the all-float run of the same schedule.
---workload batch: 64 small reconstructions (torus knots + helices, depths 5-7) solved concurrently,
-in solves/s.  `value` is the
-device time per solve with the system resident in HBM; `e2e` repeats the whole public-API
-pipeline per step from host buffers (samples host->device, build, solve, solution device->host).
-Every array of a level exceeds the 129 MB L2 (coefficients 137 MB in FP32, stencils 3.7 GB), so no
-flush is inserted between steps.
+Metric: the time of one solve from the built system that ends at the energy of the all-FP64 run
+of the reference's schedule to 1e-6 relative (energies evaluated in FP64).  One step = one full
+solve (fresh initial guess): the reference's cascadic paired Gauss-Seidel schedule with FP32
+relaxation, except levels 0-3, which relax in FP64 (there the cascadic solve sits at the zero
+stationary point and leaves it from components that float rounding would change: with those levels
+in double the depth-8 grid stays within 1e-5 relative L2 of the FP64 run).  The line reports the
+FP64 run's energy and the result's distance from it (`target`, `error_vs_fp64`), and other
+precision bands beside the configured one (`variants`).  `value` is the device time per solve with
+the system resident in HBM (CUDA events on the library's stream); `e2e` repeats the whole
+public-API pipeline per step from host buffers (samples host->device, build, solve, solution
+device->host).  Every array of a level exceeds the 129 MB L2 (coefficients 137 MB in FP32,
+stencils 3.7 GB), so no flush is inserted between steps.
+--workload batch: 64 small reconstructions (torus knots + helices, depths 5-7) solved
+concurrently, in solves/s.
 
---impl reference times the CPU restatement of the reference algorithm (oracle/, the reference's
-cascadic paired Gauss-Seidel schedule, all host threads) on a bounded sample of the same input
-(depth 6 build + sweeps) and scales its node-update rate to the depth-8 schedule.
+--impl reference runs the CPU restatement of the reference's cascadic solve (oracle/, FP64, all
+host threads) on the same input and depth: one complete solve, timed in --steps parts of about
+equal node updates whose times add up to the solve (the build runs before them, untimed).  The
+reference's own binaries are compiled from its sources, which the GPU machine does not have.
+`cpu_baseline` of the GB300 line is a shorter estimate: sweeps of the same input at a smaller depth,
+scaled by node updates.
 """
 from __future__ import annotations
 
@@ -42,7 +47,6 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "Depth-8 time-to-1e-6-residual, learned+FP32 vs plain FP64 GPU; stencil HBM GB/s"
 
 # DRAM bytes (read + write) per colour node of one 3D FP32 colour launch, from ncu captures of the
 # depth-7 launch (profiles/gs_colour_lanes_kernel_link_depth7_fp32.txt,
@@ -63,14 +67,14 @@ def parse():
     ap.add_argument("--samples", type=int, default=1_000_000)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--fp64-levels", type=int, default=None,
-                    help="with fp32: levels fp64-from .. fp64-levels-1 relax in double (default 2..3 in 3D: the "
+                    help="with fp32: levels fp64-from .. fp64-levels-1 relax in double (default 0..3 in 3D: the "
                          "named configuration's FP64 coarse solve, where the cascadic solve leaves the zero "
-                         "stationary point, which keeps the double run's local minimum; none in 4D, where the "
-                         "all-float solve already has the double energy to 1e-9)")
+                         "stationary point; with them in double the result stays within 1e-5 of the double run; "
+                         "none in 4D, where the all-float solve already has the double energy to 1e-9)")
     ap.add_argument("--fp64-from", type=int, default=None)
-    ap.add_argument("--band-precision", default="df", choices=["df", "fp64"],
-                    help="arithmetic of the band's 3D levels up to 3: df = double-float on the FP32 pipe with a "
-                         "power-of-two exponent per level (default), fp64 = double")
+    ap.add_argument("--band-precision", default="fp64", choices=["df", "fp64"],
+                    help="arithmetic of the band's 3D levels up to 3: fp64 = double (default), df = double-float "
+                         "on the FP32 pipe with a power-of-two exponent per level")
     ap.add_argument("--solver", default="cascadic", choices=["cascadic", "multigrid"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -81,6 +85,14 @@ def parse():
                          "solved concurrently (torus knots + helices, depths 5-7)")
     ap.add_argument("--batch", type=int, default=64, help="reconstructions per batch")
     ap.add_argument("--batch-threads", type=int, default=0, help="host workers of the batch (0: 32)")
+    ap.add_argument("--profile-kernel", default=None,
+                    help="launch one kernel family a few times for a profiler instead of benchmarking: gs, energy, "
+                         "quadfit, prolong, gn, lgs, residual, assemble, biquad (with --depth, --samples, "
+                         "--profile-level, --profile-reps, --precision, --profile-band)")
+    ap.add_argument("--profile-level", type=int, default=None, help="level of --profile-kernel (default: finest)")
+    ap.add_argument("--profile-reps", type=int, default=3)
+    ap.add_argument("--profile-band", default=None, choices=["df", "fp64"],
+                    help="with --profile-kernel and --precision fp32: levels 2-3 in this arithmetic")
     return ap.parse_args()
 
 
@@ -197,8 +209,8 @@ def cpu_reference(pu, sk, depth, cpu_depth, steps, warmup, dim=3):
             times.append(dt)
     per_update = statistics.mean(times) / N
     full = per_update * schedule_node_updates(dim, depth)
-    return {"value": full, "unit": "s", "cores": cores, "kind": "port",
-            "sample": (f"oracle build + {steps} paired-GS sweeps at depth {cpu_depth} "
+    return {"value": full, "unit": "s", "cores": cores, "kind": "port", "estimate": True,
+            "sample": (f"estimate: oracle build + {steps} paired-GS sweeps at depth {cpu_depth} "
                        f"({N} nodes, FP64) of the same {len(pu)}-sample input; per-node-update time "
                        f"{per_update * 1e9:.1f} ns scaled to the depth-{depth} cascadic schedule "
                        f"({schedule_node_updates(dim, depth)} node updates); build took {build_s:.1f} s")}
@@ -410,10 +422,123 @@ def bench_batch(args, ws, rank, local, pg):
         print(json.dumps(line))
 
 
+def profile_kernel(args, depth):
+    """Builds the workload, sets seeded random coefficients on one level and times `reps` launches
+    (plus one warm-up launch) of one kernel family through epr_time_kernel: the launches a
+    profiler captures."""
+    import exteriorpoissonrecon_gb300 as epr
+    pu, sk = workload(args.samples, args.dim)
+    band = (dict(fp64_from=2, fp64_levels=4, band_precision=args.profile_band)
+            if args.profile_band and args.precision == "fp32" else {})
+    r = epr.Reconstructor(args.dim, depth, pu, sk, precision=args.precision, **band)
+    level = depth if args.profile_level is None else args.profile_level
+    n = r.nodes(level)
+    rng = np.random.default_rng(0)
+    r.set_coefficients(level, rng.uniform(-0.1, 0.1, n), rng.uniform(-0.1, 0.1, n))
+    ms = r.time_kernel(args.profile_kernel, level, args.profile_reps)
+    print(json.dumps({"kernel": args.profile_kernel, "dim": args.dim, "depth": depth, "level": level, "nodes": n,
+                      "precision": args.precision, "samples": int(len(pu)), "ms_per_launch": ms}))
+
+
+def precision_by_level(args, depth, dim):
+    """Arithmetic of each level's relaxation in the configured run ("f32", "f64" or "df": pairs of
+    floats with a power-of-two exponent per level); energies, norms and reductions are FP64 on
+    every level."""
+    out = {}
+    for l in range(depth + 1):
+        if args.precision == "fp64":
+            out[str(l)] = "f64"
+        elif args.fp64_from <= l < args.fp64_levels:
+            out[str(l)] = "df" if (args.band_precision == "df" and dim == 3 and l <= 3
+                                   and args.solver == "cascadic") else "f64"
+        else:
+            out[str(l)] = "f32"
+    return out
+
+
+def metric_name(dim, depth, levels):
+    band = sorted(int(l) for l, p in levels.items() if p != "f32")
+    kinds = sorted({levels[str(l)] for l in band})
+    prec = ("FP64 throughout" if all(p == "f64" for p in levels.values()) else
+            "FP32 relaxation" + (f", {'/'.join(k.upper() for k in kinds)} levels {band[0]}-{band[-1]}" if band else ""))
+    shape = "3D link" if dim == 3 else "4D Clifford-torus"
+    return (f"Depth-{depth} {shape} reconstruction: solve time to the FP64 schedule's energy (1+1e-6); "
+            f"{prec}, FP64 energies")
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def cpu_reference_full(pu, sk, dim, depth, steps, warmup):
+    """The CPU restatement of the reference's cascadic solve (oracle/, FP64, all host threads) on
+    the whole workload: one complete solve of the depth-`depth` system, split into `steps` timed
+    parts of about equal node updates (whole sweeps in schedule order), so each part is a bounded
+    piece of CPU work and their sum is the measured time of one solve.  The build runs before the
+    timed parts; `warmup` untimed sweeps of a level-5 scratch problem warm the thread pool."""
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    o = O.Oracle(dim, depth, threads=cores)
+    o.set_samples(pu, sk)
+    t0 = time.perf_counter()
+    o.build()
+    build_s = time.perf_counter() - t0
+    wl = min(depth, 5)
+    rng = np.random.default_rng(0)
+    xw, yw = rng.uniform(-1e-2, 1e-2, o.nodes(wl)), rng.uniform(-1e-2, 1e-2, o.nodes(wl))
+    for _ in range(warmup):
+        xw, yw = o.gs(wl, xw, yw, 1)
+    steps = max(int(steps), 1)
+    times = []
+    total = None
+    done = False
+    for k in range(steps):
+        t0 = time.perf_counter()
+        if total is None:
+            total = o.solve_begin()  # the random start belongs to the solve
+        target = total if k == steps - 1 else (k + 1) * total // steps
+        done = o.solve_advance(target)
+        if k == steps - 1:
+            e = o.solve_finish()  # the final energy evaluation belongs to the solve too
+        times.append(time.perf_counter() - t0)
+    assert done, "the stepped solve did not complete"
+    solve_s = sum(times)
+    return {"value": solve_s, "unit": "s", "cores": cores, "kind": "port", "cpu": cpu_model(),
+            "sample": (f"one complete depth-{depth} cascadic solve (FP64, {total} node updates) of the same "
+                       f"{len(pu)}-sample input by the CPU restatement of the reference, measured in {steps} "
+                       f"parts of about equal node updates whose times add up to the solve; the build before it "
+                       f"took {build_s:.1f} s (untimed)"),
+            "energy": float(e[1] + e[2]), "initial_energy": float(e[0]), "build_s": build_s,
+            "part_s": [round(t, 4) for t in times]}
+
+
+def xy_errors(x, y, X, Y):
+    """Relative L2 distance of (x, y) from (X, Y) over both channels, as they are and after the
+    rotation of the (x, y) plane that aligns them best (the energy is invariant under rotating
+    (x, y): the wedge, screening and Dirichlet terms are, and so is the frame term since B is
+    antisymmetric)."""
+    n = float(np.sqrt((X * X + Y * Y).sum()))
+    raw = float(np.sqrt(((x - X) ** 2 + (y - Y) ** 2).sum())) / n
+    th = math.atan2(float((x * Y - y * X).sum()), float((x * X + y * Y).sum()))
+    c, s = math.cos(th), math.sin(th)
+    rot = float(np.sqrt(((c * x - s * y - X) ** 2 + (s * x + c * y - Y) ** 2).sum())) / n
+    return raw, rot, th
+
+
 def main():
     args = parse()
     ws, rank, local, pg = dist_setup(args)
     depth = args.depth if args.depth is not None else (8 if args.dim == 3 else 6)
+    if args.profile_kernel:
+        return profile_kernel(args, depth)
     if args.workload == "batch":
         if args.dim != 3:
             raise SystemExit("the batched workload is 3D")
@@ -421,27 +546,30 @@ def main():
     if args.fp64_levels is None:
         args.fp64_levels = 4 if args.dim == 3 else 0
     if args.fp64_from is None:
-        args.fp64_from = 2 if args.dim == 3 else 0
+        args.fp64_from = 0
     cpu_depth = args.cpu_depth if args.dim == 3 else min(args.cpu_depth, 4)
     dim = args.dim
     pu, sk = workload(args.samples, dim)
+    levels = precision_by_level(args, depth, dim)
+    metric = metric_name(dim, depth, levels)
     name = f"link-1M+10%spot-3D-depth{depth}" if dim == 3 else f"clifford-torus-1M-4D-depth{depth}"
     config = {"workload": name, "samples": int(len(pu)), "depth": depth,
               "dim": dim, "nodes": (2 ** depth + 1) ** dim, "unknowns": 2 * (2 ** depth + 1) ** dim,
               "solver": args.solver, "precision": args.precision,
               "fp64_levels": [args.fp64_from, args.fp64_levels] if args.precision == "fp32" else None,
               "band_precision": args.band_precision if args.precision == "fp32" else None,
+              "precision_by_level": levels, "energy_precision": "f64",
               "l2": "inputs larger than L2 (no flush)",
               "parallelism": f"replicas{ws}"}
 
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_reference(pu, sk, depth, cpu_depth, args.steps, args.warmup, dim)
-        line = {"metric": METRIC, "value": cb["value"], "unit": "s", "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": cb["value"] * 1e3, "higher_is_better": False,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": config, "impl": "reference", "cpu_baseline": cb,
+        cb = cpu_reference_full(pu, sk, dim, depth, args.steps, args.warmup)
+        line = {"metric": metric, "value": cb["value"], "unit": "s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": cb["value"] * 1e3 / max(args.steps, 1),
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": config, "impl": "reference", "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -490,7 +618,8 @@ def main():
         r2.close()
     e2e_v = allmax(pg, statistics.mean(e2e_s)) if e2e_s else None
 
-    line = {"metric": METRIC, "value": per_step_s, "unit": "s", "n_gpus": ws, "steps": args.steps,
+    energy = st["fit_energy"] + st["reg_energy"]  # evaluated in FP64 from the result's coefficients
+    line = {"metric": metric, "value": per_step_s, "unit": "s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step_s * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
             "data": "synthetic", "config": config, "clocks": clk, "gpu_launches": int(launches),
@@ -498,45 +627,51 @@ def main():
             "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "parts": e2e_parts[-1] if e2e_parts else None},
             "build_ms": build_ms, "wall_s": wall,
-            "final_energy": st["fit_energy"] + st["reg_energy"], "initial_energy": st["initial_energy"],
+            "final_energy": energy, "initial_energy": st["initial_energy"],
             "unknown_sweeps_per_s": 2 * schedule_node_updates(dim, depth) / per_step_s}
-    # error of the result against the double-precision run of the same schedule (the CUDA FP64
-    # path reproduces the reference's algorithm to 1e-9 on the pinned cases)
+    # the target energy: the all-FP64 run of the same schedule (the CUDA FP64 path reproduces the
+    # reference's algorithm to 1e-9 on the pinned cases), and the result's distance from it
     if args.precision == "fp32" and not args.no_fp64_check:
-        xs32 = r.coefficients(depth)[0]
+        xs32 = r.coefficients(depth)
+        lv32 = [r.coefficients(l) for l in range(depth + 1)]
         r64 = epr.Reconstructor(dim, depth, pu, sk, precision="fp64", solver=args.solver, device=local)
         st64 = r64.solve()
-        xs64 = r64.coefficients(depth)[0]
-        e32, e64 = line["final_energy"], st64["fit_energy"] + st64["reg_energy"]
-        line["error_vs_fp64"] = {"energy_fp64": e64, "energy_rel_diff": (e32 - e64) / e64,
-                                 "finest_x_rel_l2": float(np.linalg.norm(xs32 - xs64) / np.linalg.norm(xs64)),
-                                 "fp64_solve_s": st64["solve_ms"] / 1e3}
-        # the same schedule with every level in float: faster, but the cascadic solve leaves the zero
-        # stationary point at levels 3-4 from components that rounding decides, so it ends in another
-        # local minimum
-        rm = epr.Reconstructor(dim, depth, pu, sk, precision="fp32", fp64_levels=0, solver=args.solver, device=local)
-        for _ in range(3):
-            stm = rm.solve()
-        em = stm["fit_energy"] + stm["reg_energy"]
-        xsm = rm.coefficients(depth)[0]
-        line["all_levels_fp32"] = {
-            "fp64_levels": 0, "solve_s": stm["solve_ms"] / 1e3, "energy": em, "energy_rel_diff_vs_fp64": (em - e64) / e64,
-            "finest_x_rel_l2_vs_fp64": float(np.linalg.norm(xsm - xs64) / np.linalg.norm(xs64)),
-            "speedup_vs_fp64_solve": st64["solve_ms"] / stm["solve_ms"]}
-        line["error_vs_fp64"]["speedup_vs_fp64_solve"] = st64["solve_ms"] / (per_step_s * 1e3)
-        rm.close()
-        if args.fp64_levels > args.fp64_from:
-            # the same band in the other arithmetic (double against double-float)
-            other = "fp64" if args.band_precision == "df" else "df"
-            rb = epr.Reconstructor(dim, depth, pu, sk, precision="fp32", fp64_levels=args.fp64_levels,
-                                   fp64_from=args.fp64_from, band_precision=other, solver=args.solver, device=local)
+        e64 = st64["fit_energy"] + st64["reg_energy"]
+        xs64 = r64.coefficients(depth)
+        lv64 = [r64.coefficients(l) for l in range(depth + 1)]
+        raw, rot, th = xy_errors(xs32[0], xs32[1], xs64[0], xs64[1])
+        per_level = [xy_errors(a[0], a[1], b[0], b[1])[0] for a, b in zip(lv32, lv64) if np.any(b[0]) or np.any(b[1])]
+        g64 = r64.gradient(depth)
+        g32 = r64.gradient(depth, xs32[0], xs32[1])  # the result's gradient, in FP64
+        line["target"] = {"energy_fp64_schedule": e64, "energy": energy, "tolerance": 1e-6,
+                          "rel": (energy - e64) / e64, "reached": bool(energy <= e64 * (1 + 1e-6))}
+        line["error_vs_fp64"] = {"energy_fp64": e64, "energy_rel_diff": (energy - e64) / e64,
+                                 "xy_rel_l2": raw, "xy_rel_l2_rotation_aligned": rot, "rotation_rad": th,
+                                 "max_level_xy_rel_l2": max(per_level),
+                                 "grad_norm": float(np.sqrt((g32[0] ** 2 + g32[1] ** 2).sum())),
+                                 "grad_norm_fp64_run": float(np.sqrt((g64[0] ** 2 + g64[1] ** 2).sum())),
+                                 "fp64_solve_s": st64["solve_ms"] / 1e3,
+                                 "speedup_vs_fp64_solve": st64["solve_ms"] / (per_step_s * 1e3)}
+        # the same schedule with other precision bands, beside the configured one
+        variants = {"all_levels_fp32": dict(fp64_levels=0)}
+        if dim == 3:
+            variants["df_levels_2_3"] = dict(fp64_from=2, fp64_levels=4, band_precision="df")
+            other = "df" if args.band_precision == "fp64" else "fp64"
+            variants[f"{other}_levels_{args.fp64_from}_{args.fp64_levels - 1}"] = dict(
+                fp64_from=args.fp64_from, fp64_levels=args.fp64_levels, band_precision=other)
+        line["variants"] = {}
+        for vname, kw in variants.items():
+            rv = epr.Reconstructor(dim, depth, pu, sk, precision="fp32", solver=args.solver, device=local, **kw)
             for _ in range(3):
-                stb = rb.solve()
-            eb = stb["fit_energy"] + stb["reg_energy"]
-            line[f"band_{other}"] = {"solve_s": stb["solve_ms"] / 1e3, "energy": eb,
-                                     "energy_rel_diff_vs_fp64": (eb - e64) / e64,
-                                     "speedup_vs_fp64_solve": st64["solve_ms"] / stb["solve_ms"]}
-            rb.close()
+                sv = rv.solve()
+            ev = sv["fit_energy"] + sv["reg_energy"]
+            xv = rv.coefficients(depth)
+            vr, vrot, _ = xy_errors(xv[0], xv[1], xs64[0], xs64[1])
+            line["variants"][vname] = {"solve_s": sv["solve_ms"] / 1e3, "energy": ev,
+                                       "energy_rel_diff_vs_fp64": (ev - e64) / e64, "xy_rel_l2": vr,
+                                       "xy_rel_l2_rotation_aligned": vrot,
+                                       "speedup_vs_fp64_solve": st64["solve_ms"] / sv["solve_ms"]}
+            rv.close()
         r64.close()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference(pu, sk, depth, cpu_depth, 2, 1, dim)

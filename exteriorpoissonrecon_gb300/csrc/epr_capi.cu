@@ -21,7 +21,6 @@
 #include "epr_kernels.h"
 #include "epr_mg.h"
 #include "epr_poly.h"
-#include "epr_setup.h"
 
 namespace {
 
@@ -235,14 +234,20 @@ LevelPtrs<Real> level_ptrs(Context *c, int l)
     return p;
 }
 
+// Energies are evaluated in double at every level, whatever arithmetic the level relaxes in: a
+// float or double-float level's working copy is first converted into its double coefficients,
+// and the element integrals, stencil forms and sums run on the double stencils, which every level
+// keeps resident.  (The float energy kernel remains for epr_energy_noalloc's float mode and the kernel timer.)
 bool Context::energy(int l, double *out3)
 {
-    bool fp32 = lvl32(l);
-    if (lvlDF(l) && !pull_xy(l)) return false;  // evaluated in double
+    if (lvl32(l) || lvlDF(l))
+    {
+        if (!pull_xy(l)) return false;
+        launches++;
+    }
     with_dim(this, [&](auto dd) {
         constexpr int D = decltype(dd)::value;
-        if (fp32) launch_energy<D, float>(level_ptrs<float>(this, l), levels[l].xy32, red, stream);
-        else launch_energy<D, double>(level_ptrs<double>(this, l), levels[l].xy64, red, stream);
+        launch_energy<D, double>(level_ptrs<double>(this, l), levels[l].xy64, red, stream);
         return 0;
     });
     launches += 2;

@@ -24,7 +24,9 @@
 namespace epr {
 namespace {
 
-// block partials (4 per block, kMaxBlocks blocks) followed by the 4 raw sums of the final pass
+// block partials (4 per block, kMaxBlocks blocks) followed by the 4 raw sums of the final pass;
+// the energy reduction never uses more than kMaxBlocks blocks whatever the level's size, so this
+// array serves every level the library accepts (0..10 in 3D, 0..7 in 4D)
 constexpr int kScratchDoubles = 4 * Reduce::kMaxBlocks + 4;
 static __device__ __align__(256) double g_energy_scratch[kScratchDoubles];
 
@@ -63,6 +65,30 @@ double *scratch_for_device(int device, const char **err)
 
 thread_local char g_noalloc_error[256];
 
+// Makes `device` current for the lifetime of the guard and puts the caller's current device back
+// afterwards, so that a host passing another device than its current one keeps its own setting.
+class DeviceGuard
+{
+  public:
+    DeviceGuard() = default;
+    bool select(int device)
+    {
+        if (cudaGetDevice(&saved_) != cudaSuccess) { cudaGetLastError(); return false; }
+        if (saved_ == device) return true;
+        if (cudaSetDevice(device) != cudaSuccess) { cudaGetLastError(); return false; }
+        restore_ = true;
+        return true;
+    }
+    ~DeviceGuard()
+    {
+        if (restore_) cudaSetDevice(saved_);
+    }
+
+  private:
+    int saved_ = 0;
+    bool restore_ = false;
+};
+
 }  // namespace
 }  // namespace epr
 
@@ -83,18 +109,11 @@ extern "C" int epr_energy_noalloc(int device, int dim, int level, int precision,
     if (precision != EPR_FP64 && precision != EPR_FP32) return fail(EPR_ERR_ARG, "unknown precision");
     if (!xy || !A || !B || !out3) return fail(EPR_ERR_ARG, "null device pointer");
     if (device < 0 || device >= kMaxDevices) return fail(EPR_ERR_ARG, "device ordinal out of range");
-    // the reduction uses at most kMaxBlocks blocks whatever the level size; check the bound the
-    // fixed array is sized for before touching it
-    int64_t N = 1, NE = 1;
-    for (int d = 0; d < dim; d++) { N *= (int64_t)((1 << level) + 1); NE *= (int64_t)(1 << level); }
-    int64_t blocks = ((N > NE ? N : NE) + 127) / 128;
-    if (blocks > Reduce::kMaxBlocks) blocks = Reduce::kMaxBlocks;
-    if (4 * blocks + 4 > kScratchDoubles) return fail(EPR_ERR_ARG, "level needs more scratch than the fixed array holds");
-    if (cudaSetDevice(device) != cudaSuccess)
-    {
-        cudaGetLastError();
-        return fail(EPR_ERR_CUDA, "cannot select the CUDA device");
-    }
+    static_assert(kScratchDoubles >= 4 * Reduce::kMaxBlocks + 4, "the reduction's block partials must fit");
+    int64_t N = 1;
+    for (int d = 0; d < dim; d++) N *= (int64_t)((1 << level) + 1);
+    DeviceGuard guard;
+    if (!guard.select(device)) return fail(EPR_ERR_CUDA, "cannot select the CUDA device");
     const char *err = nullptr;
     double *scratch = scratch_for_device(device, &err);
     if (!scratch) return fail(EPR_ERR_CUDA, err ? err : "cudaGetSymbolAddress failed");

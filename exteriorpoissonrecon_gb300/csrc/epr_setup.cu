@@ -28,7 +28,7 @@
 #include <cub/cub.cuh>
 
 #include "epr_common.cuh"
-#include "epr_setup.h"
+#include "epr_context.h"
 
 namespace epr {
 

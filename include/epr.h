@@ -161,8 +161,11 @@ int epr_gn_matvec(epr_ctx *ctx, int level, const double *dx, const double *dy, d
 /* Runs the configured solver; stats may be NULL. */
 int epr_solve(epr_ctx *ctx, epr_stats *stats);
 /* Builds (build != 0) and solves n independent reconstructions concurrently on one GPU: `threads`
- * host threads (<= 0: 8) each take whole reconstructions, largest first, and drive them on the
- * contexts' own streams, so their kernels overlap on the device.  The contexts must be distinct and
+ * host threads (<= 0: 8) each take whole reconstructions, largest first, and drive each one on a
+ * non-blocking stream the worker owns (created together, so that concurrent workers sit on
+ * distinct hardware work queues), so their kernels overlap on the device.  A context's own stream
+ * is synchronised before the worker takes the context over and gets the context back afterwards;
+ * when the call returns nothing is in flight on either stream.  The contexts must be distinct and
  * on the same device; they may differ in dim, depth, samples and parameters, and each computes
  * exactly what epr_build + epr_solve compute for it alone.  stats[i] and status[i] (either may be
  * NULL) receive context i's statistics and return code.  Returns EPR_OK, or the code of the first
@@ -225,11 +228,12 @@ int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, doubl
  *         node i at [o * N + i]), 3^dim N values of the precision's type;
  *   out3  3 doubles: fitting energy, regularisation energy, wedge square norm (as epr_energy).
  * The work is enqueued on `stream` (NULL = default stream) of `device`; the caller synchronises.
- * The block partial sums use a fixed 128 KiB device array inside the library (one copy per GPU,
- * held until exit); levels up to 10 (3D) / 7 (4D) fit, anything needing more is rejected.  The
- * first call on a device looks the array's address up and caches it, so make that first call
- * before any stream capture.  Calls that overlap on the GPU share the array and race: serialise
- * them.  Errors: epr_noalloc_last_error(). */
+ * The caller's current device is left as it was.  The block partial sums use a fixed 128 KiB
+ * device array inside the library (one copy per GPU, held until exit), which holds the partial
+ * sums of any level; the accepted levels are the library's range, 0..10 (3D) / 0..7 (4D), and
+ * other levels are rejected.  The first call on a device looks the array's address up and caches
+ * it, so make that first call before any stream capture.  Calls that overlap on the GPU share the
+ * array and race: serialise them.  Errors: epr_noalloc_last_error(). */
 int epr_energy_noalloc(int device, int dim, int level, int precision, const void *xy, const void *A,
                        const void *B, double c, double *out3, void *stream);
 const char *epr_noalloc_last_error(void);

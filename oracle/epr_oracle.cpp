@@ -1232,16 +1232,38 @@ struct Oracle
     // the linearisation of the wedge residual; the result is half the Hessian of the GN model.
     void gnMatvec(int level, const double *x, const double *y, const double *dx, const double *dy, double *ox, double *oy) const
     {
+        GridIdx<D> g(1 << level);
+        size_t N = g.nodes();
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < (long)N; i++) gnNode(level, g, (size_t)i, x, y, dx, dy, &ox[i], &oy[i]);
+    }
+
+    // the Gauss-Newton product at the nodes idx[0..n) only (out[k] belongs to node idx[k]): the
+    // same per-node arithmetic, for comparisons at sizes where the whole product is too slow here
+    void gnMatvecAt(int level, const double *x, const double *y, const double *dx, const double *dy, const int64_t *idx,
+                    size_t n, double *ox, double *oy) const
+    {
+        GridIdx<D> g(1 << level);
+#pragma omp parallel for schedule(static)
+        for (long k = 0; k < (long)n; k++) gnNode(level, g, (size_t)idx[k], x, y, dx, dy, &ox[k], &oy[k]);
+    }
+
+    void quadfitAt(int level, const double *x, const double *y, const int64_t *idx, size_t n, double *out) const
+    {
+        GridIdx<D> g(1 << level);
+#pragma omp parallel for schedule(static)
+        for (long k = 0; k < (long)n; k++) quadfitNode(level, g, (size_t)idx[k], x, y, &out[(size_t)k * 5]);
+    }
+
+    void gnNode(int level, const GridIdx<D> &g, size_t i, const double *x, const double *y, const double *dx,
+                const double *dy, double *ox, double *oy) const
+    {
         const LevelSystem &L = levels[level];
         int r = 1 << level;
-        GridIdx<D> g(r);
-        size_t N = g.nodes();
         double vol = std::pow(1. / r, D);
-#pragma omp parallel for schedule(static)
-        for (long i = 0; i < (long)N; i++)
         {
             int I[D];
-            g.node((size_t)i, I);
+            g.node(i, I);
             double sx = 0, sy = 0;
             for (int c = 0; c < (1 << D); c++)
             {
@@ -1275,8 +1297,8 @@ struct Oracle
                 }
             }
             const double *a = &L.A[(size_t)i * T::S];
-            ox[i] = sx + ColumnDot(g, a, I, dx);
-            oy[i] = sy + ColumnDot(g, a, I, dy);
+            *ox = sx + ColumnDot(g, a, I, dx);
+            *oy = sy + ColumnDot(g, a, I, dy);
         }
     }
 
@@ -1708,6 +1730,71 @@ struct Oracle
         }
     }
 
+    // The cascadic schedule of solve() (ExteriorPoisson.h:315-409, paired GS only) run in pieces,
+    // so that a caller can time one whole solve in several bounded parts: begin() sets the random
+    // start, advance() relaxes whole sweeps in schedule order (prolonging at each level's end)
+    // until `target` node updates have been done since begin(), finish() returns the energies.
+    // The arithmetic is solve()'s, sweep for sweep.
+    struct Stepper
+    {
+        std::vector<std::vector<double>> X, Y;
+        int level = 0, sweep = 0, minD = 0, maxD = 0;
+        int64_t done = 0, total = 0;
+    } st;
+
+    int64_t sweepsAt(int l) const { return (int64_t)std::ceil(std::pow(P.i_mult, depth - l) * P.gs_iters); }
+
+    int64_t solveBegin()
+    {
+        st = Stepper();
+        st.minD = std::min(P.min_solve_depth, depth);
+        st.maxD = P.max_solve_depth < 0 ? depth : std::min(P.max_solve_depth, depth);
+        st.X.resize(depth + 1);
+        st.Y.resize(depth + 1);
+        for (int l = 0; l <= depth; l++) { st.X[l].assign(NumNodes(D, l), 0.); st.Y[l].assign(NumNodes(D, l), 0.); }
+        srand(P.seed);
+        std::vector<double> &X0 = st.X[st.minD], &Y0 = st.Y[st.minD];
+        for (size_t i = 0; i < X0.size(); i++) { X0[i] = RandomDouble(); Y0[i] = RandomDouble(); }
+        double e[3];
+        energy(st.minD, X0.data(), Y0.data(), e);
+        double s = std::sqrt(std::sqrt(c / e[2]));
+        for (size_t i = 0; i < X0.size(); i++) { X0[i] *= s; Y0[i] *= s; }
+        st.level = st.minD;
+        for (int l = st.minD; l <= st.maxD; l++) st.total += sweepsAt(l) * (int64_t)NumNodes(D, l);
+        return st.total;
+    }
+
+    // returns 1 when the schedule is complete
+    int solveAdvance(int64_t target)
+    {
+        while (st.level <= st.maxD && st.done < target)
+        {
+            const int l = st.level;
+            gs(l, st.X[l].data(), st.Y[l].data(), 1);
+            st.done += (int64_t)NumNodes(D, l);
+            if (++st.sweep == sweepsAt(l))
+            {
+                if (l < st.maxD)
+                {
+                    std::vector<double> px(st.X[l + 1].size()), py(st.Y[l + 1].size());
+                    prolong(l, st.X[l].data(), px.data());
+                    prolong(l, st.Y[l].data(), py.data());
+                    for (size_t i = 0; i < px.size(); i++) { st.X[l + 1][i] += px[i]; st.Y[l + 1][i] += py[i]; }
+                }
+                st.level++;
+                st.sweep = 0;
+            }
+        }
+        return st.level > st.maxD ? 1 : 0;
+    }
+
+    void solveFinish(double *eout)
+    {
+        double e[3];
+        energy(st.maxD, st.X[st.maxD].data(), st.Y[st.maxD].data(), e);
+        eout[0] = c; eout[1] = e[0]; eout[2] = e[1];
+    }
+
     long get(const std::string &name, int level, double *out) const
     {
         auto put = [&](const std::vector<double> &v) { if (out) std::copy(v.begin(), v.end(), out); return (long)v.size(); };
@@ -1882,6 +1969,22 @@ int epr_oracle_quadfit(epr_oracle *o, int level, const double *x, const double *
     return 0;
 }
 
+int epr_oracle_quadfit_at(epr_oracle *o, int level, const double *x, const double *y, const int64_t *idx, size_t n,
+                          double *out)
+{
+    if (!o) return -1;
+    DISPATCH(o, { self->quadfitAt(level, x, y, idx, n, out); });
+    return 0;
+}
+
+int epr_oracle_gn_matvec_at(epr_oracle *o, int level, const double *x, const double *y, const double *dx,
+                            const double *dy, const int64_t *idx, size_t n, double *ox, double *oy)
+{
+    if (!o) return -1;
+    DISPATCH(o, { self->gnMatvecAt(level, x, y, dx, dy, idx, n, ox, oy); });
+    return 0;
+}
+
 int epr_oracle_gradient(epr_oracle *o, int level, const double *x, const double *y, double *gx, double *gy)
 {
     if (!o) return -1;
@@ -1972,6 +2075,27 @@ int epr_oracle_gn_matvec(epr_oracle *o, int level, const double *x, const double
 {
     if (!o) return -1;
     DISPATCH(o, { self->gnMatvec(level, x, y, dx, dy, ox, oy); });
+    return 0;
+}
+
+int64_t epr_oracle_solve_begin(epr_oracle *o)
+{
+    if (!o) return -1;
+    DISPATCH(o, { return self->solveBegin(); });
+    return -1;
+}
+
+int epr_oracle_solve_advance(epr_oracle *o, int64_t target_node_updates)
+{
+    if (!o) return -1;
+    DISPATCH(o, { return self->solveAdvance(target_node_updates); });
+    return -1;
+}
+
+int epr_oracle_solve_finish(epr_oracle *o, double *energies_out)
+{
+    if (!o) return -1;
+    DISPATCH(o, { self->solveFinish(energies_out); });
     return 0;
 }
 

@@ -14,6 +14,7 @@
 #ifndef EPR_ORACLE_H
 #define EPR_ORACLE_H
 #include <stddef.h>
+#include <stdint.h>
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -69,6 +70,11 @@ int epr_oracle_energy(epr_oracle *o, int level, const double *x, const double *y
 /* quadraticFit at every node: out is N x 5 (Q20, Q02, Q11, Q10, Q01), SystemEnergy.h:542-643 */
 int epr_oracle_quadfit(epr_oracle *o, int level, const double *x, const double *y, double *out);
 /* gradient of the energy: gx, gy (N each) */
+/* quadfit / Gauss-Newton product at the nodes idx[0..n) only (row k belongs to node idx[k]) */
+int epr_oracle_quadfit_at(epr_oracle *o, int level, const double *x, const double *y, const int64_t *idx, size_t n,
+                          double *out);
+int epr_oracle_gn_matvec_at(epr_oracle *o, int level, const double *x, const double *y, const double *dx,
+                            const double *dy, const int64_t *idx, size_t n, double *ox, double *oy);
 int epr_oracle_gradient(epr_oracle *o, int level, const double *x, const double *y, double *gx, double *gy);
 /* paired Gauss-Seidel, iters full sweeps over the 2^Dim parity colours (ExteriorPoissonSolvers.h:156-196) */
 int epr_oracle_gs(epr_oracle *o, int level, double *x, double *y, int iters);
@@ -104,6 +110,12 @@ int epr_oracle_gn_matvec(epr_oracle *o, int level, const double *x, const double
 /* cascadic solve (ExteriorPoisson.h:315-409); x_out,y_out receive the hierarchical coefficients of
  * every level concatenated (level 0 first); energies_out = (E0, fit, reg). */
 int epr_oracle_solve(epr_oracle *o, double *x_out, double *y_out, double *energies_out);
+/* The same cascadic solve in pieces: begin (random start; returns the schedule's node updates),
+ * advance (whole sweeps in order until target node updates are done; 1 when complete), finish
+ * (energies as epr_oracle_solve's: c, fit, reg). */
+int64_t epr_oracle_solve_begin(epr_oracle *o);
+int epr_oracle_solve_advance(epr_oracle *o, int64_t target_node_updates);
+int epr_oracle_solve_finish(epr_oracle *o, double *energies_out);
 
 #ifdef __cplusplus
 }

@@ -64,6 +64,9 @@ def lib():
         L.epr_oracle_energy.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P]
         L.epr_oracle_quadfit.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P]
         L.epr_oracle_gradient.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, P]
+        I64 = ctypes.POINTER(ctypes.c_int64)
+        L.epr_oracle_quadfit_at.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, I64, ctypes.c_size_t, P]
+        L.epr_oracle_gn_matvec_at.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, P, I64, ctypes.c_size_t, P, P]
         L.epr_oracle_gs.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, ctypes.c_int]
         L.epr_oracle_prolong.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P]
         L.epr_oracle_gs_shifted.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, ctypes.c_int, P, P]
@@ -80,6 +83,10 @@ def lib():
         L.epr_oracle_mg_vcycle.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, ctypes.c_int, ctypes.c_int]
         L.epr_oracle_gn_matvec.argtypes = [ctypes.c_void_p, ctypes.c_int, P, P, P, P, P, P]
         L.epr_oracle_solve.argtypes = [ctypes.c_void_p, P, P, P]
+        L.epr_oracle_solve_begin.restype = ctypes.c_int64
+        L.epr_oracle_solve_begin.argtypes = [ctypes.c_void_p]
+        L.epr_oracle_solve_advance.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+        L.epr_oracle_solve_finish.argtypes = [ctypes.c_void_p, P]
         _lib = L
     return _lib
 
@@ -163,6 +170,25 @@ class Oracle:
         lib().epr_oracle_quadfit(self._h, level, _p(np.ascontiguousarray(x, np.float64)),
                                  _p(np.ascontiguousarray(y, np.float64)), _p(out))
         return out
+
+    def quadfit_at(self, level, x, y, idx):
+        """quadfit rows of the nodes idx only."""
+        idx = np.ascontiguousarray(idx, np.int64)
+        out = np.zeros((len(idx), 5))
+        lib().epr_oracle_quadfit_at(self._h, level, _p(np.ascontiguousarray(x, np.float64)),
+                                    _p(np.ascontiguousarray(y, np.float64)),
+                                    idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), len(idx), _p(out))
+        return out
+
+    def gn_matvec_at(self, level, x, y, dx, dy, idx):
+        """Gauss-Newton product at the nodes idx only."""
+        idx = np.ascontiguousarray(idx, np.int64)
+        ox = np.zeros(len(idx))
+        oy = np.zeros(len(idx))
+        a = [np.ascontiguousarray(v, np.float64) for v in (x, y, dx, dy)]
+        lib().epr_oracle_gn_matvec_at(self._h, level, *[_p(v) for v in a],
+                                      idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), len(idx), _p(ox), _p(oy))
+        return ox, oy
 
     def gradient(self, level, x, y):
         gx = np.zeros(self.nodes(level))
@@ -262,3 +288,18 @@ class Oracle:
             ys.append(y[off:off + n])
             off += n
         return xs, ys, e
+
+    def solve_begin(self) -> int:
+        """Starts the cascadic solve (random start); returns its total node updates."""
+        return int(lib().epr_oracle_solve_begin(self._h))
+
+    def solve_advance(self, target_node_updates: int) -> bool:
+        """Relaxes whole sweeps in schedule order until target node updates are done; True when the
+        schedule is complete."""
+        return bool(lib().epr_oracle_solve_advance(self._h, int(target_node_updates)))
+
+    def solve_finish(self):
+        """(c, fit energy, regularisation energy) of the stepped solve."""
+        e = np.zeros(3)
+        lib().epr_oracle_solve_finish(self._h, _p(e))
+        return e

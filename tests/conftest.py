@@ -13,7 +13,12 @@ def pytest_configure(config):
 
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
+# fixtures with every probe the harness writes (including the multigrid and bi-quadratic probes)
 GOLDEN_CASES = ["knot3_d4", "link3_d4", "cliff4_d3"]
+# every fixture of a full build + solve: the cases above plus the plain-method configuration
+# exactly as specified (torus knot, 4096 regular samples, depth 5), which stores the build, the
+# energies, fits, sweeps and the solve but not the probes pinned at depth 4 already
+SOLVE_CASES = GOLDEN_CASES + ["knot3_d5"]
 
 
 def load_golden(name):

@@ -35,7 +35,12 @@ CASES = [
     ("knot3_d4", "knot", 4096, 0, 4, [2, 4]),
     ("link3_d4", "link", 6000, 3, 4, [1, 4]),
     ("cliff4_d3", "clifford", 4000, 5, 3, [1, 2]),
+    # the plain-method configuration exactly: (3,2) torus knot, 4096 samples regular in t, no
+    # noise, depth 5 (33^3 nodes)
+    # (stencils of level 3 only, and no multigrid probes: those are pinned at depth 4 already)
+    ("knot3_d5", "knot", 4096, 0, 5, [3]),
 ]
+SLIM = {"knot3_d5"}
 
 # solver variants of the reference's CLI: name, base case, extra harness flags
 VARIANTS = [
@@ -113,7 +118,8 @@ def make(name, workload, n, seed, depth, stencil_levels):
             fx[f"skew_l{l}"] = L(f"skew_l{l}")
         for k in ("mg_M", "mg_b", "mg_gs1", "mg_v1", "mg_v2", "qa_x", "qa_y", "qa_dx", "qa_dy", "qa_u", "qa_v",
                   "qa_gx", "qa_gy", "qa_biquad", "qa_step", "qa_newton"):
-            fx[k] = L(k)
+            if name not in SLIM:
+                fx[k] = L(k)
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **fx)
     print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB")
@@ -139,6 +145,12 @@ def make_tree(name, workload, n, seed, depth, flags):
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: make -C oracle ref")
+    only = set(sys.argv[1:])  # fixture names to (re)write; all when none are given
+    if only:
+        for case in CASES:
+            if case[0] in only:
+                make(*case)
+        sys.exit(0)
     for case in CASES:
         make(*case)
     for v in VARIANTS:

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import exteriorpoissonrecon_gb300 as epr
-from conftest import GOLDEN_CASES, load_golden
+from conftest import SOLVE_CASES, load_golden
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -20,7 +20,7 @@ def rel(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
-@pytest.fixture(scope="module", params=GOLDEN_CASES)
+@pytest.fixture(scope="module", params=SOLVE_CASES)
 def built(request):
     g = load_golden(request.param)
     dim = g["pos"].shape[1]
@@ -72,6 +72,23 @@ def test_quadfit_and_gs(built):
         assert rel(gy, g[f"gsy_d{l}"]) < 1e-11
 
 
+def test_gradient(built):
+    """epr_gradient against the linear terms of the reference's quadraticFit (SystemEnergy.h:542-643):
+    1e-11 in FP64; the FP32 context's float kernel within 1e-5."""
+    g, r, dim, depth = built
+    r32 = epr.Reconstructor(dim, depth, g["pos"], g["skew"], precision="fp32")
+    for key in g:
+        if not key.startswith("quadfit_d"):
+            continue
+        l = int(key[len("quadfit_d"):])
+        x, y = g[f"xr_d{l}"], g[f"yr_d{l}"]
+        gx, gy = r.gradient(l, x, y)
+        assert rel(gx, g[key][:, 3]) < 1e-11 and rel(gy, g[key][:, 4]) < 1e-11
+        fx, fy = r32.gradient(l, x, y)
+        assert rel(fx, g[key][:, 3]) < 1e-5 and rel(fy, g[key][:, 4]) < 1e-5
+    r32.close()
+
+
 def test_cascadic_solve_matches_reference(built):
     g, r, dim, depth = built
     st = r.solve()
@@ -112,6 +129,8 @@ def test_system_upload_path():
 
 @pytest.mark.parametrize("dim,depth,workload,n", [(3, 6, "link", 60000), (4, 4, "clifford", 60000)])
 def test_against_oracle_larger(dim, depth, workload, n):
+    """Build, energy, fits, gradient, sweeps and the Gauss-Newton product against the oracle on
+    inputs larger than the fixtures: FP64 to 1e-10 - 1e-12, the FP32 kernels to 1e-5."""
     pos, frames = epr.samples.make_workload(workload, n, seed=11)
     pu, _ = epr.unit_cube(pos)
     sk = epr.pack_skew(frames)
@@ -141,6 +160,62 @@ def test_against_oracle_larger(dim, depth, workload, n):
     mx, my = r.gn_matvec(depth, dx, dy)
     omx, omy = o.gn_matvec(depth, x, y, dx, dy)
     assert rel(mx, omx) < 1e-11 and rel(my, omy) < 1e-11
+    ogx, ogy = o.gradient(depth, x, y)
+    gx, gy = r.gradient(depth, x, y)
+    assert rel(gx, ogx) < 1e-11 and rel(gy, ogy) < 1e-11
+    # the float kernels (gradient = the fit's linear terms, Gauss-Newton product) within 1e-5
+    r32 = epr.Reconstructor(dim, depth, pu, sk, precision="fp32")
+    fx, fy = r32.gradient(depth, x, y)
+    assert rel(fx, ogx) < 1e-5 and rel(fy, ogy) < 1e-5
+    r32.set_coefficients(depth, x, y)
+    fmx, fmy = r32.gn_matvec(depth, dx, dy)
+    assert rel(fmx, omx) < 1e-5 and rel(fmy, omy) < 1e-5
+    e32 = r32.energy(depth, x, y)
+    # evaluated in double from the float context's coefficients (x, y rounded to float on upload)
+    assert rel(e32, eo) < 1e-6
+    r32.close()
+
+
+def test_against_oracle_4d_depth5():
+    """4D at depth 5 (33^4 = 1,185,921 nodes, 81-point stencils), the largest 4D size whose oracle
+    comparison fits test time: the build (measure, S, B, R on three levels) and the energy in full,
+    the quadratic fits, gradient and Gauss-Newton product at 3,000 sampled nodes (the oracle's
+    per-node arithmetic; a whole 4D fit there takes minutes on the CPU).  FP64 to 1e-10 - 1e-12,
+    the FP32 kernels to 1e-5."""
+    dim, depth = 4, 5
+    pos, frames = epr.samples.make_workload("clifford", 100000, seed=11)
+    pu, _ = epr.unit_cube(pos)
+    sk = epr.pack_skew(frames)
+    o = O.Oracle(dim, depth)
+    o.set_samples(pu, sk)
+    o.build()
+    r = epr.Reconstructor(dim, depth, pu, sk)
+    assert rel(r.get("measure"), o.get("measure")) < 1e-12
+    assert rel(r.get("S"), o.get("S")) < 1e-11
+    for l in (depth, depth - 1, 0):
+        assert rel(r.get("B", l), o.get("B", l)) < 1e-11
+        assert rel(r.get("R", l), o.get("R", l)) < 1e-10
+    rng = np.random.default_rng(1)
+    N = o.nodes(depth)
+    x, y = rng.uniform(-1, 1, N), rng.uniform(-1, 1, N)
+    dx, dy = rng.uniform(-1, 1, N), rng.uniform(-1, 1, N)
+    eo = o.energy(depth, x, y)
+    assert rel(r.energy(depth, x, y), eo) < 1e-12
+    idx = np.sort(rng.choice(N, 3000, replace=False))
+    qo = o.quadfit_at(depth, x, y, idx)
+    assert rel(r.quadfit(depth, x, y)[idx], qo) < 1e-11
+    omx, omy = o.gn_matvec_at(depth, x, y, dx, dy, idx)
+    r.set_coefficients(depth, x, y)
+    mx, my = r.gn_matvec(depth, dx, dy)
+    assert rel(mx[idx], omx) < 1e-11 and rel(my[idx], omy) < 1e-11
+    r32 = epr.Reconstructor(dim, depth, pu, sk, precision="fp32")
+    fx, fy = r32.gradient(depth, x, y)
+    assert rel(fx[idx], qo[:, 3]) < 1e-5 and rel(fy[idx], qo[:, 4]) < 1e-5
+    r32.set_coefficients(depth, x, y)
+    fmx, fmy = r32.gn_matvec(depth, dx, dy)
+    assert rel(fmx[idx], omx) < 1e-5 and rel(fmy[idx], omy) < 1e-5
+    r32.close()
+    r.close()
 
 
 @pytest.mark.parametrize("name", ["knot3_d4_separate", "knot3_d4_single", "knot3_d4_seed7_min2"])
@@ -192,27 +267,36 @@ def test_double_band_keeps_the_double_minimum():
     assert abs(e["band"] - e["fp64"]) < 1e-6 * e["fp64"]
 
 
-def test_full_size_mixed_precision_reaches_double_energy():
-    """The benchmark's full size (3D link, 1.1M samples, depth 8, 257^3 nodes): the float solve with
-    levels 2-3 in double-float ends at the all-double solve's energy to 1e-6, and a repeated solve
-    (graph replay) gives the same bits.  Size-independent checks, as the oracle cannot run this size
-    in test time."""
+def _xy_rel_l2(x, y, X, Y):
+    return float(np.sqrt(((x - X) ** 2 + (y - Y) ** 2).sum() / (X * X + Y * Y).sum()))
+
+
+def test_full_size_mixed_precision_matches_double_run():
+    """The benchmark's full size (3D link, 1.1M samples, depth 8, 257^3 nodes): FP32 relaxation
+    with levels 0-3 in FP64 ends at the all-double run's energy to 1e-6 (both evaluated in FP64)
+    and its finest grid within 1e-5 relative L2 of the double run's, every coarser level too; a
+    repeated solve (graph replay) gives the same bits.  Size-independent checks, as the oracle
+    cannot run this size in test time."""
     pos, fr = epr.samples.make_workload("link", 1_000_000, seed=0)
     pu, _ = epr.unit_cube(pos)
     sk = epr.pack_skew(fr)
     r64 = epr.Reconstructor(3, 8, pu, sk, precision="fp64")
     s64 = r64.solve()
     e64 = s64["fit_energy"] + s64["reg_energy"]
+    ref = [r64.coefficients(l) for l in range(9)]
     r64.close()
-    r = epr.Reconstructor(3, 8, pu, sk, precision="fp32", fp64_from=2, fp64_levels=4, band_precision="df")
+    r = epr.Reconstructor(3, 8, pu, sk, precision="fp32", fp64_from=0, fp64_levels=4, band_precision="fp64")
     s1 = r.solve()
-    x1 = r.coefficients(8)[0]
+    x1 = r.coefficients(8)
     s2 = r.solve()
-    x2 = r.coefficients(8)[0]
+    x2 = r.coefficients(8)
     e = s2["fit_energy"] + s2["reg_energy"]
     assert abs(e - e64) < 1e-6 * e64, (e, e64)
-    assert s1["fit_energy"] == s2["fit_energy"] and np.array_equal(x1, x2)
+    assert s1["fit_energy"] == s2["fit_energy"] and np.array_equal(x1[0], x2[0]) and np.array_equal(x1[1], x2[1])
     assert s2["initial_energy"] == s64["initial_energy"]
+    for l in range(9):
+        xl = r.coefficients(l)
+        assert _xy_rel_l2(xl[0], xl[1], *ref[l]) < 1e-5, l
     r.close()
 
 

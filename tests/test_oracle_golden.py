@@ -4,7 +4,7 @@ largest magnitude; FP64 throughout."""
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, load_golden
+from conftest import GOLDEN_CASES, SOLVE_CASES, load_golden
 from oracle import oracle as O
 
 
@@ -15,15 +15,29 @@ def rel(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
-@pytest.fixture(scope="module", params=GOLDEN_CASES)
+_BUILT = {}
+
+
+def _built(name):
+    if name not in _BUILT:
+        g = load_golden(name)
+        dim = g["pos"].shape[1]
+        depth = int(g["depth"])
+        o = O.Oracle(dim, depth)
+        o.set_samples(g["pos"], g["skew"])
+        o.build()
+        _BUILT[name] = (g, o, dim, depth)
+    return _BUILT[name]
+
+
+@pytest.fixture(scope="module", params=SOLVE_CASES)
 def case(request):
-    g = load_golden(request.param)
-    dim = g["pos"].shape[1]
-    depth = int(g["depth"])
-    o = O.Oracle(dim, depth)
-    o.set_samples(g["pos"], g["skew"])
-    o.build()
-    return g, o, dim, depth
+    return _built(request.param)
+
+
+@pytest.fixture(scope="module", params=GOLDEN_CASES)
+def probe_case(request):
+    return _built(request.param)
 
 
 def test_unit_cube(case):
@@ -91,6 +105,39 @@ def test_quadfit_and_gs(case):
         assert rel(gy, g[f"gsy_d{l}"]) < 1e-11
 
 
+def test_gradient(case):
+    """dE/dx_i and dE/dy_i: the linear terms of the reference's quadraticFit at every node
+    (SystemEnergy.h:542-643; its generic gradient d() needs quadraticApproximation, which the
+    reconstructor's energy does not implement, SystemEnergy.h:248-254, 321-333), and central
+    differences of the energy (the SystemEnergy.h:345-361 check) at a few nodes."""
+    g, o, dim, depth = case
+    for key in g:
+        if not key.startswith("quadfit_d"):
+            continue
+        l = int(key[len("quadfit_d"):])
+        x, y = g[f"xr_d{l}"], g[f"yr_d{l}"]
+        gx, gy = o.gradient(l, x, y)
+        assert rel(gx, g[key][:, 3]) < 1e-11
+        assert rel(gy, g[key][:, 4]) < 1e-11
+    l = depth
+    x, y = g[f"xr_d{l}"], g[f"yr_d{l}"]
+    gx, gy = o.gradient(l, x, y)
+    h = 1e-4 * max(np.abs(x).max(), np.abs(y).max())
+    rng = np.random.default_rng(3)
+    for i in rng.choice(len(x), 4, replace=False):
+        for which, gv in ((0, gx), (1, gy)):
+            e = []
+            for sgn in (1.0, -1.0):
+                xp, yp = x.copy(), y.copy()
+                (xp if which == 0 else yp)[i] += sgn * h
+                v = o.energy(l, xp, yp)
+                e.append(v[0] + v[1])
+            fd = (e[0] - e[1]) / (2 * h)
+            # the energy is quartic in one coefficient: the central difference is off by h^2 / 6
+            # times its third derivative
+            assert abs(fd - gv[i]) <= 1e-6 * max(np.abs(gv).max(), 1e-300), (i, which, fd, gv[i])
+
+
 def test_prolongation(case):
     g, o, dim, depth = case
     for l in range(depth):
@@ -106,6 +153,19 @@ def test_cascadic_solve(case):
     for l in range(depth + 1):
         assert rel(xs[l], g[f"solx_d{l}"]) < 1e-9
         assert rel(ys[l], g[f"soly_d{l}"]) < 1e-9
+
+
+def test_stepped_solve(case):
+    """The cascadic solve run in parts (as the benchmark's CPU arm times it) ends at the reference's
+    energies: the same sweeps in the same order."""
+    g, o, dim, depth = case
+    total = o.solve_begin()
+    for k in range(5):
+        done = o.solve_advance(total if k == 4 else (k + 1) * total // 5)
+    assert done
+    e = o.solve_finish()
+    ref = g["sol_energies"]
+    assert abs(e[1] - ref[0]) < 1e-10 * ref[0] and abs(e[2] - ref[1]) < 1e-10 * ref[1]
 
 
 ORACLE_NAMES = {"separate": "separate", "singleLevel": "single_level", "gsIters": "gs_iters", "seed": "seed",
@@ -130,9 +190,9 @@ def test_solver_variants(name):
         assert rel(ys[l], g[f"soly_d{l}"]) < 1e-9
 
 
-def test_linear_multigrid(case):
+def test_linear_multigrid(probe_case):
     """GSRelaxer sweep and MGSolver V-cycles (MG.h:57-72, 150-187) on M = R + dWeight K."""
-    g, o, dim, depth = case
+    g, o, dim, depth = probe_case
     M, b = g["mg_M"], g["mg_b"]
     x = o.linear_gs(depth, M, b, np.zeros_like(b))
     assert rel(x, g["mg_gs1"]) < 1e-12
@@ -142,10 +202,10 @@ def test_linear_multigrid(case):
     assert rel(x2, g["mg_v2"]) < 1e-10
 
 
-def test_wedge_gram(case):
+def test_wedge_gram(probe_case):
     """u^T G_x v = <x^u, x^v> and <u^y, v^y> against the reference's bilinear wedge integral."""
     from conftest import stencil_apply
-    g, o, dim, depth = case
+    g, o, dim, depth = probe_case
     Gx = o.wedge_gram(depth, g["qa_x"])
     Gy = o.wedge_gram(depth, g["qa_y"])
     U, V = g["qa_u"], g["qa_v"]
@@ -155,8 +215,8 @@ def test_wedge_gram(case):
     assert rel(gy, g["qa_gy"]) < 1e-12
 
 
-def test_biquadratic_fit_and_line_searches(case):
-    g, o, dim, depth = case
+def test_biquadratic_fit_and_line_searches(probe_case):
+    g, o, dim, depth = probe_case
     x, y, dx, dy = g["qa_x"], g["qa_y"], g["qa_dx"], g["qa_dy"]
     q = o.biquadratic_fit(depth, x, y, dx, dy, as_reference=True)
     assert rel(q, g["qa_biquad"]) < 1e-12
@@ -170,11 +230,11 @@ def test_biquadratic_fit_and_line_searches(case):
         assert abs(p - (e[0] + e[1])) < 1e-11 * abs(p)
 
 
-def test_alternating_system_and_solve(case):
+def test_alternating_system_and_solve(probe_case):
     """The half-step systems are the exact quadratic models of E in one field (checked against the
     exact bi-quadratic expansion); AlternatingSolve never increases the energy."""
     from conftest import stencil_apply
-    g, o, dim, depth = case
+    g, o, dim, depth = probe_case
     x, y, d = g["qa_x"], g["qa_y"], g["qa_dx"]
     zero = np.zeros_like(x)
     for which in (0, 1):
