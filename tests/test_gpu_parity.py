@@ -271,12 +271,13 @@ def _xy_rel_l2(x, y, X, Y):
     return float(np.sqrt(((x - X) ** 2 + (y - Y) ** 2).sum() / (X * X + Y * Y).sum()))
 
 
-def test_full_size_mixed_precision_matches_double_run():
+@pytest.mark.parametrize("band", ["df", "fp64"])
+def test_full_size_mixed_precision_matches_double_run(band):
     """The benchmark's full size (3D link, 1.1M samples, depth 8, 257^3 nodes): FP32 relaxation
-    with levels 0-3 in FP64 ends at the all-double run's energy to 1e-6 (both evaluated in FP64)
-    and its finest grid within 1e-5 relative L2 of the double run's, every coarser level too; a
-    repeated solve (graph replay) gives the same bits.  Size-independent checks, as the oracle
-    cannot run this size in test time."""
+    with levels 0-3 in double-float (the benchmark's band) or in FP64 ends at the all-double run's
+    energy to 1e-6 (both evaluated in FP64) and its finest grid within 1e-5 relative L2 of the
+    double run's, every coarser level too; a repeated solve (graph replay) gives the same bits.
+    Size-independent checks, as the oracle cannot run this size in test time."""
     pos, fr = epr.samples.make_workload("link", 1_000_000, seed=0)
     pu, _ = epr.unit_cube(pos)
     sk = epr.pack_skew(fr)
@@ -285,7 +286,7 @@ def test_full_size_mixed_precision_matches_double_run():
     e64 = s64["fit_energy"] + s64["reg_energy"]
     ref = [r64.coefficients(l) for l in range(9)]
     r64.close()
-    r = epr.Reconstructor(3, 8, pu, sk, precision="fp32", fp64_from=0, fp64_levels=4, band_precision="fp64")
+    r = epr.Reconstructor(3, 8, pu, sk, precision="fp32", fp64_from=0, fp64_levels=4, band_precision=band)
     s1 = r.solve()
     x1 = r.coefficients(8)
     s2 = r.solve()
