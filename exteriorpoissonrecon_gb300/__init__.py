@@ -59,6 +59,9 @@ class Params(ctypes.Structure):
         ("separate", ctypes.c_int),
         ("fp64_from", ctypes.c_int),
         ("band_precision", ctypes.c_int),
+        ("warm_start", ctypes.c_int),
+        ("max_extra_sweeps", ctypes.c_int),
+        ("target_energy", ctypes.c_double),
     ]
 
 
@@ -118,6 +121,8 @@ class Stats(ctypes.Structure):
         ("cycles", ctypes.c_int),
         ("node_updates", ctypes.c_int64),
         ("kernel_launches", ctypes.c_int64),
+        ("extra_sweeps", ctypes.c_int),
+        ("reached_target", ctypes.c_int),
     ]
 
     def as_dict(self):
@@ -190,6 +195,29 @@ def load():
     L.epr_biquadratic_fit.argtypes = [vp, ctypes.c_int, P, P, ctypes.c_int, P]
     L.epr_step_size.argtypes = [P, P]
     L.epr_newton_update.argtypes = [P, ctypes.c_int, P]
+    # learned warm start (tensor-core U-Net)
+    F = ctypes.POINTER(ctypes.c_float)
+    L.epr_conv3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, vp, vp,
+                            ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
+    L.epr_conv3_wgrad.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp,
+                                  ctypes.c_int, vp, vp, ctypes.c_size_t, vp]
+    L.epr_conv3_wgrad_scratch.restype = ctypes.c_size_t
+    L.epr_conv3_wgrad_scratch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.epr_conv_last_error.restype = ctypes.c_char_p
+    L.epr_unet_create.restype = vp
+    L.epr_unet_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64]
+    L.epr_unet_destroy.argtypes = [vp]
+    L.epr_unet_last_error.restype = ctypes.c_char_p
+    L.epr_unet_last_error.argtypes = [vp]
+    L.epr_unet_params.argtypes = [vp, F, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t), ctypes.c_int]
+    L.epr_unet_grid.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_size_t),
+                                ctypes.POINTER(ctypes.c_size_t)]
+    L.epr_unet_input.argtypes = [vp, vp, vp]
+    L.epr_unet_target.argtypes = [vp, vp, vp]
+    L.epr_unet_forward.argtypes = [vp, vp, vp, P, vp]
+    L.epr_unet_gradients.argtypes = [vp, vp, vp, F, P]
+    L.epr_unet_train_step.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.c_float, P]
+    L.epr_unet_warm_start.argtypes = [vp, vp, P]
     _lib = L
     return L
 

@@ -347,6 +347,26 @@ class CRandom
     random_data data_;
 };
 
+bool Context::random_start(int level, double *energy_out)
+{
+    CRandom rng((unsigned int)P.seed);
+    const int64_t N = levels[level].N;
+    std::vector<double> x(N), y(N);
+    for (int64_t i = 0; i < N; i++) { x[i] = rng.next_double(); y[i] = rng.next_double(); }
+    if (!upload_xy(level, x.data(), y.data())) return false;
+    double e[3];
+    if (!energy(level, e)) return false;
+    const double s = std::sqrt(std::sqrt(c / e[2]));
+    for (int64_t i = 0; i < N; i++) { x[i] *= s; y[i] *= s; }
+    if (!upload_xy(level, x.data(), y.data())) return false;
+    if (energy_out)
+    {
+        if (!energy(level, e)) return false;
+        *energy_out = e[0] + e[1];
+    }
+    return true;
+}
+
 // host planar arrays <-> device pairs: the two arrays travel as they are and the (de)interleaving
 // runs on the device
 bool Context::upload_xy(int l, const double *x, const double *y)
@@ -431,24 +451,14 @@ bool Context::solve_cascadic()
     cudaEventRecord(ev0, stream);
     for (int l = 0; l <= depth; l++)
     {
+        if (P.warm_start && l == minD) continue;  // the given start
         if (!cuda_ok(cudaMemsetAsync(levels[l].xy64, 0, sizeof(double) * 2 * levels[l].N, stream), "clear")) return false;
         if (fp32 && !cuda_ok(cudaMemsetAsync(levels[l].xy32, 0, sizeof(float) * 2 * levels[l].N, stream), "clear")) return false;
         if (levels[l].xyd && !cuda_ok(cudaMemsetAsync(levels[l].xyd, 0, sizeof(df) * 2 * levels[l].N, stream), "clear")) return false;
     }
-    if (!cuda_ok(cudaMemsetAsync(d_kexp, 0, sizeof(int) * (depth + 1), stream), "clear")) return false;
+    if (!P.warm_start && !cuda_ok(cudaMemsetAsync(d_kexp, 0, sizeof(int) * (depth + 1), stream), "clear")) return false;
     // random initial guess at the coarsest solve level, scaled to the target's magnitude
-    {
-        CRandom rng((unsigned int)P.seed);
-        int64_t N = levels[minD].N;
-        std::vector<double> x(N), y(N);
-        for (int64_t i = 0; i < N; i++) { x[i] = rng.next_double(); y[i] = rng.next_double(); }
-        if (!upload_xy(minD, x.data(), y.data())) return false;
-        double e[3];
-        if (!energy(minD, e)) return false;
-        double s = std::sqrt(std::sqrt(c / e[2]));
-        for (int64_t i = 0; i < N; i++) { x[i] *= s; y[i] *= s; }
-        if (!upload_xy(minD, x.data(), y.data())) return false;
-    }
+    if (!P.warm_start && !random_start(minD, nullptr)) return false;
     if (P.single_level)
     {
         // prolong the initial guess to the finest solve level, clear the coarser levels and relax
@@ -490,6 +500,22 @@ bool Context::solve_cascadic()
             printf("Error[%2d]: %9.5f -> %.5f = %.5f + %.5f\n", 1 << l, e0[0] + e0[1], e1[0] + e1[1], e1[0], e1[1]);
         }
         if (l < maxD && !prolong_add(l)) return false;
+    }
+    stats.extra_sweeps = 0;
+    stats.reached_target = 0;
+    if (P.target_energy > 0)
+    {
+        // time to a target energy: the finest solve level relaxes on, one sweep at a time, until its
+        // FP64 energy reaches the target (the checks belong to the timed solve)
+        double e[3];
+        for (;;)
+        {
+            if (!energy(maxD, e)) return false;
+            if (e[0] + e[1] <= P.target_energy || stats.extra_sweeps >= P.max_extra_sweeps) break;
+            if (!gs(maxD, 1)) return false;
+            stats.extra_sweeps++;
+        }
+        stats.reached_target = e[0] + e[1] <= P.target_energy ? 1 : 0;
     }
     cudaEventRecord(ev1, stream);
     if (!check_errors()) return false;
@@ -572,6 +598,9 @@ void epr_default_params(epr_params *p)
     p->band_precision = EPR_BAND_FP64;
     p->single_level = 0;
     p->separate = 0;
+    p->warm_start = 0;
+    p->max_extra_sweeps = 0;
+    p->target_energy = 0;
 }
 
 const char *epr_global_error(void) { return g_error.c_str(); }
@@ -590,6 +619,8 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
     if (p.fp64_from < 0 || p.fp64_levels < 0) { g_error = "fp64_from and fp64_levels must not be negative"; return nullptr; }
     if (p.band_precision != EPR_BAND_FP64 && p.band_precision != EPR_BAND_DF) { g_error = "unknown band precision"; return nullptr; }
     if (p.solver == EPR_SOLVER_MULTIGRID && (p.max_cycles < 0 || !(p.tolerance >= 0))) { g_error = "bad multigrid cycle cap or tolerance"; return nullptr; }
+    if (p.max_extra_sweeps < 0 || !(p.target_energy >= 0)) { g_error = "bad target energy or extra-sweep cap"; return nullptr; }
+    if (p.warm_start && p.single_level) { g_error = "a warm start and --singleLevel cannot be combined"; return nullptr; }
     if (cudaSetDevice(p.device) != cudaSuccess)
     {
         g_error = std::string("cannot select CUDA device: ") + cudaGetErrorString(cudaGetLastError());

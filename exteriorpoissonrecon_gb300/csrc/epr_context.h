@@ -107,6 +107,10 @@ struct Context
     bool upload_xy(int l, const double *x, const double *y);
     bool download_xy(int l, double *x, double *y, bool fromSolution);
     bool solve_cascadic();
+    // the reference's random start on `level` (rand() pairs after srand(seed), scaled by the fourth
+    // root of c over the wedge square norm, ExteriorPoisson.h:333-341), set as the level's
+    // coefficients; *energy (may be null) receives its total energy
+    bool random_start(int level, double *energy);
 };
 
 // the text epr_global_error() returns (per host thread)

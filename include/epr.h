@@ -49,6 +49,9 @@
  *   epr_get_array
  *       read-only views of the reference's internal state (TreeEstimator::measure/noise/depth
  *       GridSamples.inl:838-862, S(E) ExteriorPoisson.h:290-307, _R/_B SystemEnergy.h:172-175)
+ *   epr_conv3*, epr_unet_*
+ *       no reference counterpart: the learned warm start replaces the reference's random initial
+ *       guess (ExteriorPoisson.h:333-341) and the coarse levels of its cascadic schedule
  */
 #ifndef EPR_H
 #define EPR_H
@@ -103,6 +106,13 @@ typedef struct epr_params {
                              its 3D levels up to 3 in double-float (pairs of floats, 48 bits, on the
                              FP32 pipe, with a power-of-two exponent per level) and the rest in double;
                              cascadic solver only */
+    int warm_start;       /* 1: the solve starts from the coefficients already set on level minSolveDepth
+                             (epr_set_coefficients or epr_unet_warm_start) instead of the reference's
+                             random start (0) */
+    int max_extra_sweeps; /* with target_energy: cap on the finest-level sweeps added after the schedule (0) */
+    double target_energy; /* > 0: after the schedule the finest solve level keeps relaxing, one paired
+                             Gauss-Seidel sweep at a time, until its FP64 energy is <= target_energy or
+                             max_extra_sweeps were added; the energy checks are part of the timed solve (0) */
 } epr_params;
 
 typedef struct epr_stats {
@@ -116,6 +126,8 @@ typedef struct epr_stats {
     int cycles;              /* multigrid cycles run */
     int64_t node_updates;    /* paired Gauss-Seidel node updates performed */
     int64_t kernel_launches; /* kernels this library launched during the solve */
+    int extra_sweeps;        /* finest-level sweeps added to reach target_energy */
+    int reached_target;      /* 1 when the final energy is <= target_energy (0 without a target) */
 } epr_stats;
 
 void epr_default_params(epr_params *p);
@@ -270,6 +282,65 @@ int epr_newton_update(const double *q9, int steps, double *st2);
 
 /* Waits for all work of the context. */
 int epr_synchronize(epr_ctx *ctx);
+
+/* ---- Learned warm start ------------------------------------------------------------------------
+ * No counterpart in the reference, whose solve starts from random coefficients at its coarsest solve
+ * level (ExteriorPoisson.h:333-341): a 3D convolutional U-Net (16-32-64-128 channels, 3x3x3
+ * kernels, BF16 weights and activations, FP32 accumulation on the tensor cores) predicts the
+ * regular (x, y) coefficients of one level L of the cascadic solve (L = 6: 65^3 nodes) from the
+ * density and frame splats of that level, and the solve then runs from level L (warm_start = 1,
+ * min_solve_depth = L).  The network is trained on the GPU by the library's own forward and
+ * backward kernels on solves the method computes.
+ *
+ * Activation layout of the primitives: BF16, channels-last (value of voxel v, channel c at
+ * [v * ld + c]) on an n^3 node grid (voxel index with axis 0 slowest); ld and channel offsets
+ * multiples of 8, buffers 16-byte aligned; all pointers device memory; work enqueued on `stream`. */
+
+/* out = relu?(conv3x3x3(in) + bias): cin a multiple of 16, cout in {16, 32, 48, 64, 96, 128, 192};
+ * w: cout x 27 cin BF16 (row co, column tap * cin + ci, tap = 9 (dz+1) + 3 (dy+1) + (dx+1));
+ * flip != 0 uses the neighbour v - offset instead of v + offset (the data gradient of a
+ * convolution is this with the weights transposed: row ci, column tap * cout + co). */
+int epr_conv3(int device, int n, int cin, int cout, const void *in, int ldi, const void *w, const float *bias,
+              void *out, int ldo, int relu, int flip, void *stream);
+/* dw[(tap, ci)][co] = sum_v in[v + offset(tap)][ci] dz[v][co] (FP32, 27 cin x cout, overwritten);
+ * scratch: epr_conv3_wgrad_scratch(n, cin, cout) floats of device memory. */
+int epr_conv3_wgrad(int device, int n, int cin, int cout, const void *in, int ldi, const void *dz, int ldz, float *dw,
+                    float *scratch, size_t scratch_floats, void *stream);
+size_t epr_conv3_wgrad_scratch(int n, int cin, int cout);
+const char *epr_conv_last_error(void);
+
+typedef struct epr_unet epr_unet;
+/* A network for level `level` (3..8) on `device`, He-initialised from `seed`.  NULL on error
+ * (epr_unet_last_error(NULL)). */
+epr_unet *epr_unet_create(int device, int level, uint64_t seed);
+void epr_unet_destroy(epr_unet *net);
+const char *epr_unet_last_error(const epr_unet *net);
+/* FP32 master parameters (count in *count): copied to host (set = 0) or from host (set != 0). */
+int epr_unet_params(epr_unet *net, float *host, size_t cap, size_t *count, int set);
+/* nodes per axis of the network's grid, bytes of one input (n^3 x 16 BF16), floats of one target
+ * or prediction (n^3 x 2). */
+int epr_unet_grid(const epr_unet *net, int *nodes_per_axis, size_t *input_bytes, size_t *target_floats);
+/* The network input of a built 3D context (depth >= the network's level): channel 0 the density
+ * weight, channels 1-3 the frame splat, each divided by its maximum magnitude, channels 4-15 zero;
+ * into dev_input (NULL: the network's own input buffer). */
+int epr_unet_input(epr_unet *net, epr_ctx *ctx, void *dev_input);
+/* The training target of a solved context: its level-L regular (x, y) coefficients as FP32 pairs. */
+int epr_unet_target(epr_unet *net, epr_ctx *ctx, float *dev_target);
+/* Prediction (n^3 x 2 FP32) for an input (NULL: the network's own); with dev_target, *loss is the
+ * training loss 1 - (<p,t>^2 + <p x t>^2) / (|p|^2 |t|^2), invariant under scaling and rotating p. */
+int epr_unet_forward(epr_unet *net, const void *dev_input, float *dev_pred, double *loss, const void *dev_target);
+/* Loss and the gradient of every parameter (host, count floats, the master layout) for one pair. */
+int epr_unet_gradients(epr_unet *net, const void *dev_input, const void *dev_target, float *host_grads, double *loss);
+/* One Adam step on the mean loss of `batch` (input, target) pairs in device memory. */
+int epr_unet_train_step(epr_unet *net, int batch, const void *const *dev_inputs, const void *const *dev_targets,
+                        float lr, double *loss);
+/* Warm start of a built context: predicts its level-L coefficients, scales them by the factor that
+ * minimises the energy along the prediction (E(s p) is a quartic in s: one energy evaluation gives
+ * it), and sets them as the level's coefficients; falls back to the reference's random start on
+ * that level when the scaled prediction's energy is not below both the random start's and the zero
+ * function's.  info (4 doubles, may be NULL): used (1 / 0), energy of the scaled prediction, energy
+ * of the random start, scale. */
+int epr_unet_warm_start(epr_unet *net, epr_ctx *ctx, double *info);
 
 #ifdef __cplusplus
 }
