@@ -184,6 +184,7 @@ def load():
     L.epr_get_array.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, P, ctypes.c_size_t,
                                 ctypes.POINTER(ctypes.c_size_t)]
     L.epr_synchronize.argtypes = [vp]
+    L.epr_get_density.argtypes = [vp, ctypes.c_int, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
     L.epr_time_kernel.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P]
     L.epr_energy_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp,
                                      ctypes.c_double, vp, vp]
@@ -343,6 +344,15 @@ class Reconstructor:
         out = np.zeros(n.value)
         self._check(load().epr_get_array(self._h, name.encode(), level, _p(out), n.value, ctypes.byref(n)))
         return out
+
+    def density(self, level: int) -> np.ndarray:
+        """The density estimator's data at the vertices of `level`: (nodes, 1 + dim + dim^2) =
+        weight sum, position sum, covariance sum (TreeEstimator, GridSamples.h:232-277)."""
+        n = ctypes.c_size_t(0)
+        self._check(load().epr_get_density(self._h, level, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value)
+        self._check(load().epr_get_density(self._h, level, _p(out), n.value, ctypes.byref(n)))
+        return out.reshape(self.nodes(level), -1)
 
     # ---------------------------------------------------------------- per-level operators
     def set_coefficients(self, level, x, y):

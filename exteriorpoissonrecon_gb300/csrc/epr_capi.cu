@@ -64,6 +64,13 @@ bool Context::alloc(void **p, size_t bytes, const char *what)
 {
     *p = nullptr;
     if (bytes == 0) return true;
+    if (alloc_cap && alloc_total + bytes > alloc_cap)
+    {
+        fail(EPR_ERR_NOMEM, "%s: %zu bytes exceed the allocation cap (%zu of %zu bytes allocated)", what, bytes, alloc_total,
+             alloc_cap);
+        return false;
+    }
+    alloc_total += bytes;
     return cuda_ok(cudaMallocAsync(p, bytes, stream), what);
 }
 
@@ -641,6 +648,7 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
     c->dim = dim;
     c->depth = depth;
     c->P = p;
+    if (const char *v = getenv("EPR_ALLOC_CAP_BYTES")) c->alloc_cap = (size_t)strtoull(v, nullptr, 10);
     c->levels.resize(depth + 1);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess)
@@ -974,6 +982,24 @@ int epr_get_array(epr_ctx *ctx, const char *name, int level, double *out, size_t
         return EPR_OK;
     }
     EPR_RETURN(ctx, ctx->setup.get(*ctx, nm, out, cap, count));
+}
+
+int epr_get_density(epr_ctx *ctx, int level, double *out, size_t cap, size_t *count)
+{
+    EPR_CHECK_CTX(ctx);
+    EPR_CHECK_LEVEL(ctx, level);
+    const size_t W = (size_t)(1 + ctx->dim + ctx->dim * ctx->dim);
+    const size_t num = W * (size_t)ctx->levels[level].N;
+    if (count) *count = num;
+    if (!out) return EPR_OK;
+    if ((int)ctx->setup.density.size() <= level || !ctx->setup.density[level])
+    {
+        ctx->fail(EPR_ERR_STATE, "the density estimator is not available before epr_build");
+        return EPR_ERR_STATE;
+    }
+    if (cap < num) { ctx->fail(EPR_ERR_ARG, "output too small (%zu < %zu)", cap, num); return EPR_ERR_ARG; }
+    EPR_RETURN(ctx, ctx->cuda_ok(cudaMemcpyAsync(out, ctx->setup.density[level], sizeof(double) * num, cudaMemcpyDeviceToHost, ctx->stream), "copy") &&
+                        ctx->cuda_ok(cudaStreamSynchronize(ctx->stream), "sync"));
 }
 
 int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, double *ms)

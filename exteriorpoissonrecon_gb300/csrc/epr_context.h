@@ -77,6 +77,10 @@ struct Context
     bool solved = false;
     epr_stats stats{};
     int64_t launches = 0;  // kernels launched since the last epr_solve started
+    // fault injection: device bytes this context may allocate in total (0 = no cap), from the
+    // EPR_ALLOC_CAP_BYTES environment variable at epr_create; allocations beyond it fail as an
+    // out-of-memory would (EPR_ERR_NOMEM)
+    size_t alloc_cap = 0, alloc_total = 0;
     Setup setup;
     MGHierarchy *mg = nullptr;  // linear multigrid storage (epr_mg.cu), allocated on first use
     // the relaxation sequence of the cascadic solve captured as one CUDA graph (built on the first

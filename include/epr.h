@@ -46,6 +46,9 @@
  *       Reconstructor::Reconstructor + solve (ExteriorPoisson.h:59-81) for many inputs at once
  *   epr_generate_samples / epr_set_generated_samples
  *       the Sample tool's shapes and noise              Include/Samples.h, Sample/Sample.cpp:137-199
+ *   epr_get_density
+ *       the density estimator's tree data: TreeEstimator (GridSamples.h:232-277, DensityAndNoiseInfo
+ *       GridSamples.h:79-94), which the reference writes to its .density.tree
  *   epr_get_array
  *       read-only views of the reference's internal state (TreeEstimator::measure/noise/depth
  *       GridSamples.inl:838-862, S(E) ExteriorPoisson.h:290-307, _R/_B SystemEnergy.h:172-175)
@@ -68,7 +71,9 @@ extern "C" {
 #define EPR_ERR_CUDA (-2)     /* a CUDA runtime call failed */
 #define EPR_ERR_STATE (-3)    /* call out of order (e.g. solve before build) */
 #define EPR_ERR_NUMERIC (-4)  /* a kernel produced a non-finite value */
-#define EPR_ERR_NOMEM (-5)    /* device allocation failed */
+#define EPR_ERR_NOMEM (-5)    /* device allocation failed (or exceeded the cap that the environment variable
+                                 EPR_ALLOC_CAP_BYTES, read at epr_create, sets on a context's total
+                                 allocations: fault injection for out-of-memory handling) */
 
 #define EPR_FP64 0  /* all arithmetic in double (parity with the reference to 1e-12) */
 #define EPR_FP32 1  /* smoothing / matvecs in float; energies, norms and the coarse solve in double */
@@ -215,6 +220,13 @@ int epr_set_generated_samples(epr_ctx *ctx, const epr_sampler *sampler, size_t n
 /* Hierarchical solution coefficients of one level after epr_solve (what the reference writes to
  * its .tree file: level 0 regular, level d > 0 the residual x[d] - P x[d-1]). */
 int epr_get_solution(epr_ctx *ctx, int level, double *x, double *y);
+
+/* The density estimator of a built context (TreeEstimator's splat, GridSamples.h:232-277): for each
+ * vertex of level `level` ((2^level+1)^dim, axis 0 slowest; the reference's tree nodes of depth
+ * level+1 inside the unit cube) the splatted weight sum, position sum (dim) and covariance sum
+ * (dim x dim, row-major): 1 + dim + dim^2 doubles per vertex; vertices the reference's tree never
+ * creates hold zeros.  count receives the number of doubles; out may be NULL to query it. */
+int epr_get_density(epr_ctx *ctx, int level, double *out, size_t cap, size_t *count);
 
 /* Named internal arrays copied to host memory: "measure", "noise", "depth" (per sample),
  * "S" (per finest element, packed), "leaf_depth", "R", "B" (per level, column stencils), "c".

@@ -125,8 +125,62 @@ def make(name, workload, n, seed, depth, stencil_levels):
     print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+REF_EXTRACT = os.path.join(ROOT, "oracle", "_ref", "Extract")
+REF_SIMPLICES = os.path.join(ROOT, "oracle", "_ref", "ref_simplices")
+
+
+def read_mesh(path):
+    """Vertex positions and polygon index lists of the reference's binary PLY output."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from extract_check import read_mesh as rm
+    return rm(path)
+
+
+def make_simplices():
+    """The reference's oriented simplices of the unit cube (3D and 4D) as printed by
+    oracle/ref_simplices."""
+    out = subprocess.run([REF_SIMPLICES], check=True, capture_output=True, text=True).stdout.splitlines()
+    fx, i = {}, 0
+    while i < len(out):
+        _, dim, _, num = out[i].split()
+        dim, num = int(dim), int(num)
+        rows = [list(map(int, out[i + 1 + k].split())) for k in range(num)]
+        fx[f"simplices{dim}"] = np.array(rows, dtype=np.int64).reshape(num, dim + 1, dim)
+        i += 1 + num
+    path = os.path.join(HERE, "cube_simplices.npz")
+    np.savez_compressed(path, **fx)
+    print(f"{path}: {os.path.getsize(path) / 1e6:.3f} MB")
+
+
+def make_zero_set(name, workload, n, seed, depth, ref_tree=None):
+    """The reference Extract's zero set of the reference's own reconstruction of a named workload
+    (positions are regenerated from the seeded generator; `ref_tree` reuses a .tree made already)."""
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "out")
+        tree = ref_tree
+        energies = None
+        if tree is None:
+            pos, frames = samples.make_workload(workload, n, seed=seed)
+            ply = os.path.join(td, "in.ply")
+            samples.write_ply(ply, pos, frames)
+            r = subprocess.run([REF_CLI, "--in", ply, "--out", out, "--depth", str(depth), "--aRadius", "-1", "--verbose"],
+                               check=True, capture_output=True, text=True)
+            tree = out + ".tree"
+            energies = r.stdout.strip().splitlines()[-1]
+        subprocess.run([REF_EXTRACT, "--in", tree, "--out", out + "_zero.ply"], check=True, capture_output=True)
+        V, F = read_mesh(out + "_zero.ply")
+    fx = {"depth": np.array(depth), "workload": np.array(workload), "n": np.array(n), "seed": np.array(seed),
+          "zero_vertices": V, "zero_simplices": np.array([list(f) for f in F], dtype=np.int64).reshape(len(F), -1)}
+    if energies:
+        fx["log"] = np.array(energies)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **fx)
+    print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB, {len(V)} vertices")
+
+
 def make_tree(name, workload, n, seed, depth, flags):
-    """The reference command line's own .tree output for a PLY input (frames stored in full)."""
+    """The reference command line's own .tree output for a PLY input (frames stored in full), and
+    the regular coefficient grids the reference's Extract writes from it (--grid)."""
     pos, frames = samples.make_workload(workload, n, seed=seed)
     with tempfile.TemporaryDirectory() as td:
         ply = os.path.join(td, "in.ply")
@@ -136,7 +190,18 @@ def make_tree(name, workload, n, seed, depth, flags):
                        check=True, capture_output=True)
         with open(out + ".tree", "rb") as f:
             tree = np.frombuffer(f.read(), dtype=np.uint8)
-    fx = {"depth": np.array(depth), "world_pos": pos, "frames": frames, "flags": np.array(flags, dtype=str), "tree": tree}
+        subprocess.run([REF_EXTRACT, "--in", out + ".tree", "--grid", out, "--out", out + "_zero.ply"], check=True,
+                       capture_output=True)
+        grids = []
+        for c in range(2):
+            with open(out + f".{c}.grid", "rb") as f:
+                grids.append(np.frombuffer(f.read(), dtype=np.uint8))
+        V, F = read_mesh(out + "_zero.ply")
+    fx = {"depth": np.array(depth), "world_pos": pos, "frames": frames, "flags": np.array(flags, dtype=str), "tree": tree,
+          "grid0": grids[0], "grid1": grids[1]}
+    if pos.shape[1] == 3:  # the zero curve (the oracle's extraction is 3D)
+        fx["zero_vertices"] = V
+        fx["zero_simplices"] = np.array([list(f) for f in F], dtype=np.int64).reshape(len(F), -1)
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **fx)
     print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB")
@@ -146,14 +211,29 @@ if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: make -C oracle ref")
     only = set(sys.argv[1:])  # fixture names to (re)write; all when none are given
+    TREES = [("knot3_d4_tree", "knot", 4096, 0, 4, []), ("cliff4_d3_tree", "clifford", 3000, 9, 3, ["--gsIters", "5"])]
+    # the reference's zero set of the benchmark's input (3D link, 1.1M samples, depth 8): the
+    # reference run takes ~15 minutes on 8 cores
+    ZERO_SETS = [("link3_d8_zero_set", "link", 1_000_000, 0, 8)]
     if only:
         for case in CASES:
             if case[0] in only:
                 make(*case)
+        for case in TREES:
+            if case[0] in only:
+                make_tree(*case)
+        if "cube_simplices" in only:
+            make_simplices()
+        for case in ZERO_SETS:
+            if case[0] in only:
+                make_zero_set(*case)
         sys.exit(0)
     for case in CASES:
         make(*case)
     for v in VARIANTS:
         make_variant(*v)
-    make_tree("knot3_d4_tree", "knot", 4096, 0, 4, [])
-    make_tree("cliff4_d3_tree", "clifford", 3000, 9, 3, ["--gsIters", "5"])
+    for case in TREES:
+        make_tree(*case)
+    make_simplices()
+    for case in ZERO_SETS:
+        make_zero_set(*case)

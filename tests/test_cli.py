@@ -57,6 +57,38 @@ def test_usage_and_argument_errors(cli):
     assert r.returncode == 2 and "bandPrecision" in r.stderr
 
 
+def _write(path, data: bytes):
+    with open(path, "wb") as f:
+        f.write(data)
+
+
+def test_faulty_input_files_fail_cleanly(cli):
+    """Host-side fault injection: truncated, garbled and incomplete PLY files and an empty sample
+    set end with a non-zero exit and a message, before any device work (the reference prints and
+    exits 0, Exceptions.h:102-107)."""
+    pos, fr = samples.torus_knot(64)
+    with tempfile.TemporaryDirectory() as td:
+        good = os.path.join(td, "good.ply")
+        samples.write_ply(good, pos, fr)
+        raw = open(good, "rb").read()
+        cases = {
+            "truncated.ply": (raw[:-100], "truncated"),
+            "garbled.ply": (b"plx" + raw[3:], "not a PLY"),
+            "noframes.ply": (raw.replace(b"property double skew_2_2\n", b""), "skew_2_2"),
+            "empty.ply": (raw[:raw.index(b"end_header\n") + 11].replace(b"element vertex 64", b"element vertex 0"),
+                          "Expected some samples"),
+            "missing.ply": (None, "cannot open"),
+        }
+        for name, (data, msg) in cases.items():
+            path = os.path.join(td, name)
+            if data is not None:
+                _write(path, data)
+            r = subprocess.run([cli, "--in", path, "--out", os.path.join(td, "o"), "--depth", "3"], capture_output=True,
+                               text=True, timeout=120)
+            assert r.returncode != 0 and msg in r.stderr, (name, r.returncode, r.stderr)
+            assert not os.path.exists(os.path.join(td, "o.tree"))
+
+
 def test_tree_parser_reads_reference_output():
     g = load_golden("knot3_d4_tree")
     dim, h, xf, xs, ys, md = parse_tree(g["tree"].tobytes())
@@ -77,16 +109,24 @@ def test_cli_tree_matches_reference_tree(cli, name):
         assert r.returncode == 0, r.stderr
         with open(out + ".tree", "rb") as f:
             mine = parse_tree(f.read())
-        with open(out + ".0.grid", "rb") as f:
-            grid = f.read()
+        grids = []
+        for c in range(2):
+            with open(out + f".{c}.grid", "rb") as f:
+                grids.append(f.read())
     ref = parse_tree(g["tree"].tobytes())
     assert mine[0] == ref[0] and mine[1] == ref[1] and mine[5] == ref[5]
     assert np.allclose(mine[2], ref[2], rtol=1e-14, atol=1e-14)
     for a, b in zip(mine[3] + mine[4], ref[3] + ref[4]):
         assert a.shape == b.shape
         assert np.abs(a - b).max() <= 1e-9 * max(np.abs(b).max(), 1e-30)
+    # the regular coefficient grid against the one the reference's Extract writes from the
+    # reference's own .tree (regularCoefficients, Hat.adaptive.inl:154-176; RegularGrid::Write,
+    # RegularGrid.inl:441-472): the same text header (dimensions and transform) and the same values
     dim = ref[0]
-    assert grid.startswith(f"G{dim}\n1 DOUBLE\n".encode())
-    # finest regular coefficients = sum of the prolonged hierarchical levels
     n = (2 ** depth + 1) ** dim
-    assert grid[-8 * n:] and len(np.frombuffer(grid[-8 * n:], "<f8")) == n
+    for c, mine_grid in enumerate(grids):
+        want = g[f"grid{c}"].tobytes()
+        assert mine_grid[:-8 * n] == want[:-8 * n], (mine_grid[:200], want[:200])
+        a = np.frombuffer(mine_grid[-8 * n:], "<f8")
+        b = np.frombuffer(want[-8 * n:], "<f8")
+        assert np.abs(a - b).max() <= 1e-9 * np.abs(b).max()

@@ -81,3 +81,26 @@ def test_degenerate_inputs():
     with pytest.raises(epr.EprError) as e:
         r.set_samples(pu, epr.pack_skew(frames))
     assert code(e.value) == EPR_ERR_ARG
+
+
+def test_allocation_cap_fails_like_out_of_memory(monkeypatch):
+    """Host-side fault injection of device out-of-memory: with EPR_ALLOC_CAP_BYTES set, the context
+    whose allocations exceed the cap fails with EPR_ERR_NOMEM and a message, nothing is left
+    half-built, and a context created without the cap works."""
+    import exteriorpoissonrecon_gb300 as epr
+    g = load_golden("knot3_d4")
+    monkeypatch.setenv("EPR_ALLOC_CAP_BYTES", str(3 << 20))  # the context fits (2.7 MB), its build does not
+    r = epr.Reconstructor(3, 4)
+    r.set_samples(g["pos"], g["skew"])
+    with pytest.raises(epr.EprError) as e:
+        r.build()
+    assert "[-5]" in str(e.value) and "allocation cap" in str(e.value)
+    r.close()
+    monkeypatch.setenv("EPR_ALLOC_CAP_BYTES", "1000")  # below what the context itself needs
+    with pytest.raises(epr.EprError) as e:
+        epr.Reconstructor(3, 4)
+    assert "allocation cap" in str(e.value)
+    monkeypatch.delenv("EPR_ALLOC_CAP_BYTES")
+    r = epr.Reconstructor(3, 4, g["pos"], g["skew"])
+    st = r.solve()
+    assert abs(st["fit_energy"] - g["sol_energies"][0]) < 1e-10 * g["sol_energies"][0]

@@ -36,6 +36,14 @@ def test_estimator(built):
     assert rel(r.get("noise"), g["est_noise"]) < 1e-9
 
 
+def test_density_estimator(built):
+    """epr_get_density: the estimator's splatted weight, position and covariance sums at every
+    level against the reference's tree (TreeEstimator, GridSamples.inl:740-771)."""
+    g, r, dim, depth = built
+    for l in range(depth + 1):
+        assert rel(r.density(l), g[f"density_l{l}"]) < 1e-12, l
+
+
 def test_frame_field(built):
     g, r, dim, depth = built
     assert np.array_equal(r.get("leaf_depth"), g["leaf_depth"])
