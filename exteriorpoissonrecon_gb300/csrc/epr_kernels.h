@@ -46,6 +46,9 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
 // 4: as 1 without the point-split update of the small 3D levels)
 void set_gs_variant(int v);
 void set_lanes_variant(int v);
+// 1 (default): 3D levels 0-1 relax in gs_tiny_kernel (one warp per node-element incidence of a
+// colour); 0: in the block kernels
+void set_tiny_levels(int v);
 // double-float levels: pairs stored as x 2^-k with k = kexp[level] (epr_df.cuh)
 void launch_df_push(const double *in, df *out, int64_t n, int *kexp, int level, cudaStream_t s);
 void launch_df_pull(const df *in, double *out, int64_t n, const int *kexp, int level, cudaStream_t s);

@@ -950,6 +950,264 @@ __global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L,
     for (int64_t k = threadIdx.x; k < 2 * g.N; k += blockDim.x) L.xy[k] = xy[k];
 }
 
+
+// ---------------------------------------------------------------------------------------------
+// The two coarsest 3D levels (resolution 1 and 2: 8 and 27 nodes), all sweeps in one block with
+// one warp per (node, element) incidence of a colour.  Every colour of these levels has the same
+// number of incidences (resolution 1: one node with its one element; resolution 2: eight, e.g. the
+// eight corner nodes with one element each, or the centre node with all eight), so warp w owns the
+// w-th incidence of every colour (nodes in colour order, elements in corner order).  Lanes 0-11
+// integrate the element's wedge component K = lane / 4 at the Gauss-point pair lane % 4 in the
+// canonical orientation (as gs_update_split3); lanes 16-31 take the node's stencil column (offsets
+// lane - 16 and lane) in the node's first incidence; each half-warp sums with shuffles.  At
+// resolution 1 the single warp applies the step itself (no block barrier at all); at resolution 2
+// the warps of a node meet in shared memory, two barriers per colour.  The coefficients and both
+// stencils live in shared memory for the whole schedule.  Double-float levels rescale their stored
+// coefficients after every sweep as the other kernels do.
+// ---------------------------------------------------------------------------------------------
+template <typename Real>
+__device__ __forceinline__ bool exceeds(Real v, double t)
+{
+    return (double)v > t;
+}
+// a double-float compares by its leading float unless that is within a factor of two of t
+template <>
+__device__ __forceinline__ bool exceeds<df>(df v, double t)
+{
+    const float tf = (float)t;
+    if (v.hi > 2.f * tf) return true;
+    if (v.hi < 0.5f * tf) return false;
+    return (double)v.hi + (double)v.lo > t;
+}
+template <typename Real>
+__device__ __forceinline__ Real abs_value(Real v)
+{
+    return v < (Real)0 ? -v : v;
+}
+template <>
+__device__ __forceinline__ df abs_value<df>(df v)
+{
+    return v.hi < 0.f ? -v : v;
+}
+template <typename Real>
+__device__ __forceinline__ bool finite_value(Real v)
+{
+    return isfinite((double)v);
+}
+template <>
+__device__ __forceinline__ bool finite_value<df>(df v)
+{
+    return isfinite(v.hi) && isfinite(v.lo);
+}
+
+// node_step with the singularity tests in the level's own arithmetic
+template <typename Real>
+__device__ __forceinline__ bool node_step_tiny(const Real *q, int separate, Real &p0, Real &p1)
+{
+    Real h00 = (Real)2 * q[0], h11 = (Real)2 * q[1], h01 = q[2];
+    if (separate)
+    {
+        p0 = 0;
+        p1 = 0;
+        if (exceeds<Real>(h00, 1e-20)) p0 = -((h01 + h01) * p1 + q[3]) / ((Real)2 * h00);
+        if (exceeds<Real>(h11, 1e-20)) p1 = -((h01 + h01) * p0 + q[4]) / ((Real)2 * h11);
+        return true;
+    }
+    Real det = h00 * h11 - h01 * h01;
+    if (!exceeds<Real>(abs_value<Real>(det), 1e-20)) return false;
+    p0 = -(h11 * q[3] - h01 * q[4]) / det / (Real)2;
+    p1 = -(-h01 * q[3] + h00 * q[4]) / det / (Real)2;
+    return true;
+}
+
+template <typename Real, int LEVEL>
+__global__ void __launch_bounds__(LEVEL == 0 ? 32 : 256) gs_tiny_kernel(LevelPtrs<Real> L, int iters, unsigned int *err,
+                                                                          int separate, int *kexp)
+{
+    static_assert(LEVEL == 0 || LEVEL == 1, "resolution 1 or 2");
+    constexpr int NW = LEVEL == 0 ? 1 : 8;  // incidences per colour
+    constexpr int R = 1 << LEVEL, N1 = R + 1, NN = N1 * N1 * N1, S = 27;
+    constexpr int s0 = N1 * N1, s1 = N1;
+    constexpr bool kDF = std::is_same<Real, df>::value;
+    __shared__ Real2<Real> xy[NN];
+    __shared__ Real As[S * NN], Bs[S * NN];
+    __shared__ Real part[NW][10];
+    // each warp's incidence of each colour: node index, node coordinates, element corner A, whether
+    // it is the node's first incidence and how many the node has (shared memory, so that the
+    // colour loop indexes it without a local-memory stack)
+    __shared__ int incNode[8][NW], incA[8][NW], incCnt[8][NW], incI[8][NW][3], incFirst[8][NW];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k < NN; k += blockDim.x) xy[k] = ld2(L.xy, k);
+    for (int k = threadIdx.x; k < S * NN; k += blockDim.x)
+    {
+        As[k] = L.A[k];
+        Bs[k] = L.B[k];
+    }
+    if (threadIdx.x < 8)
+    {
+        const int c = threadIdx.x;
+        const Grid<3> g(LEVEL);
+        const Colour<3> col(g, c);
+        int w = 0;
+        for (int j = 0; j < (int)col.n; j++)
+        {
+            int I[3];
+            col.node(j, I);
+            int cnt = 0;
+            for (int A = 0; A < 8; A++)
+            {
+                bool ok = true;
+                for (int d = 0; d < 3; d++) { const int e = I[d] - cbit<3>(A, d); ok = ok && e >= 0 && e < R; }
+                if (ok) cnt++;
+            }
+            int k = 0;
+            for (int A = 0; A < 8; A++)
+            {
+                bool ok = true;
+                for (int d = 0; d < 3; d++) { const int e = I[d] - cbit<3>(A, d); ok = ok && e >= 0 && e < R; }
+                if (!ok || w >= NW) continue;
+                incNode[c][w] = (I[0] * N1 + I[1]) * N1 + I[2];
+                incA[c][w] = A;
+                incFirst[c][w] = k == 0;
+                incCnt[c][w] = cnt;
+                for (int d = 0; d < 3; d++) incI[c][w][d] = I[d];
+                w++;
+                k++;
+            }
+        }
+    }
+    __syncthreads();
+    Real wmul = wedge_mult<Real>(kexp, LEVEL);
+    for (int it = 0; it < iters; it++)
+    {
+#pragma unroll 1
+        for (int c = 0; c < 8; c++)
+        {
+            const int i = incNode[c][warp], A = incA[c][warp];
+            const bool first = incFirst[c][warp] != 0;
+            Real r[5] = {0, 0, 0, 0, 0};
+            if (lane < 12)
+            {
+                const int K = lane >> 2, pq = lane & 3;
+                const int pax[3] = {(K == 2) ? 1 : 0, (K == 0) ? 1 : 2, (K == 0) ? 2 : (K == 1 ? 1 : 0)};
+                int sd[3];
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+                {
+                    const int stride = pax[a] == 0 ? s0 : (pax[a] == 1 ? s1 : 1);
+                    sd[a] = ((A >> (2 - pax[a])) & 1) ? -stride : stride;
+                }
+                Real x[8], y[8];
+#pragma unroll
+                for (int cc = 0; cc < 8; cc++)
+                {
+                    int jj = i;
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+                        if (cbit<3>(cc, a)) jj += sd[a];
+                    const Real2<Real> v = xy[jj];
+                    x[cc] = v.x;
+                    y[cc] = v.y;
+                }
+                component_fit_pq3<Real>(x, y, pq >> 1, pq & 1, r);
+            }
+            else if (lane >= 16 && first)
+            {
+#pragma unroll
+                for (int half = 0; half < 2; half++)
+                {
+                    const int o = lane - 16 + 16 * half;
+                    if (o >= S) continue;
+                    const int off[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+                    bool in = true;
+#pragma unroll
+                    for (int d = 0; d < 3; d++) { const int q = incI[c][warp][d] + off[d]; in = in && q >= 0 && q <= R; }
+                    if (!in) continue;
+                    const int jj = i + off[0] * s0 + off[1] * s1 + off[2];
+                    const Real a = As[o * NN + i], b = Bs[o * NN + i];
+                    const Real2<Real> q = xy[jj];
+                    r[0] += a * q.x;
+                    r[1] += a * q.y;
+                    if (o == 13) r[4] = a;
+                    else { r[2] += b * q.x; r[3] += b * q.y; }
+                }
+            }
+            // sums within each half-warp: lane 0 the wedge integrals, lane 16 the stencil sums
+#pragma unroll
+            for (int k = 0; k < 5; k++)
+#pragma unroll
+                for (int o = 8; o > 0; o >>= 1) r[k] += shfl_xor_any(r[k], o);
+            Real stc[5];
+#pragma unroll
+            for (int k = 0; k < 5; k++) stc[k] = shfl_any(r[k], 16);
+            bool apply = false;
+            Real h[5], sv[5];
+            if (NW == 1)
+            {
+                apply = lane == 0;
+#pragma unroll
+                for (int k = 0; k < 5; k++) { h[k] = r[k]; sv[k] = stc[k]; }
+            }
+            else
+            {
+                if (lane == 0)
+#pragma unroll
+                    for (int k = 0; k < 5; k++) { part[warp][k] = r[k]; part[warp][5 + k] = stc[k]; }
+                __syncthreads();
+                apply = lane == 0 && first;
+                if (apply)
+                {
+#pragma unroll
+                    for (int k = 0; k < 5; k++)
+                    {
+                        h[k] = part[warp][k];
+                        sv[k] = part[warp][5 + k];
+                    }
+                    for (int w2 = 1; w2 < incCnt[c][warp]; w2++)
+#pragma unroll
+                        for (int k = 0; k < 5; k++) h[k] += part[warp + w2][k];
+                }
+            }
+            if (apply)
+            {
+                const Real sc = (Real)wedge_scale<3>(R) * wmul;
+                Real q[5];
+                q[0] = h[0] * sc + sv[4];
+                q[1] = h[1] * sc + sv[4];
+                q[2] = (Real)2 * h[2] * sc;
+                q[3] = (Real)2 * h[3] * sc + (Real)2 * sv[0] - (Real)2 * sv[3];
+                q[4] = (Real)2 * h[4] * sc + (Real)2 * sv[1] + (Real)2 * sv[2];
+                Real p0, p1;
+                if (node_step_tiny<Real>(q, separate, p0, p1))
+                {
+                    Real2<Real> cur = xy[i];
+                    cur.x += p0;
+                    cur.y += p1;
+                    if (!finite_value<Real>(cur.x) || !finite_value<Real>(cur.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
+                    xy[i] = cur;
+                }
+            }
+            if (NW == 1) __syncwarp();
+            else __syncthreads();
+        }
+        if constexpr (kDF)
+            if (kexp)
+            {
+                // keep the stored coefficients near 1: a new power-of-two exponent after every sweep
+                const int shift = df_rescale_shift(reinterpret_cast<const df *>(xy), 2 * NN);
+                if (shift)
+                {
+                    df *v = reinterpret_cast<df *>(xy);
+                    for (int k = threadIdx.x; k < 2 * NN; k += blockDim.x) v[k] = ldexp_df(v[k], shift);
+                    if (threadIdx.x == 0) kexp[LEVEL] -= shift;
+                    __syncthreads();
+                    wmul = wedge_mult<Real>(kexp, LEVEL);
+                }
+            }
+    }
+    for (int k = threadIdx.x; k < NN; k += blockDim.x) reinterpret_cast<Real2<Real> *>(L.xy)[k] = xy[k];
+}
+
 template <int D, typename Real>
 __global__ void __launch_bounds__(kThreads) gn_matvec_kernel(LevelPtrs<Real> L, const Real *xy, const Real *dxy, Real *out)
 {
@@ -1082,6 +1340,7 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n)
 inline unsigned int blocks_for(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
 
 int g_lanes_variant = 1;  // 0: scalar float element fit in the lane kernel, 1: packed
+int g_tiny_levels = 1;    // 1: 3D levels 0-1 by gs_tiny_kernel, 0: by the block kernels of gs_level_kernel
 int g_gs_variant = 1;  // 0: one thread per node, 1: 2^D lanes per node (row grid), 2: 2^D lanes per node (flat grid),
                        // 4: as 1 without the point-split update of the small 3D levels
 
@@ -1159,6 +1418,17 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
 
 void set_gs_variant(int v) { g_gs_variant = v; }
 void set_lanes_variant(int v) { g_lanes_variant = v; }
+void set_tiny_levels(int v) { g_tiny_levels = v; }
+
+// all sweeps of a 3D level 0 or 1 in gs_tiny_kernel (one warp per incidence of a colour)
+template <typename Real>
+bool launch_tiny_level(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s, int separate, int *kexp)
+{
+    if (!g_tiny_levels || L.level > 1) return false;
+    if (L.level == 0) gs_tiny_kernel<Real, 0><<<1, 32, 0, s>>>(L, iters, err, separate, kexp);
+    else gs_tiny_kernel<Real, 1><<<1, 256, 0, s>>>(L, iters, err, separate, kexp);
+    return true;
+}
 
 // shared-memory carve-out of the single-block level kernels whose stencils live in shared memory
 constexpr size_t kLevelSmemLimit = 200 * 1024;
@@ -1193,6 +1463,8 @@ int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cud
 {
     Grid<D> g(L.level);
     if (iters <= 0) return 0;
+    if constexpr (D == 3)
+        if (g.N <= persistentMaxNodes && launch_tiny_level<Real>(L, iters, err, s, separate, nullptr)) return 1;
     if (g.N <= persistentMaxNodes)
     {
         constexpr int MT = persistent_threads<D, Real>();
@@ -1307,6 +1579,7 @@ int launch_gs_sweeps_df(const LevelPtrs<df> &L, int iters, unsigned int *err, cu
 {
     Grid<3> g(L.level);
     if (iters <= 0) return 0;
+    if (g.N <= persistentMaxNodes && launch_tiny_level<df>(L, iters, err, s, separate, kexp)) return 1;
     if (g.N <= persistentMaxNodes)
     {
         constexpr int MT = persistent_threads<3, df>();

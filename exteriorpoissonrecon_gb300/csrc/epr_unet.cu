@@ -4,8 +4,9 @@
 // reference, whose solve starts from random coefficients at its coarsest solve level
 // (ExteriorPoisson.h:333-341); the prediction replaces that start and the levels below it.
 //
-// Network (node grids of resolution 2^L, 2^L + 1 nodes per axis; level L = 6: 65^3 nodes):
-//   enc0 conv(4 -> 16) @L, enc1 conv(16 -> 32) @L-1, enc2 conv(32 -> 64) @L-2, bott conv(64 -> 128)
+// Network (node grids of resolution 2^L, 2^L + 1 nodes per axis; level L = 6: 65^3 nodes; the
+// 15 input channels are listed at input_write_kernel):
+//   enc0 conv(15 -> 16) @L, enc1 conv(16 -> 32) @L-1, enc2 conv(32 -> 64) @L-2, bott conv(64 -> 128)
 //   @L-3, then dec2 conv(128 + 64 -> 64) @L-2, dec1 conv(64 + 32 -> 32) @L-1, dec0 conv(32 + 16 ->
 //   16) @L, head conv(16 -> 2) @L; every conv 3x3x3 with zero padding, ReLU after all but the head.
 //   Between levels: full-weighting restriction (the multilinear weights of the prolongation, 1/8
@@ -306,18 +307,49 @@ __global__ void input_max_kernel(const double *density, const double *skew, int 
     }
 }
 
-// channels: density weight / max, the three frame components / max |frame|, then zeros (16)
+// channels (16, all scale-free): 0 density weight / max; 1-3 frame components / max |frame|;
+// 4-6 the splatted samples' mean offset from the vertex, in cells (0 without weight); 7-9 the
+// frame's direction (frame / |frame|, 0 where |frame| < 1e-3 max); 10 |frame| / max;
+// 11-13 the vertex's coordinates in [-1, 1]; 14 log(1 + weight / max) / log 2; 15 zero
 __global__ void input_write_kernel(const double *density, const double *skew, int nvox, const unsigned int *mx, bf16 *out)
 {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nvox) return;
     const float wm = __uint_as_float(mx[0]), sm = __uint_as_float(mx[1]);
     const float iw = wm > 0.f ? 1.f / wm : 0.f, is = sm > 0.f ? 1.f / sm : 0.f;
+    int n = 1;
+    while ((int64_t)n * n * n < nvox) n++;
+    int z, y, x;
+    vox_coords(v, n, z, y, x);
+    const double *dv = density + (int64_t)v * 13;
+    const double w = dv[0];
+    float o32[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) o32[j] = 0.f;
+    o32[0] = (float)w * iw;
+    float sn = 0.f;
+    for (int k = 0; k < 3; k++)
+    {
+        const float sk = (float)skew[(int64_t)v * 3 + k];
+        o32[1 + k] = sk * is;
+        sn += sk * sk;
+    }
+    sn = sqrtf(sn);
+    if (w > 0)
+    {
+        const int c[3] = {z, y, x};
+        for (int k = 0; k < 3; k++) o32[4 + k] = (float)(dv[1 + k] / w * (n - 1) - c[k]);
+    }
+    if (sn > 1e-3f * sm && sn > 0.f)
+        for (int k = 0; k < 3; k++) o32[7 + k] = (float)skew[(int64_t)v * 3 + k] / sn;
+    o32[10] = sn * is;
+    o32[11] = 2.f * z / (n - 1) - 1.f;
+    o32[12] = 2.f * y / (n - 1) - 1.f;
+    o32[13] = 2.f * x / (n - 1) - 1.f;
+    o32[14] = log1pf(o32[0]) / 0.69314718f;
     __align__(16) bf16 o[16];
 #pragma unroll
-    for (int j = 0; j < 16; j++) o[j] = __float2bfloat16(0.f);
-    o[0] = __float2bfloat16((float)density[(int64_t)v * 13] * iw);
-    for (int k = 0; k < 3; k++) o[1 + k] = __float2bfloat16((float)skew[(int64_t)v * 3 + k] * is);
+    for (int j = 0; j < 16; j++) o[j] = __float2bfloat16(o32[j]);
     uint4 *d = reinterpret_cast<uint4 *>(out + (int64_t)v * 16);
     d[0] = reinterpret_cast<const uint4 *>(o)[0];
     d[1] = reinterpret_cast<const uint4 *>(o)[1];
@@ -640,7 +672,7 @@ bool build_net(epr_unet *net, uint64_t seed)
     const int lv = net->level;
     for (int k = 0; k < 4; k++) net->n[k] = (1 << (lv - k)) + 1;
     struct Spec { int cin, cinReal, cout, level; bool relu; };
-    const Spec spec[NLAYERS] = {{16, 4, 16, 0, true},   {16, 16, 32, 1, true},  {32, 32, 64, 2, true},  {64, 64, 128, 3, true},
+    const Spec spec[NLAYERS] = {{16, 15, 16, 0, true},   {16, 16, 32, 1, true},  {32, 32, 64, 2, true},  {64, 64, 128, 3, true},
                                 {192, 192, 64, 2, true}, {96, 96, 32, 1, true}, {48, 48, 16, 0, true},  {16, 16, 16, 0, false}};
     size_t off = 0;
     net->L.resize(NLAYERS);

@@ -251,7 +251,8 @@ def train(count: int = 512, epochs: int = 40, batch: int = 8, lr: float = 1e-3, 
         hist["holdout_loss"].append(holdout_loss())
         log(f"epoch {ep + 1}/{epochs}: train {hist['train_loss'][-1]:.4f} held-out {hist['holdout_loss'][-1]:.4f}")
     hist["train_s"] = time.perf_counter() - t1
-    hist["shapes"] = {k: names.count(k) for k in sorted(set(n.split("_")[0] for n in names))} if names else {}
+    kinds = [n.split("_")[0].rstrip("0123456789") for n in names]
+    hist["shapes"] = {k: kinds.count(k) for k in sorted(set(kinds))}
     return net, hist
 
 

@@ -332,9 +332,11 @@ int epr_unet_params(epr_unet *net, float *host, size_t cap, size_t *count, int s
 /* nodes per axis of the network's grid, bytes of one input (n^3 x 16 BF16), floats of one target
  * or prediction (n^3 x 2). */
 int epr_unet_grid(const epr_unet *net, int *nodes_per_axis, size_t *input_bytes, size_t *target_floats);
-/* The network input of a built 3D context (depth >= the network's level): channel 0 the density
- * weight, channels 1-3 the frame splat, each divided by its maximum magnitude, channels 4-15 zero;
- * into dev_input (NULL: the network's own input buffer). */
+/* The network input of a built 3D context (depth >= the network's level), 16 BF16 channels per
+ * vertex of the level, all scale-free: the density weight and the frame splat (3) divided by their
+ * maximum magnitudes, the splatted samples' mean offset from the vertex in cells (3), the frame's
+ * direction (3) and relative magnitude, the vertex coordinates in [-1, 1] (3), log(1 + weight /
+ * max) / log 2, and a zero channel; into dev_input (NULL: the network's own input buffer). */
 int epr_unet_input(epr_unet *net, epr_ctx *ctx, void *dev_input);
 /* The training target of a solved context: its level-L regular (x, y) coefficients as FP32 pairs. */
 int epr_unet_target(epr_unet *net, epr_ctx *ctx, float *dev_target);

@@ -20,7 +20,7 @@ import numpy as np
 TAPS = [(t // 9 - 1, (t // 3) % 3 - 1, t % 3 - 1) for t in range(27)]
 
 # layers: (GEMM input channels, real input channels, output channels, network level, relu)
-LAYERS = [("enc0", 16, 4, 16, 0, True), ("enc1", 16, 16, 32, 1, True), ("enc2", 32, 32, 64, 2, True),
+LAYERS = [("enc0", 16, 15, 16, 0, True), ("enc1", 16, 16, 32, 1, True), ("enc2", 32, 32, 64, 2, True),
           ("bott", 64, 64, 128, 3, True), ("dec2", 192, 192, 64, 2, True), ("dec1", 96, 96, 32, 1, True),
           ("dec0", 48, 48, 16, 0, True), ("head", 16, 16, 16, 0, False)]
 

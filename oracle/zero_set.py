@@ -16,8 +16,9 @@ only): what Extract does with a `.tree` of the regular indexer (Extract/Extract.
     * vertices go to world coordinates by the `.tree`'s voxel-to-world transform.
 
 Cells are pre-selected by a necessary condition (both fields change sign or vanish on the cell's
-corners), which leaves the extracted set unchanged.  The comparison helpers resample segments at a
-tenth of a cell and measure the symmetric Hausdorff distance (scipy's k-d tree).
+corners), which leaves the extracted set unchanged.  The comparison samples each curve's segments
+at a tenth of a cell and measures exact point-to-segment distances to the other curve (symmetric
+Hausdorff distance; scipy's k-d tree finds the candidate segments).
 """
 from __future__ import annotations
 
@@ -139,10 +140,53 @@ def resample_segments(segs: np.ndarray, h: float) -> np.ndarray:
 
 
 def hausdorff(P: np.ndarray, Q: np.ndarray) -> float:
+    """Symmetric Hausdorff distance of two point sets."""
     from scipy.spatial import cKDTree
     if len(P) == 0 or len(Q) == 0:
         return 0.0 if len(P) == len(Q) else float("inf")
     return float(max(cKDTree(Q).query(P)[0].max(), cKDTree(P).query(Q)[0].max()))
+
+
+def _point_segment_distance(P, A, B):
+    d = B - A
+    L2 = (d * d).sum(-1)
+    t = np.where(L2 > 0, ((P - A) * d).sum(-1) / np.where(L2 > 0, L2, 1), 0.0)
+    t = np.clip(t, 0.0, 1.0)
+    return np.linalg.norm(P - (A + t[..., None] * d), axis=-1)
+
+
+def directed_distance(segs_a: np.ndarray, segs_b: np.ndarray, h: float) -> float:
+    """max over points of the curve A (its segments sampled every h) of the distance to the curve B
+    (exact point-to-segment distances).  Candidate segments of B are the k nearest by midpoint; a
+    point is settled once its k-th nearest midpoint is farther than its best distance plus half the
+    longest segment of B (no unexamined segment can then come closer), else k grows."""
+    from scipy.spatial import cKDTree
+    if len(segs_a) == 0:
+        return 0.0
+    if len(segs_b) == 0:
+        return float("inf")
+    P = resample_segments(segs_a, h)
+    mids = 0.5 * (segs_b[:, 0] + segs_b[:, 1])
+    half = 0.5 * float(np.linalg.norm(segs_b[:, 1] - segs_b[:, 0], axis=1).max())
+    tree = cKDTree(mids)
+    best = np.full(len(P), np.inf)
+    todo = np.arange(len(P))
+    k = 16
+    while len(todo):
+        kk = min(k, len(segs_b))
+        dk, idx = tree.query(P[todo], kk)
+        dk, idx = dk.reshape(len(todo), kk), idx.reshape(len(todo), kk)
+        dist = _point_segment_distance(P[todo][:, None, :], segs_b[idx, 0], segs_b[idx, 1]).min(axis=1)
+        best[todo] = dist
+        settled = (kk == len(segs_b)) | (dk[:, -1] > dist + half)
+        todo = todo[~settled]
+        k *= 4
+    return float(best.max())
+
+
+def curve_hausdorff(segs_a: np.ndarray, segs_b: np.ndarray, h: float) -> float:
+    """Symmetric Hausdorff distance of two polylines given as segment lists."""
+    return max(directed_distance(segs_a, segs_b, h), directed_distance(segs_b, segs_a, h))
 
 
 def tree_zero_set(raw: bytes, simplices: np.ndarray):

@@ -169,8 +169,15 @@ def make_zero_set(name, workload, n, seed, depth, ref_tree=None):
             energies = r.stdout.strip().splitlines()[-1]
         subprocess.run([REF_EXTRACT, "--in", tree, "--out", out + "_zero.ply"], check=True, capture_output=True)
         V, F = read_mesh(out + "_zero.ply")
+    if energies is None and os.environ.get("EPR_REF_LOG"):
+        # the verbose log of the run that wrote `ref_tree`: its final energy and time lines
+        with open(os.environ["EPR_REF_LOG"]) as f:
+            lines = [l.strip() for l in f if l.strip().startswith(("Error:", "Executed"))]
+        energies = " | ".join(lines)
+    # float32 positions (1e-7 relative, far below the 0.1-cell criterion) keep the fixture small
     fx = {"depth": np.array(depth), "workload": np.array(workload), "n": np.array(n), "seed": np.array(seed),
-          "zero_vertices": V, "zero_simplices": np.array([list(f) for f in F], dtype=np.int64).reshape(len(F), -1)}
+          "zero_vertices": V.astype(np.float32),
+          "zero_simplices": np.array([list(f) for f in F], dtype=np.int32).reshape(len(F), -1)}
     if energies:
         fx["log"] = np.array(energies)
     path = os.path.join(HERE, name + ".npz")
@@ -213,7 +220,7 @@ if __name__ == "__main__":
     only = set(sys.argv[1:])  # fixture names to (re)write; all when none are given
     TREES = [("knot3_d4_tree", "knot", 4096, 0, 4, []), ("cliff4_d3_tree", "clifford", 3000, 9, 3, ["--gsIters", "5"])]
     # the reference's zero set of the benchmark's input (3D link, 1.1M samples, depth 8): the
-    # reference run takes ~15 minutes on 8 cores
+    # reference run takes ~6 minutes on 8 cores
     ZERO_SETS = [("link3_d8_zero_set", "link", 1_000_000, 0, 8)]
     if only:
         for case in CASES:
@@ -226,7 +233,9 @@ if __name__ == "__main__":
             make_simplices()
         for case in ZERO_SETS:
             if case[0] in only:
-                make_zero_set(*case)
+                # EPR_REF_TREE: a .tree the reference already wrote for this input (and EPR_REF_LOG
+                # its verbose log), instead of running the reference here
+                make_zero_set(*case, ref_tree=os.environ.get("EPR_REF_TREE"))
         sys.exit(0)
     for case in CASES:
         make(*case)

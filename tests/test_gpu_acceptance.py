@@ -39,7 +39,7 @@ def _zero_set_distance(cli, pos, frames, depth, flags, ref_vertices, ref_simplic
         with open(out + ".tree", "rb") as f:
             segs, cell = Z.tree_zero_set(f.read(), simp)
     ref = ref_vertices[ref_simplices]
-    d = Z.hausdorff(Z.resample_segments(segs, cell / 10), Z.resample_segments(ref, cell / 10))
+    d = Z.curve_hausdorff(segs, ref, cell / 10)
     return d / cell, len(segs), len(ref)
 
 

@@ -5,8 +5,9 @@ Tolerances: the convolution primitives take BF16 operands exactly and accumulate
 forward and data-gradient outputs (stored in BF16) are within one BF16 rounding (2^-8 relative) of
 the oracle's float64 sums of the same operands, and the FP32 weight gradient within 1e-4 relative;
 the whole network's loss and parameter gradients, with the oracle rounding to BF16 where the GPU
-stores BF16, within 2e-2 relative in norm per layer (rounding-boundary flips of BF16 intermediates
-move individual values by one BF16 step)."""
+stores BF16, within 2e-2 relative in norm per layer's weights and 5e-2 per layer's biases (bias
+gradients are sums of cancelling BF16 values; rounding-boundary flips of BF16 intermediates move
+individual values by one BF16 step)."""
 import ctypes
 
 import numpy as np
@@ -119,7 +120,7 @@ def test_network_gradients_match_oracle(torch):
         assert lib.epr_unet_params(h, params.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), cnt, None, 1) == 0
         n = 2 ** level + 1
         x = np.zeros((n, n, n, 16))
-        x[..., :4] = rng.uniform(-1, 1, size=(n, n, n, 4))
+        x[..., :15] = rng.uniform(-1, 1, size=(n, n, n, 15))
         x = U.bf16(x)
         t = rng.normal(size=(n, n, n, 2))
         dx = _dev_bf16(torch, x.reshape(-1, 16))
@@ -135,7 +136,8 @@ def test_network_gradients_match_oracle(torch):
             gw, rw = grads[wo:wo + 27 * cin * cout], g[wo:wo + 27 * cin * cout]
             gb, rb = grads[bo:bo + cout], g[bo:bo + cout]
             assert np.linalg.norm(gw - rw) <= 2e-2 * np.linalg.norm(rw) + 1e-12, name
-            assert np.linalg.norm(gb - rb) <= 2e-2 * np.linalg.norm(rb) + 1e-12, name
+            # a bias gradient is a sum over all voxels of BF16 values that largely cancel
+            assert np.linalg.norm(gb - rb) <= 5e-2 * np.linalg.norm(rb) + 1e-12, name
         # the prediction itself
         pred = torch.zeros((n ** 3, 2), dtype=torch.float32, device="cuda")
         assert lib.epr_unet_forward(h, _ptr(dx), _ptr(pred), None, None) == 0
@@ -155,7 +157,7 @@ def test_training_steps_reduce_the_loss(torch):
     ins, tgts = [], []
     for k in range(4):
         x = np.zeros((n, n, n, 16))
-        x[..., :4] = rng.uniform(-1, 1, size=(n, n, n, 4))
+        x[..., :15] = rng.uniform(-1, 1, size=(n, n, n, 15))
         ins.append(_dev_bf16(torch, x.reshape(-1, 16)))
         # a smooth target field
         g = np.linspace(0, 1, n)

@@ -53,7 +53,7 @@ def test_network_backward_matches_central_differences():
         p[bo:bo + cout] = 0.05 * rng.normal(size=cout)
     n = 2 ** level + 1
     x = np.zeros((n, n, n, 16))
-    x[..., :4] = rng.uniform(-1, 1, size=(n, n, n, 4))
+    x[..., :15] = rng.uniform(-1, 1, size=(n, n, n, 15))
     t = rng.normal(size=(n, n, n, 2))
     L, g = U.UNet(p, level).gradients(x, t)
 
@@ -65,7 +65,7 @@ def test_network_backward_matches_central_differences():
     # a few parameters of every layer (weights with real input channels and the bias)
     picks = []
     for name, (wo, bo, cin, cout, lv, relu) in lay.items():
-        creal = 4 if name == "enc0" else cin
+        creal = 15 if name == "enc0" else cin
         coutr = 2 if name == "head" else cout
         for _ in range(3):
             t_, ci, co = rng.integers(27), rng.integers(creal), rng.integers(coutr)

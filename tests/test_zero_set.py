@@ -13,7 +13,7 @@ def test_extraction_matches_reference_extract():
     segs, cell = Z.tree_zero_set(g["tree"].tobytes(), simp)
     ref = g["zero_vertices"][g["zero_simplices"]]
     assert len(segs) == len(ref)
-    d = Z.hausdorff(Z.resample_segments(segs, cell / 10), Z.resample_segments(ref, cell / 10))
+    d = Z.curve_hausdorff(segs, ref, cell / 10)
     assert d <= 1e-9 * cell, d / cell
 
 
