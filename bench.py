@@ -435,6 +435,22 @@ def profile_kernel(args, depth):
     profiler captures."""
     import exteriorpoissonrecon_gb300 as epr
     pu, sk = workload(args.samples, args.dim)
+    if args.profile_kernel == "unet":
+        # the warm-start network's forward pass on the workload's level-6 input, `reps` times (every
+        # layer's tensor-core convolution, transfers and glue kernels)
+        from exteriorpoissonrecon_gb300 import learned as LW
+        net = LW.WarmStartNet.load() if os.path.exists(LW.WEIGHTS) else LW.WarmStartNet(level=6)
+        r = epr.Reconstructor(3, depth, pu, sk, precision="fp32", max_solve_depth=net.level)
+        net.input(r)
+        ms = []
+        for _ in range(args.profile_reps + 1):
+            t0 = time.perf_counter()
+            net.predict()
+            ms.append((time.perf_counter() - t0) * 1e3)
+        print(json.dumps({"kernel": "unet", "level": net.level, "voxels": net.n ** 3, "ms_per_forward_wall": min(ms[1:])}))
+        net.close()
+        r.close()
+        return
     band = (dict(fp64_from=2, fp64_levels=4, band_precision=args.profile_band)
             if args.profile_band and args.precision == "fp32" else {})
     r = epr.Reconstructor(args.dim, depth, pu, sk, precision=args.precision, **band)

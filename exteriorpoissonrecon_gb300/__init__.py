@@ -185,6 +185,8 @@ def load():
                                 ctypes.POINTER(ctypes.c_size_t)]
     L.epr_synchronize.argtypes = [vp]
     L.epr_get_density.argtypes = [vp, ctypes.c_int, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    L.epr_get_density_refined.argtypes = [vp, ctypes.c_int, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    L.epr_write_density_tree.argtypes = [vp, P, ctypes.c_char_p]
     L.epr_time_kernel.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P]
     L.epr_energy_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp,
                                      ctypes.c_double, vp, vp]
@@ -353,6 +355,23 @@ class Reconstructor:
         out = np.zeros(n.value)
         self._check(load().epr_get_density(self._h, level, _p(out), n.value, ctypes.byref(n)))
         return out.reshape(self.nodes(level), -1)
+
+    def density_refined(self, t: int) -> np.ndarray:
+        """1 where the density tree's depth-t cell has children ((2^t)^dim flags, axis 0 most
+        significant)."""
+        n = ctypes.c_size_t(0)
+        self._check(load().epr_get_density_refined(self._h, t, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, np.uint8)
+        self._check(load().epr_get_density_refined(self._h, t, out.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n)))
+        return out
+
+    def write_density_tree(self, path: str, voxel_to_world: np.ndarray):
+        """The reference's <out>.density.tree (ExteriorPoissonRecon.cpp:272-277) for this build;
+        voxel_to_world is (dim+1)^2 doubles in the .tree's (column, row) order."""
+        xf = np.ascontiguousarray(voxel_to_world, dtype=np.float64).ravel()
+        if xf.size != (self.dim + 1) ** 2:
+            raise ValueError("voxel_to_world must hold (dim+1)^2 values")
+        self._check(load().epr_write_density_tree(self._h, _p(xf), os.fsencode(path)))
 
     # ---------------------------------------------------------------- per-level operators
     def set_coefficients(self, level, x, y):

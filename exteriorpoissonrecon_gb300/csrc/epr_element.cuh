@@ -319,6 +319,50 @@ __device__ __forceinline__ void component_fit_pq3(const Real *x, const Real *y, 
     }
 }
 
+// component_fit_pq3 for a run-time Gauss-point pair: the A-differences are interpolated along B
+// with the hat values of the pair's own Gauss point (scalars picked from two constants), which
+// forms exactly the table row that component_fit_pq3 indexes, while the corner arrays stay
+// constant-indexed in registers (the products and their order are component_fit_pq3's)
+template <typename Real>
+__device__ __forceinline__ void component_fit_pq3_sel(const Real *x, const Real *y, int gp, int gq, Real *h)
+{
+    using Cp = Component<3, 0>;
+    const Real q0 = gq ? hat2<Real>(0, 1) : hat2<Real>(0, 0), q1 = gq ? hat2<Real>(1, 1) : hat2<Real>(1, 0);
+    const Real p0 = gp ? hat2<Real>(0, 1) : hat2<Real>(0, 0), p1 = gp ? hat2<Real>(1, 1) : hat2<Real>(1, 0);
+    Real xP[2], xQ[2], yP[2], yQ[2];
+#pragma unroll
+    for (int bo = 0; bo < 2; bo++)
+    {
+        // derivative along P interpolated at Q's point gq, and along Q at P's point gp
+        xP[bo] = q0 * (x[Cp::corner(1, 0, bo)] - x[Cp::corner(0, 0, bo)]) + q1 * (x[Cp::corner(1, 1, bo)] - x[Cp::corner(0, 1, bo)]);
+        yP[bo] = q0 * (y[Cp::corner(1, 0, bo)] - y[Cp::corner(0, 0, bo)]) + q1 * (y[Cp::corner(1, 1, bo)] - y[Cp::corner(0, 1, bo)]);
+        xQ[bo] = p0 * (x[Cp::corner(0, 1, bo)] - x[Cp::corner(0, 0, bo)]) + p1 * (x[Cp::corner(1, 1, bo)] - x[Cp::corner(1, 0, bo)]);
+        yQ[bo] = p0 * (y[Cp::corner(0, 1, bo)] - y[Cp::corner(0, 0, bo)]) + p1 * (y[Cp::corner(1, 1, bo)] - y[Cp::corner(1, 0, bo)]);
+    }
+    const Real w2 = gp == gq ? (gp ? (Real)(Gauss::W2(1) * Gauss::W2(1)) : (Real)(Gauss::W2(0) * Gauss::W2(0)))
+                             : (Real)(Gauss::W2(0) * Gauss::W2(1));
+    const Real hq = gq ? hat2<Real>(0, 1) : hat2<Real>(0, 0), hp = p0;
+#pragma unroll
+    for (int go = 0; go < 3; go++)
+    {
+        const Real lo = hat3<Real>(0, go);
+        const Real w = w2 * (Real)other_weight<1>(go);
+        const Real phP = (Real)-1 * hq * lo;
+        const Real phQ = (Real)-1 * hp * lo;
+        const Real xp = derivative_at<1, Real>(xP, go), xq = derivative_at<1, Real>(xQ, go);
+        const Real yp = derivative_at<1, Real>(yP, go), yq = derivative_at<1, Real>(yQ, go);
+        const Real W = yp * xq - xp * yq;
+        const Real U = yp * phQ - phP * yq;
+        const Real V = phP * xq - xp * phQ;
+        const Real wU = w * U, wV = w * V;
+        h[0] += wU * U;
+        h[1] += wV * V;
+        h[2] += wU * V;
+        h[3] += wU * W;
+        h[4] += wV * W;
+    }
+}
+
 template <int D, typename Real>
 __device__ __forceinline__ void element_fit(const Real *x, const Real *y, int A, Real *h)
 {

@@ -1015,8 +1015,10 @@ __device__ __forceinline__ bool node_step_tiny(const Real *q, int separate, Real
     }
     Real det = h00 * h11 - h01 * h01;
     if (!exceeds<Real>(abs_value<Real>(det), 1e-20)) return false;
-    p0 = -(h11 * q[3] - h01 * q[4]) / det / (Real)2;
-    p1 = -(-h01 * q[3] + h00 * q[4]) / det / (Real)2;
+    // -H^{-1} grad / 2 with one division
+    const Real m = (Real)-0.5 / det;
+    p0 = (h11 * q[3] - h01 * q[4]) * m;
+    p1 = (-h01 * q[3] + h00 * q[4]) * m;
     return true;
 }
 
@@ -1109,7 +1111,7 @@ __global__ void __launch_bounds__(LEVEL == 0 ? 32 : 256) gs_tiny_kernel(LevelPtr
                     x[cc] = v.x;
                     y[cc] = v.y;
                 }
-                component_fit_pq3<Real>(x, y, pq >> 1, pq & 1, r);
+                component_fit_pq3_sel<Real>(x, y, pq >> 1, pq & 1, r);
             }
             else if (lane >= 16 && first)
             {

@@ -356,12 +356,12 @@ __global__ void input_write_kernel(const double *density, const double *skew, in
 }
 
 // interleaved double coefficients (x, y) = scale * prediction
-__global__ void pred_to_xy_kernel(const float *pred, int nvox, double scale, double *xy)
+__global__ void pred_to_xy_kernel(const float *pred, int nvox, double sx, double sy, double *xy)
 {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nvox) return;
-    xy[2 * v] = scale * (double)pred[2 * v];
-    xy[2 * v + 1] = scale * (double)pred[2 * v + 1];
+    xy[2 * v] = sx * (double)pred[2 * v];
+    xy[2 * v + 1] = sy * (double)pred[2 * v + 1];
 }
 
 // target of a training pair: the level's regular double coefficients as FP32 pairs
@@ -1042,13 +1042,18 @@ int epr_unet_warm_start(epr_unet *net, epr_ctx *ctx, double *info)
     if (!epr::unet_input(net, *ctx, net->in0.p) || !forward(net, net->in0) || !check_flag(net))
         return net->err.empty() ? EPR_ERR_CUDA : EPR_ERR_ARG;
     // the prediction at unit scale as the level's coefficients, its energy terms, then the scale
-    // that minimises E(s p) = s^4 W + s^2 (reg - 2 y^T B x) + c
+    // that minimises E(s p) = s^4 W + s^2 (reg - 2 y^T B x) + c.  The reflection (x, -y) of the
+    // prediction has the same W and reg and the opposite cross term (its wedge is the negated
+    // one), so the same evaluation gives its quartic too: the orientation with the lower minimum
+    // is taken.
     const int nv = (int)net->in0.vox();
-    epr::unet::pred_to_xy_kernel<<<epr::unet::nblk(nv, 256), 256, 0, net->stream>>>(net->pred, nv, 1.0, ctx->levels[L].xy64);
+    epr::unet::pred_to_xy_kernel<<<epr::unet::nblk(nv, 256), 256, 0, net->stream>>>(net->pred, nv, 1.0, 1.0, ctx->levels[L].xy64);
     if (!net->cuda(cudaGetLastError(), "prediction") || !net->cuda(cudaStreamSynchronize(net->stream), "sync")) return EPR_ERR_CUDA;
     double e[3];
     if (!ctx->push_xy(L) || !ctx->energy(L, e)) return ctx->status ? ctx->status : EPR_ERR_CUDA;
-    const double W = e[2], a2 = e[1] + (e[0] - e[2] - ctx->c);
+    const double cross = e[0] - e[2] - ctx->c;  // -2 y^T B x
+    const bool reflect = cross > 0;
+    const double W = e[2], a2 = e[1] + (reflect ? -cross : cross);
     double s = 0, epred = ctx->c;
     if (W > 0 && a2 < 0)
     {
@@ -1061,13 +1066,13 @@ int epr_unet_warm_start(epr_unet *net, epr_ctx *ctx, double *info)
     const bool use = s > 0 && epred < eplain && epred < ctx->c;
     if (use)
     {
-        epr::unet::pred_to_xy_kernel<<<epr::unet::nblk(nv, 256), 256, 0, net->stream>>>(net->pred, nv, s, ctx->levels[L].xy64);
+        epr::unet::pred_to_xy_kernel<<<epr::unet::nblk(nv, 256), 256, 0, net->stream>>>(net->pred, nv, s, reflect ? -s : s, ctx->levels[L].xy64);
         if (!net->cuda(cudaGetLastError(), "prediction") || !net->cuda(cudaStreamSynchronize(net->stream), "sync") || !ctx->push_xy(L))
             return EPR_ERR_CUDA;
     }
     if (info)
     {
-        info[0] = use ? 1 : 0;
+        info[0] = use ? (reflect ? 2 : 1) : 0;
         info[1] = epred;
         info[2] = eplain;
         info[3] = s;

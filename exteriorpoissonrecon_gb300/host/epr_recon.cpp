@@ -9,7 +9,9 @@
 //   * only the regular indexer exists here, so --aRadius defaults to -1 and any other value is an
 //     error (the reference's default, 3, selects its adaptive octree indexer);
 //   * errors exit with a non-zero status (the reference prints and exits 0);
-//   * --project (blade fitting from a random start) is not offered; --density trees are not written.
+//   * --project (blade fitting from a random start) is not offered.
+// <out>.density.tree is written as the reference writes it (the estimator's tree, epr_write_density_tree),
+// with zero words where the reference's file holds memory addresses.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -416,6 +418,11 @@ int main(int argc, char **argv)
         }
         Put(fp, (uint32_t)a.depth);  // HierarchicalRegularIndexer::write (Hat.adaptive.inl:198-203)
         fclose(fp);
+        // <out>.density.tree: the density estimator (ExteriorPoissonRecon.cpp:272-277)
+        std::vector<double> xf;
+        for (int c = 0; c <= D; c++)
+            for (int r = 0; r <= D; r++) xf.push_back(v2w(c, r));
+        Check(ctx, epr_write_density_tree(ctx, xf.data(), (a.out + ".density.tree").c_str()), "epr_write_density_tree");
     }
     if (!a.grid.empty())
     {

@@ -103,6 +103,11 @@ class WarmStartNet:
         self._check(load().epr_unet_forward(self._h, ctypes.c_void_p(dev_input), None, ctypes.byref(l), ctypes.c_void_p(dev_target)))
         return l.value
 
+    def predict(self, dev_input: int | None = None):
+        """One forward pass on dev_input (device address) or the network's own input buffer; the
+        prediction stays in the network's device memory."""
+        self._check(load().epr_unet_forward(self._h, ctypes.c_void_p(dev_input) if dev_input else None, None, None, None))
+
     def train_step(self, inputs, targets, lr: float) -> float:
         b = len(inputs)
         ai = (ctypes.c_void_p * b)(*inputs)
@@ -117,8 +122,8 @@ class WarmStartNet:
         reference's random start there when the prediction does not lower the energy."""
         info = np.zeros(4)
         self._check(load().epr_unet_warm_start(self._h, r._h, info.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
-        return {"used": bool(info[0]), "energy_predicted": float(info[1]), "energy_random_start": float(info[2]),
-                "scale": float(info[3])}
+        return {"used": bool(info[0]), "reflected": bool(info[0] == 2), "energy_predicted": float(info[1]),
+                "energy_random_start": float(info[2]), "scale": float(info[3])}
 
 
 # ---------------------------------------------------------------------------------------------

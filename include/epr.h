@@ -46,9 +46,12 @@
  *       Reconstructor::Reconstructor + solve (ExteriorPoisson.h:59-81) for many inputs at once
  *   epr_generate_samples / epr_set_generated_samples
  *       the Sample tool's shapes and noise              Include/Samples.h, Sample/Sample.cpp:137-199
- *   epr_get_density
- *       the density estimator's tree data: TreeEstimator (GridSamples.h:232-277, DensityAndNoiseInfo
- *       GridSamples.h:79-94), which the reference writes to its .density.tree
+ *   epr_get_density / epr_get_density_refined
+ *       the density estimator's tree data and structure: TreeEstimator (GridSamples.h:232-277,
+ *       DensityAndNoiseInfo GridSamples.h:79-94)
+ *   epr_write_density_tree
+ *       the <out>.density.tree file: ExteriorPoissonRecon.cpp:272-277 with TreeEstimator::write
+ *       (GridSamples.inl:734-738) and RegularTreeNode::write (Misha/RegularTree.inl:615-642)
  *   epr_get_array
  *       read-only views of the reference's internal state (TreeEstimator::measure/noise/depth
  *       GridSamples.inl:838-862, S(E) ExteriorPoisson.h:290-307, _R/_B SystemEnergy.h:172-175)
@@ -228,6 +231,21 @@ int epr_get_solution(epr_ctx *ctx, int level, double *x, double *y);
  * creates hold zeros.  count receives the number of doubles; out may be NULL to query it. */
 int epr_get_density(epr_ctx *ctx, int level, double *out, size_t cap, size_t *count);
 
+/* The density tree's structure: out[cell] = 1 where the cell of tree depth t (0 .. depth+1; cells
+ * (2^t)^dim, axis 0 most significant) has children.  The root (t = 0) always has children and the
+ * cells of depth+1 never do.  count receives (2^t)^dim; out may be NULL to query it. */
+int epr_get_density_refined(epr_ctx *ctx, int t, uint8_t *out, size_t cap, size_t *count);
+
+/* Writes the density estimator's tree to `path` in the reference's .density.tree layout: the
+ * voxel-to-world transform (voxel_to_world: (dim+1)^2 doubles in the order the .tree stores them,
+ * element (column c, row r) at c (dim+1) + r) after one 8-byte zero word, the tree's nodes depth
+ * first (each node's 2^dim children as one block before their subtrees; 136-byte nodes in 3D,
+ * 208-byte in 4D: u16 depth, u16 offsets, parent and children words, weight, position and
+ * covariance sums), then the target samples per cell 2^(dim-2).  Words that hold memory addresses
+ * in the reference's file are written as zero (parent) or 1 (children present).  Needs a built
+ * context; EPR_ERR_ARG when the file cannot be written. */
+int epr_write_density_tree(epr_ctx *ctx, const double *voxel_to_world, const char *path);
+
 /* Named internal arrays copied to host memory: "measure", "noise", "depth" (per sample),
  * "S" (per finest element, packed), "leaf_depth", "R", "B" (per level, column stencils), "c".
  * count receives the number of doubles; out may be NULL to query it. */
@@ -350,10 +368,12 @@ int epr_unet_train_step(epr_unet *net, int batch, const void *const *dev_inputs,
                         float lr, double *loss);
 /* Warm start of a built context: predicts its level-L coefficients, scales them by the factor that
  * minimises the energy along the prediction (E(s p) is a quartic in s: one energy evaluation gives
- * it), and sets them as the level's coefficients; falls back to the reference's random start on
- * that level when the scaled prediction's energy is not below both the random start's and the zero
- * function's.  info (4 doubles, may be NULL): used (1 / 0), energy of the scaled prediction, energy
- * of the random start, scale. */
+ * it), and sets them as the level's coefficients; the prediction's reflection (x, -y), whose wedge
+ * is the negated one, is taken instead when its minimum is lower (the same evaluation gives it).
+ * Falls back to the reference's random start on that level when the scaled prediction's energy is
+ * not below both the random start's and the zero function's.  info (4 doubles, may be NULL): used
+ * (1, 2 when reflected, 0 when not used), energy of the scaled prediction, energy of the random
+ * start, scale. */
 int epr_unet_warm_start(epr_unet *net, epr_ctx *ctx, double *info);
 
 #ifdef __cplusplus

@@ -1816,6 +1816,13 @@ struct Oracle
             for (size_t i = 0; i < cells.size(); i++) v.push_back((double)(cellStart[i + 1] - cellStart[i]));
             return put(v);
         }
+        if (name == "density_refined")
+        {
+            // 1 where the density tree's depth-`level` cell has children (level 0..depth+1)
+            if (level < 0 || level > depth + 1) return -1;
+            std::vector<double> v(density.refined[level].begin(), density.refined[level].end());
+            return put(v);
+        }
         if (level < 0 || level > depth) return -1;
         if (name == "R") return put(levels[level].R);
         if (name == "B") return put(levels[level].B);

@@ -186,8 +186,9 @@ def make_zero_set(name, workload, n, seed, depth, ref_tree=None):
 
 
 def make_tree(name, workload, n, seed, depth, flags):
-    """The reference command line's own .tree output for a PLY input (frames stored in full), and
-    the regular coefficient grids the reference's Extract writes from it (--grid)."""
+    """The reference command line's own .tree and .density.tree outputs for a PLY input (frames
+    stored in full), and the regular coefficient grids the reference's Extract writes from the
+    .tree (--grid)."""
     pos, frames = samples.make_workload(workload, n, seed=seed)
     with tempfile.TemporaryDirectory() as td:
         ply = os.path.join(td, "in.ply")
@@ -197,6 +198,8 @@ def make_tree(name, workload, n, seed, depth, flags):
                        check=True, capture_output=True)
         with open(out + ".tree", "rb") as f:
             tree = np.frombuffer(f.read(), dtype=np.uint8)
+        with open(out + ".density.tree", "rb") as f:
+            density_tree = np.frombuffer(f.read(), dtype=np.uint8)
         subprocess.run([REF_EXTRACT, "--in", out + ".tree", "--grid", out, "--out", out + "_zero.ply"], check=True,
                        capture_output=True)
         grids = []
@@ -205,7 +208,7 @@ def make_tree(name, workload, n, seed, depth, flags):
                 grids.append(np.frombuffer(f.read(), dtype=np.uint8))
         V, F = read_mesh(out + "_zero.ply")
     fx = {"depth": np.array(depth), "world_pos": pos, "frames": frames, "flags": np.array(flags, dtype=str), "tree": tree,
-          "grid0": grids[0], "grid1": grids[1]}
+          "grid0": grids[0], "grid1": grids[1], "density_tree": density_tree}
     if pos.shape[1] == 3:  # the zero curve (the oracle's extraction is 3D)
         fx["zero_vertices"] = V
         fx["zero_simplices"] = np.array([list(f) for f in F], dtype=np.int64).reshape(len(F), -1)
