@@ -92,6 +92,10 @@ def parse():
                          "solved concurrently (torus knots + helices, depths 5-7)")
     ap.add_argument("--batch", type=int, default=64, help="reconstructions per batch")
     ap.add_argument("--batch-threads", type=int, default=0, help="host workers of the batch (0: 32)")
+    ap.add_argument("--batch-mode", default="lockstep", choices=["lockstep", "threads"],
+                    help="lockstep: one launch per level colour for all reconstructions, the relaxation one CUDA "
+                         "graph, block shapes from the autotuner (epr_batch_*); threads: host workers driving "
+                         "whole solves on their own streams (epr_batch_solve)")
     ap.add_argument("--profile-kernel", default=None,
                     help="launch one kernel family a few times for a profiler instead of benchmarking: gs, energy, "
                          "quadfit, prolong, gn, lgs, residual, assemble, biquad (with --depth, --samples, "
@@ -336,7 +340,7 @@ def bench_batch(args, ws, rank, local, pg):
               "precision": args.precision,
               "fp64_levels": [args.fp64_from, args.fp64_levels] if args.precision == "fp32" else None,
               "band_precision": args.band_precision if args.precision == "fp32" else None,
-              "threads": args.batch_threads,
+              "threads": args.batch_threads, "mode": args.batch_mode,
               "l2": "working set (tens of GB of stencils) far larger than L2 (no flush)",
               "parallelism": f"replicas{ws}"}
     if args.impl == "reference":
@@ -356,9 +360,22 @@ def bench_batch(args, ws, rank, local, pg):
     make = lambda prec, kw: [epr.Reconstructor(3, d, pu, sk, build=False, precision=prec, device=local, **kw)
                              for d, pu, sk in inputs]
     recons = make(args.precision, mixed)
-    # the first batch builds and launches directly; the second captures each context's CUDA graph
-    for i in range(max(args.warmup, 2)):
-        epr.batch_solve(recons, build=(i == 0), threads=args.batch_threads)
+    tuning = None
+    if args.batch_mode == "lockstep":
+        lock = epr.LockstepBatch(recons, threads=args.batch_threads)
+        # the first run builds every member and captures the batch's graph; the autotuner then
+        # times the block shapes of every per-colour level on the members' data
+        lock.run(build=True)
+        tune_ms = lock.tune(reps=3)
+        tuning = {"tiles": lock.info()["tiles"], "sweep_ms_per_shape": tune_ms.tolist()}
+        for i in range(max(args.warmup, 2)):
+            lock.run()
+        solve_batch = lambda: lock.run()
+    else:
+        # the first batch builds and launches directly; the second captures each context's CUDA graph
+        for i in range(max(args.warmup, 2)):
+            epr.batch_solve(recons, build=(i == 0), threads=args.batch_threads)
+        solve_batch = lambda: epr.batch_solve(recons, build=False, threads=args.batch_threads)
     build_ms = sum(r.stats.build_ms for r in recons)
     barrier(pg)
     clocks = ClockSampler(local)
@@ -366,9 +383,9 @@ def bench_batch(args, ws, rank, local, pg):
     times, launches = [], 0
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        st = epr.batch_solve(recons, build=False, threads=args.batch_threads)
+        st = solve_batch()
         times.append(time.perf_counter() - t0)
-        launches += sum(x["kernel_launches"] for x in st)
+        launches += st[0]["kernel_launches"] if args.batch_mode == "lockstep" else sum(x["kernel_launches"] for x in st)
     clk = clocks.stop()
     barrier(pg)
     per_step_s = allmax(pg, statistics.mean(times))
@@ -385,7 +402,14 @@ def bench_batch(args, ws, rank, local, pg):
         t0 = time.perf_counter()
         rs = [epr.Reconstructor(3, d, pu, sk, build=False, precision=args.precision, device=local, **mixed)
               for d, pu, sk in inputs]
-        epr.batch_solve(rs, build=True, threads=args.batch_threads)
+        if args.batch_mode == "lockstep":
+            lb = epr.LockstepBatch(rs, threads=args.batch_threads)
+            for l, t in enumerate(tuning["tiles"]):
+                lb.set_tile(l, t)
+            lb.run(build=True)
+            lb.close()
+        else:
+            epr.batch_solve(rs, build=True, threads=args.batch_threads)
         for r in rs:
             r.solution()
         e2e_s.append(time.perf_counter() - t0)
@@ -401,10 +425,15 @@ def bench_batch(args, ws, rank, local, pg):
             "e2e": {"value": e2e_v, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "build_ms_sum": build_ms,
             "unknown_sweeps_per_s": ws * 2 * sum(schedule_node_updates(3, d) for d in depths) / per_step_s}
-    # one at a time: the same batch solved by one host worker
-    t0 = time.perf_counter()
-    epr.batch_solve(recons, build=False, threads=1)
-    line["sequential_solves_per_s"] = len(inputs) / (time.perf_counter() - t0)
+    if tuning is not None:
+        line["autotune"] = tuning
+        line["relax_ms"] = lock.info()["relax_ms"]
+    # the same batch by host workers on their own streams, and one at a time
+    for name, thr in (("threads_solves_per_s", args.batch_threads), ("sequential_solves_per_s", 1)):
+        epr.batch_solve(recons, build=False, threads=thr)
+        t0 = time.perf_counter()
+        epr.batch_solve(recons, build=False, threads=thr)
+        line[name] = len(inputs) / (time.perf_counter() - t0)
     # error of every result against the double-precision run of the same schedule
     if args.precision == "fp32" and not args.no_fp64_check:
         for r in recons:

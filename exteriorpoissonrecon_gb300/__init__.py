@@ -180,6 +180,16 @@ def load():
     L.epr_set_generated_samples.argtypes = [vp, ctypes.POINTER(Sampler), ctypes.c_size_t, P]
     L.epr_batch_solve.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                   ctypes.POINTER(Stats), ctypes.POINTER(ctypes.c_int)]
+    L.epr_batch_create.restype = vp
+    L.epr_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int]
+    L.epr_batch_run.argtypes = [vp, ctypes.c_int, vp, vp]
+    L.epr_batch_tune.argtypes = [vp, ctypes.c_int, vp]
+    L.epr_batch_info.argtypes = [vp, vp, ctypes.c_int, vp, vp]
+    L.epr_batch_set_tile.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.epr_batch_destroy.argtypes = [vp]
+    L.epr_batch_destroy.restype = None
+    L.epr_batch_last_error.argtypes = [vp]
+    L.epr_batch_last_error.restype = ctypes.c_char_p
     L.epr_get_solution.argtypes = [vp, ctypes.c_int, P, P]
     L.epr_get_array.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, P, ctypes.c_size_t,
                                 ctypes.POINTER(ctypes.c_size_t)]
@@ -508,3 +518,60 @@ def batch_solve(recons, build: bool = True, threads: int = 0):
     if rc != EPR_OK:
         raise EprError(f"[{rc}] " + L.epr_global_error().decode())
     return [stats[i].as_dict() for i in range(n)]
+
+
+class LockstepBatch:
+    """Many 3D Reconstructors solved in lockstep (epr_batch_*): one launch per level colour for all
+    of them, the relaxation one CUDA graph, block shapes per level from the autotuner.  Each
+    result is the one its Reconstructor gives alone."""
+
+    def __init__(self, recons, threads: int = 0):
+        self.recons = list(recons)
+        L = load()
+        n = len(self.recons)
+        self._handles = (ctypes.c_void_p * max(n, 1))(*[r._h for r in self.recons])
+        self._h = L.epr_batch_create(self._handles, n, int(threads))
+        if not self._h:
+            raise EprError(L.epr_batch_last_error(None).decode())
+
+    def _check(self, rc):
+        if rc != EPR_OK:
+            raise EprError(f"[{rc}] " + load().epr_batch_last_error(self._h).decode())
+
+    def run(self, build: bool = False):
+        """Builds (when `build`) and solves every member; returns their stats dicts."""
+        n = len(self.recons)
+        stats = (Stats * max(n, 1))()
+        status = (ctypes.c_int * max(n, 1))()
+        rc = load().epr_batch_run(self._h, int(bool(build)), ctypes.byref(stats), ctypes.byref(status))
+        for i, r in enumerate(self.recons):
+            if status[i] == EPR_OK:
+                ctypes.memmove(ctypes.byref(r.stats), ctypes.byref(stats[i]), ctypes.sizeof(Stats))
+        self._check(rc)
+        return [stats[i].as_dict() for i in range(n)]
+
+    def tune(self, reps: int = 3) -> np.ndarray:
+        """Runs the autotuner; returns the (tuned levels, 3) mean sweep times per block shape."""
+        out = np.zeros(3 * 32)
+        self._check(load().epr_batch_tune(self._h, int(reps), out.ctypes.data_as(ctypes.c_void_p)))
+        rows = out.reshape(-1, 3)
+        return rows[:int(np.count_nonzero(rows.any(axis=1)))]
+
+    def set_tile(self, level: int, tile: int):
+        """Block shape index (0-2) of `level`'s colour kernel (level -1: every level)."""
+        self._check(load().epr_batch_set_tile(self._h, int(level), int(tile)))
+
+    def info(self) -> dict:
+        tiles = (ctypes.c_int * 16)()
+        ms = ctypes.c_double(0)
+        launches = ctypes.c_longlong(0)
+        self._check(load().epr_batch_info(self._h, tiles, 16, ctypes.byref(ms), ctypes.byref(launches)))
+        return {"tiles": list(tiles), "relax_ms": ms.value, "graph_launches": launches.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().epr_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

@@ -223,23 +223,6 @@ int with_dim(Context *c, F &&f)
     return f(std::integral_constant<int, 4>{});
 }
 
-template <typename Real>
-LevelPtrs<Real> level_ptrs(Context *c, int l)
-{
-    Level &L = c->levels[l];
-    LevelPtrs<Real> p;
-    p.level = l;
-    p.N = L.N;
-    if constexpr (std::is_same<Real, double>::value) { p.xy = L.xy64; p.A = L.A64; p.B = L.B64; }
-    else if constexpr (std::is_same<Real, df>::value) { p.xy = L.xyd; p.A = L.Ad; p.B = L.Bd; return p; }
-    else { p.xy = L.xy32; p.A = L.A32; p.B = L.B32; }
-    if (L.Acb && c->lvl32(l) == std::is_same<Real, float>::value)
-    {
-        p.Acb = (const Real *)L.Acb;
-        p.Bcb = (const Real *)L.Bcb;
-    }
-    return p;
-}
 
 // Energies are evaluated in double at every level, whatever arithmetic the level relaxes in: a
 // float or double-float level's working copy is first converted into its double coefficients,
@@ -450,12 +433,12 @@ bool Context::relax_levels(int minD, int maxD, bool useGraph)
 // The reference's cascadic schedule (ExteriorPoisson.h:315-409).  Each level is relaxed by paired
 // Gauss-Seidel (EPR_SOLVER_CASCADIC, the reference) or by alternating-solve rounds with linear
 // multigrid V-cycles until the gradient falls by `tolerance` (EPR_SOLVER_MULTIGRID).
-bool Context::solve_cascadic()
+// the solve's first part: every level cleared (but a warm start's level) and the reference's random
+// start on the coarsest solve level
+bool Context::solve_prologue()
 {
     const int minD = std::min(P.min_solve_depth, depth);
-    const int maxD = P.max_solve_depth < 0 ? depth : std::min(P.max_solve_depth, depth);
-    bool fp32 = P.precision == EPR_FP32;
-    cudaEventRecord(ev0, stream);
+    const bool fp32 = P.precision == EPR_FP32;
     for (int l = 0; l <= depth; l++)
     {
         if (P.warm_start && l == minD) continue;  // the given start
@@ -465,7 +448,15 @@ bool Context::solve_cascadic()
     }
     if (!P.warm_start && !cuda_ok(cudaMemsetAsync(d_kexp, 0, sizeof(int) * (depth + 1), stream), "clear")) return false;
     // random initial guess at the coarsest solve level, scaled to the target's magnitude
-    if (!P.warm_start && !random_start(minD, nullptr)) return false;
+    return P.warm_start || random_start(minD, nullptr);
+}
+
+bool Context::solve_cascadic()
+{
+    const int minD = std::min(P.min_solve_depth, depth);
+    const int maxD = P.max_solve_depth < 0 ? depth : std::min(P.max_solve_depth, depth);
+    cudaEventRecord(ev0, stream);
+    if (!solve_prologue()) return false;
     if (P.single_level)
     {
         // prolong the initial guess to the finest solve level, clear the coarser levels and relax
@@ -525,6 +516,14 @@ bool Context::solve_cascadic()
         stats.reached_target = e[0] + e[1] <= P.target_energy ? 1 : 0;
     }
     cudaEventRecord(ev1, stream);
+    return solve_epilogue();
+}
+
+// the solve's last part, after ev1 was recorded behind the relaxation: the error flag, the timing,
+// the final energy and the solution arrays every level exports
+bool Context::solve_epilogue()
+{
+    const int maxD = P.max_solve_depth < 0 ? depth : std::min(P.max_solve_depth, depth);
     if (!check_errors()) return false;
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0, ev1);

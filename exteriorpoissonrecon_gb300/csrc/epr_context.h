@@ -111,11 +111,33 @@ struct Context
     bool upload_xy(int l, const double *x, const double *y);
     bool download_xy(int l, double *x, double *y, bool fromSolution);
     bool solve_cascadic();
+    bool solve_prologue();  // levels cleared, the random start (solve_cascadic's first part)
+    bool solve_epilogue();  // error flag, timing, final energy, solution arrays (after ev1)
     // the reference's random start on `level` (rand() pairs after srand(seed), scaled by the fourth
     // root of c over the wedge square norm, ExteriorPoisson.h:333-341), set as the level's
     // coefficients; *energy (may be null) receives its total energy
     bool random_start(int level, double *energy);
 };
+
+// the arrays of level l as the solve kernels of arithmetic Real see them (the colour-blocked
+// stencil copies only where the level relaxes in that arithmetic)
+template <typename Real>
+inline LevelPtrs<Real> level_ptrs(Context *c, int l)
+{
+    Level &L = c->levels[l];
+    LevelPtrs<Real> p;
+    p.level = l;
+    p.N = L.N;
+    if constexpr (std::is_same<Real, double>::value) { p.xy = L.xy64; p.A = L.A64; p.B = L.B64; }
+    else if constexpr (std::is_same<Real, df>::value) { p.xy = L.xyd; p.A = L.Ad; p.B = L.Bd; return p; }
+    else { p.xy = L.xy32; p.A = L.A32; p.B = L.B32; }
+    if (L.Acb && c->lvl32(l) == std::is_same<Real, float>::value)
+    {
+        p.Acb = (const Real *)L.Acb;
+        p.Bcb = (const Real *)L.Bcb;
+    }
+    return p;
+}
 
 // the text epr_global_error() returns (per host thread)
 void set_global_error(const std::string &msg);

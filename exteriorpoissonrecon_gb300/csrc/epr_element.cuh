@@ -31,16 +31,13 @@ struct Component
     static constexpr int P = (K == 0) ? 1 : (K <= 2) ? 2 : (K <= 5) ? 3 : -1;
     static constexpr int Q = K - P * (P - 1) / 2;
     static constexpr int M = D - 2;
+    // the m-th axis that is neither P nor Q (Q < P): branch-free, so that with m a constant after
+    // unrolling every corner index below folds to a constant and the corner arrays the callers
+    // index stay in registers
     static constexpr int other(int m)
     {
-        int c = 0;
-        for (int d = 0; d < D; d++)
-        {
-            if (d == P || d == Q) continue;
-            if (c == m) return d;
-            c++;
-        }
-        return -1;
+        const int a = m + (m >= Q ? 1 : 0);
+        return a + (a >= P ? 1 : 0);
     }
     // corner index with the given bits on P, Q and the others (others: bit (M-1-m) of bo <-> axis other(m))
     static constexpr int corner(int bP, int bQ, int bo)
@@ -287,44 +284,12 @@ __device__ __forceinline__ void component_fit(const Real *x, const Real *y, int 
 
 // Component 0 of a 3D element in the canonical orientation (corner 0), restricted to the Gauss
 // points with the given (gp, gq): the share of one of four threads that split a component's
-// integral (the values of the points are those of component_fit).
+// integral (the values of the points are those of component_fit).  The pair is a run-time value:
+// the A-differences are interpolated along B with the hat values of the pair's own Gauss point
+// (scalars picked from two constants), so that threads with different pairs run one instruction
+// stream and the corner arrays stay constant-indexed in registers.
 template <typename Real>
 __device__ __forceinline__ void component_fit_pq3(const Real *x, const Real *y, int gp, int gq, Real *h)
-{
-    Real txP[2][2], txQ[2][2], tyP[2][2], tyQ[2][2];
-    derivative_partial<3, 0, true>(x, txP);
-    derivative_partial<3, 0, false>(x, txQ);
-    derivative_partial<3, 0, true>(y, tyP);
-    derivative_partial<3, 0, false>(y, tyQ);
-    const Real w2 = (Real)(Gauss::W2(gp) * Gauss::W2(gq));
-    const Real hq = hat2<Real>(0, gq), hp = hat2<Real>(0, gp);
-#pragma unroll
-    for (int go = 0; go < 3; go++)
-    {
-        const Real lo = hat3<Real>(0, go);
-        const Real w = w2 * (Real)other_weight<1>(go);
-        const Real phP = (Real)-1 * hq * lo;
-        const Real phQ = (Real)-1 * hp * lo;
-        const Real xp = derivative_at<1, Real>(txP[gq], go), xq = derivative_at<1, Real>(txQ[gp], go);
-        const Real yp = derivative_at<1, Real>(tyP[gq], go), yq = derivative_at<1, Real>(tyQ[gp], go);
-        const Real W = yp * xq - xp * yq;
-        const Real U = yp * phQ - phP * yq;
-        const Real V = phP * xq - xp * phQ;
-        const Real wU = w * U, wV = w * V;
-        h[0] += wU * U;
-        h[1] += wV * V;
-        h[2] += wU * V;
-        h[3] += wU * W;
-        h[4] += wV * W;
-    }
-}
-
-// component_fit_pq3 for a run-time Gauss-point pair: the A-differences are interpolated along B
-// with the hat values of the pair's own Gauss point (scalars picked from two constants), which
-// forms exactly the table row that component_fit_pq3 indexes, while the corner arrays stay
-// constant-indexed in registers (the products and their order are component_fit_pq3's)
-template <typename Real>
-__device__ __forceinline__ void component_fit_pq3_sel(const Real *x, const Real *y, int gp, int gq, Real *h)
 {
     using Cp = Component<3, 0>;
     const Real q0 = gq ? hat2<Real>(0, 1) : hat2<Real>(0, 0), q1 = gq ? hat2<Real>(1, 1) : hat2<Real>(1, 0);

@@ -94,4 +94,50 @@ void launch_split_pairs(const double *xy, double *x, double *y, int64_t n, cudaS
 void launch_merge_pairs(const double *x, const double *y, double *xy, int64_t n, cudaStream_t st);
 void launch_convert_f2d(const float *in, double *out, int64_t n, cudaStream_t st);
 
+// ---------------------------------------------------------------------------------------------
+// Lockstep batches (3D): one launch relaxes the same level and colour of many reconstructions,
+// each with its own arrays, sweep count and error flag.  Every reconstruction's nodes see exactly
+// the arithmetic of its own solve's kernels for that level, so the batch gives each one its own
+// solve's bits.
+// ---------------------------------------------------------------------------------------------
+template <typename Real>
+struct BatchJob
+{
+    LevelPtrs<Real> L;
+    unsigned int *err = nullptr;
+    int *kexp = nullptr;  // the reconstruction's exponent table (double-float levels), else null
+    int iters = 0;        // sweeps of this level
+    int separate = 0;
+};
+// a level-to-level transfer of one reconstruction: src and dst arrays of the transfer's types
+struct XferJob
+{
+    const void *src = nullptr;
+    void *dst = nullptr;
+    int *kexp = nullptr;
+};
+// the colour kernels' block shapes a batch may pick (none changes any node's arithmetic):
+// levels whose colours have at most 125 nodes: nodes per block of the point-split kernel;
+// larger levels: threads per block of the lane kernel (8 lanes per node)
+constexpr int kSplitTiles[3] = {1, 2, 4};
+constexpr int kLanesTiles[3] = {64, 128, 256};
+constexpr int kDefaultTile = 1;  // index into the tables: the solo solve's shapes (2 nodes, 128 threads)
+// all sweeps of 3D level 0 or 1 of `count` reconstructions (jobs[0..count))
+template <typename Real>
+void launch_tiny_batch(const BatchJob<Real> *jobs, int level, int count, cudaStream_t s);
+// one colour of a level >= 2 of jobs[0..count) with the block shape kSplitTiles / kLanesTiles[tile]
+template <typename Real>
+void launch_colour_batch(const BatchJob<Real> *jobs, int level, int colour, int count, int tile, cudaStream_t s);
+// a new exponent for each double-float level of jobs[0..count) (once per sweep)
+void launch_df_rescale_batch(const BatchJob<df> *jobs, int count, cudaStream_t s);
+// fine += P coarse for jobs[0..count) (src coarse, dst fine)
+template <typename Real>
+void launch_prolong_add_batch(const XferJob *jobs, int coarseLevel, int count, cudaStream_t s);
+// elementwise n values: float -> double, double -> float, double-float -> double (the exponent of
+// `level`), double -> double-float (a new exponent for `level`, one block per reconstruction)
+void launch_f2d_batch(const XferJob *jobs, int64_t n, int count, cudaStream_t s);
+void launch_d2f_batch(const XferJob *jobs, int64_t n, int count, cudaStream_t s);
+void launch_df_pull_batch(const XferJob *jobs, int64_t n, int level, int count, cudaStream_t s);
+void launch_df_push_batch(const XferJob *jobs, int64_t n, int level, int count, cudaStream_t s);
+
 }  // namespace epr

@@ -789,20 +789,34 @@ __device__ __forceinline__ void gs_update_split3(const LevelPtrs<Real> &L, Real 
 // latency-bound
 constexpr int kSplitNodes = 2;
 constexpr int64_t kSplitMaxColourNodes = 125;
-template <typename Real>
-__global__ void __launch_bounds__(128 * kSplitNodes) gs_colour_split3_kernel(LevelPtrs<Real> L, Colour<3> col, int64_t cbBase,
-                                                                              unsigned int *err, int separate,
-                                                                              const int *kexp = nullptr)
+// NPB nodes per block (block = 128 NPB threads); the block shape does not change any node's arithmetic
+template <typename Real, int NPB>
+__device__ __forceinline__ void gs_split3_body(const LevelPtrs<Real> &L, const Colour<3> &col, int64_t cbBase, unsigned int *err,
+                                               int separate, const int *kexp, int block)
 {
-    __shared__ Real part[kSplitNodes][4][5];
+    __shared__ Real part[NPB][4][5];
     const Real wmul = wedge_mult<Real>(kexp, L.level);
     Grid<3> g(L.level);
-    const int64_t j = (int64_t)blockIdx.x * kSplitNodes + (threadIdx.x >> 7);
+    const int64_t j = (int64_t)block * NPB + (threadIdx.x >> 7);
     const bool active = j < col.n;
     int I[3] = {0, 0, 0};
     if (active) col.node(j, I);
     const Real *Ac = L.Acb ? L.Acb + cbBase : nullptr, *Bc = L.Bcb ? L.Bcb + cbBase : nullptr;
     gs_update_split3<Real>(L, L.xy, g, I, active, err, separate, Ac, Bc, j, col.n, part[threadIdx.x >> 7], wmul);
+}
+template <typename Real>
+__global__ void __launch_bounds__(128 * kSplitNodes) gs_colour_split3_kernel(LevelPtrs<Real> L, Colour<3> col, int64_t cbBase,
+                                                                              unsigned int *err, int separate,
+                                                                              const int *kexp = nullptr)
+{
+    gs_split3_body<Real, kSplitNodes>(L, col, cbBase, err, separate, kexp, blockIdx.x);
+}
+// the same colour of every reconstruction of a lockstep batch: grid.y = reconstruction
+template <typename Real, int NPB>
+__global__ void __launch_bounds__(128 * NPB) gs_colour_split3_batch_kernel(const BatchJob<Real> *jobs, Colour<3> col, int64_t cbBase)
+{
+    const BatchJob<Real> &b = jobs[blockIdx.y];
+    gs_split3_body<Real, NPB>(b.L, col, cbBase, b.err, b.separate, b.kexp, blockIdx.x);
 }
 
 template <int D, typename Real>
@@ -823,29 +837,46 @@ __device__ __forceinline__ void gs_update_lanes(const LevelPtrs<Real> &L, const 
 template <int D, typename Real>
 constexpr int lanes_min_blocks() { return (D == 3 && sizeof(Real) == 4) ? 10 : 1; }
 
+template <int D, typename Real, bool Packed, int TPB>
+__device__ __forceinline__ void gs_lanes_body(const LevelPtrs<Real> &L, const Colour<D> &col, int64_t cbBase, unsigned int *err,
+                                              int separate, int bx, int by, int bz)
+{
+    Grid<D> g(L.level);
+    constexpr int NPB = TPB >> D;
+    const int A = threadIdx.x & ((1 << D) - 1);
+    const int tl = bx * NPB + (threadIdx.x >> D);
+    int I[D];
+    I[D - 1] = 2 * tl + col.par[D - 1];
+    I[D - 2] = 2 * by + col.par[D - 2];
+    if constexpr (D == 3) I[0] = 2 * bz + col.par[0];
+    else
+    {
+        I[1] = 2 * (bz % col.cnt[1]) + col.par[1];
+        I[0] = 2 * (bz / col.cnt[1]) + col.par[0];
+    }
+    // index of the node in the colour (axis 0 slowest)
+    const int64_t jc = ((int64_t)bz * col.cnt[D - 2] + by) * col.cnt[D - 1] + tl;
+    const Real *Ac = L.Acb ? L.Acb + cbBase : nullptr, *Bc = L.Bcb ? L.Bcb + cbBase : nullptr;
+    gs_update_lanes_at<D, Real, Packed>(L, L.xy, g, I, tl < col.cnt[D - 1], A, err, separate, Ac, Bc, jc, col.n);
+}
+
 template <int D, typename Real, int MinBlocks = lanes_min_blocks<D, Real>(), bool Packed = false>
 __global__ void __launch_bounds__(kThreads, MinBlocks) gs_colour_lanes_kernel(LevelPtrs<Real> L, Colour<D> col,
                                                                               int64_t cbBase, unsigned int *err,
                                                                               int separate)
 {
-    Grid<D> g(L.level);
-    constexpr int NPB = kThreads >> D;
-    const int A = threadIdx.x & ((1 << D) - 1);
-    const int tl = blockIdx.x * NPB + (threadIdx.x >> D);
-    int I[D];
-    I[D - 1] = 2 * tl + col.par[D - 1];
-    I[D - 2] = 2 * (int)blockIdx.y + col.par[D - 2];
-    if constexpr (D == 3) I[0] = 2 * (int)blockIdx.z + col.par[0];
-    else
-    {
-        int z = (int)blockIdx.z;
-        I[1] = 2 * (z % col.cnt[1]) + col.par[1];
-        I[0] = 2 * (z / col.cnt[1]) + col.par[0];
-    }
-    // index of the node in the colour (axis 0 slowest)
-    const int64_t jc = ((int64_t)blockIdx.z * col.cnt[D - 2] + blockIdx.y) * col.cnt[D - 1] + tl;
-    const Real *Ac = L.Acb ? L.Acb + cbBase : nullptr, *Bc = L.Bcb ? L.Bcb + cbBase : nullptr;
-    gs_update_lanes_at<D, Real, Packed>(L, L.xy, g, I, tl < col.cnt[D - 1], A, err, separate, Ac, Bc, jc, col.n);
+    gs_lanes_body<D, Real, Packed, kThreads>(L, col, cbBase, err, separate, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// the same colour of every reconstruction of a lockstep batch (3D): block = TPB threads (TPB / 8
+// nodes along the last axis), grid.z = reconstruction x the colour's count on axis 0
+template <typename Real, int TPB, int MinBlocks, bool Packed>
+__global__ void __launch_bounds__(TPB, MinBlocks) gs_colour_lanes_batch_kernel(const BatchJob<Real> *jobs, Colour<3> col,
+                                                                               int64_t cbBase)
+{
+    const int m = blockIdx.z / col.cnt[0], bz = blockIdx.z - m * col.cnt[0];
+    const BatchJob<Real> &b = jobs[m];
+    gs_lanes_body<3, Real, Packed, TPB>(b.L, col, cbBase, b.err, b.separate, blockIdx.x, blockIdx.y, bz);
 }
 
 // Flat variant: consecutive groups of 2^D threads take consecutive nodes of the colour (32-bit
@@ -1023,8 +1054,7 @@ __device__ __forceinline__ bool node_step_tiny(const Real *q, int separate, Real
 }
 
 template <typename Real, int LEVEL>
-__global__ void __launch_bounds__(LEVEL == 0 ? 32 : 256) gs_tiny_kernel(LevelPtrs<Real> L, int iters, unsigned int *err,
-                                                                          int separate, int *kexp)
+__device__ __forceinline__ void gs_tiny_body(const LevelPtrs<Real> &L, int iters, unsigned int *err, int separate, int *kexp)
 {
     static_assert(LEVEL == 0 || LEVEL == 1, "resolution 1 or 2");
     constexpr int NW = LEVEL == 0 ? 1 : 8;  // incidences per colour
@@ -1111,7 +1141,7 @@ __global__ void __launch_bounds__(LEVEL == 0 ? 32 : 256) gs_tiny_kernel(LevelPtr
                     x[cc] = v.x;
                     y[cc] = v.y;
                 }
-                component_fit_pq3_sel<Real>(x, y, pq >> 1, pq & 1, r);
+                component_fit_pq3<Real>(x, y, pq >> 1, pq & 1, r);
             }
             else if (lane >= 16 && first)
             {
@@ -1210,6 +1240,22 @@ __global__ void __launch_bounds__(LEVEL == 0 ? 32 : 256) gs_tiny_kernel(LevelPtr
     for (int k = threadIdx.x; k < NN; k += blockDim.x) reinterpret_cast<Real2<Real> *>(L.xy)[k] = xy[k];
 }
 
+template <typename Real, int LEVEL>
+__global__ void __launch_bounds__(LEVEL == 0 ? 32 : 256) gs_tiny_kernel(LevelPtrs<Real> L, int iters, unsigned int *err,
+                                                                          int separate, int *kexp)
+{
+    gs_tiny_body<Real, LEVEL>(L, iters, err, separate, kexp);
+}
+
+// every reconstruction of a lockstep batch at once: one block per reconstruction, each with its
+// own sweep count
+template <typename Real, int LEVEL>
+__global__ void __launch_bounds__(LEVEL == 0 ? 32 : 256) gs_tiny_batch_kernel(const BatchJob<Real> *jobs)
+{
+    const BatchJob<Real> &b = jobs[blockIdx.x];
+    gs_tiny_body<Real, LEVEL>(b.L, b.iters, b.err, b.separate, b.kexp);
+}
+
 template <int D, typename Real>
 __global__ void __launch_bounds__(kThreads) gn_matvec_kernel(LevelPtrs<Real> L, const Real *xy, const Real *dxy, Real *out)
 {
@@ -1253,10 +1299,9 @@ __global__ void __launch_bounds__(kThreads) gn_matvec_kernel(LevelPtrs<Real> L, 
 }
 
 template <int D, typename Real>
-__global__ void prolong_kernel(int coarseLevel, const Real *coarse, Real *fine, int add)
+__device__ __forceinline__ void prolong_at(int coarseLevel, const Real *coarse, Real *fine, int add, int64_t i)
 {
     Grid<D> gc(coarseLevel), gf(coarseLevel + 1);
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= gf.N) return;
     int F[D];
     gf.node(i, F);
@@ -1282,6 +1327,30 @@ __global__ void prolong_kernel(int coarseLevel, const Real *coarse, Real *fine, 
     Real2<Real> *o = reinterpret_cast<Real2<Real> *>(fine);
     if (add) { Real2<Real> cur = o[i]; o[i] = Real2<Real>{cur.x + sx, cur.y + sy}; }
     else o[i] = Real2<Real>{sx, sy};
+}
+template <int D, typename Real>
+__global__ void prolong_kernel(int coarseLevel, const Real *coarse, Real *fine, int add)
+{
+    prolong_at<D, Real>(coarseLevel, coarse, fine, add, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+// grid.y = reconstruction of a lockstep batch
+template <typename Real>
+__global__ void prolong_add_batch_kernel(const XferJob *jobs, int coarseLevel)
+{
+    const XferJob &j = jobs[blockIdx.y];
+    prolong_at<3, Real>(coarseLevel, (const Real *)j.src, (Real *)j.dst, 1, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+__global__ void f2d_batch_kernel(const XferJob *jobs, int64_t n)
+{
+    const XferJob &j = jobs[blockIdx.y];
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) ((double *)j.dst)[i] = (double)((const float *)j.src)[i];
+}
+__global__ void d2f_batch_kernel(const XferJob *jobs, int64_t n)
+{
+    const XferJob &j = jobs[blockIdx.y];
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) ((float *)j.dst)[i] = (float)((const double *)j.src)[i];
 }
 
 template <int D, typename Real>
@@ -1509,16 +1578,23 @@ int launch_gs_sweeps(const LevelPtrs<Real> &L, int iters, unsigned int *err, cud
 // ---------------------------------------------------------------------------------------------
 // double-float levels (3D levels 0-3 of the float solve's coarse band)
 // ---------------------------------------------------------------------------------------------
-__global__ void df_rescale_kernel(df *xy, int64_t n, int *kexp, int level)
+__device__ __forceinline__ void df_rescale_body(df *xy, int64_t n, int *kexp, int level)
 {
     const int shift = df_rescale_shift(xy, n);
     if (!shift) return;
     for (int64_t k = threadIdx.x; k < n; k += blockDim.x) xy[k] = ldexp_df(xy[k], shift);
     if (threadIdx.x == 0) kexp[level] -= shift;
 }
+__global__ void df_rescale_kernel(df *xy, int64_t n, int *kexp, int level) { df_rescale_body(xy, n, kexp, level); }
+// one block per reconstruction of a lockstep batch
+__global__ void df_rescale_batch_kernel(const BatchJob<df> *jobs)
+{
+    const BatchJob<df> &b = jobs[blockIdx.x];
+    df_rescale_body(b.L.xy, 2 * b.L.N, b.kexp, b.L.level);
+}
 
 // double coefficients -> pairs at the level's new exponent (the largest magnitude in [1, 2))
-__global__ void df_push_kernel(const double *in, df *out, int64_t n, int *kexp, int level)
+__device__ __forceinline__ void df_push_body(const double *in, df *out, int64_t n, int *kexp, int level)
 {
     __shared__ double wmax[32];
     __shared__ int k;
@@ -1537,6 +1613,19 @@ __global__ void df_push_kernel(const double *in, df *out, int64_t n, int *kexp, 
     }
     __syncthreads();
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) out[i] = df(ldexp(in[i], -k));
+}
+__global__ void df_push_kernel(const double *in, df *out, int64_t n, int *kexp, int level) { df_push_body(in, out, n, kexp, level); }
+__global__ void df_push_batch_kernel(const XferJob *jobs, int64_t n, int level)
+{
+    const XferJob &j = jobs[blockIdx.x];
+    df_push_body((const double *)j.src, (df *)j.dst, n, j.kexp, level);
+}
+__global__ void df_pull_batch_kernel(const XferJob *jobs, int64_t n, int level)
+{
+    const XferJob &j = jobs[blockIdx.y];
+    const int k = j.kexp[level];
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) ((double *)j.dst)[i] = ldexp((double)((const df *)j.src)[i], k);
 }
 
 __global__ void df_pull_kernel(const df *in, double *out, int64_t n, const int *kexp, int level)
@@ -1682,6 +1771,109 @@ void launch_convert_f2d(const float *in, double *out, int64_t n, cudaStream_t st
 {
     if (n) f2d_kernel<<<blocks_for(n, 256), 256, 0, st>>>(in, out, n);
 }
+
+// ---------------------------------------------------------------------------------------------
+// lockstep batches (3D)
+// ---------------------------------------------------------------------------------------------
+template <typename Real>
+void launch_tiny_batch(const BatchJob<Real> *jobs, int level, int count, cudaStream_t s)
+{
+    if (count <= 0) return;
+    if (level == 0) gs_tiny_batch_kernel<Real, 0><<<count, 32, 0, s>>>(jobs);
+    else gs_tiny_batch_kernel<Real, 1><<<count, 256, 0, s>>>(jobs);
+}
+
+template <typename Real, int TPB>
+static void launch_lanes_batch(const BatchJob<Real> *jobs, const Grid<3> &g, const Colour<3> &col, int64_t cb, int count,
+                               cudaStream_t s)
+{
+    constexpr bool kFloat = std::is_same<Real, float>::value;
+    // float: the packed fit with the solo kernel's register cap (9 blocks of 128 threads per SM)
+    constexpr int MinBlocks = kFloat ? (TPB == 64 ? 18 : TPB == 128 ? 9 : 4) : 1;
+    constexpr int NPB = TPB >> 3;
+    // grid.z = reconstruction x axis-0 count, at most 65,535: chunks of reconstructions
+    const int per = std::max(1, 65535 / col.cnt[0]);
+    for (int m0 = 0; m0 < count; m0 += per)
+    {
+        const int cnt = std::min(per, count - m0);
+        dim3 grid((unsigned)((col.cnt[2] + NPB - 1) / NPB), (unsigned)col.cnt[1], (unsigned)(cnt * col.cnt[0]));
+        gs_colour_lanes_batch_kernel<Real, TPB, MinBlocks, kFloat><<<grid, TPB, 0, s>>>(jobs + m0, col, cb);
+    }
+}
+
+template <typename Real, int NPB>
+static void launch_split3_batch(const BatchJob<Real> *jobs, const Colour<3> &col, int64_t cb, int count, cudaStream_t s)
+{
+    for (int m0 = 0; m0 < count; m0 += 65535)
+    {
+        const int cnt = std::min(65535, count - m0);
+        dim3 grid((unsigned)((col.n + NPB - 1) / NPB), (unsigned)cnt);
+        gs_colour_split3_batch_kernel<Real, NPB><<<grid, 128 * NPB, 0, s>>>(jobs + m0, col, cb);
+    }
+}
+
+template <typename Real>
+void launch_colour_batch(const BatchJob<Real> *jobs, int level, int colour, int count, int tile, cudaStream_t s)
+{
+    if (count <= 0) return;
+    Grid<3> g(level);
+    Colour<3> col(g, colour);
+    if (col.n == 0) return;
+    const int64_t cb = colour_block_base<3>(g, colour);
+    if (col.n <= kSplitMaxColourNodes)
+    {
+        // the solo solve's choice for these levels (the point-split kernel)
+        if (tile == 0) launch_split3_batch<Real, 1>(jobs, col, cb, count, s);
+        else if (tile == 2) launch_split3_batch<Real, 4>(jobs, col, cb, count, s);
+        else launch_split3_batch<Real, 2>(jobs, col, cb, count, s);
+        return;
+    }
+    if constexpr (std::is_same<Real, df>::value) return;  // double-float levels are 3D levels <= 3
+    else
+    {
+        if (tile == 0) launch_lanes_batch<Real, 64>(jobs, g, col, cb, count, s);
+        else if (tile == 2) launch_lanes_batch<Real, 256>(jobs, g, col, cb, count, s);
+        else launch_lanes_batch<Real, 128>(jobs, g, col, cb, count, s);
+    }
+}
+
+void launch_df_rescale_batch(const BatchJob<df> *jobs, int count, cudaStream_t s)
+{
+    if (count > 0) df_rescale_batch_kernel<<<count, 256, 0, s>>>(jobs);
+}
+
+template <typename Real>
+void launch_prolong_add_batch(const XferJob *jobs, int coarseLevel, int count, cudaStream_t s)
+{
+    if (count <= 0) return;
+    Grid<3> gf(coarseLevel + 1);
+    prolong_add_batch_kernel<Real><<<dim3(blocks_for(gf.N, 256), (unsigned)count), 256, 0, s>>>(jobs, coarseLevel);
+}
+void launch_f2d_batch(const XferJob *jobs, int64_t n, int count, cudaStream_t s)
+{
+    if (count > 0 && n) f2d_batch_kernel<<<dim3(blocks_for(n, 256), (unsigned)count), 256, 0, s>>>(jobs, n);
+}
+void launch_d2f_batch(const XferJob *jobs, int64_t n, int count, cudaStream_t s)
+{
+    if (count > 0 && n) d2f_batch_kernel<<<dim3(blocks_for(n, 256), (unsigned)count), 256, 0, s>>>(jobs, n);
+}
+void launch_df_pull_batch(const XferJob *jobs, int64_t n, int level, int count, cudaStream_t s)
+{
+    if (count > 0 && n) df_pull_batch_kernel<<<dim3(blocks_for(n, 256), (unsigned)count), 256, 0, s>>>(jobs, n, level);
+}
+void launch_df_push_batch(const XferJob *jobs, int64_t n, int level, int count, cudaStream_t s)
+{
+    if (count > 0 && n) df_push_batch_kernel<<<count, 256, 0, s>>>(jobs, n, level);
+}
+
+template void launch_tiny_batch<float>(const BatchJob<float> *, int, int, cudaStream_t);
+template void launch_tiny_batch<double>(const BatchJob<double> *, int, int, cudaStream_t);
+template void launch_tiny_batch<df>(const BatchJob<df> *, int, int, cudaStream_t);
+template void launch_colour_batch<float>(const BatchJob<float> *, int, int, int, int, cudaStream_t);
+template void launch_colour_batch<double>(const BatchJob<double> *, int, int, int, int, cudaStream_t);
+template void launch_colour_batch<df>(const BatchJob<df> *, int, int, int, int, cudaStream_t);
+template void launch_prolong_add_batch<float>(const XferJob *, int, int, cudaStream_t);
+template void launch_prolong_add_batch<double>(const XferJob *, int, int, cudaStream_t);
 
 #define EPR_INSTANTIATE(D, R)                                                                          \
     template void launch_energy<D, R>(const LevelPtrs<R> &, const R *, const Reduce &, cudaStream_t);   \

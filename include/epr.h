@@ -41,8 +41,8 @@
  *       SystemEnergy::biQuadraticFit                        Include/SystemEnergy.h:78,499-540
  *   epr_step_size / epr_newton_update
  *       SystemEnergy::stepSize / newtonUpdate               Include/SystemEnergy.h:66-69,256-303
- *   epr_batch_solve
- *       no reference counterpart: the reference reconstructs one input per process; this runs
+ *   epr_batch_solve, epr_batch_create / run / tune / info / destroy
+ *       no reference counterpart: the reference reconstructs one input per process; these run
  *       Reconstructor::Reconstructor + solve (ExteriorPoisson.h:59-81) for many inputs at once
  *   epr_generate_samples / epr_set_generated_samples
  *       the Sample tool's shapes and noise              Include/Samples.h, Sample/Sample.cpp:137-199
@@ -192,6 +192,38 @@ int epr_solve(epr_ctx *ctx, epr_stats *stats);
  * failing context in index order (epr_global_error() names it).  The contexts must not be used by
  * other threads meanwhile. */
 int epr_batch_solve(epr_ctx *const *ctxs, int n, int build, int threads, epr_stats *stats, int *status);
+
+/* Lockstep batch of 3D reconstructions: the cascadic schedule of every member advances level by
+ * level, and each level's relaxation is a few launches for all members together (levels 0-1: one
+ * block per member for all its sweeps; from level 2 on one launch per sweep and colour whose grid
+ * spans the colour's nodes of every member still sweeping that level).  The whole relaxation is
+ * one CUDA graph, captured on the first epr_batch_run and replayed while the members' arrays stay
+ * where they are.  Members may differ in depth, samples, sweep counts and parameters, but must run
+ * the plain cascadic schedule (no multigrid, single level, verbose, warm start or target energy),
+ * share the minimum solve depth and relax each level in the same arithmetic; every member gets
+ * exactly the bits of its own epr_solve.  The contexts must be distinct, on one device, and not be
+ * used elsewhere while the batch runs.  NULL on failure (epr_batch_last_error(NULL)). */
+typedef struct epr_batch epr_batch;
+epr_batch *epr_batch_create(epr_ctx *const *ctxs, int n, int threads);
+/* Builds (build != 0) every member, then solves them all: member prologues (levels cleared, random
+ * start) and epilogues (error flags, final energies, solution arrays) on `threads` host workers,
+ * the relaxation as the batch's graph.  stats[i].solve_ms is the batch relaxation's device time,
+ * shared by all members.  stats / status as for epr_batch_solve. */
+int epr_batch_run(epr_batch *b, int build, epr_stats *stats, int *status);
+/* The autotuner: for every level relaxed by per-colour launches, times `reps` sweeps of all members
+ * in each of the three block shapes of its colour kernel (levels whose colours have at most 125
+ * nodes: 1, 2 or 4 nodes per block of the point-split kernel; larger levels: 64, 128 or 256 threads
+ * per block of the lane kernel) on the members' current coefficients, which it restores, and keeps
+ * the fastest shape per level for the next runs.  No shape changes any node's arithmetic.  ms_out
+ * (may be NULL) receives 3 mean sweep times per tuned level, coarsest first.  Needs built members. */
+int epr_batch_tune(epr_batch *b, int reps, double *ms_out);
+/* Sets level's block shape index (0-2; level -1: every level) by hand, in place of the tuner's. */
+int epr_batch_set_tile(epr_batch *b, int level, int tile);
+/* tiles[l] (l < cap): the block shape index (0-2) level l uses; relax_ms: the last run's relaxation
+ * time; launches: kernel launches in the batch's graph. */
+int epr_batch_info(epr_batch *b, int *tiles, int cap, double *relax_ms, long long *launches);
+void epr_batch_destroy(epr_batch *b);
+const char *epr_batch_last_error(epr_batch *b);
 
 /* Synthetic samples generated on the device (the reference's Sample tool: Include/Samples.h shapes,
  * Sample/Sample.cpp:137-199 noise).  Random numbers: Philox4x32-10 keyed by seed, one counter per

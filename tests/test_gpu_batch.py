@@ -102,3 +102,103 @@ def test_rebuild_gives_the_same_system():
     r.build()
     assert np.array_equal(r.get("B", it["depth"]), b0) and np.array_equal(r.get("S"), s0)
     r.close()
+
+
+# ---------------------------------------------------------------------------------------------
+# lockstep batches (epr_batch_*): one launch per level colour for all members, one graph, tuned tiles
+# ---------------------------------------------------------------------------------------------
+
+def _lockstep_inputs(kw):
+    """3D members of uneven depths (3-6, so that levels 2-6 run per-colour launches with members
+    dropping out as their schedules end), sample counts and sweep counts, in one precision
+    configuration, plus the reference's golden knot."""
+    items = []
+    for w in epr.samples.batch_workloads(7, seed=11, n_range=(2000, 60000), depths=(3, 4, 5, 6)):
+        pu, _ = epr.unit_cube(w["pos"])
+        items.append(dict(dim=3, depth=w["depth"], pos=pu, skew=epr.pack_skew(w["frames"]), kw=dict(kw)))
+    items[1]["kw"]["gs_iters"] = 7  # another sweep count on every level
+    items[2]["kw"]["separate"] = 1
+    g = load_golden("knot3_d4")
+    items.append(dict(dim=3, depth=int(g["depth"]), pos=g["pos"], skew=g["skew"], kw=dict(kw)))
+    return items
+
+
+@pytest.mark.parametrize("kw", [dict(precision="fp32", fp64_from=0, fp64_levels=4, band_precision="df"),
+                                dict(precision="fp32", fp64_from=2, fp64_levels=4),
+                                dict()], ids=["df_band", "fp64_band", "fp64"])
+def test_lockstep_batch_matches_individual_solves(kw):
+    items = _lockstep_inputs(kw)
+    alone = []
+    for it in items:
+        r = _recon(it, True)
+        alone.append(_result(r, r.solve()))
+        r.close()
+    recons = [_recon(it, False) for it in items]
+    b = epr.LockstepBatch(recons, threads=4)
+    try:
+        # the first run builds and captures the graph, the second replays it, the third runs the
+        # tuned block shapes (a new graph)
+        for rnd in range(3):
+            if rnd == 2:
+                times = b.tune(reps=2)
+                assert times.shape[1] == 3 and len(times) >= 1 and (times > 0).all()
+                assert all(0 <= t <= 2 for t in b.info()["tiles"])
+            stats = b.run(build=(rnd == 0))
+            for k, (r, st) in enumerate(zip(recons, stats)):
+                got = _result(r, st)
+                assert np.array_equal(got[0], alone[k][0]) and np.array_equal(got[1], alone[k][1]), (rnd, k)
+                assert got[2] == alone[k][2] and got[3] == alone[k][3], (rnd, k)
+        info = b.info()
+        assert info["relax_ms"] > 0 and info["graph_launches"] > 0
+    finally:
+        b.close()
+        for r in recons:
+            r.close()
+
+
+def test_lockstep_batch_every_block_shape_gives_the_same_bits():
+    """Each of the three block shapes of every per-colour level, forced by hand, gives the solo bits."""
+    kw = dict(precision="fp32", fp64_from=0, fp64_levels=4, band_precision="df")
+    items = _lockstep_inputs(kw)[:4]
+    alone = []
+    for it in items:
+        r = _recon(it, True)
+        alone.append(_result(r, r.solve()))
+        r.close()
+    lib = epr.load()
+    for shape in range(3):
+        recons = [_recon(it, True) for it in items]
+        b = epr.LockstepBatch(recons, threads=2)
+        b.set_tile(-1, shape)
+        stats = b.run()
+        assert all(t == shape for t in b.info()["tiles"]), b.info()
+        for k, (r, st) in enumerate(zip(recons, stats)):
+            got = _result(r, st)
+            assert np.array_equal(got[0], alone[k][0]) and np.array_equal(got[1], alone[k][1]), (shape, k)
+        b.close()
+        for r in recons:
+            r.close()
+    with pytest.raises(epr.EprError):
+        epr.LockstepBatch([_recon(items[0], True)]).set_tile(0, 3)
+    assert lib is not None
+
+
+def test_lockstep_batch_rejects_members_it_cannot_share():
+    items = _lockstep_inputs({})[:2]
+    pos, fr = epr.samples.make_workload("clifford", 3000, seed=5)
+    pu, _ = epr.unit_cube(pos)
+    four = epr.Reconstructor(4, 2, pu, epr.pack_skew(fr))
+    three = _recon(items[0], True)
+    mg = _recon(dict(items[1], kw=dict(solver="multigrid")), True)
+    mixed = _recon(dict(items[1], kw=dict(precision="fp32")), True)
+    try:
+        for bad, msg in (([three, four], "3D"), ([three, mg], "cascadic"), ([three, mixed], "arithmetic")):
+            b = epr.LockstepBatch(bad)
+            with pytest.raises(epr.EprError, match=msg):
+                b.run()
+            b.close()
+        with pytest.raises(epr.EprError, match="twice"):
+            epr.LockstepBatch([three, three])
+    finally:
+        for r in (four, three, mg, mixed):
+            r.close()
