@@ -53,6 +53,8 @@ template <typename Real>
 __device__ __forceinline__ Real hat2(int b, int g) { return b ? (Real)Gauss::X2(g) : (Real)(1.0 - Gauss::X2(g)); }
 template <typename Real>
 __device__ __forceinline__ Real hat3(int b, int g) { return b ? (Real)Gauss::X3(g) : (Real)(1.0 - Gauss::X3(g)); }
+template <typename Real>
+__host__ __device__ constexpr Real hat3c(int b, int g) { return b ? Real(Gauss::X3(g)) : Real(1.0 - Gauss::X3(g)); }
 
 // Derivative of a multilinear corner field along axis A (the "derived" axis), tabulated at
 // 2 Gauss points of axis B (the partner axis of the component) and 3 Gauss points of each other
@@ -307,15 +309,22 @@ __device__ __forceinline__ void component_fit_pq3(const Real *x, const Real *y, 
     const Real w2 = gp == gq ? (gp ? (Real)(Gauss::W2(1) * Gauss::W2(1)) : (Real)(Gauss::W2(0) * Gauss::W2(0)))
                              : (Real)(Gauss::W2(0) * Gauss::W2(1));
     const Real hq = gq ? hat2<Real>(0, 1) : hat2<Real>(0, 0), hp = p0;
-#pragma unroll
+    // the three other-axis points in a rolled loop (the hat values and weights picked from
+    // constants): a third of the code of the unrolled loop for the kernels that run this fit for
+    // thousands of dependent single-node updates
+    constexpr Real kLo[3] = {hat3c<Real>(0, 0), hat3c<Real>(0, 1), hat3c<Real>(0, 2)};
+    constexpr Real kHi[3] = {hat3c<Real>(1, 0), hat3c<Real>(1, 1), hat3c<Real>(1, 2)};
+    constexpr Real kW[3] = {(Real)Gauss::W3(0), (Real)Gauss::W3(1), (Real)Gauss::W3(2)};
+#pragma unroll 1
     for (int go = 0; go < 3; go++)
     {
-        const Real lo = hat3<Real>(0, go);
-        const Real w = w2 * (Real)other_weight<1>(go);
+        const Real lo = go == 0 ? kLo[0] : go == 1 ? kLo[1] : kLo[2];
+        const Real hi = go == 0 ? kHi[0] : go == 1 ? kHi[1] : kHi[2];
+        const Real w = w2 * (go == 0 ? kW[0] : go == 1 ? kW[1] : kW[2]);
         const Real phP = (Real)-1 * hq * lo;
         const Real phQ = (Real)-1 * hp * lo;
-        const Real xp = derivative_at<1, Real>(xP, go), xq = derivative_at<1, Real>(xQ, go);
-        const Real yp = derivative_at<1, Real>(yP, go), yq = derivative_at<1, Real>(yQ, go);
+        const Real xp = lo * xP[0] + hi * xP[1], xq = lo * xQ[0] + hi * xQ[1];
+        const Real yp = lo * yP[0] + hi * yP[1], yq = lo * yQ[0] + hi * yQ[1];
         const Real W = yp * xq - xp * yq;
         const Real U = yp * phQ - phP * yq;
         const Real V = phP * xq - xp * phQ;
