@@ -16,7 +16,10 @@
 // All routines work in reference-element units; integrals over the physical element (side 1/r)
 // are the returned sums times r^(4-D)/2, which the callers apply (a power of two: exact).
 #pragma once
+#include <type_traits>
+
 #include "epr_common.cuh"
+#include "epr_df.cuh"
 
 namespace epr {
 
@@ -309,15 +312,10 @@ __device__ __forceinline__ void component_fit_pq3(const Real *x, const Real *y, 
     const Real w2 = gp == gq ? (gp ? (Real)(Gauss::W2(1) * Gauss::W2(1)) : (Real)(Gauss::W2(0) * Gauss::W2(0)))
                              : (Real)(Gauss::W2(0) * Gauss::W2(1));
     const Real hq = gq ? hat2<Real>(0, 1) : hat2<Real>(0, 0), hp = p0;
-    // the three other-axis points in a rolled loop (the hat values and weights picked from
-    // constants): a third of the code of the unrolled loop for the kernels that run this fit for
-    // thousands of dependent single-node updates
     constexpr Real kLo[3] = {hat3c<Real>(0, 0), hat3c<Real>(0, 1), hat3c<Real>(0, 2)};
     constexpr Real kHi[3] = {hat3c<Real>(1, 0), hat3c<Real>(1, 1), hat3c<Real>(1, 2)};
     constexpr Real kW[3] = {(Real)Gauss::W3(0), (Real)Gauss::W3(1), (Real)Gauss::W3(2)};
-#pragma unroll 1
-    for (int go = 0; go < 3; go++)
-    {
+    auto point = [&](int go) {
         const Real lo = go == 0 ? kLo[0] : go == 1 ? kLo[1] : kLo[2];
         const Real hi = go == 0 ? kHi[0] : go == 1 ? kHi[1] : kHi[2];
         const Real w = w2 * (go == 0 ? kW[0] : go == 1 ? kW[1] : kW[2]);
@@ -334,6 +332,19 @@ __device__ __forceinline__ void component_fit_pq3(const Real *x, const Real *y, 
         h[2] += wU * V;
         h[3] += wU * W;
         h[4] += wV * W;
+    };
+    // the three other-axis points: in double-float a rolled loop (the hat values and weights
+    // picked from constants), a third of the code of the unrolled one, for the kernels that run
+    // this fit for thousands of dependent single-node updates and are bound by instruction fetch
+    if constexpr (std::is_same<Real, df>::value)
+    {
+#pragma unroll 1
+        for (int go = 0; go < 3; go++) point(go);
+    }
+    else
+    {
+#pragma unroll
+        for (int go = 0; go < 3; go++) point(go);
     }
 }
 

@@ -62,6 +62,34 @@ ColourBlocks<D> colour_blocks(int level)
     return cb;
 }
 
+// The multigrid's colour-blocked stencils in 16-byte vectors: coefficient o of the j-th node of
+// colour c sits at base[c] + ((o / W) n_c + j) W + o % W with W = 16 / sizeof(Real), a node's last
+// vector padded with zeros, so that a thread loads its node's column with ceil(S / W) 128-bit
+// loads (consecutive threads, consecutive vectors) instead of S scalar ones.
+template <int D, typename Real>
+struct VecLayout
+{
+    static constexpr int W = 16 / (int)sizeof(Real);
+    static constexpr int G = (Dims<D>::S + W - 1) / W;
+    using Vec = typename std::conditional<sizeof(Real) == 4, float4, double2>::type;
+};
+
+template <int D, typename Real>
+ColourBlocks<D> colour_blocks_vec(int level)
+{
+    Grid<D> g(level);
+    ColourBlocks<D> cb;
+    int64_t at = 0;
+    for (int c = 0; c < (1 << D); c++)
+    {
+        Colour<D> col(g, c);
+        cb.base[c] = at;
+        cb.count[c] = col.n;
+        at += col.n * VecLayout<D, Real>::G * VecLayout<D, Real>::W;
+    }
+    return cb;
+}
+
 // neighbour of node i at stencil offset o, or -1 outside the grid
 template <int D>
 __device__ __forceinline__ int64_t neighbour(const Grid<D> &g, const int *I, int64_t i, int o)
@@ -96,6 +124,25 @@ __global__ void to_colour_blocks_kernel(int level, const double *M, ColourBlocks
     Real *dst = out + cb.base[c] + j;
     const int64_t n = cb.count[c];
     for (int o = 0; o < Dims<D>::S; o++) dst[o * n] = (Real)M[(int64_t)o * g.N + i];
+}
+
+// natural offset-major double stencil -> the multigrid's vector colour blocks; grid.y = colour
+template <int D, typename Real>
+__global__ void to_colour_blocks_vec_kernel(int level, const double *M, ColourBlocks<D> cb, Real *out)
+{
+    using V = VecLayout<D, Real>;
+    const int c = blockIdx.y;
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= cb.count[c]) return;
+    Grid<D> g(level);
+    Colour<D> col(g, c);
+    int I[D];
+    col.node(j, I);
+    const int64_t i = g.node(I);
+    Real *dst = out + cb.base[c];
+    const int64_t n = cb.count[c];
+    for (int o = 0; o < V::G * V::W; o++)
+        dst[((int64_t)(o / V::W) * n + j) * V::W + o % V::W] = o < Dims<D>::S ? (Real)M[(int64_t)o * g.N + i] : (Real)0;
 }
 
 // component d of stencil offset o (axis 0 slowest), in {-1, 0, 1}
@@ -134,42 +181,61 @@ __device__ __forceinline__ Real coef_load(const Real *p)
     if constexpr (Streaming) return __ldcs(p);
     else return __ldg(p);
 }
+template <bool Streaming, typename Vec>
+__device__ __forceinline__ Vec vec_load(const Vec *p)
+{
+    if constexpr (Streaming) return __ldcs(p);
+    else return __ldg(p);
+}
+template <typename Vec, typename Real>
+__device__ __forceinline__ Real vec_at(const Vec &v, int e)
+{
+    if constexpr (sizeof(Real) == 4) return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+    else return e == 0 ? v.x : v.y;
+}
 
+// sum_o M[o] x[i + off(o)] over the stencil of node i, the coefficients from the vector colour
+// blocks (Mc = the colour's block); interior nodes take the unrolled path with compile-time
+// offsets, boundary nodes check every neighbour.  centre receives M[centre].  The sum runs over o
+// in increasing order, as with scalar loads.
 template <int D, typename Real, bool Streaming = false>
 __device__ __forceinline__ Real stencil_dot(const Real *__restrict__ Mc, int64_t n, int64_t j, const Real *x, uint32_t i,
-                                            const int *I, const uint32_t *st, int r)
+                                            const int *I, const uint32_t *st, int r, Real &centre)
 {
+    using V = VecLayout<D, Real>;
+    using Vec = typename V::Vec;
     constexpr int S = Dims<D>::S;
+    const Vec *Mv = reinterpret_cast<const Vec *>(Mc) + j;
     bool interior = true;
 #pragma unroll
     for (int d = 0; d < D; d++) interior = interior && I[d] > 0 && I[d] < r;
     Real s = 0;
-    if (interior)
-    {
+    centre = 0;
 #pragma unroll
-        for (int o = 0; o < S; o++)
-        {
-            int64_t k = (int64_t)i;
-#pragma unroll
-            for (int d = 0; d < D; d++) k += (int64_t)offset_of<D>(o, d) * (int64_t)st[d];
-            s += coef_load<Streaming>(Mc + (int64_t)o * n + j) * x[k];
-        }
-    }
-    else
+    for (int gv = 0; gv < V::G; gv++)
     {
-#pragma unroll 9
-        for (int o = 0; o < S; o++)
+        const Vec v = vec_load<Streaming>(Mv + (int64_t)gv * n);
+#pragma unroll
+        for (int e = 0; e < V::W; e++)
         {
+            const int o = gv * V::W + e;
+            if (o >= S) break;
+            const Real m = vec_at<Vec, Real>(v, e);
+            if (o == Dims<D>::CENTER) centre = m;
             int64_t k = (int64_t)i;
             bool ok = true;
 #pragma unroll
             for (int d = 0; d < D; d++)
             {
-                const int off = offset_of<D>(o, d), q = I[d] + off;
-                ok = ok && q >= 0 && q <= r;
+                const int off = offset_of<D>(o, d);
+                if (!interior)
+                {
+                    const int q = I[d] + off;
+                    ok = ok && q >= 0 && q <= r;
+                }
                 k += (int64_t)off * (int64_t)st[d];
             }
-            if (ok) s += coef_load<Streaming>(Mc + (int64_t)o * n + j) * x[k];
+            if (interior || ok) s += m * x[k];
         }
     }
     return s;
@@ -198,8 +264,9 @@ __global__ void __launch_bounds__(kThreads, MinBlocks) linear_gs_colour_kernel(i
     node_strides<D>(r, st);
     int I[D];
     const uint32_t i = colour_node<D>(col, st, (uint32_t)j, I);
-    const Real s = stencil_dot<D, Real, Streaming>(Mc, n, j, x, i, I, st, r);
-    x[i] += (__ldg(b + i) - s) / coef_load<Streaming>(Mc + (int64_t)Dims<D>::CENTER * n + j);
+    Real centre;
+    const Real s = stencil_dot<D, Real, Streaming>(Mc, n, j, x, i, I, st, r, centre);
+    x[i] += (__ldg(b + i) - s) / centre;
 }
 
 // r = b - M x over every node, colour-blocked coefficients; grid.y = colour
@@ -218,7 +285,8 @@ __global__ void __launch_bounds__(kThreads) residual_cb_kernel(int level, const 
     node_strides<D>(res, st);
     int I[D];
     const uint32_t i = colour_node<D>(col, st, (uint32_t)j, I);
-    r[i] = b[i] - stencil_dot<D, Real>(M + cb.base[c], n, j, x, i, I, st, res);
+    Real centre;
+    r[i] = b[i] - stencil_dot<D, Real>(M + cb.base[c], n, j, x, i, I, st, res, centre);
 }
 
 // r = b - M x with the natural double stencil (the refinement residual of the float mode)
@@ -706,6 +774,13 @@ void release_mg(Context &c)
     c.mg = nullptr;
 }
 
+// values per node of the vector colour blocks
+template <typename Real>
+static size_t vec_stencil_values(int dim)
+{
+    return dim == 3 ? (size_t)VecLayout<3, Real>::G * VecLayout<3, Real>::W : (size_t)VecLayout<4, Real>::G * VecLayout<4, Real>::W;
+}
+
 // (re)allocates the hierarchy for levels 0..top
 static bool mg_prepare(Context &c, int top)
 {
@@ -725,7 +800,9 @@ static bool mg_prepare(Context &c, int top)
         m.f32 = c.lvl32(l) && m.N >= kFloatMinNodes;
         const size_t rs = m.f32 ? sizeof(float) : sizeof(double);
         if (!c.alloc((void **)&m.M64, sizeof(double) * S * m.N, "alloc mg stencil") ||
-            !c.alloc(&m.Mcb, rs * S * m.N, "alloc mg stencil") || !c.alloc(&m.x, rs * m.N, "alloc mg x") ||
+            !c.alloc(&m.Mcb, (m.f32 ? vec_stencil_values<float>(c.dim) : vec_stencil_values<double>(c.dim)) * rs * m.N,
+                     "alloc mg stencil") ||
+            !c.alloc(&m.x, rs * m.N, "alloc mg x") ||
             !c.alloc(&m.b, rs * m.N, "alloc mg b") || !c.alloc(&m.r, rs * m.N, "alloc mg r"))
             return false;
     }
@@ -759,11 +836,11 @@ static bool mg_build(Context &c, int top, int lo)
             for (int l = top; l > 0; l--) launch_galerkin<D>(l, h.L[l].M64, h.L[l - 1].M64, c.stream);
         for (int l = std::max(lo, 1); l <= top; l++)
         {
-            ColourBlocks<D> cb = colour_blocks<D>(l);
-            dim3 grid(blocks(cb.count[0]), 1 << D);
             with_real(h.L[l].f32, [&](auto rv) {
                 using R = decltype(rv);
-                to_colour_blocks_kernel<D, R><<<grid, kThreads, 0, c.stream>>>(l, h.L[l].M64, cb, (R *)h.L[l].Mcb);
+                ColourBlocks<D> cb = colour_blocks_vec<D, R>(l);
+                dim3 grid(blocks(cb.count[0]), 1 << D);
+                to_colour_blocks_vec_kernel<D, R><<<grid, kThreads, 0, c.stream>>>(l, h.L[l].M64, cb, (R *)h.L[l].Mcb);
             });
             c.launches++;
         }
@@ -805,7 +882,7 @@ template <int D, typename Real>
 static void mg_sweeps(Context &c, int l, const Real *b, Real *x, int iters)
 {
     MGLevel &m = c.mg->L[l];
-    ColourBlocks<D> cb = colour_blocks<D>(l);
+    ColourBlocks<D> cb = colour_blocks_vec<D, Real>(l);
     for (int it = 0; it < iters; it++)
         for (int col = 0; col < (1 << D); col++)
         {
@@ -826,7 +903,7 @@ static void mg_vcycle(Context &c, int top, int iters)
         with_real(m.f32, [&](auto rv) {
             using R = decltype(rv);
             mg_sweeps<D, R>(c, l, (const R *)m.b, (R *)m.x, iters);
-            ColourBlocks<D> cb = colour_blocks<D>(l);
+            ColourBlocks<D> cb = colour_blocks_vec<D, R>(l);
             residual_cb_kernel<D, R><<<dim3(blocks(cb.count[0]), 1 << D), kThreads, 0, c.stream>>>(
                 l, (const R *)m.Mcb, cb, (const R *)m.b, (const R *)m.x, (R *)m.r);
             with_real(mc.f32, [&](auto cv) {
@@ -1077,7 +1154,7 @@ bool time_mg_kernel(Context &c, const char *kernel, int level, int reps, double 
     auto run = [&]() {
         mg_dim(c, [&](auto dd) {
             constexpr int D = decltype(dd)::value;
-            ColourBlocks<D> cb = colour_blocks<D>(level);
+            ColourBlocks<D> cb = m.f32 ? colour_blocks_vec<D, float>(level) : colour_blocks_vec<D, double>(level);
             if (k == "lgs")
             {
                 if (m.f32)

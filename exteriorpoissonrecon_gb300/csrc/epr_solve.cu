@@ -750,13 +750,14 @@ __device__ __forceinline__ void gs_update_split3(const LevelPtrs<Real> &L, Real 
             }
         }
     }
+    // warp sums, the rounds rolled (small code for the instruction cache; the same additions)
+#pragma unroll 1
+    for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-    for (int k = 0; k < 5; k++)
-    {
+        for (int k = 0; k < 5; k++) v[k] += shfl_xor_any(v[k], o);
+    if (lane == 0)
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] += shfl_xor_any(v[k], o);
-        if (lane == 0) part[wp][k] = v[k];
-    }
+        for (int k = 0; k < 5; k++) part[wp][k] = v[k];
     __syncthreads();
     if (active && t == 0)
     {
@@ -1164,11 +1165,23 @@ __device__ __forceinline__ void gs_tiny_body(const LevelPtrs<Real> &L, int iters
                     else { r[2] += b * q.x; r[3] += b * q.y; }
                 }
             }
-            // sums within each half-warp: lane 0 the wedge integrals, lane 16 the stencil sums
+            // sums within each half-warp: lane 0 the wedge integrals, lane 16 the stencil sums (in
+            // double-float at resolution 1 the rounds stay rolled: with one warp, instruction fetch
+            // is the bound, and the pair additions' code then fits the instruction cache)
+            if constexpr (kDF && LEVEL == 0)
+            {
+#pragma unroll 1
+                for (int o = 8; o > 0; o >>= 1)
 #pragma unroll
-            for (int k = 0; k < 5; k++)
+                    for (int k = 0; k < 5; k++) r[k] += shfl_xor_any(r[k], o);
+            }
+            else
+            {
 #pragma unroll
-                for (int o = 8; o > 0; o >>= 1) r[k] += shfl_xor_any(r[k], o);
+                for (int o = 8; o > 0; o >>= 1)
+#pragma unroll
+                    for (int k = 0; k < 5; k++) r[k] += shfl_xor_any(r[k], o);
+            }
             Real stc[5];
 #pragma unroll
             for (int k = 0; k < 5; k++) stc[k] = shfl_any(r[k], 16);
