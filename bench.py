@@ -55,7 +55,7 @@ sys.path.insert(0, ROOT)
 # profiles/linear_gs_colour_kernel_link_depth7_fp32.txt); a depth-8 launch's traffic is these times
 # its colour nodes (traffic grows in proportion with the nodes).
 GS_DRAM_BYTES_PER_COLOUR_NODE_FP32 = (76.39296e6 + 4.034304e6) / 274625
-LGS_DRAM_BYTES_PER_COLOUR_NODE_FP32 = (40.49792e6 + 1.28e3) / 274625
+LGS_DRAM_BYTES_PER_COLOUR_NODE_FP32 = (42.062336e6 + 768) / 274625
 
 
 def parse():
@@ -229,6 +229,32 @@ def cpu_reference(pu, sk, depth, cpu_depth, steps, warmup, dim=3):
                        f"({schedule_node_updates(dim, depth)} node updates); build took {build_s:.1f} s")}
 
 
+def measured_fp32_tflops():
+    """FP32 FMA throughput of this GPU as a dense FP32 SGEMM reaches it (TF32 off): the measured
+    denominator of the relaxation kernel's compute fraction."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        a @ b
+        best = None
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            a @ b
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        del a, b
+        return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
 def kernel_rooflines(r, dim, depth, precision, clk):
     """Roofline objects of the two relaxation kernels on the finest level of reconstruction r: one
     parity colour of the paired Gauss-Seidel sweep (the solve's dominant kernel) and one colour of
@@ -250,7 +276,8 @@ def kernel_rooflines(r, dim, depth, precision, clk):
     node_flops = (2 ** dim) * K * (4 * 34 + 4 * 3 ** (dim - 2) * 21) + 8 * S + 30
     gs_flops = node_flops * colour_nodes
     sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_nominal = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_peak = measured_fp32_tflops() if precision == "fp32" else None
     gs_traffic = GS_DRAM_BYTES_PER_COLOUR_NODE_FP32 * colour_nodes if fp32 else None
     roofline = {"bound": "hbm", "kernel": "gs_colour_lanes_kernel", "achieved": achieved, "peak": hbm_peak,
                 "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_kind, "traffic": gs_traffic,
@@ -259,9 +286,11 @@ def kernel_rooflines(r, dim, depth, precision, clk):
                          "the finest level's colour launches take share_of_step of the step, the rest is the "
                          "coarser levels (levels 0-3: thousands of latency-bound launches)"),
                 "compute": {"algorithmic_flops_per_launch": gs_flops, "achieved_tflops": gs_flops / (gs_ms * 1e-3) / 1e12,
-                            "peak_tflops": fp32_peak if precision == "fp32" else None,
-                            "peak_source": "nominal FP32 at the sampled SM clock",
-                            "frac": (gs_flops / (gs_ms * 1e-3) / 1e12 / fp32_peak) if precision == "fp32" else None}}
+                            "peak_tflops": fp32_peak,
+                            "peak_source": "measured: FP32 SGEMM (cuBLAS through torch, TF32 off), 8192^3, best of 5",
+                            "frac": (gs_flops / (gs_ms * 1e-3) / 1e12 / fp32_peak) if fp32_peak else None,
+                            "nominal_tflops": fp32_nominal if precision == "fp32" else None,
+                            "frac_of_nominal": (gs_flops / (gs_ms * 1e-3) / 1e12 / fp32_nominal) if precision == "fp32" else None}}
 
     # stored-stencil relaxation (the smoother of the linear multigrid, MG.h GSRelaxer): one colour of
     # the linear Gauss-Seidel sweep on the alternating y-system of the finest level, colour-blocked
@@ -277,7 +306,8 @@ def kernel_rooflines(r, dim, depth, precision, clk):
     return roofline, stencil_roofline
 
 
-BATCH_METRIC = "Batched reconstructions per second (3D torus knots + helices, depths 5-7, FP32 smoothing, FP64 levels 0-3)"
+BATCH_METRIC = ("Batched reconstructions per second (3D torus knots + helices, depths 5-7, FP32 relaxation, "
+                "double-float levels 0-3, FP64 energies)")
 
 
 def batch_inputs(count, seed=0):
@@ -321,8 +351,9 @@ def cpu_batch_reference(inputs):
 
 
 def bench_batch(args, ws, rank, local, pg):
-    """Many small reconstructions at once (epr_batch_solve): one step = solving every reconstruction
-    of the batch once from its built system; value = reconstructions per second over all replicas.
+    """Many small reconstructions at once (a lockstep batch, epr_batch_*, or host workers,
+    epr_batch_solve): one step = solving every reconstruction of the batch once from its built
+    system; value = reconstructions per second over all replicas.
     Levels 0-3 relax in double-float (the coarse solve; in float, rounding on the two coarsest levels
     moves a few reconstructions of the mix by up to 1.6e-5 in energy), the others in float.  32 host
     workers keep 32 reconstructions in flight, on 32 hardware work queues."""

@@ -850,9 +850,11 @@ static bool mg_build(Context &c, int top, int lo)
     return c.launch_ok("mg hierarchy");
 }
 
-// variant of the linear GS colour kernel (EPR_LGS_VARIANT): 0 default (float: at most 51 registers,
-// read-only loads; double: 32 registers, streaming coefficient loads), 1 32 registers + streaming,
-// 2 no register cap, 3 32 registers + read-only loads
+// variant of the linear GS colour kernel (EPR_LGS_VARIANT): 0 default (32 registers, 8 blocks of 256
+// threads per SM, streaming coefficient loads: the coefficients are read once per sweep, the x
+// vector stays in L2; depth 8, one colour: 0.060 ms float = 0.78 of the measured copy bandwidth,
+// 0.187 ms double), 1 the same, 2 no register cap (0.094 / 0.204 ms), 3 32 registers + read-only
+// loads (0.063 / 0.187 ms)
 static int lgs_variant()
 {
     static const int v = [] {
@@ -872,8 +874,6 @@ static void launch_lgs_colour(int l, int col, const Real *Mc, int64_t n, const R
         linear_gs_colour_kernel<D, Real, 1, false><<<blocks(n), kThreads, 0, s>>>(l, col, Mc, n, b, x);
     else if (v == 3)
         linear_gs_colour_kernel<D, Real, 8, false><<<blocks(n), kThreads, 0, s>>>(l, col, Mc, n, b, x);
-    else if constexpr (sizeof(Real) == 4)
-        linear_gs_colour_kernel<D, Real, 5, false><<<blocks(n), kThreads, 0, s>>>(l, col, Mc, n, b, x);
     else
         linear_gs_colour_kernel<D, Real, 8, true><<<blocks(n), kThreads, 0, s>>>(l, col, Mc, n, b, x);
 }
