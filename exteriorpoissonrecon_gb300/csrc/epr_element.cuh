@@ -287,6 +287,59 @@ __device__ __forceinline__ void component_fit(const Real *x, const Real *y, int 
     }
 }
 
+// The two steps of component_fit_pq3 for callers that spread a pair's three other-axis points
+// over threads: the pair's derivative tables (setup) and one point's terms (point).
+template <typename Real>
+struct PairTables
+{
+    Real xP[2], xQ[2], yP[2], yQ[2], w2, hq, hp;
+};
+
+template <typename Real>
+__device__ __forceinline__ void component_setup_pq3(const Real *x, const Real *y, int gp, int gq, PairTables<Real> &t)
+{
+    using Cp = Component<3, 0>;
+    const Real q0 = gq ? hat2<Real>(0, 1) : hat2<Real>(0, 0), q1 = gq ? hat2<Real>(1, 1) : hat2<Real>(1, 0);
+    const Real p0 = gp ? hat2<Real>(0, 1) : hat2<Real>(0, 0), p1 = gp ? hat2<Real>(1, 1) : hat2<Real>(1, 0);
+#pragma unroll
+    for (int bo = 0; bo < 2; bo++)
+    {
+        // derivative along P interpolated at Q's point gq, and along Q at P's point gp
+        t.xP[bo] = q0 * (x[Cp::corner(1, 0, bo)] - x[Cp::corner(0, 0, bo)]) + q1 * (x[Cp::corner(1, 1, bo)] - x[Cp::corner(0, 1, bo)]);
+        t.yP[bo] = q0 * (y[Cp::corner(1, 0, bo)] - y[Cp::corner(0, 0, bo)]) + q1 * (y[Cp::corner(1, 1, bo)] - y[Cp::corner(0, 1, bo)]);
+        t.xQ[bo] = p0 * (x[Cp::corner(0, 1, bo)] - x[Cp::corner(0, 0, bo)]) + p1 * (x[Cp::corner(1, 1, bo)] - x[Cp::corner(1, 0, bo)]);
+        t.yQ[bo] = p0 * (y[Cp::corner(0, 1, bo)] - y[Cp::corner(0, 0, bo)]) + p1 * (y[Cp::corner(1, 1, bo)] - y[Cp::corner(1, 0, bo)]);
+    }
+    t.w2 = gp == gq ? (gp ? (Real)(Gauss::W2(1) * Gauss::W2(1)) : (Real)(Gauss::W2(0) * Gauss::W2(0)))
+                    : (Real)(Gauss::W2(0) * Gauss::W2(1));
+    t.hq = gq ? hat2<Real>(0, 1) : hat2<Real>(0, 0);
+    t.hp = p0;
+}
+
+template <typename Real>
+__device__ __forceinline__ void component_point_pq3(const PairTables<Real> &t, int go, Real *h)
+{
+    constexpr Real kLo[3] = {hat3c<Real>(0, 0), hat3c<Real>(0, 1), hat3c<Real>(0, 2)};
+    constexpr Real kHi[3] = {hat3c<Real>(1, 0), hat3c<Real>(1, 1), hat3c<Real>(1, 2)};
+    constexpr Real kW[3] = {(Real)Gauss::W3(0), (Real)Gauss::W3(1), (Real)Gauss::W3(2)};
+    const Real lo = go == 0 ? kLo[0] : go == 1 ? kLo[1] : kLo[2];
+    const Real hi = go == 0 ? kHi[0] : go == 1 ? kHi[1] : kHi[2];
+    const Real w = t.w2 * (go == 0 ? kW[0] : go == 1 ? kW[1] : kW[2]);
+    const Real phP = (Real)-1 * t.hq * lo;
+    const Real phQ = (Real)-1 * t.hp * lo;
+    const Real xp = lo * t.xP[0] + hi * t.xP[1], xq = lo * t.xQ[0] + hi * t.xQ[1];
+    const Real yp = lo * t.yP[0] + hi * t.yP[1], yq = lo * t.yQ[0] + hi * t.yQ[1];
+    const Real W = yp * xq - xp * yq;
+    const Real U = yp * phQ - phP * yq;
+    const Real V = phP * xq - xp * phQ;
+    const Real wU = w * U, wV = w * V;
+    h[0] += wU * U;
+    h[1] += wV * V;
+    h[2] += wU * V;
+    h[3] += wU * W;
+    h[4] += wV * W;
+}
+
 // Component 0 of a 3D element in the canonical orientation (corner 0), restricted to the Gauss
 // points with the given (gp, gq): the share of one of four threads that split a component's
 // integral (the values of the points are those of component_fit).  The pair is a run-time value:

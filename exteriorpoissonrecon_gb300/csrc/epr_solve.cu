@@ -452,13 +452,27 @@ __device__ __forceinline__ Real wedge_mult(const int *kexp, int level)
     else return (Real)1;
 }
 
+// A block's row of nodes staged in shared memory (3D lane kernel): the (x, y) pairs of the 3 x 3 x W
+// grid points around the row (W = 2 nodes-per-block + 1 along the last axis) and the rows' stencil
+// columns, loaded once per block with coalesced loads, so that a node's 8 lanes read their corners
+// and neighbours from shared memory instead of re-fetching them through L1 / L2.
+template <typename Real>
+struct LaneStage
+{
+    const Real2<Real> *tile = nullptr;
+    int tcentre = 0;  // tile index of the node (the tile's row length is a template parameter)
+    const Real *As = nullptr, *Bs = nullptr;  // column o of the block's t-th node at o npb + t
+    int npb = 0, t = 0;
+};
+
 // Ac, Bc (optional): the colour's block of the colour-blocked stencils, the node being the colour's
-// jc-th of nc; otherwise the natural stencils L.A, L.B are read.
-template <int D, typename Real, bool Packed = false>
+// jc-th of nc; otherwise the natural stencils L.A, L.B are read.  Staged (3D): corners, neighbours
+// and stencil columns come from stg (the same values, so the same arithmetic).
+template <int D, typename Real, bool Packed = false, bool Staged = false, int SW = 1>
 __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Real *xy, const Grid<D> &g, const int *I, bool active,
                                                    int A, unsigned int *err, int separate = 0, const Real *Ac = nullptr,
                                                    const Real *Bc = nullptr, int64_t jc = 0, int64_t nc = 0,
-                                                   Real wmul = (Real)1)
+                                                   Real wmul = (Real)1, const LaneStage<Real> &stg = LaneStage<Real>())
 {
     constexpr int C = 1 << D, S = Dims<D>::S;
     int64_t i = 0;
@@ -472,6 +486,8 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
         st[D - 1] = 1;
 #pragma unroll
         for (int d = D - 2; d >= 0; d--) st[d] = st[d + 1] * (g.r + 1);
+        // strides of the staged tile (3 x 3 x SW), compile-time constants
+        constexpr int tst[3] = {3 * SW, SW, 1};
         uint32_t iu = 0;
         bool ok = true;
 #pragma unroll
@@ -492,11 +508,22 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
 #pragma unroll
                 for (int cc = 0; cc < C; cc++)
                 {
-                    int jj = (int)iu;
+                    if constexpr (Staged)
+                    {
+                        int tj = stg.tcentre;
 #pragma unroll
-                    for (int d = 0; d < D; d++)
-                        if (cbit<D>(cc, d)) jj += sd[d];
-                    c2[cc] = ld2(xy, (int64_t)(uint32_t)jj);
+                        for (int d = 0; d < 3; d++)
+                            if (cbit<3>(cc, d)) tj += cbit<3>(A, d) ? -tst[d] : tst[d];
+                        c2[cc] = stg.tile[tj];
+                    }
+                    else
+                    {
+                        int jj = (int)iu;
+#pragma unroll
+                        for (int d = 0; d < D; d++)
+                            if (cbit<D>(cc, d)) jj += sd[d];
+                        c2[cc] = ld2(xy, (int64_t)(uint32_t)jj);
+                    }
                 }
                 element_fit_packed<D>(c2, h);
             }
@@ -506,11 +533,23 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
 #pragma unroll
                 for (int cc = 0; cc < C; cc++)
                 {
-                    int jj = (int)iu;
+                    Real2<Real> v;
+                    if constexpr (Staged)
+                    {
+                        int tj = stg.tcentre;
 #pragma unroll
-                    for (int d = 0; d < D; d++)
-                        if (cbit<D>(cc, d)) jj += sd[d];
-                    Real2<Real> v = ld2(xy, (int64_t)(uint32_t)jj);
+                        for (int d = 0; d < 3; d++)
+                            if (cbit<3>(cc, d)) tj += cbit<3>(A, d) ? -tst[d] : tst[d];
+                        v = stg.tile[tj];
+                    }
+                    else
+                    {
+                        int jj = (int)iu;
+#pragma unroll
+                        for (int d = 0; d < D; d++)
+                            if (cbit<D>(cc, d)) jj += sd[d];
+                        v = ld2(xy, (int64_t)(uint32_t)jj);
+                    }
                     x[cc] = v.x;
                     y[cc] = v.y;
                 }
@@ -532,7 +571,12 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
             }
             if (!in) continue;
             Real a, b;
-            if (Ac)
+            if constexpr (Staged)
+            {
+                a = stg.As[o * stg.npb + stg.t];
+                b = stg.Bs[o * stg.npb + stg.t];
+            }
+            else if (Ac)
             {
                 a = Ac[(int64_t)o * nc + jc];
                 b = Bc[(int64_t)o * nc + jc];
@@ -542,7 +586,9 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
                 a = L.A[(int64_t)o * L.N + i];
                 b = L.B[(int64_t)o * L.N + i];
             }
-            Real2<Real> v = ld2(xy, (int64_t)(uint32_t)jj);
+            Real2<Real> v;
+            if constexpr (Staged) v = stg.tile[stg.tcentre + off[0] * tst[0] + off[1] * tst[1] + off[2] * tst[2]];
+            else v = ld2(xy, (int64_t)(uint32_t)jj);
             ax += a * v.x;
             ay += a * v.y;
             if (o == Dims<D>::CENTER) acen = a;
@@ -838,7 +884,7 @@ __device__ __forceinline__ void gs_update_lanes(const LevelPtrs<Real> &L, const 
 template <int D, typename Real>
 constexpr int lanes_min_blocks() { return (D == 3 && sizeof(Real) == 4) ? 10 : 1; }
 
-template <int D, typename Real, bool Packed, int TPB>
+template <int D, typename Real, bool Packed, int TPB, bool Stage = false>
 __device__ __forceinline__ void gs_lanes_body(const LevelPtrs<Real> &L, const Colour<D> &col, int64_t cbBase, unsigned int *err,
                                               int separate, int bx, int by, int bz)
 {
@@ -858,15 +904,54 @@ __device__ __forceinline__ void gs_lanes_body(const LevelPtrs<Real> &L, const Co
     // index of the node in the colour (axis 0 slowest)
     const int64_t jc = ((int64_t)bz * col.cnt[D - 2] + by) * col.cnt[D - 1] + tl;
     const Real *Ac = L.Acb ? L.Acb + cbBase : nullptr, *Bc = L.Bcb ? L.Bcb + cbBase : nullptr;
+    if constexpr (D == 3 && Stage)
+        if (Ac)
+        {
+            // stage the row's 3 x 3 x W neighbourhood and its nodes' stencil columns (every thread of
+            // the block takes part; Ac is the same for the whole block)
+            constexpr int W = 2 * NPB + 1, S = Dims<3>::S;
+            __shared__ Real2<Real> tile[9 * W];
+            __shared__ Real As[S * NPB], Bs[S * NPB];
+            const int x0 = 2 * bx * NPB + col.par[2] - 1, y0 = I[1] - 1, z0 = I[0] - 1;
+            for (int k = threadIdx.x; k < 9 * W; k += TPB)
+            {
+                const int lz = k / (3 * W), ly = (k / W) % 3, lx = k % W;
+                const int gz = z0 + lz, gy = y0 + ly, gx = x0 + lx;
+                if (gz >= 0 && gz <= g.r && gy >= 0 && gy <= g.r && gx >= 0 && gx <= g.r)
+                    tile[k] = ld2(L.xy, ((int64_t)gz * (g.r + 1) + gy) * (g.r + 1) + gx);
+            }
+            const int nrow = min(NPB, col.cnt[2] - bx * NPB);  // the block's nodes in the colour
+            const int64_t jc0 = ((int64_t)bz * col.cnt[1] + by) * col.cnt[2] + (int64_t)bx * NPB;
+            for (int k = threadIdx.x; k < S * NPB; k += TPB)
+            {
+                const int o = k / NPB, t = k - o * NPB;
+                if (t < nrow)
+                {
+                    As[k] = Ac[(int64_t)o * col.n + jc0 + t];
+                    Bs[k] = Bc[(int64_t)o * col.n + jc0 + t];
+                }
+            }
+            __syncthreads();
+            LaneStage<Real> stg;
+            stg.tile = tile;
+            stg.t = tl - bx * NPB;
+            stg.tcentre = 4 * W + 2 * stg.t + 1;
+            stg.As = As;
+            stg.Bs = Bs;
+            stg.npb = NPB;
+            gs_update_lanes_at<D, Real, Packed, true, W>(L, L.xy, g, I, tl < col.cnt[D - 1], A, err, separate, Ac, Bc, jc,
+                                                        col.n, (Real)1, stg);
+            return;
+        }
     gs_update_lanes_at<D, Real, Packed>(L, L.xy, g, I, tl < col.cnt[D - 1], A, err, separate, Ac, Bc, jc, col.n);
 }
 
-template <int D, typename Real, int MinBlocks = lanes_min_blocks<D, Real>(), bool Packed = false>
+template <int D, typename Real, int MinBlocks = lanes_min_blocks<D, Real>(), bool Packed = false, bool Stage = false>
 __global__ void __launch_bounds__(kThreads, MinBlocks) gs_colour_lanes_kernel(LevelPtrs<Real> L, Colour<D> col,
                                                                               int64_t cbBase, unsigned int *err,
                                                                               int separate)
 {
-    gs_lanes_body<D, Real, Packed, kThreads>(L, col, cbBase, err, separate, blockIdx.x, blockIdx.y, blockIdx.z);
+    gs_lanes_body<D, Real, Packed, kThreads, Stage>(L, col, cbBase, err, separate, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // the same colour of every reconstruction of a lockstep batch (3D): block = TPB threads (TPB / 8
@@ -1253,6 +1338,159 @@ __device__ __forceinline__ void gs_tiny_body(const LevelPtrs<Real> &L, int iters
     for (int k = threadIdx.x; k < NN; k += blockDim.x) reinterpret_cast<Real2<Real> *>(L.xy)[k] = xy[k];
 }
 
+// Level 0 (resolution 1: 8 nodes, one element, one node per colour) with four warps instead of
+// one: warp K < 3 integrates wedge component K of the node's element, lane = (Gauss-point pair,
+// other-axis point) (12 lanes, one point each), warp 3 the node's stencil column (lane = offset);
+// warp sums, one block barrier, thread 0 the node step.  A colour phase's dependent path is then one
+// point's setup and terms instead of three, spread over the SM's four sub-partitions.
+template <typename Real>
+__device__ __forceinline__ void gs_tiny0_body(const LevelPtrs<Real> &L, int iters, unsigned int *err, int separate, int *kexp)
+{
+    constexpr int NN = 8, S = 27, s0 = 4, s1 = 2;
+    constexpr bool kDF = std::is_same<Real, df>::value;
+    __shared__ Real2<Real> xy[NN];
+    __shared__ Real As[S * NN], Bs[S * NN];
+    __shared__ Real part[4][5];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k < NN; k += blockDim.x) xy[k] = ld2(L.xy, k);
+    for (int k = threadIdx.x; k < S * NN; k += blockDim.x)
+    {
+        As[k] = L.A[k];
+        Bs[k] = L.B[k];
+    }
+    __syncthreads();
+    Real wmul = wedge_mult<Real>(kexp, 0);
+    for (int it = 0; it < iters; it++)
+    {
+#pragma unroll 1
+        for (int c = 0; c < 8; c++)
+        {
+            // the colour's node: coordinate d = parity bit d of the colour; the element's corner of
+            // the node has the node's coordinates as its bits
+            const int I0 = c & 1, I1 = (c >> 1) & 1, I2 = (c >> 2) & 1;
+            const int i = (I0 * 2 + I1) * 2 + I2;
+            const int A = (I0 << 2) | (I1 << 1) | I2;
+            Real r[5] = {0, 0, 0, 0, 0};
+            if (warp < 3 && lane < 12)
+            {
+                const int K = warp, pq = lane / 3, go = lane - 3 * (lane / 3);
+                const int pax[3] = {(K == 2) ? 1 : 0, (K == 0) ? 1 : 2, (K == 0) ? 2 : (K == 1 ? 1 : 0)};
+                int sd[3];
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+                {
+                    const int stride = pax[a] == 0 ? s0 : (pax[a] == 1 ? s1 : 1);
+                    sd[a] = ((A >> (2 - pax[a])) & 1) ? -stride : stride;
+                }
+                Real x[8], y[8];
+#pragma unroll
+                for (int cc = 0; cc < 8; cc++)
+                {
+                    int jj = i;
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+                        if (cbit<3>(cc, a)) jj += sd[a];
+                    const Real2<Real> v = xy[jj];
+                    x[cc] = v.x;
+                    y[cc] = v.y;
+                }
+                PairTables<Real> t;
+                component_setup_pq3<Real>(x, y, pq >> 1, pq & 1, t);
+                component_point_pq3<Real>(t, go, r);
+            }
+            else if (warp == 3 && lane < S)
+            {
+                const int o = lane;
+                const int off[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+                const int q0 = I0 + off[0], q1 = I1 + off[1], q2 = I2 + off[2];
+                if (q0 >= 0 && q0 <= 1 && q1 >= 0 && q1 <= 1 && q2 >= 0 && q2 <= 1)
+                {
+                    const Real a = As[o * NN + i], b = Bs[o * NN + i];
+                    const Real2<Real> q = xy[i + off[0] * s0 + off[1] * s1 + off[2]];
+                    r[0] = a * q.x;
+                    r[1] = a * q.y;
+                    if (o == 13) r[4] = a;
+                    else { r[2] = b * q.x; r[3] = b * q.y; }
+                }
+            }
+            // warp sums (in double-float the rounds stay rolled: small code for the instruction cache)
+            if constexpr (kDF)
+            {
+#pragma unroll 1
+                for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                    for (int k = 0; k < 5; k++) r[k] += shfl_xor_any(r[k], o);
+            }
+            else
+            {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                    for (int k = 0; k < 5; k++) r[k] += shfl_xor_any(r[k], o);
+            }
+            if (lane == 0)
+#pragma unroll
+                for (int k = 0; k < 5; k++) part[warp][k] = r[k];
+            __syncthreads();
+            if (threadIdx.x == 0)
+            {
+                Real h[5], sv[5];
+#pragma unroll
+                for (int k = 0; k < 5; k++)
+                {
+                    h[k] = (part[0][k] + part[1][k]) + part[2][k];
+                    sv[k] = part[3][k];
+                }
+                const Real sc = (Real)wedge_scale<3>(1) * wmul;
+                Real q[5];
+                q[0] = h[0] * sc + sv[4];
+                q[1] = h[1] * sc + sv[4];
+                q[2] = (Real)2 * h[2] * sc;
+                q[3] = (Real)2 * h[3] * sc + (Real)2 * sv[0] - (Real)2 * sv[3];
+                q[4] = (Real)2 * h[4] * sc + (Real)2 * sv[1] + (Real)2 * sv[2];
+                Real p0, p1;
+                if (node_step_tiny<Real>(q, separate, p0, p1))
+                {
+                    Real2<Real> cur = xy[i];
+                    cur.x += p0;
+                    cur.y += p1;
+                    if (!finite_value<Real>(cur.x) || !finite_value<Real>(cur.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
+                    xy[i] = cur;
+                }
+            }
+            __syncthreads();
+        }
+        if constexpr (kDF)
+            if (kexp)
+            {
+                // keep the stored coefficients near 1: a new power-of-two exponent after every sweep
+                const int shift = df_rescale_shift(reinterpret_cast<const df *>(xy), 2 * NN);
+                if (shift)
+                {
+                    df *v = reinterpret_cast<df *>(xy);
+                    for (int k = threadIdx.x; k < 2 * NN; k += blockDim.x) v[k] = ldexp_df(v[k], shift);
+                    if (threadIdx.x == 0) kexp[0] -= shift;
+                    __syncthreads();
+                    wmul = wedge_mult<Real>(kexp, 0);
+                }
+            }
+    }
+    for (int k = threadIdx.x; k < NN; k += blockDim.x) reinterpret_cast<Real2<Real> *>(L.xy)[k] = xy[k];
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(128) gs_tiny0_kernel(LevelPtrs<Real> L, int iters, unsigned int *err, int separate, int *kexp)
+{
+    gs_tiny0_body<Real>(L, iters, err, separate, kexp);
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(128) gs_tiny0_batch_kernel(const BatchJob<Real> *jobs)
+{
+    const BatchJob<Real> &b = jobs[blockIdx.x];
+    gs_tiny0_body<Real>(b.L, b.iters, b.err, b.separate, b.kexp);
+}
+
 template <typename Real, int LEVEL>
 __global__ void __launch_bounds__(LEVEL == 0 ? 32 : 256) gs_tiny_kernel(LevelPtrs<Real> L, int iters, unsigned int *err,
                                                                           int separate, int *kexp)
@@ -1424,7 +1662,8 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n)
 inline unsigned int blocks_for(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
 
 int g_lanes_variant = 1;  // 0: scalar float element fit in the lane kernel, 1: packed
-int g_tiny_levels = 1;    // 1: 3D levels 0-1 by gs_tiny_kernel, 0: by the block kernels of gs_level_kernel
+int g_tiny_levels = 1;    // 1: 3D levels 0-1 by gs_tiny0_kernel / gs_tiny_kernel, 2: level 0 by the one-warp
+                          // gs_tiny_kernel, 0: by the block kernels of gs_level_kernel
 int g_gs_variant = 1;  // 0: one thread per node, 1: 2^D lanes per node (row grid), 2: 2^D lanes per node (flat grid),
                        // 4: as 1 without the point-split update of the small 3D levels
 
@@ -1490,10 +1729,18 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
         // float: the element integrals on the packed two-wide FP32 instructions (3D: 0.614 against
         // 0.680 ms per depth-8 colour; registers capped at 56, 9 resident blocks, where the
         // scalar fit ran best at 48); EPR_LANES_VARIANT=0 selects the scalar fit
+        // (EPR_LANES_VARIANT 2 and 3: the block's row of nodes staged in shared memory, 9 or 8
+        // resident blocks: 0.741 and 0.785 against 0.601 ms per depth-8 colour -- the kernel is
+        // bound by instruction issue, and the staging adds instructions and a block barrier)
         if constexpr (std::is_same<Real, float>::value)
             if (g_lanes_variant != 0)
             {
-                gs_colour_lanes_kernel<D, Real, D == 3 ? 9 : 1, true><<<grid, kThreads, 0, s>>>(L, col, cb, err, separate);
+                if (g_lanes_variant == 2)
+                    gs_colour_lanes_kernel<D, Real, D == 3 ? 9 : 1, true, true><<<grid, kThreads, 0, s>>>(L, col, cb, err, separate);
+                else if (g_lanes_variant == 3)
+                    gs_colour_lanes_kernel<D, Real, D == 3 ? 8 : 1, true, true><<<grid, kThreads, 0, s>>>(L, col, cb, err, separate);
+                else
+                    gs_colour_lanes_kernel<D, Real, D == 3 ? 9 : 1, true><<<grid, kThreads, 0, s>>>(L, col, cb, err, separate);
                 return;
             }
         gs_colour_lanes_kernel<D, Real><<<grid, kThreads, 0, s>>>(L, col, cb, err, separate);
@@ -1509,7 +1756,11 @@ template <typename Real>
 bool launch_tiny_level(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s, int separate, int *kexp)
 {
     if (!g_tiny_levels || L.level > 1) return false;
-    if (L.level == 0) gs_tiny_kernel<Real, 0><<<1, 32, 0, s>>>(L, iters, err, separate, kexp);
+    if (L.level == 0)
+    {
+        if (g_tiny_levels == 2) gs_tiny_kernel<Real, 0><<<1, 32, 0, s>>>(L, iters, err, separate, kexp);
+        else gs_tiny0_kernel<Real><<<1, 128, 0, s>>>(L, iters, err, separate, kexp);
+    }
     else gs_tiny_kernel<Real, 1><<<1, 256, 0, s>>>(L, iters, err, separate, kexp);
     return true;
 }
@@ -1792,7 +2043,11 @@ template <typename Real>
 void launch_tiny_batch(const BatchJob<Real> *jobs, int level, int count, cudaStream_t s)
 {
     if (count <= 0) return;
-    if (level == 0) gs_tiny_batch_kernel<Real, 0><<<count, 32, 0, s>>>(jobs);
+    if (level == 0)
+    {
+        if (g_tiny_levels == 2) gs_tiny_batch_kernel<Real, 0><<<count, 32, 0, s>>>(jobs);
+        else gs_tiny0_batch_kernel<Real><<<count, 128, 0, s>>>(jobs);
+    }
     else gs_tiny_batch_kernel<Real, 1><<<count, 256, 0, s>>>(jobs);
 }
 
