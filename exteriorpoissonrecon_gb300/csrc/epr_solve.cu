@@ -13,6 +13,8 @@
 #include <cstring>
 #include <type_traits>
 
+#include <cooperative_groups.h>
+
 #include "epr_common.cuh"
 #include "epr_element.cuh"
 #include "epr_kernels.h"
@@ -1478,6 +1480,208 @@ __device__ __forceinline__ void gs_tiny0_body(const LevelPtrs<Real> &L, int iter
     for (int k = threadIdx.x; k < NN; k += blockDim.x) reinterpret_cast<Real2<Real> *>(L.xy)[k] = xy[k];
 }
 
+// Level 1 (resolution 2: 27 nodes, 8 node-element incidences per colour) on a cluster of two
+// blocks of four warps, one warp per incidence, so that each SM sub-partition issues for one warp
+// (in one block of eight warps two share each sub-partition and a colour phase takes both warps'
+// instructions).  Each block keeps a replica of the level's coefficients in its shared memory; a
+// warp writes its incidence's sums into both blocks, the node's owner (the warp of its first
+// incidence) applies the step to both replicas, and two cluster barriers order each colour.  The
+// arithmetic and its order are gs_tiny_body<Real, 1>'s, so the results are its bits.
+template <typename Real>
+__device__ __forceinline__ void gs_tiny1_cluster_body(const LevelPtrs<Real> &L, int iters, unsigned int *err, int separate, int *kexp)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    constexpr int NW = 8, R = 2, N1 = 3, NN = 27, S = 27, s0 = 9, s1 = 3;
+    constexpr bool kDF = std::is_same<Real, df>::value;
+    __shared__ Real2<Real> xy[NN];
+    __shared__ Real As[S * NN], Bs[S * NN];
+    __shared__ Real part[NW][10];
+    __shared__ int incNode[8][NW], incA[8][NW], incCnt[8][NW], incI[8][NW][3], incFirst[8][NW];
+    const unsigned rank = cluster.block_rank();
+    const int warp = (int)rank * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;  // the incidence
+    Real2<Real> *peerXY = cluster.map_shared_rank(xy, rank ^ 1u);
+    Real *peerPart = cluster.map_shared_rank(&part[0][0], rank ^ 1u);
+    for (int k = threadIdx.x; k < NN; k += blockDim.x) xy[k] = ld2(L.xy, k);
+    for (int k = threadIdx.x; k < S * NN; k += blockDim.x)
+    {
+        As[k] = L.A[k];
+        Bs[k] = L.B[k];
+    }
+    if (threadIdx.x < 8)
+    {
+        const int c = threadIdx.x;
+        const Grid<3> g(1);
+        const Colour<3> col(g, c);
+        int w = 0;
+        for (int j = 0; j < (int)col.n; j++)
+        {
+            int I[3];
+            col.node(j, I);
+            int cnt = 0;
+            for (int A = 0; A < 8; A++)
+            {
+                bool ok = true;
+                for (int d = 0; d < 3; d++) { const int e = I[d] - cbit<3>(A, d); ok = ok && e >= 0 && e < R; }
+                if (ok) cnt++;
+            }
+            int k = 0;
+            for (int A = 0; A < 8; A++)
+            {
+                bool ok = true;
+                for (int d = 0; d < 3; d++) { const int e = I[d] - cbit<3>(A, d); ok = ok && e >= 0 && e < R; }
+                if (!ok || w >= NW) continue;
+                incNode[c][w] = (I[0] * N1 + I[1]) * N1 + I[2];
+                incA[c][w] = A;
+                incFirst[c][w] = k == 0;
+                incCnt[c][w] = cnt;
+                for (int d = 0; d < 3; d++) incI[c][w][d] = I[d];
+                w++;
+                k++;
+            }
+        }
+    }
+    cluster.sync();  // both replicas and tables ready before any remote write
+    Real wmul = wedge_mult<Real>(kexp, 1);
+    for (int it = 0; it < iters; it++)
+    {
+#pragma unroll 1
+        for (int c = 0; c < 8; c++)
+        {
+            const int i = incNode[c][warp], A = incA[c][warp];
+            const bool first = incFirst[c][warp] != 0;
+            Real r[5] = {0, 0, 0, 0, 0};
+            if (lane < 12)
+            {
+                const int K = lane >> 2, pq = lane & 3;
+                const int pax[3] = {(K == 2) ? 1 : 0, (K == 0) ? 1 : 2, (K == 0) ? 2 : (K == 1 ? 1 : 0)};
+                int sd[3];
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+                {
+                    const int stride = pax[a] == 0 ? s0 : (pax[a] == 1 ? s1 : 1);
+                    sd[a] = ((A >> (2 - pax[a])) & 1) ? -stride : stride;
+                }
+                Real x[8], y[8];
+#pragma unroll
+                for (int cc = 0; cc < 8; cc++)
+                {
+                    int jj = i;
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+                        if (cbit<3>(cc, a)) jj += sd[a];
+                    const Real2<Real> v = xy[jj];
+                    x[cc] = v.x;
+                    y[cc] = v.y;
+                }
+                component_fit_pq3<Real>(x, y, pq >> 1, pq & 1, r);
+            }
+            else if (lane >= 16 && first)
+            {
+#pragma unroll
+                for (int half = 0; half < 2; half++)
+                {
+                    const int o = lane - 16 + 16 * half;
+                    if (o >= S) continue;
+                    const int off[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+                    bool in = true;
+#pragma unroll
+                    for (int d = 0; d < 3; d++) { const int q = incI[c][warp][d] + off[d]; in = in && q >= 0 && q <= R; }
+                    if (!in) continue;
+                    const int jj = i + off[0] * s0 + off[1] * s1 + off[2];
+                    const Real a = As[o * NN + i], b = Bs[o * NN + i];
+                    const Real2<Real> q = xy[jj];
+                    r[0] += a * q.x;
+                    r[1] += a * q.y;
+                    if (o == 13) r[4] = a;
+                    else { r[2] += b * q.x; r[3] += b * q.y; }
+                }
+            }
+#pragma unroll
+            for (int o = 8; o > 0; o >>= 1)
+#pragma unroll
+                for (int k = 0; k < 5; k++) r[k] += shfl_xor_any(r[k], o);
+            Real stc[5];
+#pragma unroll
+            for (int k = 0; k < 5; k++) stc[k] = shfl_any(r[k], 16);
+            if (lane == 0)
+#pragma unroll
+                for (int k = 0; k < 5; k++)
+                {
+                    part[warp][k] = r[k];
+                    part[warp][5 + k] = stc[k];
+                    peerPart[warp * 10 + k] = r[k];
+                    peerPart[warp * 10 + 5 + k] = stc[k];
+                }
+            cluster.sync();  // every incidence's sums in both blocks
+            if (lane == 0 && first)
+            {
+                Real h[5], sv[5];
+#pragma unroll
+                for (int k = 0; k < 5; k++)
+                {
+                    h[k] = part[warp][k];
+                    sv[k] = part[warp][5 + k];
+                }
+                for (int w2 = 1; w2 < incCnt[c][warp]; w2++)
+#pragma unroll
+                    for (int k = 0; k < 5; k++) h[k] += part[warp + w2][k];
+                const Real sc = (Real)wedge_scale<3>(R) * wmul;
+                Real q[5];
+                q[0] = h[0] * sc + sv[4];
+                q[1] = h[1] * sc + sv[4];
+                q[2] = (Real)2 * h[2] * sc;
+                q[3] = (Real)2 * h[3] * sc + (Real)2 * sv[0] - (Real)2 * sv[3];
+                q[4] = (Real)2 * h[4] * sc + (Real)2 * sv[1] + (Real)2 * sv[2];
+                Real p0, p1;
+                if (node_step_tiny<Real>(q, separate, p0, p1))
+                {
+                    Real2<Real> cur = xy[i];
+                    cur.x += p0;
+                    cur.y += p1;
+                    if (!finite_value<Real>(cur.x) || !finite_value<Real>(cur.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
+                    xy[i] = cur;
+                    peerXY[i] = cur;
+                }
+            }
+            cluster.sync();  // both replicas updated before the next colour reads them
+        }
+        if constexpr (kDF)
+            if (kexp)
+            {
+                // both replicas hold the same values, so both blocks pick the same new exponent
+                const int shift = df_rescale_shift(reinterpret_cast<const df *>(xy), 2 * NN);
+                if (shift)
+                {
+                    df *v = reinterpret_cast<df *>(xy);
+                    for (int k = threadIdx.x; k < 2 * NN; k += blockDim.x) v[k] = ldexp_df(v[k], shift);
+                    if (rank == 0 && threadIdx.x == 0) kexp[1] -= shift;
+                }
+                // no remote write of the next sweep before the peer's rescale; the new exponent
+                // (written by the first block) visible to both
+                cluster.sync();
+                if (shift) wmul = wedge_mult<Real>(kexp, 1);
+            }
+    }
+    if (rank == 0)
+        for (int k = threadIdx.x; k < NN; k += blockDim.x) reinterpret_cast<Real2<Real> *>(L.xy)[k] = xy[k];
+    cluster.sync();  // no block leaves while its peer may still address its shared memory
+}
+
+template <typename Real>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128) gs_tiny1_kernel(LevelPtrs<Real> L, int iters, unsigned int *err,
+                                                                                int separate, int *kexp)
+{
+    gs_tiny1_cluster_body<Real>(L, iters, err, separate, kexp);
+}
+
+template <typename Real>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128) gs_tiny1_batch_kernel(const BatchJob<Real> *jobs)
+{
+    const BatchJob<Real> &b = jobs[blockIdx.x >> 1];
+    gs_tiny1_cluster_body<Real>(b.L, b.iters, b.err, b.separate, b.kexp);
+}
+
 template <typename Real>
 __global__ void __launch_bounds__(128) gs_tiny0_kernel(LevelPtrs<Real> L, int iters, unsigned int *err, int separate, int *kexp)
 {
@@ -1662,8 +1866,9 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n)
 inline unsigned int blocks_for(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
 
 int g_lanes_variant = 1;  // 0: scalar float element fit in the lane kernel, 1: packed
-int g_tiny_levels = 1;    // 1: 3D levels 0-1 by gs_tiny0_kernel / gs_tiny_kernel, 2: level 0 by the one-warp
-                          // gs_tiny_kernel, 0: by the block kernels of gs_level_kernel
+int g_tiny_levels = 1;    // 1: 3D levels 0-1 by gs_tiny0_kernel / gs_tiny1_kernel, 2: level 0 by the one-warp
+                          // gs_tiny_kernel, 3: level 1 by the one-block gs_tiny_kernel, 0: by the block
+                          // kernels of gs_level_kernel
 int g_gs_variant = 1;  // 0: one thread per node, 1: 2^D lanes per node (row grid), 2: 2^D lanes per node (flat grid),
                        // 4: as 1 without the point-split update of the small 3D levels
 
@@ -1761,7 +1966,11 @@ bool launch_tiny_level(const LevelPtrs<Real> &L, int iters, unsigned int *err, c
         if (g_tiny_levels == 2) gs_tiny_kernel<Real, 0><<<1, 32, 0, s>>>(L, iters, err, separate, kexp);
         else gs_tiny0_kernel<Real><<<1, 128, 0, s>>>(L, iters, err, separate, kexp);
     }
-    else gs_tiny_kernel<Real, 1><<<1, 256, 0, s>>>(L, iters, err, separate, kexp);
+    // level 1: the two-block cluster in double-float and double (33.7 against 43.0 ms, 73 against 112
+    // ms at depth 8); float keeps the one-block kernel (8.8 against 11.4 ms: its phases are short
+    // enough for the cluster barriers to dominate)
+    else if (g_tiny_levels == 3 || std::is_same<Real, float>::value) gs_tiny_kernel<Real, 1><<<1, 256, 0, s>>>(L, iters, err, separate, kexp);
+    else gs_tiny1_kernel<Real><<<2, 128, 0, s>>>(L, iters, err, separate, kexp);
     return true;
 }
 
@@ -2048,7 +2257,8 @@ void launch_tiny_batch(const BatchJob<Real> *jobs, int level, int count, cudaStr
         if (g_tiny_levels == 2) gs_tiny_batch_kernel<Real, 0><<<count, 32, 0, s>>>(jobs);
         else gs_tiny0_batch_kernel<Real><<<count, 128, 0, s>>>(jobs);
     }
-    else gs_tiny_batch_kernel<Real, 1><<<count, 256, 0, s>>>(jobs);
+    else if (g_tiny_levels == 3 || std::is_same<Real, float>::value) gs_tiny_batch_kernel<Real, 1><<<count, 256, 0, s>>>(jobs);
+    else gs_tiny1_batch_kernel<Real><<<2 * count, 128, 0, s>>>(jobs);
 }
 
 template <typename Real, int TPB>
