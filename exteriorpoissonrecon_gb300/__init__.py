@@ -62,6 +62,7 @@ class Params(ctypes.Structure):
         ("warm_start", ctypes.c_int),
         ("max_extra_sweeps", ctypes.c_int),
         ("target_energy", ctypes.c_double),
+        ("project", ctypes.c_int),
     ]
 
 
@@ -134,7 +135,7 @@ _FLAG_NAMES = {
     "sWeight": "s_weight", "dWeight": "d_weight", "nSigma": "n_sigma", "iMult": "i_mult",
     "tRadius": "t_radius", "dRadius": "d_radius", "gsIters": "gs_iters",
     "minSolveDepth": "min_solve_depth", "maxSolveDepth": "max_solve_depth", "seed": "seed",
-    "singleLevel": "single_level", "separate": "separate",
+    "singleLevel": "single_level", "separate": "separate", "project": "project",
 }
 
 

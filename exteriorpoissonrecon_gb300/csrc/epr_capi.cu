@@ -607,6 +607,7 @@ void epr_default_params(epr_params *p)
     p->warm_start = 0;
     p->max_extra_sweeps = 0;
     p->target_energy = 0;
+    p->project = 0;
 }
 
 const char *epr_global_error(void) { return g_error.c_str(); }

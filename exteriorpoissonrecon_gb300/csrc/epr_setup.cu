@@ -684,8 +684,69 @@ struct SkewGrids
     int depth;
 };
 
+// FitBlade (ExteriorPoisson.h:411-438) of a packed skew matrix (entry (i, j), j < i, in (i, j)
+// order; the matrix m(i, j) = p, m(j, i) = -p in the reference's (column, row) indexing,
+// Hat.inl:45-52): the power iteration v2 = Next(v1), v1 <- -Next(v2) with
+// Next(v) = normalised (m v - (v . m v) v), stopped when |v1 - v1'|^2 < 1e-10 or after 1000 steps
+// (the command line's ProjectionIterations / ProjectionEpslion, ExteriorPoissonRecon.cpp:48-49);
+// then a, b = v1, v2 scaled by |m|^(1/2) (Frobenius) and p(i, j) = (a_j b_i - a_i b_j) / 2.  The
+// iteration starts from m's largest column (in m's image, never in its kernel; the reference starts
+// from a random unit vector, which converges to the same blade).
 template <int D>
-__global__ void element_frame_kernel(SkewGrids<D> G, double *S, int *leaf)
+__device__ void project_blade(double *p)
+{
+    double m[D][D];
+    double sq = 0;
+    for (int i = 0; i < D; i++) m[i][i] = 0;
+    for (int i = 0, idx = 0; i < D; i++)
+        for (int j = 0; j < i; j++, idx++)
+        {
+            // the reference's SquareMatrix is indexed (column, row) and S() * v sums over columns:
+            // as a row-major matrix, row j column i holds p and row i column j holds -p
+            m[j][i] = p[idx];
+            m[i][j] = -p[idx];
+            sq += 2 * p[idx] * p[idx];
+        }
+    if (sq == 0) return;
+    auto next = [&](const double *v, double *out) {
+        double w[D], dot = 0, n2 = 0;
+        for (int i = 0; i < D; i++)
+        {
+            w[i] = 0;
+            for (int j = 0; j < D; j++) w[i] += m[i][j] * v[j];
+        }
+        for (int i = 0; i < D; i++) dot += v[i] * w[i];
+        for (int i = 0; i < D; i++) { w[i] -= dot * v[i]; n2 += w[i] * w[i]; }
+        const double n = sqrt(n2);
+        for (int i = 0; i < D; i++) out[i] = w[i] / n;
+    };
+    double v1[D], v2[D];
+    int best = 0;
+    double bn = -1;
+    for (int k = 0; k < D; k++)
+    {
+        double n2 = 0;
+        for (int i = 0; i < D; i++) n2 += m[i][k] * m[i][k];
+        if (n2 > bn) { bn = n2; best = k; }
+    }
+    for (int i = 0; i < D; i++) { v1[i] = m[i][best] / sqrt(bn); v2[i] = 0; }
+    for (int s = 0; s < 1000; s++)
+    {
+        double nv1[D];
+        next(v1, v2);
+        next(v2, nv1);
+        double d2 = 0;
+        for (int i = 0; i < D; i++) { nv1[i] = -nv1[i]; d2 += (v1[i] - nv1[i]) * (v1[i] - nv1[i]); }
+        if (d2 < 1e-10) break;
+        for (int i = 0; i < D; i++) v1[i] = nv1[i];
+    }
+    const double scale = sqrt(sqrt(sq));
+    for (int i = 0, idx = 0; i < D; i++)
+        for (int j = 0; j < i; j++, idx++) p[idx] = ((v1[j] * scale) * (v2[i] * scale) - (v1[i] * scale) * (v2[j] * scale)) / 2.;
+}
+
+template <int D>
+__global__ void element_frame_kernel(SkewGrids<D> G, double *S, int *leaf, int project)
 {
     constexpr int K = D * (D - 1) / 2;
     int r = 1 << G.depth;
@@ -736,6 +797,7 @@ __global__ void element_frame_kernel(SkewGrids<D> G, double *S, int *leaf)
             for (int k = 0; k < K; k++) acc[k] += g[vi * K + k] * w;
         }
     }
+    if (project) project_blade<D>(acc);
     for (int k = 0; k < K; k++) S[e * K + k] = acc[k];
     leaf[e] = L;
 }
@@ -1274,7 +1336,7 @@ bool build_impl(Context &c, Setup &st)
         for (int l = 0; l <= depth; l++) G.g[l] = st.skewGrid[l];
         for (int t = 0; t <= depth + 1 && t < 12; t++) G.refined[t] = st.refinedS[t];
         G.depth = depth;
-        element_frame_kernel<D><<<nblocks(gfine.NE, 128), 128, 0, s>>>(G, st.S, st.leaf);
+        element_frame_kernel<D><<<nblocks(gfine.NE, 128), 128, 0, s>>>(G, st.S, st.leaf, c.P.project);
     }
     double *dsum = nullptr;
     if (!dalloc(c, &dsum, 4, "sums")) return false;

@@ -9,7 +9,10 @@
 //   * only the regular indexer exists here, so --aRadius defaults to -1 and any other value is an
 //     error (the reference's default, 3, selects its adaptive octree indexer);
 //   * errors exit with a non-zero status (the reference prints and exits 0);
-//   * --project (blade fitting from a random start) is not offered.
+//   * --project fits every element's blade by the power iteration from a fixed start, each element
+//     with the full iteration budget (1000 steps, 1e-10); the reference starts from random vectors
+//     and passes one shared step budget by reference to all elements (FitBlade's `steps`,
+//     ExteriorPoisson.h:303, 412), so in 4D its blades depend on thread timing.
 // <out>.density.tree is written as the reference writes it (the estimator's tree, epr_write_density_tree),
 // with zero words where the reference's file holds memory addresses.
 #include <cmath>
@@ -291,7 +294,6 @@ int main(int argc, char **argv)
     Args a = Parse(argc, argv);
     if (a.in.empty()) { Usage(argv[0]); return EXIT_SUCCESS; }
     if (a.aRadius != -1) Fail("only the regular grid (--aRadius -1) is implemented; the adaptive indexer is not", 2);
-    if (a.project) Fail("--project is not supported", 2);
     if (a.precision != "fp32" && a.precision != "fp64") Fail("--precision must be fp64 or fp32", 2);
     if (a.solver != "cascadic" && a.solver != "multigrid") Fail("--solver must be cascadic or multigrid", 2);
     if (a.bandPrecision != "fp64" && a.bandPrecision != "df") Fail("--bandPrecision must be fp64 or df", 2);
@@ -367,6 +369,7 @@ int main(int argc, char **argv)
     p.device = a.device;
     p.single_level = a.singleLevel ? 1 : 0;
     p.separate = a.separate ? 1 : 0;
+    p.project = a.project ? 1 : 0;
 
     epr_ctx *ctx = epr_create(D, a.depth, &p);
     if (!ctx) Fail(std::string("epr_create: ") + epr_global_error());

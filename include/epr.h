@@ -121,6 +121,8 @@ typedef struct epr_params {
     double target_energy; /* > 0: after the schedule the finest solve level keeps relaxing, one paired
                              Gauss-Seidel sweep at a time, until its FP64 energy is <= target_energy or
                              max_extra_sweeps were added; the energy checks are part of the timed solve (0) */
+    int project;          /* --project: every element's S(E) projected onto its best blade before the
+                             constraint is built (FitBlade, ExteriorPoisson.h:300-305, 411-438) (0) */
 } epr_params;
 
 typedef struct epr_stats {

@@ -144,6 +144,67 @@ struct LevelSystem
 
 // Dense per-tree-level splat storage: tree depth t (1..D+1) has resolution 2^(t-1) and
 // (2^(t-1)+1)^D vertices; level index l = t-1.
+// FitBlade (ExteriorPoisson.h:411-438): the skew matrix p (packed as the reference's
+// SkewSymmetricMatrix: entry (i, j), j < i, in (i, j) order; the matrix m(i, j) = p, m(j, i) = -p in
+// the reference's (column, row) indexing, Hat.inl:45-52) replaced by
+// the blade a ^ b of the power iteration v2 = Next(v1), v1 <- -Next(v2), Next(v) = normalised
+// (m v - (v . m v) v), stopped when |v1 - v1'|^2 < 1e-10 or after 1000 steps
+// (ExteriorPoissonRecon.cpp:48-49), then a, b = v1, v2 scaled by |m|^(1/2) (Frobenius norm) and
+// p(i, j) = (a_j b_i - a_i b_j) / 2.  The start is the column of m with the largest norm (it lies in
+// m's image, so the iteration never meets m's kernel); the reference starts from a random unit
+// vector, which converges to the same blade.
+template <int D>
+static void ProjectBlade(double *p)
+{
+    double m[D][D] = {};
+    double sq = 0;
+    for (int i = 0, idx = 0; i < D; i++)
+        for (int j = 0; j < i; j++, idx++)
+        {
+            // the reference's SquareMatrix is indexed (column, row) and S() * v sums over columns:
+            // as a row-major matrix, row j column i holds p and row i column j holds -p
+            m[j][i] = p[idx];
+            m[i][j] = -p[idx];
+            sq += 2 * p[idx] * p[idx];
+        }
+    if (sq == 0) return;
+    auto next = [&](const double *v, double *out) {
+        double w[D], dot = 0, n2 = 0;
+        for (int i = 0; i < D; i++)
+        {
+            w[i] = 0;
+            for (int j = 0; j < D; j++) w[i] += m[i][j] * v[j];
+        }
+        for (int i = 0; i < D; i++) dot += v[i] * w[i];
+        for (int i = 0; i < D; i++) { w[i] -= dot * v[i]; n2 += w[i] * w[i]; }
+        const double n = std::sqrt(n2);
+        for (int i = 0; i < D; i++) out[i] = w[i] / n;
+    };
+    double v1[D], v2[D] = {};
+    int best = 0;
+    double bn = -1;
+    for (int k = 0; k < D; k++)
+    {
+        double n2 = 0;
+        for (int i = 0; i < D; i++) n2 += m[i][k] * m[i][k];
+        if (n2 > bn) { bn = n2; best = k; }
+    }
+    for (int i = 0; i < D; i++) v1[i] = m[i][best] / std::sqrt(bn);
+    for (int s = 0; s < 1000; s++)
+    {
+        double nv1[D];
+        next(v1, v2);
+        next(v2, nv1);
+        double d2 = 0;
+        for (int i = 0; i < D; i++) { nv1[i] = -nv1[i]; d2 += (v1[i] - nv1[i]) * (v1[i] - nv1[i]); }
+        if (d2 < 1e-10) break;
+        for (int i = 0; i < D; i++) v1[i] = nv1[i];
+    }
+    const double scale = std::sqrt(std::sqrt(sq));
+    for (int i = 0, idx = 0; i < D; i++)
+        for (int j = 0; j < i; j++, idx++) p[idx] = ((v1[j] * scale) * (v2[i] * scale) - (v1[i] * scale) * (v2[j] * scale)) / 2.;
+}
+
 template <int D>
 struct DenseTree
 {
@@ -652,6 +713,7 @@ struct Oracle
                 interp(skewTree, t, p, tmp);
                 for (int k = 0; k < T::K; k++) acc[k] += tmp[k];
             }
+            if (P.project) ProjectBlade<D>(acc);
             for (int k = 0; k < T::K; k++) S[e * T::K + k] = acc[k];
         }
         double cc = 0;
@@ -1855,6 +1917,7 @@ void epr_oracle_default_params(epr_oracle_params *p)
     p->d_weight = 0.00625;
     p->n_sigma = 0.25;
     p->i_mult = 2.;
+    p->project = 0;
     p->t_radius = 1;
     p->d_radius = 1;
     p->gs_iters = 10;

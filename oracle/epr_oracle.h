@@ -37,6 +37,8 @@ typedef struct epr_oracle_params {
     int separate;         /* --separate */
     int alt_rounds;       /* > 0: relax every level with this many AlternatingSolve rounds (one
                              V-cycle of gs_iters relaxations per half-step) instead of paired GS */
+    int project;          /* --project: S(E) projected onto its best blade (ExteriorPoisson.h:300-305,
+                             411-438) */
 } epr_oracle_params;
 
 void epr_oracle_default_params(epr_oracle_params *p);

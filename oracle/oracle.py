@@ -32,6 +32,7 @@ class Params(ctypes.Structure):
         ("single_level", ctypes.c_int),
         ("separate", ctypes.c_int),
         ("alt_rounds", ctypes.c_int),
+        ("project", ctypes.c_int),
     ]
 
 

@@ -86,6 +86,7 @@ struct Params
     unsigned int tRadius = 1, dRadius = 1, gsIters = 10, seed = 0, minSolveDepth = 0;
     int solve = 1;
     int separate = 0, singleLevel = 0;
+    int project = 0;  // --project: the reference's blade projection of S(E) (ExteriorPoisson.h:300-305)
 };
 
 template <unsigned int Dim>
@@ -279,6 +280,23 @@ static void Run(const std::string &in, unsigned int depth, const std::string &ou
         }
         SaveF64(path("S"), S, {NE, K});
         SaveI64(path("leaf_depth"), leaf, {NE});
+        if (P.project)
+        {
+            // the reference's FitBlade of every element's S, each with the full iteration budget of
+            // the command line (ProjectionIterations, ProjectionEpslion: ExteriorPoissonRecon.cpp:48-49)
+            std::vector<double> Sp(NE * K);
+            srand(P.seed);
+            for (size_t e = 0; e < NE; e++)
+            {
+                Hat::SkewSymmetricMatrix<double, Dim> s;
+                for (unsigned int k = 0; k < K; k++) s[k] = S[e * K + k];
+                unsigned int steps = 1000;
+                std::pair<Point<double, Dim>, Point<double, Dim>> blade = ExteriorPoisson::FitBlade<Dim>(s, steps, 1e-10);
+                Hat::SkewSymmetricMatrix<double, Dim> sp(blade.first, blade.second);
+                for (unsigned int k = 0; k < K; k++) Sp[e * K + k] = sp[k];
+            }
+            SaveF64(path("S_project"), Sp, {NE, K});
+        }
     }
 
     // Full reconstructor (ExteriorPoissonRecon.cpp:220-245)
@@ -286,7 +304,8 @@ static void Run(const std::string &in, unsigned int depth, const std::string &ou
     const double nSigma = P.nSigma;
     auto NoiseToWeight = [nSigma](double x) { return exp(-x * x / (2. * nSigma * nSigma)); };
     ExteriorPoisson::Reconstructor<Dim, Energy> recon(hIndexer, depth, P.minSolveDepth, depth,
-        [&](size_t i) { return hermite[i]; }, orderedSampler, estimator, NoiseToWeight, P.dWeight, P.sWeight, P.tRadius, 0, 1e-10, false);
+        [&](size_t i) { return hermite[i]; }, orderedSampler, estimator, NoiseToWeight, P.dWeight, P.sWeight, P.tRadius,
+        P.project ? 1000u : 0u, 1e-10, false);
 
     {
         std::vector<double> c = {recon._energies.back()._c};
@@ -468,6 +487,7 @@ int main(int argc, char **argv)
         else if (k == "--solve") P.solve = (int)v;
         else if (k == "--separate") P.separate = (int)v;
         else if (k == "--singleLevel") P.singleLevel = (int)v;
+        else if (k == "--project") P.project = (int)v;
         else { fprintf(stderr, "unknown flag %s\n", k.c_str()); return 2; }
     }
     mkdir(out.c_str(), 0755);

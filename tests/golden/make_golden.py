@@ -47,6 +47,10 @@ VARIANTS = [
     ("knot3_d4_separate", "knot", 4096, 0, 4, ["--separate", "1"]),
     ("knot3_d4_single", "knot", 4096, 0, 4, ["--singleLevel", "1", "--gsIters", "40"]),
     ("knot3_d4_seed7_min2", "knot", 4096, 0, 4, ["--seed", "7", "--minSolveDepth", "2", "--iMult", "1.5"]),
+    # --project: the reference's blade projection of S(E) (its FitBlade of every element with the
+    # command line's full iteration budget) and, in 3D, the whole solve on the projected system
+    ("knot3_d4_project", "knot", 4096, 0, 4, ["--project", "1"]),
+    ("cliff4_d3_project", "clifford", 4000, 5, 3, ["--project", "1"]),
 ]
 
 
@@ -64,6 +68,9 @@ def make_variant(name, workload, n, seed, depth, flags):
         for l in range(depth + 1):
             fx[f"solx_d{l}"] = L(f"solx_d{l}")
             fx[f"soly_d{l}"] = L(f"soly_d{l}")
+        if os.path.exists(os.path.join(out, "S_project.npy")):
+            fx["S"] = L("S")
+            fx["S_project"] = L("S_project")
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **fx)
     print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB")
@@ -229,6 +236,9 @@ if __name__ == "__main__":
         for case in CASES:
             if case[0] in only:
                 make(*case)
+        for v in VARIANTS:
+            if v[0] in only:
+                make_variant(*v)
         for case in TREES:
             if case[0] in only:
                 make_tree(*case)

@@ -27,7 +27,7 @@ def test_params_struct_matches_defaults():
     assert q.s_weight == 50 and q.gs_iters == 20 and q.precision == epr.EPR_FP32
     assert p.band_precision == epr.EPR_BAND_FP64
     assert epr.default_params(band_precision="df").band_precision == epr.EPR_BAND_DF
-    assert ctypes.sizeof(epr.Params) == 120  # warm start, extra-sweep cap and target energy after band_precision
+    assert ctypes.sizeof(epr.Params) == 128  # warm start, extra-sweep cap, target energy and projection after band_precision
 
 
 def test_line_searches_host_only():

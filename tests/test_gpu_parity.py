@@ -356,3 +356,27 @@ def test_edge_inputs_match_oracle(name):
     st = r.solve()
     _, _, eo = o.solve()
     assert abs(st["fit_energy"] - eo[1]) < 1e-9 * eo[1] and abs(st["reg_energy"] - eo[2]) < 1e-9 * eo[2]
+
+
+@pytest.mark.parametrize("name,tol", [("knot3_d4_project", 1e-12), ("cliff4_d3_project", 2e-5)])
+def test_blade_projection(name, tol):
+    """--project: S(E) on the GPU against the reference's FitBlade of every element, and the whole
+    solve on the projected system against the oracle's.  (The reference's own solve with --project
+    is not comparable: its projection draws random start vectors from rand() inside a parallel loop
+    before the solve's random start is drawn from the same generator.)"""
+    g = load_golden(name)
+    dim, depth = g["pos"].shape[1], int(g["depth"])
+    r = epr.Reconstructor(dim, depth, g["pos"], g["skew"], project=1)
+    assert rel(r.get("S"), g["S_project"]) < tol
+    if dim == 3:
+        st = r.solve()
+        o = O.Oracle(dim, depth, project=1)
+        o.set_samples(g["pos"], g["skew"])
+        o.build()
+        xs, ys, e = o.solve()
+        assert abs(st["fit_energy"] - e[1]) < 1e-10 * e[1]
+        assert abs(st["reg_energy"] - e[2]) < 1e-10 * e[2]
+        gx, gy = r.solution()
+        for l in range(depth + 1):
+            assert rel(gx[l], xs[l]) < 1e-9 and rel(gy[l], ys[l]) < 1e-9
+    r.close()

@@ -251,3 +251,20 @@ def test_alternating_system_and_solve(probe_case):
     x1, y1 = o.alternating_solve(lev, xs, ys, iters=2, vcycles=2, gs_iters=2)
     e1 = o.energy(lev, x1, y1)
     assert e1[0] + e1[1] < e0[0] + e0[1]
+
+
+@pytest.mark.parametrize("name,tol", [("knot3_d4_project", 1e-12), ("cliff4_d3_project", 2e-5)])
+def test_blade_projection(name, tol):
+    """--project: every element's S(E) against the reference's FitBlade of it (ExteriorPoisson.h:
+    411-438, the command line's 1000 steps and 1e-10).  In 3D every S(E) is already a blade and
+    both iterations end on it (to rounding); in 4D both stop within the reference's 1e-10 on the
+    iterate, from different starts (the reference's is random), so they agree to ~1e-5."""
+    g = load_golden(name)
+    dim = g["pos"].shape[1]
+    o = O.Oracle(dim, int(g["depth"]), project=1)
+    o.set_samples(g["pos"], g["skew"])
+    o.build()
+    assert rel(o.get("S"), g["S_project"]) < tol
+    # the reference's projection scales |S| by 1/sqrt(2) (a blade's packed entries carry the 1/2 of
+    # SkewSymmetricMatrix(v1, v2), Hat.inl:33-38, while its scale uses the full matrix norm)
+    assert abs(np.linalg.norm(g["S_project"]) / np.linalg.norm(g["S"]) - 2 ** -0.5) < 1e-6
