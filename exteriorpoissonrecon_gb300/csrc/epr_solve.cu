@@ -361,6 +361,65 @@ __device__ __forceinline__ bool node_step(const Real *q, int separate, Real &p0,
     return true;
 }
 
+// Comparisons and finiteness tests in a level's own arithmetic: a double-float tests its pair
+// without converting to FP64 where the leading float decides.
+template <typename Real>
+__device__ __forceinline__ bool exceeds(Real v, double t)
+{
+    return (double)v > t;
+}
+// a double-float compares by its leading float unless that is within a factor of two of t
+template <>
+__device__ __forceinline__ bool exceeds<df>(df v, double t)
+{
+    const float tf = (float)t;
+    if (v.hi > 2.f * tf) return true;
+    if (v.hi < 0.5f * tf) return false;
+    return (double)v.hi + (double)v.lo > t;
+}
+template <typename Real>
+__device__ __forceinline__ Real abs_value(Real v)
+{
+    return v < (Real)0 ? -v : v;
+}
+template <>
+__device__ __forceinline__ df abs_value<df>(df v)
+{
+    return v.hi < 0.f ? -v : v;
+}
+template <typename Real>
+__device__ __forceinline__ bool finite_value(Real v)
+{
+    return isfinite((double)v);
+}
+template <>
+__device__ __forceinline__ bool finite_value<df>(df v)
+{
+    return isfinite(v.hi) && isfinite(v.lo);
+}
+
+// node_step with the singularity tests in the level's own arithmetic
+template <typename Real>
+__device__ __forceinline__ bool node_step_tiny(const Real *q, int separate, Real &p0, Real &p1)
+{
+    Real h00 = (Real)2 * q[0], h11 = (Real)2 * q[1], h01 = q[2];
+    if (separate)
+    {
+        p0 = 0;
+        p1 = 0;
+        if (exceeds<Real>(h00, 1e-20)) p0 = -((h01 + h01) * p1 + q[3]) / ((Real)2 * h00);
+        if (exceeds<Real>(h11, 1e-20)) p1 = -((h01 + h01) * p0 + q[4]) / ((Real)2 * h11);
+        return true;
+    }
+    Real det = h00 * h11 - h01 * h01;
+    if (!exceeds<Real>(abs_value<Real>(det), 1e-20)) return false;
+    // -H^{-1} grad / 2 with one division
+    const Real m = (Real)-0.5 / det;
+    p0 = (h11 * q[3] - h01 * q[4]) * m;
+    p1 = (-h01 * q[3] + h00 * q[4]) * m;
+    return true;
+}
+
 // Paired Gauss-Seidel update of node j of a parity colour.
 template <int D, typename Real>
 __device__ __forceinline__ void gs_update(const LevelPtrs<Real> &L, const Grid<D> &g, const Colour<D> &col, int64_t j, unsigned int *err,
@@ -821,12 +880,15 @@ __device__ __forceinline__ void gs_update_split3(const LevelPtrs<Real> &L, Real 
         q[3] = (Real)2 * h[3] * sc + (Real)2 * ax - (Real)2 * by;
         q[4] = (Real)2 * h[4] * sc + (Real)2 * ay + (Real)2 * bx;
         Real p0, p1;
-        if (node_step<Real>(q, separate, p0, p1))
+        // double-float levels test and divide in pair arithmetic (no FP64 conversions, one
+        // division); float and FP64 levels keep the two-division form of the other kernels
+        constexpr bool pair = std::is_same<Real, df>::value;
+        if (pair ? node_step_tiny<Real>(q, separate, p0, p1) : node_step<Real>(q, separate, p0, p1))
         {
             Real2<Real> cur = ld2(xy, i);
             cur.x += p0;
             cur.y += p1;
-            if (!isfinite((double)cur.x) || !isfinite((double)cur.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
+            if (!finite_value<Real>(cur.x) || !finite_value<Real>(cur.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
             reinterpret_cast<Real2<Real> *>(xy)[i] = cur;
         }
     }
@@ -1084,63 +1146,6 @@ __global__ void __launch_bounds__(MaxThreads) gs_level_kernel(LevelPtrs<Real> L,
 // stencils live in shared memory for the whole schedule.  Double-float levels rescale their stored
 // coefficients after every sweep as the other kernels do.
 // ---------------------------------------------------------------------------------------------
-template <typename Real>
-__device__ __forceinline__ bool exceeds(Real v, double t)
-{
-    return (double)v > t;
-}
-// a double-float compares by its leading float unless that is within a factor of two of t
-template <>
-__device__ __forceinline__ bool exceeds<df>(df v, double t)
-{
-    const float tf = (float)t;
-    if (v.hi > 2.f * tf) return true;
-    if (v.hi < 0.5f * tf) return false;
-    return (double)v.hi + (double)v.lo > t;
-}
-template <typename Real>
-__device__ __forceinline__ Real abs_value(Real v)
-{
-    return v < (Real)0 ? -v : v;
-}
-template <>
-__device__ __forceinline__ df abs_value<df>(df v)
-{
-    return v.hi < 0.f ? -v : v;
-}
-template <typename Real>
-__device__ __forceinline__ bool finite_value(Real v)
-{
-    return isfinite((double)v);
-}
-template <>
-__device__ __forceinline__ bool finite_value<df>(df v)
-{
-    return isfinite(v.hi) && isfinite(v.lo);
-}
-
-// node_step with the singularity tests in the level's own arithmetic
-template <typename Real>
-__device__ __forceinline__ bool node_step_tiny(const Real *q, int separate, Real &p0, Real &p1)
-{
-    Real h00 = (Real)2 * q[0], h11 = (Real)2 * q[1], h01 = q[2];
-    if (separate)
-    {
-        p0 = 0;
-        p1 = 0;
-        if (exceeds<Real>(h00, 1e-20)) p0 = -((h01 + h01) * p1 + q[3]) / ((Real)2 * h00);
-        if (exceeds<Real>(h11, 1e-20)) p1 = -((h01 + h01) * p0 + q[4]) / ((Real)2 * h11);
-        return true;
-    }
-    Real det = h00 * h11 - h01 * h01;
-    if (!exceeds<Real>(abs_value<Real>(det), 1e-20)) return false;
-    // -H^{-1} grad / 2 with one division
-    const Real m = (Real)-0.5 / det;
-    p0 = (h11 * q[3] - h01 * q[4]) * m;
-    p1 = (-h01 * q[3] + h00 * q[4]) * m;
-    return true;
-}
-
 template <typename Real, int LEVEL>
 __device__ __forceinline__ void gs_tiny_body(const LevelPtrs<Real> &L, int iters, unsigned int *err, int separate, int *kexp)
 {

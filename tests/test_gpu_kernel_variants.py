@@ -1,0 +1,55 @@
+"""A kernel variant that must not change any bit: the two-block cluster kernel of level 1 against
+the one-block kernel (EPR_TINY_LEVELS=1 / 3), in double-float and double, through whole solves
+(direct launches and the graph replay).  The variant is chosen when the library creates its first
+context, so each run is its own process."""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+SCRIPT = r"""
+import json, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import exteriorpoissonrecon_gb300 as epr
+pos, fr = epr.samples.make_workload("link", 30000, seed=4)
+pu, _ = epr.unit_cube(pos)
+sk = epr.pack_skew(fr)
+out = {}
+for name, kw in (("df", dict(precision="fp32", fp64_from=0, fp64_levels=4, band_precision="df")),
+                 ("fp64", dict())):
+    r = epr.Reconstructor(3, 5, pu, sk, **kw)
+    r.solve()
+    r.solve()  # the graph replay
+    xs, ys = r.solution()
+    out[name] = [np.concatenate(xs).tolist(), np.concatenate(ys).tolist()]
+    r.close()
+print(json.dumps(out))
+"""
+
+
+def _run(env):
+    e = dict(os.environ)
+    e.update(env)
+    r = subprocess.run([sys.executable, "-c", SCRIPT, ROOT], capture_output=True, text=True, env=e, timeout=600)
+    assert r.returncode == 0, r.stderr
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+@pytest.mark.parametrize("env", [{"EPR_TINY_LEVELS": "3"}])
+def test_launch_variants_give_the_same_bits(env):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    base = _run({})
+    other = _run(env)
+    for name in ("df", "fp64"):
+        for a, b in zip(base[name], other[name]):
+            assert np.array_equal(np.array(a), np.array(b)), (env, name)
