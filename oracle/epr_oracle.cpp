@@ -358,6 +358,13 @@ struct Oracle
     std::vector<int> leafDepth;
     double c = 0;
     std::vector<LevelSystem> levels;
+    // adaptive indexer (empty for the regular grid): per level the node status (0 none, 1 indexed,
+    // 2 active), the node of every function index, the element of every element index
+    std::vector<std::vector<uint8_t>> status;
+    std::vector<std::vector<int64_t>> fnodes, enodes;
+    std::vector<int64_t> nActive;
+    std::vector<uint8_t> elemIndexed;  // finest level
+    bool adaptive() const { return !status.empty(); }
 
     Oracle(int depth_, const epr_oracle_params &p) : depth(depth_), P(p) { levels.resize(depth + 1); }
 
@@ -716,9 +723,11 @@ struct Oracle
             if (P.project) ProjectBlade<D>(acc);
             for (int k = 0; k < T::K; k++) S[e * T::K + k] = acc[k];
         }
+        // c: the elements of the indexer (SystemEnergy.h:452-461), divided by all r^Dim
         double cc = 0;
         for (size_t e = 0; e < NE; e++)
         {
+            if (!elemIndexed.empty() && !elemIndexed[e]) continue;
             double s2 = 0;
             for (int k = 0; k < T::K; k++) s2 += 2 * S[e * T::K + k] * S[e * T::K + k];
             cc += s2;
@@ -825,7 +834,10 @@ struct Oracle
                 while (true)
                 {
                     const double *s = &S[g.elem(E) * T::K];
-                    for (int a = 0; a < D; a++)
+                    // the adaptive indexer's stiffness integrates its own elements only
+                    // (Hat.scalars.inl:1634-1643: elements without an index contribute nothing)
+                    const bool counted = elemIndexed.empty() || elemIndexed[g.elem(E)];
+                    for (int a = 0; counted && a < D; a++)
                         for (int b = 0; b < D; b++)
                         {
                             if (a == b) continue;
@@ -950,9 +962,106 @@ struct Oracle
         return Mc;
     }
 
+    // -------------------------------------------------------------------------------------------
+    // HierarchicalAdaptedIndexer (Hat.adaptive.inl:342-732) on the dense grids.
+    // Active functions of level d (_addSamples, :565-643): every interior node I (0 <= I <= 2^d) in
+    // the window A - K .. A + K + 1 of the level-d ancestor A = E >> (depth - d) of a sample cell E
+    // (K = aRadius; the window is the (K, K+1) element-function neighbour key of the cell's tree node
+    // at every depth).  Their indices follow the tree's depth-first order, i.e. Morton order with
+    // axis 0 in the lowest bit of every level (child c of a tree node has offset 2 O + bit d of c).
+    // _finalize (:646-728): for the active functions of each level in index order and their 3^Dim
+    // neighbours in window order (axis 0 slowest), a neighbour that is an interior node without an
+    // index gets the next function index (an indexed but inactive function), and a neighbour that
+    // is an interior element (0 <= E < 2^d) on the lower side of the function (E <= I on every
+    // axis) without an index gets the next element index.
+    // -------------------------------------------------------------------------------------------
+    void buildAdaptive()
+    {
+        const int K = P.adaptive_radius;
+        status.assign(depth + 1, {});
+        fnodes.assign(depth + 1, {});
+        enodes.assign(depth + 1, {});
+        nActive.assign(depth + 1, 0);
+        for (int d = 0; d <= depth; d++)
+        {
+            const int r = 1 << d;
+            GridIdx<D> g(r);
+            std::vector<uint8_t> &st = status[d];
+            st.assign(g.nodes(), 0);
+            for (size_t ci = 0; ci < cells.size(); ci++)
+            {
+                int lo[D], hi[D];
+                for (int k = 0; k < D; k++)
+                {
+                    const int A = cells[ci][k] >> (depth - d);
+                    lo[k] = std::max(A - K, 0);
+                    hi[k] = std::min(A + K + 1, r);
+                }
+                int I[D];
+                for (int k = 0; k < D; k++) I[k] = lo[k];
+                while (true)
+                {
+                    st[g.node(I)] = 2;
+                    int k = D - 1;
+                    for (; k >= 0; k--) { if (++I[k] <= hi[k]) break; I[k] = lo[k]; }
+                    if (k < 0) break;
+                }
+            }
+            // active functions in Morton order
+            std::vector<std::pair<uint64_t, int64_t>> act;
+            for (size_t i = 0; i < st.size(); i++)
+                if (st[i] == 2)
+                {
+                    int I[D];
+                    g.node(i, I);
+                    uint64_t key = 0;
+                    for (int b = d; b >= 0; b--)
+                    {
+                        uint64_t c = 0;
+                        for (int k = 0; k < D; k++) c |= (uint64_t)((I[k] >> b) & 1) << k;
+                        key = (key << D) | c;
+                    }
+                    act.push_back({key, (int64_t)i});
+                }
+            std::sort(act.begin(), act.end());
+            nActive[d] = (int64_t)act.size();
+            for (auto &a : act) fnodes[d].push_back(a.second);
+            std::vector<uint8_t> elemSeen((size_t)std::pow(r, D), 0);
+            for (size_t a = 0; a < act.size(); a++)
+            {
+                int I[D];
+                g.node((size_t)act[a].second, I);
+                for (int w = 0; w < T::S; w++)
+                {
+                    int off[D], Nn[D];
+                    StencilOffset<D>(w, off);
+                    bool fn = true, el = true;
+                    for (int k = 0; k < D; k++)
+                    {
+                        Nn[k] = I[k] + off[k];
+                        if (Nn[k] < 0 || Nn[k] > r) fn = false;
+                        if (Nn[k] < 0 || Nn[k] >= r || off[k] > 0) el = false;
+                    }
+                    if (fn)
+                    {
+                        const size_t ni = g.node(Nn);
+                        if (st[ni] == 0) { st[ni] = 1; fnodes[d].push_back((int64_t)ni); }
+                    }
+                    if (el)
+                    {
+                        const size_t ei = g.elem(Nn);
+                        if (!elemSeen[ei]) { elemSeen[ei] = 1; enodes[d].push_back((int64_t)ei); }
+                    }
+                }
+            }
+            if (d == depth) elemIndexed = elemSeen;
+        }
+    }
+
     void build()
     {
         orderSamples();
+        if (P.adaptive_radius >= 0) buildAdaptive();
         buildDensity();
         buildSkew();
         buildS();
@@ -1181,6 +1290,8 @@ struct Oracle
             g.node(i, I);
             int m = 0;
             for (int d = 0; d < D; d++) if (I[d] & 1) m |= 1 << d;
+            // the colour lists hold the active functions only (ExteriorPoisson.h:161-169)
+            if (adaptive() && status[level][i] != 2) continue;
             colours[m].push_back(i);
         }
         for (int it = 0; it < iters; it++)
@@ -1247,7 +1358,9 @@ struct Oracle
                 for (; d >= 0; d--) { if (++sel[d] < nopt[d]) break; sel[d] = 0; }
                 if (d < 0) break;
             }
-            xf[i] = s;
+            // the adaptive prolongation reaches the indexed fine functions only (ffChildNeighbors,
+            // Hat.scalars.inl:1747-1779)
+            xf[i] = adaptive() && status[level + 1][i] == 0 ? 0. : s;
         }
     }
 
@@ -1725,6 +1838,18 @@ struct Oracle
         return double(v) / RAND_MAX_SQUARED;
     }
 
+    // the unscaled random start: two draws per function in function-index order
+    // (ExteriorPoisson.h:333-334), the adaptive indexer's order when there is one
+    void randomStart(int l, std::vector<double> &X, std::vector<double> &Y) const
+    {
+        if (!adaptive())
+        {
+            for (size_t i = 0; i < X.size(); i++) { X[i] = RandomDouble(); Y[i] = RandomDouble(); }
+            return;
+        }
+        for (int64_t node : fnodes[l]) { X[(size_t)node] = RandomDouble(); Y[(size_t)node] = RandomDouble(); }
+    }
+
     // cascadic solve (ExteriorPoisson.h:315-409)
     void solve(double *xout, double *yout, double *eout)
     {
@@ -1733,7 +1858,7 @@ struct Oracle
         std::vector<std::vector<double>> X(depth + 1), Y(depth + 1);
         for (int l = 0; l <= depth; l++) { X[l].assign(NumNodes(D, l), 0.); Y[l].assign(NumNodes(D, l), 0.); }
         srand(P.seed);
-        for (size_t i = 0; i < X[minD].size(); i++) { X[minD][i] = RandomDouble(); Y[minD][i] = RandomDouble(); }
+        randomStart(minD, X[minD], Y[minD]);
         {
             double e[3];
             energy(minD, X[minD].data(), Y[minD].data(), e);
@@ -1816,7 +1941,7 @@ struct Oracle
         for (int l = 0; l <= depth; l++) { st.X[l].assign(NumNodes(D, l), 0.); st.Y[l].assign(NumNodes(D, l), 0.); }
         srand(P.seed);
         std::vector<double> &X0 = st.X[st.minD], &Y0 = st.Y[st.minD];
-        for (size_t i = 0; i < X0.size(); i++) { X0[i] = RandomDouble(); Y0[i] = RandomDouble(); }
+        randomStart(st.minD, X0, Y0);
         double e[3];
         energy(st.minD, X0.data(), Y0.data(), e);
         double s = std::sqrt(std::sqrt(c / e[2]));
@@ -1886,6 +2011,16 @@ struct Oracle
             return put(v);
         }
         if (level < 0 || level > depth) return -1;
+        if (name == "status" || name == "fnodes" || name == "enodes" || name == "nactive")
+        {
+            if (!adaptive()) return -1;
+            if (name == "nactive") return put(std::vector<double>{(double)nActive[level]});
+            const auto &src = name == "fnodes" ? fnodes[level] : enodes[level];
+            std::vector<double> v;
+            if (name == "status") v.assign(status[level].begin(), status[level].end());
+            else v.assign(src.begin(), src.end());
+            return put(v);
+        }
         if (name == "R") return put(levels[level].R);
         if (name == "B") return put(levels[level].B);
         if (name == "A") return put(levels[level].A);
@@ -1928,6 +2063,7 @@ void epr_oracle_default_params(epr_oracle_params *p)
     p->single_level = 0;
     p->separate = 0;
     p->alt_rounds = 0;
+    p->adaptive_radius = -1;
 }
 
 int epr_oracle_unit_cube(int dim, size_t n, double scale, double *pos, double *xform)

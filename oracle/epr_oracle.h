@@ -39,6 +39,8 @@ typedef struct epr_oracle_params {
                              V-cycle of gs_iters relaxations per half-step) instead of paired GS */
     int project;          /* --project: S(E) projected onto its best blade (ExteriorPoisson.h:300-305,
                              411-438) */
+    int adaptive_radius;  /* --aRadius: -1 the regular grid; >= 0 the adaptive indexer's function and
+                             element sets (Hat.adaptive.inl:342-732) on the same grids */
 } epr_oracle_params;
 
 void epr_oracle_default_params(epr_oracle_params *p);
@@ -61,7 +63,9 @@ int epr_oracle_build(epr_oracle *o);
 int epr_oracle_set_level_system(epr_oracle *o, int level, const double *R, const double *B, double c);
 
 /* Named arrays: "cells","measure","noise","depth","S","leaf_depth","R","B","A","density","skew",
- * "exists". Returns the number of doubles written (out may be NULL to query the size). */
+ * "exists"; with the adaptive indexer also "status" (per node of a level: 0 no function, 1 an
+ * indexed function that is not relaxed, 2 an active one), "fnodes" (the node of every function
+ * index of a level), "enodes" (the element of every element index) and "nactive". Returns the number of doubles written (out may be NULL to query the size). */
 long epr_oracle_get(epr_oracle *o, const char *name, int level, double *out);
 
 size_t epr_oracle_num_nodes(int dim, int level);

@@ -33,6 +33,7 @@ class Params(ctypes.Structure):
         ("separate", ctypes.c_int),
         ("alt_rounds", ctypes.c_int),
         ("project", ctypes.c_int),
+        ("adaptive_radius", ctypes.c_int),
     ]
 
 

@@ -10,7 +10,7 @@
 //
 // usage: ref_harness <in.ply> <depth> <outdir> [--sWeight v] [--dWeight v] [--nSigma v]
 //                    [--tRadius k] [--dRadius k] [--gsIters k] [--iMult v] [--seed k] [--scale v]
-//                    [--minSolveDepth k] [--solve 0|1]
+//                    [--minSolveDepth k] [--solve 0|1] [--aRadius k]
 
 #include <cstdio>
 #include <cstdlib>
@@ -87,6 +87,7 @@ struct Params
     int solve = 1;
     int separate = 0, singleLevel = 0;
     int project = 0;  // --project: the reference's blade projection of S(E) (ExteriorPoisson.h:300-305)
+    int aRadius = -1;  // --aRadius >= 0: the adaptive indexer (ExteriorPoissonRecon.cpp:191-198)
 };
 
 template <unsigned int Dim>
@@ -110,25 +111,31 @@ static std::vector<std::pair<Point<double, Dim>, Hat::SkewSymmetricMatrix<double
 // Stencil layout used by every dump: entry o of node i holds M(i + off(o), i), where the offset
 // index o = sum_d (off[d] + 1) * 3^(Dim-1-d) enumerates {-1,0,1}^Dim with axis 0 slowest, and the
 // node index is the reference function index (axis 0 most significant, Hat.scalars.inl:476-481).
+// For the adaptive indexer the matrix rows and columns are the indexer's function indices; `offsets`
+// maps each to its grid offset, and the stencil of the grid node of that offset is written.
 template <unsigned int Dim>
-static std::vector<double> ColumnStencil(const Eigen::SparseMatrix<double> &M, unsigned int res)
+static std::vector<double> ColumnStencil(const Eigen::SparseMatrix<double> &M, unsigned int res,
+                                         const std::vector<Hat::Index<Dim>> *offsets = nullptr)
 {
     const unsigned int S = (unsigned int)std::pow(3, Dim);
     size_t N = (size_t)std::pow(res + 1, Dim);
     std::vector<double> out(N * S, 0.);
+    auto offsetOf = [&](size_t f) { return offsets ? (*offsets)[f] : Hat::ScalarFunctions<Dim>::FunctionIndex(f, res); };
     for (int col = 0; col < M.outerSize(); col++)
         for (Eigen::SparseMatrix<double>::InnerIterator it(M, col); it; ++it)
         {
-            Hat::Index<Dim> I = Hat::ScalarFunctions<Dim>::FunctionIndex((size_t)col, res);
-            Hat::Index<Dim> J = Hat::ScalarFunctions<Dim>::FunctionIndex((size_t)it.row(), res);
+            Hat::Index<Dim> I = offsetOf((size_t)col);
+            Hat::Index<Dim> J = offsetOf((size_t)it.row());
             unsigned int o = 0;
+            size_t node = 0;
             for (unsigned int d = 0; d < Dim; d++)
             {
                 int off = J[d] - I[d];
                 if (off < -1 || off > 1) { fprintf(stderr, "stencil entry out of window\n"); exit(1); }
                 o = o * 3 + (unsigned int)(off + 1);
+                node = node * (res + 1) + (size_t)I[d];
             }
-            out[(size_t)col * S + o] += it.value();
+            out[node * S + o] += it.value();
         }
     return out;
 }
@@ -459,6 +466,156 @@ static void Run(const std::string &in, unsigned int depth, const std::string &ou
     }
 }
 
+// The adaptive indexer (HierarchicalAdaptedIndexer, Hat.adaptive.inl:342-732) through the same
+// reconstructor.  Every level's function and element tables are dumped as grid indices in the
+// indexer's own order ("afn_d<l>": node of each function index, active ones first, "aact_d<l>" their
+// number; "ael_d<l>": element of each element index), and every per-function quantity densely on the
+// level's grid (zero where no function is indexed), so that the dense restatement compares directly.
+template <unsigned int Dim>
+static void RunAdapted(const std::string &in, unsigned int depth, const std::string &outDir, const Params &P)
+{
+    using HIndexer = Hat::HierarchicalAdaptedIndexer<Dim>;
+    using Energy = SingleCycleCascadicSystemEnergy<Dim, typename HIndexer::Indexer>;
+    auto path = [&](const std::string &s) { return outDir + "/" + s + ".npy"; };
+    const unsigned int K = Dim * (Dim - 1) / 2;
+
+    auto hermite = ReadSamples<Dim>(in);
+    size_t n = hermite.size();
+    {
+        std::vector<double> pos(n * Dim), skew(n * K);
+        for (size_t i = 0; i < n; i++)
+        {
+            for (unsigned int d = 0; d < Dim; d++) pos[i * Dim + d] = hermite[i].first[d];
+            for (unsigned int k = 0; k < K; k++) skew[i * K + k] = hermite[i].second[k];
+        }
+        SaveF64(path("world_pos"), pos, {n, Dim});
+        SaveF64(path("skew"), skew, {n, K});
+    }
+    ::SquareMatrix<double, Dim + 1> w2u = ExteriorPoisson::ToUnitCube<Dim>([&](size_t i) { return hermite[i].first; }, n, P.scale);
+    for (size_t i = 0; i < n; i++) hermite[i].first = w2u(hermite[i].first);
+    {
+        std::vector<double> pos(n * Dim);
+        for (size_t i = 0; i < n; i++) for (unsigned int d = 0; d < Dim; d++) pos[i * Dim + d] = hermite[i].first[d];
+        SaveF64(path("pos"), pos, {n, Dim});
+    }
+
+    // ExteriorPoissonRecon.cpp:191-198, 205-245
+    HIndexer hIndexer(n, [&](size_t i) { return hermite[i].first; }, (unsigned int)P.aRadius, depth);
+    OrderedSampler<Dim> orderedSampler([&](size_t i) { return hermite[i].first; }, n, 1 << depth);
+    GridSamples::TreeEstimator<Dim, 2> estimator(P.dRadius, depth, [&](size_t i) { return hermite[i].first; }, orderedSampler, true);
+    srand(P.seed);
+    const double nSigma = P.nSigma;
+    auto NoiseToWeight = [nSigma](double x) { return exp(-x * x / (2. * nSigma * nSigma)); };
+    ExteriorPoisson::Reconstructor<Dim, Energy> recon(hIndexer, depth, P.minSolveDepth, depth,
+        [&](size_t i) { return hermite[i]; }, orderedSampler, estimator, NoiseToWeight, P.dWeight, P.sWeight, P.tRadius, 0u, 1e-10, false);
+    SaveF64(path("c"), std::vector<double>{recon._energies.back()._c}, {1});
+
+    std::vector<std::vector<Hat::Index<Dim>>> offsets(depth + 1);
+    std::vector<std::vector<int64_t>> nodeOf(depth + 1);
+    for (unsigned int d = 0; d <= depth; d++)
+    {
+        auto indexer = hIndexer[d];
+        const size_t r1 = ((size_t)1 << d) + 1;
+        const std::string L = "_d" + std::to_string(d);
+        std::vector<int64_t> fn(indexer.numFunctions()), el(indexer.numElements());
+        offsets[d].resize(indexer.numFunctions());
+        for (size_t f = 0; f < indexer.numFunctions(); f++)
+        {
+            Hat::Index<Dim> I = indexer.functionIndex(f);
+            offsets[d][f] = I;
+            int64_t node = 0;
+            for (unsigned int k = 0; k < Dim; k++) node = node * (int64_t)r1 + I[k];
+            fn[f] = node;
+        }
+        for (size_t e = 0; e < indexer.numElements(); e++)
+        {
+            Hat::Index<Dim> E = indexer.elementIndex(e);
+            int64_t node = 0;
+            for (unsigned int k = 0; k < Dim; k++) node = node * (int64_t)(r1 - 1) + E[k];
+            el[e] = node;
+        }
+        nodeOf[d] = fn;
+        SaveI64(path("afn" + L), fn, {fn.size()});
+        SaveI64(path("ael" + L), el, {el.size()});
+        SaveI64(path("aact" + L), std::vector<int64_t>{(int64_t)indexer.numActiveFunctions()}, {1});
+    }
+    auto dense = [&](unsigned int d, const Eigen::VectorXd &v) {
+        const size_t N = (size_t)std::pow(((size_t)1 << d) + 1, Dim);
+        std::vector<double> out(N, 0.);
+        for (size_t f = 0; f < (size_t)v.size(); f++) out[(size_t)nodeOf[d][f]] = v[f];
+        return out;
+    };
+
+    std::mt19937_64 rng(12345);
+    std::uniform_real_distribution<double> U(-1., 1.);
+    for (unsigned int d = 0; d <= depth; d++)
+    {
+        const Energy &E = recon._energies[d];
+        const unsigned int res = 1u << d;
+        const size_t N = (size_t)std::pow(res + 1, Dim), S = (size_t)std::pow(3, Dim), F = offsets[d].size();
+        const std::string L = "_d" + std::to_string(d);
+        SaveF64(path("R" + L), ColumnStencil<Dim>(E._R, res, &offsets[d]), {N, S});
+        SaveF64(path("B" + L), ColumnStencil<Dim>(E._B, res, &offsets[d]), {N, S});
+        Eigen::VectorXd x(F), y(F);
+        for (size_t i = 0; i < F; i++) x[i] = U(rng), y[i] = U(rng);
+        SaveF64(path("xr" + L), dense(d, x), {N});
+        SaveF64(path("yr" + L), dense(d, y), {N});
+        std::pair<double, double> e = E.energies(x, y);
+        SaveF64(path("energies" + L), std::vector<double>{e.first, e.second, E.wedgeSquareNorm(x, y)}, {3});
+        const size_t A = hIndexer[d].numActiveFunctions();
+        std::vector<double> q(A * 5);
+        for (size_t i = 0; i < A; i++)
+        {
+            Polynomial::Polynomial2D<2> Q = E.quadraticFit(x, y, (unsigned int)i, false, 0);
+            q[i * 5 + 0] = Q.coefficient(2, 0);
+            q[i * 5 + 1] = Q.coefficient(0, 2);
+            q[i * 5 + 2] = Q.coefficient(1, 1);
+            q[i * 5 + 3] = Q.coefficient(1, 0);
+            q[i * 5 + 4] = Q.coefficient(0, 1);
+        }
+        SaveF64(path("quadfit" + L), q, {A, 5});
+        Eigen::VectorXd gx = x, gy = y;
+        ExteriorPoissonSolvers::PairedGaussSeidelSolve<Dim>(d, recon._mcIndices[d], E, gx, gy, 1, false);
+        SaveF64(path("gsx" + L), dense(d, gx), {N});
+        SaveF64(path("gsy" + L), dense(d, gy), {N});
+        if (d < depth)
+        {
+            Eigen::VectorXd px = E.prolongation(x);
+            std::vector<double> pd = dense(d + 1, px);
+            SaveF64(path("prolong" + L), pd, {pd.size()});
+        }
+    }
+
+    if (P.solve)
+    {
+        std::streambuf *old = std::cout.rdbuf();
+        std::stringstream sink;
+        std::cout.rdbuf(sink.rdbuf());
+        for (unsigned int d = 0; d < P.minSolveDepth && d <= depth; d++) { recon._x[d].setZero(); recon._y[d].setZero(); }
+        recon.solve(P.singleLevel != 0, P.iMult, P.gsIters, P.separate != 0, false);
+        std::cout.rdbuf(old);
+        for (unsigned int d = 0; d <= depth; d++)
+        {
+            const std::string L = "_d" + std::to_string(d);
+            std::vector<double> sx = dense(d, recon._x[d]), sy = dense(d, recon._y[d]);
+            SaveF64(path("solx" + L), sx, {sx.size()});
+            SaveF64(path("soly" + L), sy, {sy.size()});
+        }
+        Eigen::VectorXd X = recon._x[0], Y = recon._y[0];
+        for (unsigned int d = 1; d <= depth; d++)
+        {
+            X = recon._energies[d - 1].prolongation(X) + recon._x[d];
+            Y = recon._energies[d - 1].prolongation(Y) + recon._y[d];
+        }
+        std::pair<double, double> e = recon._energies[depth].energies(X, Y);
+        SaveF64(path("sol_energies"), std::vector<double>{e.first, e.second}, {2});
+        std::vector<double> sX = dense(depth, X), sY = dense(depth, Y);
+        SaveF64(path("solX"), sX, {sX.size()});
+        SaveF64(path("solY"), sY, {sY.size()});
+    }
+    SaveI64(path("indexer_hash"), std::vector<int64_t>{(int64_t)typeid(HIndexer).hash_code()}, {1});
+}
+
 int main(int argc, char **argv)
 {
     if (argc < 4)
@@ -488,13 +645,20 @@ int main(int argc, char **argv)
         else if (k == "--separate") P.separate = (int)v;
         else if (k == "--singleLevel") P.singleLevel = (int)v;
         else if (k == "--project") P.project = (int)v;
+        else if (k == "--aRadius") P.aRadius = (int)v;
         else { fprintf(stderr, "unknown flag %s\n", k.c_str()); return 2; }
     }
     mkdir(out.c_str(), 0755);
     VertexFactory::PositionFactory<double, 4> pf4;
     int ft;
     std::vector<GregTurk::PlyProperty> props = PLY::ReadVertexHeader(in, ft);
-    if (pf4.plyValidReadProperties(props)) Run<4>(in, depth, out, P);
+    const bool four = pf4.plyValidReadProperties(props);
+    if (P.aRadius >= 0)
+    {
+        if (four) RunAdapted<4>(in, depth, out, P);
+        else RunAdapted<3>(in, depth, out, P);
+    }
+    else if (four) Run<4>(in, depth, out, P);
     else Run<3>(in, depth, out, P);
     return 0;
 }

@@ -27,6 +27,10 @@ def load_golden(name):
 
 
 VARIANT_CASES = ["knot3_d4_separate", "knot3_d4_single", "knot3_d4_seed7_min2"]
+# the adaptive indexer (--aRadius K): fixtures of its tables, system, probes and solve; and the
+# reference command line's own adaptive .tree files
+ADAPTIVE_CASES = ["knot3_d5_a1", "link3_d5_a0", "link3_d5_a3", "cliff4_d3_a1"]
+ADAPTIVE_TREES = {"link3_d5_a3_tree": 3, "cliff4_d3_a1_tree": 1}
 
 
 def variant_params(flags):

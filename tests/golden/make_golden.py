@@ -53,6 +53,45 @@ VARIANTS = [
     ("cliff4_d3_project", "clifford", 4000, 5, 3, ["--project", "1"]),
 ]
 
+# the adaptive indexer (--aRadius K >= 0, the reference command line's default is 3): name, workload,
+# sample count, seed, depth, K, levels whose stencils are stored
+ADAPTIVE = [
+    ("knot3_d5_a1", "knot", 4096, 0, 5, 1, [3, 5]),
+    ("link3_d5_a0", "link", 6000, 3, 5, 0, [2, 5]),
+    ("link3_d5_a3", "link", 6000, 3, 5, 3, []),
+    ("cliff4_d3_a1", "clifford", 4000, 5, 3, 1, [3]),
+]
+
+
+def make_adaptive(name, workload, n, seed, depth, K, stencil_levels):
+    """The adaptive indexer's tables (function and element order, active count per level), the
+    system of selected levels, energies / one sweep / prolongation for seeded coefficients on the
+    indexed functions, and the cascadic solve, all written densely on each level's grid."""
+    pos, frames = samples.make_workload(workload, n, seed=seed)
+    with tempfile.TemporaryDirectory() as td:
+        ply = os.path.join(td, "in.ply")
+        samples.write_ply(ply, pos, frames)
+        out = os.path.join(td, "dump")
+        subprocess.run([HARNESS, ply, str(depth), out, "--aRadius", str(K)], check=True)
+        L = lambda k: np.load(os.path.join(out, k + ".npy"))  # noqa: E731
+        fx = {"depth": np.array(depth), "a_radius": np.array(K), "pos": L("pos"), "skew": L("skew"), "c": L("c"),
+              "sol_energies": L("sol_energies"), "solX": L("solX"), "solY": L("solY"),
+              "indexer_hash": L("indexer_hash"), "stencil_levels": np.array(stencil_levels)}
+        for l in range(depth + 1):
+            for k in ("afn", "ael", "aact", "energies", "xr", "yr", "solx", "soly"):
+                fx[f"{k}_d{l}"] = L(f"{k}_d{l}")
+            if l < depth:
+                fx[f"prolong_d{l}"] = L(f"prolong_d{l}")
+        for l in stencil_levels:
+            fx[f"R_d{l}"] = L(f"R_d{l}")
+            fx[f"B_d{l}"] = L(f"B_d{l}")
+        for l in sorted({depth, max(depth - 2, 0)}):
+            for k in ("quadfit", "gsx", "gsy"):
+                fx[f"{k}_d{l}"] = L(f"{k}_d{l}")
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **fx)
+    print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB")
+
 
 def make_variant(name, workload, n, seed, depth, flags):
     """Solve results only (the system is the base case's)."""
@@ -201,7 +240,8 @@ def make_tree(name, workload, n, seed, depth, flags):
         ply = os.path.join(td, "in.ply")
         samples.write_ply(ply, pos, frames)
         out = os.path.join(td, "out")
-        subprocess.run([REF_CLI, "--in", ply, "--out", out, "--depth", str(depth), "--aRadius", "-1"] + flags,
+        radius = [] if "--aRadius" in flags else ["--aRadius", "-1"]
+        subprocess.run([REF_CLI, "--in", ply, "--out", out, "--depth", str(depth)] + radius + flags,
                        check=True, capture_output=True)
         with open(out + ".tree", "rb") as f:
             tree = np.frombuffer(f.read(), dtype=np.uint8)
@@ -228,7 +268,10 @@ if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: make -C oracle ref")
     only = set(sys.argv[1:])  # fixture names to (re)write; all when none are given
-    TREES = [("knot3_d4_tree", "knot", 4096, 0, 4, []), ("cliff4_d3_tree", "clifford", 3000, 9, 3, ["--gsIters", "5"])]
+    TREES = [("knot3_d4_tree", "knot", 4096, 0, 4, []), ("cliff4_d3_tree", "clifford", 3000, 9, 3, ["--gsIters", "5"]),
+             # the reference command line's default indexer (--aRadius 3), and a narrow one in 4D
+             ("link3_d5_a3_tree", "link", 6000, 3, 5, ["--aRadius", "3"]),
+             ("cliff4_d3_a1_tree", "clifford", 3000, 9, 3, ["--aRadius", "1", "--gsIters", "5"])]
     # the reference's zero set of the benchmark's input (3D link, 1.1M samples, depth 8): the
     # reference run takes ~6 minutes on 8 cores
     ZERO_SETS = [("link3_d8_zero_set", "link", 1_000_000, 0, 8)]
@@ -239,6 +282,9 @@ if __name__ == "__main__":
         for v in VARIANTS:
             if v[0] in only:
                 make_variant(*v)
+        for case in ADAPTIVE:
+            if case[0] in only:
+                make_adaptive(*case)
         for case in TREES:
             if case[0] in only:
                 make_tree(*case)
@@ -254,6 +300,8 @@ if __name__ == "__main__":
         make(*case)
     for v in VARIANTS:
         make_variant(*v)
+    for case in ADAPTIVE:
+        make_adaptive(*case)
     for case in TREES:
         make_tree(*case)
     make_simplices()
