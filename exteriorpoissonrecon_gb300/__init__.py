@@ -63,6 +63,7 @@ class Params(ctypes.Structure):
         ("max_extra_sweeps", ctypes.c_int),
         ("target_energy", ctypes.c_double),
         ("project", ctypes.c_int),
+        ("adaptive_radius", ctypes.c_int),
     ]
 
 
@@ -135,7 +136,7 @@ _FLAG_NAMES = {
     "sWeight": "s_weight", "dWeight": "d_weight", "nSigma": "n_sigma", "iMult": "i_mult",
     "tRadius": "t_radius", "dRadius": "d_radius", "gsIters": "gs_iters",
     "minSolveDepth": "min_solve_depth", "maxSolveDepth": "max_solve_depth", "seed": "seed",
-    "singleLevel": "single_level", "separate": "separate", "project": "project",
+    "singleLevel": "single_level", "separate": "separate", "project": "project", "aRadius": "adaptive_radius",
 }
 
 
@@ -198,6 +199,10 @@ def load():
     L.epr_get_density.argtypes = [vp, ctypes.c_int, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
     L.epr_get_density_refined.argtypes = [vp, ctypes.c_int, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
     L.epr_write_density_tree.argtypes = [vp, P, ctypes.c_char_p]
+    L.epr_write_tree.argtypes = [vp, P, ctypes.c_char_p]
+    L.epr_get_regular_coefficients.argtypes = [vp, P, P]
+    I64 = ctypes.POINTER(ctypes.c_int64)
+    L.epr_get_adaptive_index.argtypes = [vp, ctypes.c_int, I64, I64, ctypes.c_size_t, I64, ctypes.c_size_t]
     L.epr_time_kernel.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P]
     L.epr_energy_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp,
                                      ctypes.c_double, vp, vp]
@@ -383,6 +388,34 @@ class Reconstructor:
         if xf.size != (self.dim + 1) ** 2:
             raise ValueError("voxel_to_world must hold (dim+1)^2 values")
         self._check(load().epr_write_density_tree(self._h, _p(xf), os.fsencode(path)))
+
+    def write_tree(self, path: str, voxel_to_world: np.ndarray):
+        """The reference's <out>.tree (ExteriorPoissonRecon.cpp:259-270) for the last solve, with the
+        context's indexer (regular grid or adaptive); voxel_to_world as for write_density_tree."""
+        xf = np.ascontiguousarray(voxel_to_world, dtype=np.float64).ravel()
+        if xf.size != (self.dim + 1) ** 2:
+            raise ValueError("voxel_to_world must hold (dim+1)^2 values")
+        self._check(load().epr_write_tree(self._h, _p(xf), os.fsencode(path)))
+
+    def regular_coefficients(self):
+        """The finest level's coefficients as the reference's regularCoefficients computes them from
+        the solve's hierarchical levels (Hat.adaptive.inl:154-176)."""
+        n = self.nodes(self.depth)
+        x, y = np.zeros(n), np.zeros(n)
+        self._check(load().epr_get_regular_coefficients(self._h, _p(x), _p(y)))
+        return x, y
+
+    def adaptive_index(self, level: int) -> dict:
+        """The adaptive indexer's tables of a level: `fnodes` (grid node of every function index,
+        the `active` first ones relaxed) and `enodes` (grid element of every element index)."""
+        I64 = ctypes.POINTER(ctypes.c_int64)
+        counts = np.zeros(3, np.int64)
+        self._check(load().epr_get_adaptive_index(self._h, level, counts.ctypes.data_as(I64), None, 0, None, 0))
+        fn = np.zeros(max(int(counts[0]), 1), np.int64)
+        en = np.zeros(max(int(counts[2]), 1), np.int64)
+        self._check(load().epr_get_adaptive_index(self._h, level, counts.ctypes.data_as(I64), fn.ctypes.data_as(I64), fn.size,
+                                                  en.ctypes.data_as(I64), en.size))
+        return {"fnodes": fn[:counts[0]], "active": int(counts[1]), "enodes": en[:counts[2]]}
 
     # ---------------------------------------------------------------- per-level operators
     def set_coefficients(self, level, x, y):

@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libepr_cuda.so")
-SOURCES = ["epr_capi.cu", "epr_solve.cu", "epr_setup.cu", "epr_mg.cu", "epr_noalloc.cu", "epr_sampler.cu", "epr_unet.cu", "epr_density_tree.cu", "epr_batch.cu"]
+SOURCES = ["epr_capi.cu", "epr_solve.cu", "epr_setup.cu", "epr_mg.cu", "epr_noalloc.cu", "epr_sampler.cu", "epr_unet.cu", "epr_density_tree.cu", "epr_batch.cu", "epr_adaptive.cu", "epr_tree.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unused-function"]

@@ -124,9 +124,10 @@ bool make_plan(epr_batch &b)
         const std::string who = "context " + std::to_string(i) + ": ";
         if (!c->have_system) return b.fail(who + "not built");
         if (c->dim != 3) return b.fail(who + "lockstep batches are 3D");
-        if (c->P.solver != EPR_SOLVER_CASCADIC || c->P.single_level || c->P.verbose || c->P.warm_start || c->P.target_energy > 0)
-            return b.fail(who + "lockstep batches run the plain cascadic schedule (no multigrid, single level, verbose, "
-                                "warm start or target energy)");
+        if (c->P.solver != EPR_SOLVER_CASCADIC || c->P.single_level || c->P.verbose || c->P.warm_start || c->P.target_energy > 0 ||
+            c->P.adaptive_radius >= 0)
+            return b.fail(who + "lockstep batches run the plain cascadic schedule on the regular grid (no multigrid, single "
+                                "level, verbose, warm start, target energy or adaptive indexer)");
         const int m = std::min(c->P.min_solve_depth, c->depth);
         if (minD >= 0 && m != minD) return b.fail(who + "all members need the same minimum solve depth");
         minD = m;

@@ -204,6 +204,7 @@ Context::~Context()
         }
         release(red.partial); release(red.out); release(d_err); release(d_fit); release(d_kexp);
         setup.release(*this);
+        release_adaptive();
         release_mg(*this);
         if (solve_graph) cudaGraphExecDestroy(solve_graph);
         cudaStreamSynchronize(stream);
@@ -286,7 +287,7 @@ bool Context::prolong_add(int l)
         constexpr int D = decltype(dd)::value;
         if (c32 && f32)
         {
-            launch_prolong<D, float>(l, levels[l].xy32, levels[l + 1].xy32, 1, stream);
+            launch_prolong<D, float>(l, levels[l].xy32, levels[l + 1].xy32, 1, stream, status_of(l + 1));
             return 0;
         }
         // otherwise in double: refresh the double copies of a float or double-float coarse level
@@ -295,7 +296,7 @@ bool Context::prolong_add(int l)
         if (cdf) { ok = ok && pull_xy(l); launches++; }
         if (f32) { launch_convert_f2d(levels[l + 1].xy32, levels[l + 1].xy64, 2 * levels[l + 1].N, stream); launches++; }
         if (fdf) { ok = ok && pull_xy(l + 1); launches++; }
-        launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 1, stream);
+        launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 1, stream, status_of(l + 1));
         if (f32) { launch_convert_d2f(levels[l + 1].xy64, levels[l + 1].xy32, 2 * levels[l + 1].N, stream); launches++; }
         if (fdf) { ok = ok && push_xy(l + 1); launches++; }
         return 0;
@@ -341,8 +342,19 @@ bool Context::random_start(int level, double *energy_out)
 {
     CRandom rng((unsigned int)P.seed);
     const int64_t N = levels[level].N;
-    std::vector<double> x(N), y(N);
-    for (int64_t i = 0; i < N; i++) { x[i] = rng.next_double(); y[i] = rng.next_double(); }
+    std::vector<double> x(N, 0.), y(N, 0.);
+    if (adapt.empty())
+        for (int64_t i = 0; i < N; i++) { x[i] = rng.next_double(); y[i] = rng.next_double(); }
+    else
+    {
+        // the adaptive indexer's functions in its index order; the grid's other nodes hold none
+        const AdaptiveLevel &A = adapt[level];
+        std::vector<int64_t> order(A.nF);
+        if (A.nF && (!cuda_ok(cudaMemcpyAsync(order.data(), A.fnodes, sizeof(int64_t) * A.nF, cudaMemcpyDeviceToHost, stream), "copy") ||
+                     !cuda_ok(cudaStreamSynchronize(stream), "sync")))
+            return false;
+        for (int64_t f = 0; f < A.nF; f++) { x[order[f]] = rng.next_double(); y[order[f]] = rng.next_double(); }
+    }
     if (!upload_xy(level, x.data(), y.data())) return false;
     double e[3];
     if (!energy(level, e)) return false;
@@ -465,7 +477,7 @@ bool Context::solve_cascadic()
         {
             with_dim(this, [&](auto dd) {
                 constexpr int D = decltype(dd)::value;
-                launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 0, stream);
+                launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 0, stream, status_of(l + 1));
                 return 0;
             });
             launches++;
@@ -543,7 +555,7 @@ bool Context::solve_epilogue()
     {
         with_dim(this, [&](auto dd) {
             constexpr int D = decltype(dd)::value;
-            launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 0, stream);
+            launch_prolong<D, double>(l, levels[l].xy64, levels[l + 1].xy64, 0, stream, status_of(l + 1));
             return 0;
         });
     }
@@ -559,7 +571,7 @@ bool Context::solve_epilogue()
         if (!alloc((void **)&scratch, sizeof(double) * 2 * levels[l].N, "alloc scratch")) return false;
         with_dim(this, [&](auto dd) {
             constexpr int D = decltype(dd)::value;
-            launch_prolong<D, double>(l - 1, levels[l - 1].xy64, scratch, 0, stream);
+            launch_prolong<D, double>(l - 1, levels[l - 1].xy64, scratch, 0, stream, status_of(l));
             return 0;
         });
         launch_axpy<double>(levels[l].tmp64, scratch, 2 * levels[l].N, -1.0, stream);
@@ -608,6 +620,7 @@ void epr_default_params(epr_params *p)
     p->max_extra_sweeps = 0;
     p->target_energy = 0;
     p->project = 0;
+    p->adaptive_radius = -1;
 }
 
 const char *epr_global_error(void) { return g_error.c_str(); }
@@ -628,6 +641,13 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
     if (p.solver == EPR_SOLVER_MULTIGRID && (p.max_cycles < 0 || !(p.tolerance >= 0))) { g_error = "bad multigrid cycle cap or tolerance"; return nullptr; }
     if (p.max_extra_sweeps < 0 || !(p.target_energy >= 0)) { g_error = "bad target energy or extra-sweep cap"; return nullptr; }
     if (p.warm_start && p.single_level) { g_error = "a warm start and --singleLevel cannot be combined"; return nullptr; }
+    // the reference instantiates the adaptive indexer for kernel radii 0..5 (Hat.adaptive.inl:361-371)
+    if (p.adaptive_radius < -1 || p.adaptive_radius > 5) { g_error = "adaptive radius must be -1 (regular grid) or in [0,5]"; return nullptr; }
+    if (p.adaptive_radius >= 0 && p.solver != EPR_SOLVER_CASCADIC)
+    {
+        g_error = "the adaptive indexer is solved by the cascadic schedule only";
+        return nullptr;
+    }
     if (cudaSetDevice(p.device) != cudaSuccess)
     {
         g_error = std::string("cannot select CUDA device: ") + cudaGetErrorString(cudaGetLastError());
@@ -1043,7 +1063,7 @@ int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, doubl
                 if (k == "gs") epr::launch_gs_colour<D, float>(P, 0, ctx->d_err, ctx->stream);
                 else if (k == "energy") epr::launch_energy<D, float>(P, L.xy32, ctx->red, ctx->stream);
                 else if (k == "quadfit") epr::launch_quadfit<D, float>(P, L.xy32, scratch, ctx->stream);
-                else if (k == "prolong") epr::launch_prolong<D, float>(level, L.xy32, ctx->levels[level + 1].xy32, 1, ctx->stream);
+                else if (k == "prolong") epr::launch_prolong<D, float>(level, L.xy32, ctx->levels[level + 1].xy32, 1, ctx->stream, ctx->status_of(level + 1));
                 else epr::launch_gn_matvec<D, float>(P, L.xy32, (const float *)pair, (float *)out, ctx->stream);
             }
             else
@@ -1052,7 +1072,7 @@ int epr_time_kernel(epr_ctx *ctx, const char *kernel, int level, int reps, doubl
                 if (k == "gs") epr::launch_gs_colour<D, double>(P, 0, ctx->d_err, ctx->stream);
                 else if (k == "energy") epr::launch_energy<D, double>(P, L.xy64, ctx->red, ctx->stream);
                 else if (k == "quadfit") epr::launch_quadfit<D, double>(P, L.xy64, scratch, ctx->stream);
-                else if (k == "prolong") epr::launch_prolong<D, double>(level, L.xy64, ctx->levels[level + 1].xy64, 1, ctx->stream);
+                else if (k == "prolong") epr::launch_prolong<D, double>(level, L.xy64, ctx->levels[level + 1].xy64, 1, ctx->stream, ctx->status_of(level + 1));
                 else epr::launch_gn_matvec<D, double>(P, L.xy64, (const double *)pair, (double *)out, ctx->stream);
             }
             return 0;

@@ -59,6 +59,15 @@ struct Setup
     void release(Context &c);
 };
 
+// One level of the adaptive indexer (Hat::HierarchicalAdaptedIndexer) on the level's dense grid
+struct AdaptiveLevel
+{
+    uint8_t *status = nullptr;   // per node: 0 no function, 1 indexed (held fixed), 2 active
+    int64_t *fnodes = nullptr;   // node of every function index (active ones first)
+    int64_t *enodes = nullptr;   // element of every element index
+    int64_t nF = 0, nA = 0, nE = 0;
+};
+
 struct Context
 {
     int dim = 0, depth = 0;
@@ -82,6 +91,11 @@ struct Context
     // out-of-memory would (EPR_ERR_NOMEM)
     size_t alloc_cap = 0, alloc_total = 0;
     Setup setup;
+    // the adaptive indexer's levels (empty for the regular grid), built with the system
+    std::vector<AdaptiveLevel> adapt;
+    uint8_t *elem_indexed = nullptr;  // finest level: 1 for the elements the indexer holds
+    const uint8_t *status_of(int l) const { return adapt.empty() ? nullptr : adapt[l].status; }
+    void release_adaptive();
     MGHierarchy *mg = nullptr;  // linear multigrid storage (epr_mg.cu), allocated on first use
     // the relaxation sequence of the cascadic solve captured as one CUDA graph (built on the first
     // solve, replayed by the next ones), with the host-side counts of what it launches
@@ -128,6 +142,7 @@ inline LevelPtrs<Real> level_ptrs(Context *c, int l)
     LevelPtrs<Real> p;
     p.level = l;
     p.N = L.N;
+    if (!c->adapt.empty()) p.status = c->adapt[l].status;
     if constexpr (std::is_same<Real, double>::value) { p.xy = L.xy64; p.A = L.A64; p.B = L.B64; }
     else if constexpr (std::is_same<Real, df>::value) { p.xy = L.xyd; p.A = L.Ad; p.B = L.Bd; return p; }
     else { p.xy = L.xy32; p.A = L.A32; p.B = L.B32; }
@@ -138,6 +153,13 @@ inline LevelPtrs<Real> level_ptrs(Context *c, int l)
     }
     return p;
 }
+
+// the adaptive indexer's tables of every level (epr_adaptive.cu), from the finest cell map
+bool build_adaptive(Context &c, const int *cellOfFinest);
+// has-children flags of the adaptive indexer's tree per tree depth (0 .. depth + 1)
+bool adaptive_tree_refinement(Context &c, std::vector<std::vector<uint8_t>> &refined);
+// a copy of the finest frame field with the elements outside the adaptive indexer zeroed
+bool masked_frames(Context &c, const double *S, int64_t nElements, int K, double **out);
 
 // the text epr_global_error() returns (per host thread)
 void set_global_error(const std::string &msg);

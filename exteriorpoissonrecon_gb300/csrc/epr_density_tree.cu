@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "epr_context.h"
+#include "epr_tree_walk.h"
 
 namespace epr {
 namespace {
@@ -48,12 +49,6 @@ __global__ void gather_node_data_kernel(DensityLevels L, const int8_t *lev, cons
     const int l = lev[k];
     out[e] = l < 0 ? 0.0 : L.g[l][idx[k] * W + w];
 }
-
-struct NodeKey
-{
-    int t;
-    int O[4];
-};
 
 }  // namespace
 }  // namespace epr
@@ -110,7 +105,7 @@ int epr_write_density_tree(epr_ctx *ctx, const double *voxel_to_world, const cha
             return ctx->status;
     }
     if (!ctx->cuda_ok(cudaStreamSynchronize(ctx->stream), "sync")) return ctx->status;
-    auto hasChildren = [&](const NodeKey &k) -> bool {
+    auto hasChildren = [&](const TreeNodeKey &k) -> bool {
         if (k.t == 0) return true;
         if (k.t > depth) return false;
         const int side = 1 << k.t;
@@ -119,7 +114,7 @@ int epr_write_density_tree(epr_ctx *ctx, const double *voxel_to_world, const cha
         return refined[k.t][li] != 0;
     };
     // the vertex of the estimator's level t-1 a node stands for, or -1
-    auto vertex = [&](const NodeKey &k, int &lev) -> int64_t {
+    auto vertex = [&](const TreeNodeKey &k, int &lev) -> int64_t {
         lev = -1;
         if (k.t == 0) return -1;
         const int r = 1 << (k.t - 1);
@@ -154,7 +149,7 @@ int epr_write_density_tree(epr_ctx *ctx, const double *voxel_to_world, const cha
         ctx->release(dLev); ctx->release(dIdx); ctx->release(dOut);
         return ctx->status ? ctx->status : EPR_ERR_NOMEM;
     }
-    std::vector<NodeKey> keys;
+    std::vector<TreeNodeKey> keys;
     std::vector<uint8_t> kids;
     std::vector<int8_t> lev;
     std::vector<int64_t> idx;
@@ -201,33 +196,16 @@ int epr_write_density_tree(epr_ctx *ctx, const double *voxel_to_world, const cha
         keys.clear(); kids.clear(); lev.clear(); idx.clear();
         return true;
     };
-    auto emit = [&](const NodeKey &k) {
+    ok = ok && walk_tree(D, hasChildren, [&](const TreeNodeKey &k, bool has) -> bool {
+        if ((int64_t)keys.size() >= kChunkNodes && !flush()) return false;
         int l;
         const int64_t v = vertex(k, l);
         keys.push_back(k);
-        kids.push_back(hasChildren(k) ? 1 : 0);
+        kids.push_back(has ? 1 : 0);
         lev.push_back((int8_t)l);
         idx.push_back(v);
-    };
-
-    NodeKey root{};
-    emit(root);
-    std::vector<NodeKey> stack{root};
-    while (ok && !stack.empty())
-    {
-        const NodeKey p = stack.back();
-        stack.pop_back();
-        if ((int64_t)keys.size() + (1 << D) > kChunkNodes && !(ok = flush())) break;
-        NodeKey child[16];
-        for (int c = 0; c < (1 << D); c++)
-        {
-            child[c].t = p.t + 1;
-            for (int d = 0; d < D; d++) child[c].O[d] = 2 * p.O[d] + ((c >> d) & 1);
-            emit(child[c]);
-        }
-        for (int c = (1 << D) - 1; c >= 0; c--)
-            if (hasChildren(child[c])) stack.push_back(child[c]);
-    }
+        return true;
+    });
     ok = ok && flush();
     if (ok)
     {

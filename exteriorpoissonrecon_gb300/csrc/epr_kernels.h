@@ -20,6 +20,9 @@ struct LevelPtrs
     const Real *B = nullptr;  // 3^Dim * N column stencil of the frame constraint
     const Real *Acb = nullptr;  // optional colour-blocked copies of A and B (colour_block_base)
     const Real *Bcb = nullptr;
+    // adaptive indexer: per node 0 (no function), 1 (indexed, held fixed), 2 (active); the
+    // Gauss-Seidel kernels update active nodes only.  Null for the regular grid (all active).
+    const uint8_t *status = nullptr;
 };
 
 // Scratch for deterministic two-pass reductions
@@ -70,7 +73,9 @@ template <int D, typename Real>
 void launch_gn_matvec(const LevelPtrs<Real> &L, const Real *xy, const Real *dxy, Real *out, cudaStream_t s);
 // fine (2 N_f) = P coarse (2 N_c), pairs; add != 0 accumulates
 template <int D, typename Real>
-void launch_prolong(int coarseLevel, const Real *coarse, Real *fine, int add, cudaStream_t s);
+// fineStatus (adaptive indexer): fine nodes without a function (status 0) stay zero
+void launch_prolong(int coarseLevel, const Real *coarse, Real *fine, int add, cudaStream_t s,
+                    const uint8_t *fineStatus = nullptr);
 // coarse = P^T fine, pairs
 template <int D, typename Real>
 void launch_restrict(int coarseLevel, const Real *fine, Real *coarse, cudaStream_t s);

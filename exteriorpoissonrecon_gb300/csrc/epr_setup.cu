@@ -1338,9 +1338,18 @@ bool build_impl(Context &c, Setup &st)
         G.depth = depth;
         element_frame_kernel<D><<<nblocks(gfine.NE, 128), 128, 0, s>>>(G, st.S, st.leaf, c.P.project);
     }
+    // the adaptive indexer: its tables, and the frame field restricted to its elements for c and B
+    const double *Sfit = st.S;
+    double *Smasked = nullptr;
+    if (c.P.adaptive_radius >= 0)
+    {
+        if (!build_adaptive(c, st.cellOfFinest) || !masked_frames(c, st.S, gfine.NE, K, &Smasked)) return false;
+        Sfit = Smasked;
+    }
+    else c.release_adaptive();
     double *dsum = nullptr;
     if (!dalloc(c, &dsum, 4, "sums")) return false;
-    if (!device_sum(c, st.S, gfine.NE, K, dsum)) return false;
+    if (!device_sum(c, Sfit, gfine.NE, K, dsum)) return false;
     double csum = 0;
     if (!c.cuda_ok(cudaMemcpyAsync(&csum, dsum, sizeof(double), cudaMemcpyDeviceToHost, s), "copy") ||
         !c.cuda_ok(cudaStreamSynchronize(s), "sync"))
@@ -1358,7 +1367,8 @@ bool build_impl(Context &c, Setup &st)
         screening_kernel<D><<<nblocks(Lf.N, 128), 128, 0, s>>>(st.pos, st.noise, st.order, st.cellStart, st.cellOfFinest, depth,
                                                                c.P.n_sigma, dsum + 2, Lf.A64);
     }
-    constraint_kernel<D><<<nblocks(Lf.N, 128), 128, 0, s>>>(st.S, depth, Lf.B64);
+    constraint_kernel<D><<<nblocks(Lf.N, 128), 128, 0, s>>>(Sfit, depth, Lf.B64);
+    c.release(Smasked);
     if (!c.launch_ok("finest stencils")) return false;
 
     // ---- Galerkin hierarchy of R and B, then A = R + dWeight K on every level ----

@@ -361,6 +361,14 @@ __device__ __forceinline__ bool node_step(const Real *q, int separate, Real &p0,
     return true;
 }
 
+// Whether the Gauss-Seidel step of node i is applied: every node of the regular grid, the active
+// functions of the adaptive indexer (its colour lists hold those only, ExteriorPoisson.h:161-169)
+template <typename Real>
+__device__ __forceinline__ bool relaxed(const LevelPtrs<Real> &L, int64_t i)
+{
+    return L.status == nullptr || L.status[i] == 2;
+}
+
 // Comparisons and finiteness tests in a level's own arithmetic: a double-float tests its pair
 // without converting to FP64 where the leading float decides.
 template <typename Real>
@@ -433,7 +441,7 @@ __device__ __forceinline__ void gs_update(const LevelPtrs<Real> &L, const Grid<D
     Real q[5];
     node_fit<D, Real>(L, g, nc, i, L.xy, q);
     Real p0, p1;
-    if (node_step<Real>(q, separate, p0, p1))
+    if (relaxed(L, i) && node_step<Real>(q, separate, p0, p1))
     {
         Real2<Real> v = ld2(L.xy, i);
         v.x += p0;
@@ -668,7 +676,7 @@ __device__ __forceinline__ void gs_update_lanes_at(const LevelPtrs<Real> &L, Rea
     q[3] = (Real)2 * h[3] * sc + (Real)2 * ax - (Real)2 * by;
     q[4] = (Real)2 * h[4] * sc + (Real)2 * ay + (Real)2 * bx;
     Real p0, p1;
-    if (node_step<Real>(q, separate, p0, p1))
+    if (relaxed(L, i) && node_step<Real>(q, separate, p0, p1))
     {
         Real2<Real> v = ld2(xy, i);
         v.x += p0;
@@ -774,7 +782,7 @@ __device__ __forceinline__ void gs_update_warp3(const LevelPtrs<Real> &L, Real *
     q[3] = (Real)2 * h[3] * sc + (Real)2 * ax - (Real)2 * by;
     q[4] = (Real)2 * h[4] * sc + (Real)2 * ay + (Real)2 * bx;
     Real p0, p1;
-    if (node_step<Real>(q, separate, p0, p1))
+    if (relaxed(L, i) && node_step<Real>(q, separate, p0, p1))
     {
         Real2<Real> cur = ld2(xy, i);
         cur.x += p0;
@@ -883,7 +891,7 @@ __device__ __forceinline__ void gs_update_split3(const LevelPtrs<Real> &L, Real 
         // double-float levels test and divide in pair arithmetic (no FP64 conversions, one
         // division); float and FP64 levels keep the two-division form of the other kernels
         constexpr bool pair = std::is_same<Real, df>::value;
-        if (pair ? node_step_tiny<Real>(q, separate, p0, p1) : node_step<Real>(q, separate, p0, p1))
+        if (relaxed(L, i) && (pair ? node_step_tiny<Real>(q, separate, p0, p1) : node_step<Real>(q, separate, p0, p1)))
         {
             Real2<Real> cur = ld2(xy, i);
             cur.x += p0;
@@ -1315,7 +1323,7 @@ __device__ __forceinline__ void gs_tiny_body(const LevelPtrs<Real> &L, int iters
                 q[3] = (Real)2 * h[3] * sc + (Real)2 * sv[0] - (Real)2 * sv[3];
                 q[4] = (Real)2 * h[4] * sc + (Real)2 * sv[1] + (Real)2 * sv[2];
                 Real p0, p1;
-                if (node_step_tiny<Real>(q, separate, p0, p1))
+                if (relaxed(L, i) && node_step_tiny<Real>(q, separate, p0, p1))
                 {
                     Real2<Real> cur = xy[i];
                     cur.x += p0;
@@ -1456,7 +1464,7 @@ __device__ __forceinline__ void gs_tiny0_body(const LevelPtrs<Real> &L, int iter
                 q[3] = (Real)2 * h[3] * sc + (Real)2 * sv[0] - (Real)2 * sv[3];
                 q[4] = (Real)2 * h[4] * sc + (Real)2 * sv[1] + (Real)2 * sv[2];
                 Real p0, p1;
-                if (node_step_tiny<Real>(q, separate, p0, p1))
+                if (relaxed(L, i) && node_step_tiny<Real>(q, separate, p0, p1))
                 {
                     Real2<Real> cur = xy[i];
                     cur.x += p0;
@@ -1639,7 +1647,7 @@ __device__ __forceinline__ void gs_tiny1_cluster_body(const LevelPtrs<Real> &L, 
                 q[3] = (Real)2 * h[3] * sc + (Real)2 * sv[0] - (Real)2 * sv[3];
                 q[4] = (Real)2 * h[4] * sc + (Real)2 * sv[1] + (Real)2 * sv[2];
                 Real p0, p1;
-                if (node_step_tiny<Real>(q, separate, p0, p1))
+                if (relaxed(L, i) && node_step_tiny<Real>(q, separate, p0, p1))
                 {
                     Real2<Real> cur = xy[i];
                     cur.x += p0;
@@ -1759,10 +1767,18 @@ __global__ void __launch_bounds__(kThreads) gn_matvec_kernel(LevelPtrs<Real> L, 
 }
 
 template <int D, typename Real>
-__device__ __forceinline__ void prolong_at(int coarseLevel, const Real *coarse, Real *fine, int add, int64_t i)
+__device__ __forceinline__ void prolong_at(int coarseLevel, const Real *coarse, Real *fine, int add, int64_t i,
+                                           const uint8_t *fineStatus = nullptr)
 {
     Grid<D> gc(coarseLevel), gf(coarseLevel + 1);
     if (i >= gf.N) return;
+    // the adaptive prolongation reaches indexed fine functions only (ffChildNeighbors,
+    // Hat.scalars.inl:1747-1779); the others stay zero
+    if (fineStatus && fineStatus[i] == 0)
+    {
+        if (!add) reinterpret_cast<Real2<Real> *>(fine)[i] = Real2<Real>{(Real)0, (Real)0};
+        return;
+    }
     int F[D];
     gf.node(i, F);
     Real sx = 0, sy = 0;
@@ -1789,9 +1805,9 @@ __device__ __forceinline__ void prolong_at(int coarseLevel, const Real *coarse, 
     else o[i] = Real2<Real>{sx, sy};
 }
 template <int D, typename Real>
-__global__ void prolong_kernel(int coarseLevel, const Real *coarse, Real *fine, int add)
+__global__ void prolong_kernel(int coarseLevel, const Real *coarse, Real *fine, int add, const uint8_t *fineStatus)
 {
-    prolong_at<D, Real>(coarseLevel, coarse, fine, add, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+    prolong_at<D, Real>(coarseLevel, coarse, fine, add, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, fineStatus);
 }
 // grid.y = reconstruction of a lockstep batch
 template <typename Real>
@@ -2200,10 +2216,10 @@ void launch_gn_matvec(const LevelPtrs<Real> &L, const Real *xy, const Real *dxy,
 }
 
 template <int D, typename Real>
-void launch_prolong(int coarseLevel, const Real *coarse, Real *fine, int add, cudaStream_t s)
+void launch_prolong(int coarseLevel, const Real *coarse, Real *fine, int add, cudaStream_t s, const uint8_t *fineStatus)
 {
     Grid<D> gf(coarseLevel + 1);
-    prolong_kernel<D, Real><<<blocks_for(gf.N, 256), 256, 0, s>>>(coarseLevel, coarse, fine, add);
+    prolong_kernel<D, Real><<<blocks_for(gf.N, 256), 256, 0, s>>>(coarseLevel, coarse, fine, add, fineStatus);
 }
 
 template <int D, typename Real>
@@ -2365,7 +2381,7 @@ template void launch_prolong_add_batch<double>(const XferJob *, int, int, cudaSt
     template void launch_gs_colour<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t, int); \
     template int launch_gs_sweeps<D, R>(const LevelPtrs<R> &, int, unsigned int *, cudaStream_t, int, int64_t); \
     template void launch_gn_matvec<D, R>(const LevelPtrs<R> &, const R *, const R *, R *, cudaStream_t); \
-    template void launch_prolong<D, R>(int, const R *, R *, int, cudaStream_t);                         \
+    template void launch_prolong<D, R>(int, const R *, R *, int, cudaStream_t, const uint8_t *);                         \
     template void launch_restrict<D, R>(int, const R *, R *, cudaStream_t);
 
 EPR_INSTANTIATE(3, double)

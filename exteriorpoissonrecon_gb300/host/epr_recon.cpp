@@ -1,13 +1,12 @@
-// epr_recon: drop-in replacement of the reference's ExteriorPoissonRecon command line for the
-// regular-grid path (ExteriorPoissonRecon/ExteriorPoissonRecon.cpp:52-312).  It reads the same PLY
+// epr_recon: drop-in replacement of the reference's ExteriorPoissonRecon command line
+// (ExteriorPoissonRecon/ExteriorPoissonRecon.cpp:52-312), with both of its indexers: the adaptive
+// one (--aRadius 0..5, default 3, as the reference) and the regular grid (--aRadius -1).  It reads the same PLY
 // samples (x y z [w] + skew_c_r), maps them to the unit cube, runs the build and the solve on the
 // GPU through the C ABI of include/epr.h, and writes the reference's <out>.tree (readable by the
 // reference's Extract tool) and, with --grid, the regular coefficient grids <grid>.0.grid and
 // <grid>.1.grid in the format of RegularGrid::Write (Misha/RegularGrid.inl:441-472).
 //
 // Differences from the reference (documented, deliberate):
-//   * only the regular indexer exists here, so --aRadius defaults to -1 and any other value is an
-//     error (the reference's default, 3, selects its adaptive octree indexer);
 //   * errors exit with a non-zero status (the reference prints and exits 0);
 //   * --project fits every element's blade by the power iteration from a fixed start, each element
 //     with the full iteration budget (1000 steps, 1e-10); the reference starts from random vectors
@@ -34,7 +33,7 @@ struct Args
 {
     std::string in, out, grid;
     double nSigma = 0.25, scale = 1.1, sWeight = 100., dWeight = 0.00625, iMult = 2., jitter = 0.;
-    int depth = 5, seed = 0, tRadius = 1, dRadius = 1, aRadius = -1, minSolveDepth = 0, gsIters = 10, maxSolveDepth = -1;
+    int depth = 5, seed = 0, tRadius = 1, dRadius = 1, aRadius = 3, minSolveDepth = 0, gsIters = 10, maxSolveDepth = -1;
     bool singleLevel = false, separate = false, verbose = false, project = false;
     std::string precision = "fp64", solver = "cascadic", bandPrecision = "fp64";
     int device = 0, fp64Levels = 0, fp64From = 0, maxCycles = 200;
@@ -59,7 +58,7 @@ void Usage(const char *ex)
     printf("\t[--nSigma <noise-to-weight sigma>=0.25]\n");
     printf("\t[--dRadius <density kernel radius>=1]\n");
     printf("\t[--tRadius <tensor kernel radius>=1]\n");
-    printf("\t[--aRadius <adaptive radius>=-1 (only the regular grid, -1, is supported)]\n");
+    printf("\t[--aRadius <adaptive radius>=3 (-1: the regular grid)]\n");
     printf("\t[--jitter <jitter magnitude>=0]\n");
     printf("\t[--gsIters <gs iterations>=10]\n");
     printf("\t[--seed <random seed>=0]\n");
@@ -293,9 +292,11 @@ int main(int argc, char **argv)
 {
     Args a = Parse(argc, argv);
     if (a.in.empty()) { Usage(argv[0]); return EXIT_SUCCESS; }
-    if (a.aRadius != -1) Fail("only the regular grid (--aRadius -1) is implemented; the adaptive indexer is not", 2);
+    // the reference supports adaptive radii 0..5 (Hat.adaptive.inl:361-371) and -1 for the regular grid
+    if (a.aRadius < -1 || a.aRadius > 5) Fail("Only kernel radius in the range [0,5] supported: " + std::to_string(a.aRadius), 2);
     if (a.precision != "fp32" && a.precision != "fp64") Fail("--precision must be fp64 or fp32", 2);
     if (a.solver != "cascadic" && a.solver != "multigrid") Fail("--solver must be cascadic or multigrid", 2);
+    if (a.aRadius >= 0 && a.solver != "cascadic") Fail("the adaptive indexer is solved by the cascadic schedule only", 2);
     if (a.bandPrecision != "fp64" && a.bandPrecision != "df") Fail("--bandPrecision must be fp64 or df", 2);
     if (a.depth < 1) Fail("depth must be at least 1", 2);
     std::string ext = a.in.substr(a.in.find_last_of('.') + 1);
@@ -370,6 +371,7 @@ int main(int argc, char **argv)
     p.single_level = a.singleLevel ? 1 : 0;
     p.separate = a.separate ? 1 : 0;
     p.project = a.project ? 1 : 0;
+    p.adaptive_radius = a.aRadius;
 
     epr_ctx *ctx = epr_create(D, a.depth, &p);
     if (!ctx) Fail(std::string("epr_create: ") + epr_global_error());
@@ -387,54 +389,24 @@ int main(int argc, char **argv)
 
     if (!a.out.empty())
     {
-        // <out>.tree: dim, indexer type hash, XForm, x levels, y levels, max depth
-        // (ExteriorPoissonRecon.cpp:259-270, Misha/Streams.h:91-130, Misha/EigenStreams.h:47-53)
-        FILE *fp = fopen((a.out + ".tree").c_str(), "wb");
-        if (!fp) Fail("cannot write " + a.out + ".tree");
-        Put(fp, (uint32_t)D);
-        // libstdc++ typeid(Hat::HierarchicalRegularIndexer<Dim>).hash_code(), which the reference's
-        // Extract tool uses to pick the indexer type (Extract/Extract.cpp:352-359)
-        const uint64_t hash = D == 3 ? 0x5aa89c06ecbfe5e7ull : 0xc7baa56b1ac9f6abull;
-        Put(fp, hash);
-        // the reference writes the XForm object raw: one pointer-sized word that is not matrix data
-        // (never read back as such), then the (Dim+1)^2 doubles in (column, row) order
-        Put(fp, (uint64_t)0);
-        for (int c = 0; c <= D; c++)
-            for (int r = 0; r <= D; r++) Put(fp, v2w(c, r));
-        std::vector<std::vector<double>> xs(a.depth + 1), ys(a.depth + 1);
-        for (int l = 0; l <= a.depth; l++)
-        {
-            size_t N = 1;
-            for (int d = 0; d < D; d++) N *= (size_t)((1 << l) + 1);
-            xs[l].resize(N);
-            ys[l].resize(N);
-            Check(ctx, epr_get_solution(ctx, l, xs[l].data(), ys[l].data()), "epr_get_solution");
-        }
-        for (auto *v : {&xs, &ys})
-        {
-            Put(fp, (uint64_t)v->size());
-            for (auto &lv : *v)
-            {
-                Put(fp, (int64_t)lv.size());
-                fwrite(lv.data(), sizeof(double), lv.size(), fp);
-            }
-        }
-        Put(fp, (uint32_t)a.depth);  // HierarchicalRegularIndexer::write (Hat.adaptive.inl:198-203)
-        fclose(fp);
-        // <out>.density.tree: the density estimator (ExteriorPoissonRecon.cpp:272-277)
+        // <out>.tree: dim, indexer type hash, XForm, x levels, y levels, the indexer
+        // (ExteriorPoissonRecon.cpp:259-270)
         std::vector<double> xf;
         for (int c = 0; c <= D; c++)
             for (int r = 0; r <= D; r++) xf.push_back(v2w(c, r));
+        Check(ctx, epr_write_tree(ctx, xf.data(), (a.out + ".tree").c_str()), "epr_write_tree");
+        // <out>.density.tree: the density estimator (ExteriorPoissonRecon.cpp:272-277)
         Check(ctx, epr_write_density_tree(ctx, xf.data(), (a.out + ".density.tree").c_str()), "epr_write_density_tree");
     }
     if (!a.grid.empty())
     {
-        // regular coefficients of the finest level as <grid>.0.grid / <grid>.1.grid
+        // regular coefficients of the finest level as <grid>.0.grid / <grid>.1.grid, as the
+        // reference's Extract computes them from the .tree (regularCoefficients)
         size_t N = 1;
         int res = (1 << a.depth) + 1;
         for (int d = 0; d < D; d++) N *= (size_t)res;
         std::vector<double> x(N), y(N);
-        Check(ctx, epr_get_coefficients(ctx, a.depth, x.data(), y.data()), "epr_get_coefficients");
+        Check(ctx, epr_get_regular_coefficients(ctx, x.data(), y.data()), "epr_get_regular_coefficients");
         for (int c = 0; c < 2; c++)
         {
             std::string fn = a.grid + "." + std::to_string(c) + ".grid";

@@ -52,6 +52,14 @@
  *   epr_write_density_tree
  *       the <out>.density.tree file: ExteriorPoissonRecon.cpp:272-277 with TreeEstimator::write
  *       (GridSamples.inl:734-738) and RegularTreeNode::write (Misha/RegularTree.inl:615-642)
+ *   epr_write_tree
+ *       the <out>.tree file: ExteriorPoissonRecon.cpp:259-270 with HierarchicalRegularIndexer::write
+ *       (Hat.adaptive.inl:198-203) or HierarchicalAdaptedIndexer::write (Hat.adaptive.inl:399-405)
+ *   epr_get_regular_coefficients
+ *       BaseHierarchicalIndexer::regularCoefficients        Include/Hat.adaptive.inl:154-176
+ *   epr_get_adaptive_index
+ *       HierarchicalAdaptedIndexer's tables: numFunctions / numActiveFunctions / numElements,
+ *       functionIndex / elementIndex (Hat.adaptive.h:238-328, Hat.adaptive.inl:415-450)
  *   epr_get_array
  *       read-only views of the reference's internal state (TreeEstimator::measure/noise/depth
  *       GridSamples.inl:838-862, S(E) ExteriorPoisson.h:290-307, _R/_B SystemEnergy.h:172-175)
@@ -123,6 +131,13 @@ typedef struct epr_params {
                              max_extra_sweeps were added; the energy checks are part of the timed solve (0) */
     int project;          /* --project: every element's S(E) projected onto its best blade before the
                              constraint is built (FitBlade, ExteriorPoisson.h:300-305, 411-438) (0) */
+    int adaptive_radius;  /* --aRadius: -1 the regular grid (HierarchicalRegularIndexer); 0..5 the
+                             adaptive indexer (HierarchicalAdaptedIndexer, ExteriorPoissonRecon.cpp:
+                             183-198, Hat.adaptive.inl:342-732): only the functions within that many
+                             cells of a sample's cell (at every level) are relaxed, the ones a step
+                             further are held at their prolonged values, all others are zero; the
+                             constraint and c integrate the elements it holds.  Cascadic solver
+                             only (-1) */
 } epr_params;
 
 typedef struct epr_stats {
@@ -279,6 +294,33 @@ int epr_get_density_refined(epr_ctx *ctx, int t, uint8_t *out, size_t cap, size_
  * in the reference's file are written as zero (parent) or 1 (children present).  Needs a built
  * context; EPR_ERR_ARG when the file cannot be written. */
 int epr_write_density_tree(epr_ctx *ctx, const double *voxel_to_world, const char *path);
+
+/* Writes `path` as the reference's <out>.tree after a solve (ExteriorPoissonRecon.cpp:259-270): u32
+ * dim, the u64 type hash of the context's indexer (the regular grid's or the adaptive one's, as
+ * libstdc++ computes typeid(...).hash_code(); the reference's Extract selects the indexer by it),
+ * the voxel-to-world transform as in epr_write_density_tree, every level's hierarchical x and y
+ * coefficients in the indexer's function order (u64 levels, then per level i64 n and n doubles),
+ * then the indexer: the regular grid's u32 maximum depth, or the adaptive indexer's node tree (40-byte
+ * nodes in 3D, 48-byte in 4D: u16 depth, u16 offsets, parent and children words, u64 function and
+ * element index, -1 when none), its active function counts and its function and element node
+ * lists (counts, with zero address words).  Needs a solved context; EPR_ERR_ARG when the file
+ * cannot be written. */
+int epr_write_tree(epr_ctx *ctx, const double *voxel_to_world, const char *path);
+
+/* The finest level's coefficients as the reference's regularCoefficients computes them from a
+ * .tree (Hat.adaptive.inl:154-176; Extract's zero set and --grid output use them): the sum of every
+ * level's hierarchical coefficients, each prolonged to the finest grid by the regular grid's
+ * prolongation.  For the regular grid this is epr_get_coefficients(ctx, depth) after a solve; for
+ * the adaptive indexer it also extends the solution beyond the indexed functions.  x and y hold
+ * (2^depth+1)^dim doubles.  Needs a solved context. */
+int epr_get_regular_coefficients(epr_ctx *ctx, double *x, double *y);
+
+/* The adaptive indexer's tables of one level (adaptive_radius >= 0, after epr_build):
+ * counts[0] = functions, counts[1] = active functions (the first counts[1] function indices, the
+ * only ones relaxed), counts[2] = elements; fnodes (cap >= counts[0]) receives the grid node
+ * (axis 0 most significant) of every function index, enodes (cap >= counts[2]) the grid element
+ * of every element index.  Any output may be NULL.  EPR_ERR_STATE for a regular-grid context. */
+int epr_get_adaptive_index(epr_ctx *ctx, int level, int64_t *counts, int64_t *fnodes, size_t fcap, int64_t *enodes, size_t ecap);
 
 /* Named internal arrays copied to host memory: "measure", "noise", "depth" (per sample),
  * "S" (per finest element, packed), "leaf_depth", "R", "B" (per level, column stencils), "c".

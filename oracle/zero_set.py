@@ -189,9 +189,35 @@ def curve_hausdorff(segs_a: np.ndarray, segs_b: np.ndarray, h: float) -> float:
     return max(directed_distance(segs_a, segs_b, h), directed_distance(segs_b, segs_a, h))
 
 
+def tree_levels(raw: bytes):
+    """(dim, voxel-to-world, x levels, y levels, max depth) of a `.tree` of either indexer, every
+    level dense on its (2^l+1)^dim grid (the adaptive indexer's functions scattered to their nodes,
+    zero elsewhere, as regularCoefficients's ToRegular does, Hat.adaptive.inl:159-165)."""
+    h = struct.unpack_from("<Q", raw, 4)[0]
+    try:
+        from . import adapted_tree as AT
+    except ImportError:
+        import adapted_tree as AT
+    if h not in AT.HASH.values():
+        dim, _, xf, xs, ys, md = parse_tree(raw)
+        return dim, xf, xs, ys, md
+    t = AT.parse(raw)
+    dim = t["dim"]
+    xs, ys = [], []
+    for l in range(len(t["x"])):
+        r1 = 2 ** l + 1
+        sel = (t["depth"] == l + 1) & (t["findex"] >= 0)
+        nodes = np.ravel_multi_index(t["offset"][sel].T, (r1,) * dim)
+        for src, dst in ((t["x"][l], xs), (t["y"][l], ys)):
+            v = np.zeros(r1 ** dim)
+            v[nodes] = src[t["findex"][sel]]
+            dst.append(v)
+    return dim, t["xform"].reshape(dim + 1, dim + 1), xs, ys, len(xs) - 1
+
+
 def tree_zero_set(raw: bytes, simplices: np.ndarray):
     """World-space segments of the zero set of a 3D `.tree` and the world size of a finest cell."""
-    dim, _, xf, xs, ys, md = parse_tree(raw)
+    dim, xf, xs, ys, md = tree_levels(raw)
     assert dim == 3
     X, Y = regular_finest(xs, dim), regular_finest(ys, dim)
     segs = zero_set_3d(X, Y, md, simplices)

@@ -43,8 +43,10 @@ def parse_tree(raw: bytes):
 def test_usage_and_argument_errors(cli):
     r = subprocess.run([cli], capture_output=True, text=True)
     assert r.returncode == 0 and "--in" in r.stdout
-    r = subprocess.run([cli, "--in", "x.ply", "--aRadius", "3"], capture_output=True, text=True)
-    assert r.returncode == 2 and "regular grid" in r.stderr
+    r = subprocess.run([cli, "--in", "x.ply", "--aRadius", "6"], capture_output=True, text=True)
+    assert r.returncode == 2 and "[0,5]" in r.stderr
+    r = subprocess.run([cli, "--in", "x.ply", "--aRadius", "2", "--solver", "multigrid"], capture_output=True, text=True)
+    assert r.returncode == 2 and "cascadic" in r.stderr
     r = subprocess.run([cli, "--in", "x.txt"], capture_output=True, text=True)
     assert r.returncode == 2 and "ply" in r.stderr
     r = subprocess.run([cli, "--in", "x.ply", "--bogus", "1"], capture_output=True, text=True)
@@ -104,8 +106,9 @@ def test_cli_tree_matches_reference_tree(cli, name):
         ply = os.path.join(td, "in.ply")
         samples.write_ply(ply, g["world_pos"], g["frames"])
         out = os.path.join(td, "out")
-        r = subprocess.run([cli, "--in", ply, "--out", out, "--grid", out, "--depth", str(depth)] + list(g["flags"]),
-                           capture_output=True, text=True)
+        # the fixtures of the regular grid were written with --aRadius -1 (the default is 3)
+        r = subprocess.run([cli, "--in", ply, "--out", out, "--grid", out, "--depth", str(depth), "--aRadius", "-1"] +
+                           list(g["flags"]), capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
         with open(out + ".tree", "rb") as f:
             mine = parse_tree(f.read())

@@ -19,7 +19,8 @@ from exteriorpoissonrecon_gb300 import samples
 from oracle import density_tree as DT
 from oracle import oracle as O
 
-TREE_CASES = ["knot3_d4_tree", "cliff4_d3_tree"]
+# the estimator does not depend on the indexer; the adaptive fixtures come from the default command line
+TREE_CASES = ["knot3_d4_tree", "cliff4_d3_tree", "link3_d5_a3_tree", "cliff4_d3_a1_tree"]
 
 
 def _reference(name):
@@ -96,7 +97,7 @@ def test_cli_density_tree_matches_reference_file(cli, name):
         ply = os.path.join(td, "in.ply")
         samples.write_ply(ply, g["world_pos"], g["frames"])
         out = os.path.join(td, "out")
-        r = subprocess.run([cli, "--in", ply, "--out", out, "--depth", str(depth)] + list(g["flags"]),
+        r = subprocess.run([cli, "--in", ply, "--out", out, "--depth", str(depth), "--aRadius", "-1"] + list(g["flags"]),
                            capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, r.stderr
         with open(out + ".density.tree", "rb") as f:

@@ -34,7 +34,8 @@ def _zero_set_distance(cli, pos, frames, depth, flags, ref_vertices, ref_simplic
         ply = os.path.join(td, "in.ply")
         samples.write_ply(ply, pos, frames)
         out = os.path.join(td, "out")
-        r = subprocess.run([cli, "--in", ply, "--out", out, "--depth", str(depth)] + flags, capture_output=True, text=True)
+        r = subprocess.run([cli, "--in", ply, "--out", out, "--depth", str(depth), "--aRadius", "-1"] + flags, capture_output=True,
+                           text=True)
         assert r.returncode == 0, r.stderr
         with open(out + ".tree", "rb") as f:
             segs, cell = Z.tree_zero_set(f.read(), simp)

@@ -17,6 +17,19 @@ def test_extraction_matches_reference_extract():
     assert d <= 1e-9 * cell, d / cell
 
 
+def test_extraction_of_adaptive_tree_matches_reference_extract():
+    """The reference's Extract on its own adaptive .tree (the command line's default indexer): the
+    indexer's functions scattered to their grid nodes, then regular coefficients and marching
+    simplices as for the regular grid."""
+    g = load_golden("link3_d5_a3_tree")
+    simp = load_golden("cube_simplices")["simplices3"]
+    segs, cell = Z.tree_zero_set(g["tree"].tobytes(), simp)
+    ref = g["zero_vertices"][g["zero_simplices"]]
+    assert len(segs) == len(ref)
+    d = Z.curve_hausdorff(segs, ref, cell / 10)
+    assert d <= 1e-9 * cell, d / cell
+
+
 def test_simplex_table_tiles_the_cube():
     """The reference's 6 (3D) / 24 (4D) simplices each have volume 1/Dim! and positive orientation."""
     import math
