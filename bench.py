@@ -17,7 +17,9 @@ cascadic solve sits at the zero stationary point and leaves it from components t
 would change; with those levels in double(-float) the depth-8 grid stays within 1e-5 relative L2 of
 the FP64 run.  The line reports the
 FP64 run's energy and the result's distance from it (`target`, `error_vs_fp64`), and other
-precision bands beside the configured one (`variants`).  `value` is the device time per solve with
+precision bands beside the configured one (`variants`), and the same input with the reference command
+line's default indexer (`adaptive`: --aRadius 3, FP64 solve and the mixed configuration to its
+energy).  `value` is the device time per solve with
 the system resident in HBM (CUDA events on the library's stream); `e2e` repeats the whole
 public-API pipeline per step from host buffers (samples host->device, build, solve, solution
 device->host).  Every array of a level exceeds the 129 MB L2 (coefficients 137 MB in FP32,
@@ -89,6 +91,9 @@ def parse():
     ap.add_argument("--learned-cap", type=int, default=20,
                     help="finest-level sweeps the learned path may add before it falls back to the plain schedule")
     ap.add_argument("--cpu-depth", type=int, default=6)
+    ap.add_argument("--no-adaptive", action="store_true",
+                    help="skip the solve with the reference command line's default (adaptive) indexer")
+    ap.add_argument("--a-radius", type=int, default=3, help="adaptive radius of that solve (the reference's default 3)")
     ap.add_argument("--workload", default="single", choices=["single", "batch"],
                     help="single: the one large reconstruction above; batch: many small reconstructions "
                          "solved concurrently (torus knots + helices, depths 5-7)")
@@ -660,6 +665,35 @@ def learned_arm(args, pu, sk, depth, e64, device):
     return out
 
 
+def adaptive_arm(args, pu, sk, depth, device):
+    """The same input with the reference command line's default indexer (HierarchicalAdaptedIndexer,
+    --aRadius 3): its all-FP64 solve, then the benchmark's precision configuration run until its
+    FP64-evaluated energy is within 1e-6 of that solve's (the check and any extra sweeps timed)."""
+    import exteriorpoissonrecon_gb300 as epr
+    K = args.a_radius
+    r64 = epr.Reconstructor(3, depth, pu, sk, precision="fp64", aRadius=K, device=device)
+    for _ in range(2):
+        st64 = r64.solve()
+    e64 = st64["fit_energy"] + st64["reg_energy"]
+    t = r64.adaptive_index(depth)
+    r64.close()
+    r = epr.Reconstructor(3, depth, pu, sk, precision="fp32", fp64_from=0, fp64_levels=4, band_precision="df", aRadius=K,
+                          device=device, target_energy=e64 * (1 + 1e-6), max_extra_sweeps=args.target_cap)
+    for _ in range(max(args.warmup, 1)):
+        r.solve()
+    sts = [r.solve() for _ in range(max(args.steps, 1))]
+    r.close()
+    ms = [s["solve_ms"] for s in sts]
+    e = sts[-1]["fit_energy"] + sts[-1]["reg_energy"]
+    return {"a_radius": K, "nodes_finest": (2 ** depth + 1) ** 3, "functions_finest": int(len(t["fnodes"])),
+            "active_functions_finest": t["active"], "elements_finest": int(len(t["enodes"])),
+            "fp64_solve_s": st64["solve_ms"] / 1e3, "solve_s": statistics.mean(ms) / 1e3, "energy_fp64": e64,
+            "energy": e, "energy_rel_diff": (e - e64) / e64,
+            "reached_every_timed_solve": all(bool(s["reached_target"]) for s in sts),
+            "extra_sweeps_per_timed_solve": [int(s["extra_sweeps"]) for s in sts],
+            "speedup_vs_fp64_solve": st64["solve_ms"] / statistics.mean(ms)}
+
+
 def main():
     args = parse()
     ws, rank, local, pg = dist_setup(args)
@@ -821,6 +855,8 @@ def main():
         if dim == 3 and not args.no_learned:
             line["learned"] = learned_arm(args, pu, sk, depth, e64, local)
         r64.close()
+        if dim == 3 and not args.no_adaptive:
+            line["adaptive"] = adaptive_arm(args, pu, sk, depth, local)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference(pu, sk, depth, cpu_depth, 2, 1, dim)
     if rank == 0:

@@ -648,6 +648,11 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
         g_error = "the adaptive indexer is solved by the cascadic schedule only";
         return nullptr;
     }
+    if (p.adaptive_radius >= 0 && p.warm_start)
+    {
+        g_error = "a warm start is defined on the regular grid only (adaptive_radius -1)";
+        return nullptr;
+    }
     if (cudaSetDevice(p.device) != cudaSuccess)
     {
         g_error = std::string("cannot select CUDA device: ") + cudaGetErrorString(cudaGetLastError());

@@ -136,8 +136,8 @@ typedef struct epr_params {
                              183-198, Hat.adaptive.inl:342-732): only the functions within that many
                              cells of a sample's cell (at every level) are relaxed, the ones a step
                              further are held at their prolonged values, all others are zero; the
-                             constraint and c integrate the elements it holds.  Cascadic solver
-                             only (-1) */
+                             constraint and c integrate the elements it holds.  Cascadic solver,
+                             no warm start (-1) */
 } epr_params;
 
 typedef struct epr_stats {
