@@ -163,6 +163,23 @@ __global__ void discover_kernel(const int64_t *fnodes, int64_t nA, const uint8_t
     }
 }
 
+// 1 for the colour's nodes that are active (colour-local index jc, Colour::node order)
+template <int D>
+__global__ void colour_active_flags_kernel(const uint8_t *status, Grid<D> g, Colour<D> col, uint8_t *flags)
+{
+    const int64_t jc = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (jc >= col.n) return;
+    int I[D];
+    col.node(jc, I);
+    flags[jc] = status[g.node(I)] == 2 ? 1 : 0;
+}
+
+__global__ void iota32_kernel(int *v, int64_t n)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (int)i;
+}
+
 __global__ void iota_kernel(int64_t *v, int64_t n)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -367,6 +384,37 @@ bool build_impl(Context &c, const int *cellOfFinest)
             }
         }
         c.release(keys); c.release(keysOut); c.release(vals); c.release(valsOut); c.release(keyE);
+        // every colour's active nodes as colour-local indices, in colour order (the relaxation's
+        // work lists)
+        uint8_t *flags = nullptr;
+        int *num = nullptr, *seq = nullptr;
+        ok = ok && dalloc(c, &A.clist, (size_t)std::max<int64_t>(A.nA, 1), "colour lists") && dalloc(c, &flags, (size_t)g.N, "flags") &&
+             dalloc(c, &num, 1, "count") && dalloc(c, &seq, (size_t)g.N, "sequence");
+        if (ok) iota32_kernel<<<nblk(g.N, 256), 256, 0, s>>>(seq, g.N);
+        A.coff[0] = 0;
+        for (int col = 0; ok && col < (1 << D); col++)
+        {
+            Colour<D> cl(g, col);
+            colour_active_flags_kernel<D><<<nblk(cl.n, 256), 256, 0, s>>>(A.status, g, cl, flags);
+            size_t bytes = 0;
+            cub::DeviceSelect::Flagged(nullptr, bytes, seq, flags, A.clist + A.coff[col], num, (int)cl.n, s);
+            void *tmp = nullptr;
+            ok = c.alloc(&tmp, bytes, "colour lists");
+            if (ok) cub::DeviceSelect::Flagged(tmp, bytes, seq, flags, A.clist + A.coff[col], num, (int)cl.n, s);
+            int h = 0;
+            ok = ok && c.launch_ok("colour lists") && c.cuda_ok(cudaMemcpyAsync(&h, num, sizeof(int), cudaMemcpyDeviceToHost, s), "copy") &&
+                 c.cuda_ok(cudaStreamSynchronize(s), "sync");
+            c.release(tmp);
+            A.coff[col + 1] = A.coff[col] + h;
+        }
+        if (ok && A.coff[1 << D] != A.nA)
+        {
+            c.fail(EPR_ERR_STATE, "adaptive level %d: colour lists hold %d of %lld active nodes", d, A.coff[1 << D], (long long)A.nA);
+            ok = false;
+        }
+        c.release(flags);
+        c.release(num);
+        c.release(seq);
     }
     c.release(counts);
     freeOcc();
@@ -512,6 +560,7 @@ void Context::release_adaptive()
         release(A.status);
         release(A.fnodes);
         release(A.enodes);
+        release(A.clist);
     }
     adapt.clear();
     release(elem_indexed);

@@ -675,6 +675,7 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
     c->depth = depth;
     c->P = p;
     if (const char *v = getenv("EPR_ALLOC_CAP_BYTES")) c->alloc_cap = (size_t)strtoull(v, nullptr, 10);
+    if (const char *v = getenv("EPR_ADAPTIVE_LISTS")) c->adaptive_lists = atoi(v) != 0;
     c->levels.resize(depth + 1);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess)

@@ -66,6 +66,8 @@ struct AdaptiveLevel
     int64_t *fnodes = nullptr;   // node of every function index (active ones first)
     int64_t *enodes = nullptr;   // element of every element index
     int64_t nF = 0, nA = 0, nE = 0;
+    int *clist = nullptr;        // active nodes of every parity colour (colour-local indices)
+    int coff[17] = {0};          // colour c at clist[coff[c] .. coff[c+1])
 };
 
 struct Context
@@ -94,6 +96,9 @@ struct Context
     // the adaptive indexer's levels (empty for the regular grid), built with the system
     std::vector<AdaptiveLevel> adapt;
     uint8_t *elem_indexed = nullptr;  // finest level: 1 for the elements the indexer holds
+    // adaptive levels relax per-colour lists of their active nodes (EPR_ADAPTIVE_LISTS=0 at context
+    // creation: every node of the colour, the inactive ones skipped; the same bits)
+    bool adaptive_lists = true;
     const uint8_t *status_of(int l) const { return adapt.empty() ? nullptr : adapt[l].status; }
     void release_adaptive();
     MGHierarchy *mg = nullptr;  // linear multigrid storage (epr_mg.cu), allocated on first use
@@ -142,7 +147,13 @@ inline LevelPtrs<Real> level_ptrs(Context *c, int l)
     LevelPtrs<Real> p;
     p.level = l;
     p.N = L.N;
-    if (!c->adapt.empty()) p.status = c->adapt[l].status;
+    if (!c->adapt.empty())
+    {
+        const AdaptiveLevel &A = c->adapt[l];
+        p.status = A.status;
+        p.alist = c->adaptive_lists ? A.clist : nullptr;
+        for (int k = 0; k <= (1 << c->dim); k++) p.aoff[k] = A.coff[k];
+    }
     if constexpr (std::is_same<Real, double>::value) { p.xy = L.xy64; p.A = L.A64; p.B = L.B64; }
     else if constexpr (std::is_same<Real, df>::value) { p.xy = L.xyd; p.A = L.Ad; p.B = L.Bd; return p; }
     else { p.xy = L.xy32; p.A = L.A32; p.B = L.B32; }

@@ -23,6 +23,11 @@ struct LevelPtrs
     // adaptive indexer: per node 0 (no function), 1 (indexed, held fixed), 2 (active); the
     // Gauss-Seidel kernels update active nodes only.  Null for the regular grid (all active).
     const uint8_t *status = nullptr;
+    // adaptive indexer: the active nodes of every parity colour as colour-local indices (the
+    // Colour::node order), colour c at alist[aoff[c] .. aoff[c+1]); the large levels relax these
+    // lists instead of the whole colour.  Null for the regular grid.
+    const int *alist = nullptr;
+    int aoff[17] = {0};
 };
 
 // Scratch for deterministic two-pass reductions

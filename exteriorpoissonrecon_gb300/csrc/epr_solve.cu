@@ -1026,6 +1026,25 @@ __global__ void __launch_bounds__(kThreads, MinBlocks) gs_colour_lanes_kernel(Le
     gs_lanes_body<D, Real, Packed, kThreads, Stage>(L, col, cbBase, err, separate, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
+// One colour of an adaptive level: the colour's active nodes from its list (colour-local indices),
+// 2^Dim lanes per node as gs_colour_lanes_kernel, each node's update computed the same way
+template <int D, typename Real, int MinBlocks = lanes_min_blocks<D, Real>(), bool Packed = false>
+__global__ void __launch_bounds__(kThreads, MinBlocks) gs_colour_lanes_list_kernel(LevelPtrs<Real> L, Colour<D> col,
+                                                                                   int64_t cbBase, const int *list, int count,
+                                                                                   unsigned int *err, int separate)
+{
+    constexpr int NPB = kThreads >> D;
+    Grid<D> g(L.level);
+    const int A = threadIdx.x & ((1 << D) - 1);
+    const int k = blockIdx.x * NPB + (threadIdx.x >> D);
+    const bool active = k < count;
+    const int64_t jc = active ? list[k] : 0;
+    int I[D];
+    col.node(jc, I);
+    const Real *Ac = L.Acb ? L.Acb + cbBase : nullptr, *Bc = L.Bcb ? L.Bcb + cbBase : nullptr;
+    gs_update_lanes_at<D, Real, Packed>(L, L.xy, g, I, active, A, err, separate, Ac, Bc, jc, col.n);
+}
+
 // the same colour of every reconstruction of a lockstep batch (3D): block = TPB threads (TPB / 8
 // nodes along the last axis), grid.z = reconstruction x the colour's count on axis 0
 template <typename Real, int TPB, int MinBlocks, bool Packed>
@@ -1943,6 +1962,24 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
                 L, col, colour_block_base<D>(g, colour), err, separate);
             return;
         }
+    if (L.alist)
+    {
+        // adaptive level: only the colour's active nodes
+        const int count = L.aoff[colour + 1] - L.aoff[colour];
+        if (count == 0) return;
+        constexpr int NPB = kThreads >> D;
+        const unsigned nb = (unsigned)((count + NPB - 1) / NPB);
+        const int64_t cb = colour_block_base<D>(g, colour);
+        const int *list = L.alist + L.aoff[colour];
+        if constexpr (std::is_same<Real, float>::value)
+            if (g_lanes_variant != 0)
+            {
+                gs_colour_lanes_list_kernel<D, Real, D == 3 ? 9 : 1, true><<<nb, kThreads, 0, s>>>(L, col, cb, list, count, err, separate);
+                return;
+            }
+        gs_colour_lanes_list_kernel<D, Real><<<nb, kThreads, 0, s>>>(L, col, cb, list, count, err, separate);
+        return;
+    }
     if (g_gs_variant == 0) gs_colour_kernel<D, Real><<<blocks_for(col.n), kThreads, 0, s>>>(L, col, err, separate);
     else if (g_gs_variant == 2)
         gs_colour_flat_kernel<D, Real><<<blocks_for(col.n << D), kThreads, 0, s>>>(L, col, err, separate);

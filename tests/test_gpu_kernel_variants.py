@@ -1,7 +1,8 @@
-"""A kernel variant that must not change any bit: the two-block cluster kernel of level 1 against
-the one-block kernel (EPR_TINY_LEVELS=1 / 3), in double-float and double, through whole solves
-(direct launches and the graph replay).  The variant is chosen when the library creates its first
-context, so each run is its own process."""
+"""Kernel variants that must not change any bit, through whole solves (direct launches and the graph
+replay) in double-float and double: the two-block cluster kernel of level 1 against the one-block
+kernel (EPR_TINY_LEVELS=1 / 3), and, with the adaptive indexer, the per-colour lists of active
+nodes against whole colours with the inactive nodes skipped (EPR_ADAPTIVE_LISTS=1 / 0).  The
+variant is chosen when the library creates its first context, so each run is its own process."""
 import json
 import os
 import subprocess
@@ -24,7 +25,9 @@ pu, _ = epr.unit_cube(pos)
 sk = epr.pack_skew(fr)
 out = {}
 for name, kw in (("df", dict(precision="fp32", fp64_from=0, fp64_levels=4, band_precision="df")),
-                 ("fp64", dict())):
+                 ("fp64", dict()),
+                 ("df_adaptive", dict(precision="fp32", fp64_from=0, fp64_levels=4, band_precision="df", aRadius=1)),
+                 ("fp64_adaptive", dict(aRadius=1))):
     r = epr.Reconstructor(3, 5, pu, sk, **kw)
     r.solve()
     r.solve()  # the graph replay
@@ -43,13 +46,13 @@ def _run(env):
     return json.loads(r.stdout.strip().splitlines()[-1])
 
 
-@pytest.mark.parametrize("env", [{"EPR_TINY_LEVELS": "3"}])
+@pytest.mark.parametrize("env", [{"EPR_TINY_LEVELS": "3"}, {"EPR_ADAPTIVE_LISTS": "0"}])
 def test_launch_variants_give_the_same_bits(env):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     base = _run({})
     other = _run(env)
-    for name in ("df", "fp64"):
+    for name in ("df", "fp64", "df_adaptive", "fp64_adaptive"):
         for a, b in zip(base[name], other[name]):
             assert np.array_equal(np.array(a), np.array(b)), (env, name)
