@@ -676,6 +676,7 @@ def adaptive_arm(args, pu, sk, depth, device):
         st64 = r64.solve()
     e64 = st64["fit_energy"] + st64["reg_energy"]
     t = r64.adaptive_index(depth)
+    active = [r64.adaptive_index(l)["active"] for l in range(depth + 1)]
     r64.close()
     r = epr.Reconstructor(3, depth, pu, sk, precision="fp32", fp64_from=0, fp64_levels=4, band_precision="df", aRadius=K,
                           device=device, target_energy=e64 * (1 + 1e-6), max_extra_sweeps=args.target_cap)
@@ -691,7 +692,33 @@ def adaptive_arm(args, pu, sk, depth, device):
             "energy": e, "energy_rel_diff": (e - e64) / e64,
             "reached_every_timed_solve": all(bool(s["reached_target"]) for s in sts),
             "extra_sweeps_per_timed_solve": [int(s["extra_sweeps"]) for s in sts],
-            "speedup_vs_fp64_solve": st64["solve_ms"] / statistics.mean(ms)}
+            "speedup_vs_fp64_solve": st64["solve_ms"] / statistics.mean(ms),
+            "cpu_port_estimate": None if args.no_cpu_baseline else cpu_reference_adaptive(pu, sk, depth, args.cpu_depth, K, active)}
+
+
+def cpu_reference_adaptive(pu, sk, depth, cpu_depth, K, active):
+    """The CPU restatement's adaptive solve on a bounded sample: build at cpu_depth with the same
+    adaptive radius, time two paired-GS sweeps there (active nodes only, all host threads), scale the
+    time per active-node update to the depth-`depth` schedule's active-node updates."""
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    o = O.Oracle(3, cpu_depth, threads=cores, adaptive_radius=K)
+    o.set_samples(pu, sk)
+    o.build()
+    n_active = int(o.get("nactive", cpu_depth)[0])
+    N = o.nodes(cpu_depth)
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1e-2, 1e-2, N)
+    y = rng.uniform(-1e-2, 1e-2, N)
+    x, y = o.gs(cpu_depth, x, y, 1)
+    t0 = time.perf_counter()
+    x, y = o.gs(cpu_depth, x, y, 2)
+    per_update = (time.perf_counter() - t0) / (2 * n_active)
+    updates = sum(math.ceil(2.0 ** (depth - l) * 10) * active[l] for l in range(depth + 1))
+    return {"value": per_update * updates, "unit": "s", "cores": cores, "kind": "port", "estimate": True,
+            "sample": (f"estimate: oracle build + 2 paired-GS sweeps at depth {cpu_depth} ({n_active} active of {N} "
+                       f"nodes, FP64, aRadius {K}); per-update time {per_update * 1e9:.1f} ns scaled to the depth-{depth} "
+                       f"schedule's {updates} active-node updates")}
 
 
 def main():
