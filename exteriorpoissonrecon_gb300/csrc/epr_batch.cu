@@ -36,7 +36,7 @@ struct LevelPlan
     int level = 0;
     int type = kTypeFloat;
     int count = 0;             // members that relax this level
-    bool tiny = false;         // all sweeps in one block per member (3D levels 0-1)
+    bool tiny = false;         // all sweeps in one launch per member (3D levels 0-1; 2 in double-float)
     std::vector<int> iters;    // per job, non-increasing
     std::vector<int> members;  // per job
     size_t off = 0;            // byte offset of the BatchJob table in the image
@@ -156,7 +156,9 @@ bool make_plan(epr_batch &b)
         }
         std::stable_sort(act.begin(), act.end());
         P.count = (int)act.size();
-        P.tiny = b.ctxs[act[0].second]->levels[l].N <= 27;
+        // all sweeps in one launch per member: levels 0-1, and level 2 in double-float on a cluster
+        // per member (the solo solve's kernels)
+        P.tiny = b.ctxs[act[0].second]->levels[l].N <= 27 || cluster_level(l, P.type == kTypeDF);
         for (auto &a : act)
         {
             P.iters.push_back(-a.first);

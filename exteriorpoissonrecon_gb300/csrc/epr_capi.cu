@@ -663,6 +663,7 @@ epr_ctx *epr_create(int dim, int depth, const epr_params *params)
         if (const char *v = getenv("EPR_GS_VARIANT")) epr::set_gs_variant(atoi(v));
         if (const char *v = getenv("EPR_LANES_VARIANT")) epr::set_lanes_variant(atoi(v));
         if (const char *v = getenv("EPR_TINY_LEVELS")) epr::set_tiny_levels(atoi(v));
+        if (const char *v = getenv("EPR_CLUSTER_LEVELS")) epr::set_cluster_levels(atoi(v));
         static uint64_t prepared = 0;  // devices whose kernel attributes are set
         if (p.device >= 0 && p.device < 64 && !(prepared & (1ull << p.device)))
         {

@@ -57,6 +57,9 @@ void set_lanes_variant(int v);
 // 1 (default): 3D levels 0-1 relax in gs_tiny_kernel (one warp per node-element incidence of a
 // colour); 0: in the block kernels
 void set_tiny_levels(int v);
+// 3D level 2 in double-float on one cluster launch (1, the default) or a launch per colour (0)
+void set_cluster_levels(int v);
+bool cluster_level(int level, bool isDF);
 // double-float levels: pairs stored as x 2^-k with k = kexp[level] (epr_df.cuh)
 void launch_df_push(const double *in, df *out, int64_t n, int *kexp, int level, cudaStream_t s);
 void launch_df_pull(const df *in, double *out, int64_t n, const int *kexp, int level, cudaStream_t s);

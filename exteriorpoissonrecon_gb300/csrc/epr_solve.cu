@@ -1714,6 +1714,236 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128) gs_tiny1_batch_
     gs_tiny1_cluster_body<Real>(b.L, b.iters, b.err, b.separate, b.kexp);
 }
 
+// ---------------------------------------------------------------------------------------------
+// 3D level 2 (resolution R = 4: 125 nodes) in double-float, all sweeps in one launch on a cluster
+// of kClusterBlocks blocks of NWB warps.  Every block keeps a replica of the level's coefficients
+// and stencils in shared memory.  Every element has exactly one corner in each parity colour, so a
+// colour's (node, element) incidences are the level's R^3 = 64 elements, one per warp.  A colour
+// phase: (1) lanes 0-11 of a warp integrate its element's wedge component x Gauss-point pair in the
+// canonical orientation of the element's colour node (as gs_tiny1_kernel), lanes 16-31 the node's
+// stencil column when the element is the node's designated one (the element on the lower side of
+// the node on every axis where there is one), and lane 0 writes the element's ten sums into the
+// block that owns the node (colour index mod the cluster size) through distributed shared memory;
+// cluster barrier; (2) one thread of the owner block per node adds its elements' sums in a fixed
+// order, takes the node step and writes the new pair into every replica; cluster barrier.  The
+// replicas are rescaled after every sweep as the other double-float kernels do.  One launch
+// replaces the level's 8 x 640 colour launches and their rescales at depth 8: 30.4 against 33.7 ms.
+// The same design measured slower elsewhere, so it is not used there: level 2 in double 65.2
+// against 58.1 ms (the FP64 fits of 64 warps on 8 SMs), and level 3 (512 elements, 8 blocks of
+// 32 warps, two elements per warp, 64 registers) 81.8 against 17.7 ms in double-float.
+// ---------------------------------------------------------------------------------------------
+constexpr int kClusterBlocks = 8;
+
+template <int LEVEL>
+struct ClusterLevel
+{
+    static constexpr int R = 1 << LEVEL, N1 = R + 1, NN = N1 * N1 * N1, NE = R * R * R, S = 27;
+    static constexpr int NWB = NE / kClusterBlocks;  // one warp per element
+    static constexpr bool kSmemStencil = true;
+    template <typename Real>
+    static constexpr size_t xy_bytes() { return (sizeof(Real2<Real>) * NN + 15) / 16 * 16; }
+    template <typename Real>
+    static constexpr size_t part_bytes() { return sizeof(Real) * 10 * NE; }
+    template <typename Real>
+    static constexpr size_t smem_bytes() { return xy_bytes<Real>() + part_bytes<Real>() + (kSmemStencil ? 2 * sizeof(Real) * S * NN : 0); }
+};
+
+template <typename Real, int LEVEL>
+__device__ __forceinline__ void gs_cluster_body(const LevelPtrs<Real> &L, int iters, unsigned int *err, int separate, int *kexp)
+{
+    namespace cg = cooperative_groups;
+    using CL = ClusterLevel<LEVEL>;
+    constexpr int R = CL::R, N1 = CL::N1, NN = CL::NN, NE = CL::NE, S = CL::S, s0 = N1 * N1, s1 = N1;
+    constexpr int NC = kClusterBlocks, W = NC * CL::NWB;
+    constexpr bool kDF = std::is_same<Real, df>::value;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ __align__(16) unsigned char cl_smem[];
+    Real2<Real> *xy = reinterpret_cast<Real2<Real> *>(cl_smem);
+    Real *part = reinterpret_cast<Real *>(cl_smem + CL::template xy_bytes<Real>());
+    Real *As = part + 10 * NE, *Bs = As + S * NN;
+    const Real *Ag = CL::kSmemStencil ? As : L.A, *Bg = CL::kSmemStencil ? Bs : L.B;
+    const unsigned rank = cluster.block_rank();
+    const int lane = threadIdx.x & 31, gw = (int)rank * CL::NWB + (threadIdx.x >> 5);
+    for (int k = threadIdx.x; k < NN; k += blockDim.x) xy[k] = ld2(L.xy, k);
+    if constexpr (CL::kSmemStencil)
+        for (int k = threadIdx.x; k < S * NN; k += blockDim.x)
+        {
+            As[k] = L.A[k];
+            Bs[k] = L.B[k];
+        }
+    cluster.sync();  // every replica ready before any remote write
+    Real wmul = wedge_mult<Real>(kexp, LEVEL);
+    const Grid<3> g(LEVEL);
+    for (int it = 0; it < iters; it++)
+    {
+#pragma unroll 1
+        for (int c = 0; c < 8; c++)
+        {
+            const int par[3] = {c & 1, (c >> 1) & 1, (c >> 2) & 1};
+            const int cnt1 = par[1] ? R / 2 : R / 2 + 1, cnt2 = par[2] ? R / 2 : R / 2 + 1;
+            // (1) element incidences
+#pragma unroll 1
+            for (int e = gw; e < NE; e += W)
+            {
+                const int E[3] = {e / (R * R), (e / R) % R, e % R};
+                int I[3], b[3];
+                bool designated = true;
+#pragma unroll
+                for (int d = 0; d < 3; d++)
+                {
+                    b[d] = par[d] ^ (E[d] & 1);
+                    I[d] = E[d] + b[d];
+                    designated = designated && E[d] == (I[d] > 0 ? I[d] - 1 : 0);
+                }
+                const int i = (I[0] * N1 + I[1]) * N1 + I[2];
+                const int A = (b[0] << 2) | (b[1] << 1) | b[2];
+                Real r[5] = {0, 0, 0, 0, 0};
+                if (lane < 12)
+                {
+                    const int K = lane >> 2, pq = lane & 3;
+                    const int pax[3] = {(K == 2) ? 1 : 0, (K == 0) ? 1 : 2, (K == 0) ? 2 : (K == 1 ? 1 : 0)};
+                    int sd[3];
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+                    {
+                        const int stride = pax[a] == 0 ? s0 : (pax[a] == 1 ? s1 : 1);
+                        sd[a] = ((A >> (2 - pax[a])) & 1) ? -stride : stride;
+                    }
+                    Real x[8], y[8];
+#pragma unroll
+                    for (int cc = 0; cc < 8; cc++)
+                    {
+                        int jj = i;
+#pragma unroll
+                        for (int a = 0; a < 3; a++)
+                            if (cbit<3>(cc, a)) jj += sd[a];
+                        const Real2<Real> v = xy[jj];
+                        x[cc] = v.x;
+                        y[cc] = v.y;
+                    }
+                    component_fit_pq3<Real>(x, y, pq >> 1, pq & 1, r);
+                }
+                else if (lane >= 16 && designated)
+                {
+#pragma unroll
+                    for (int half = 0; half < 2; half++)
+                    {
+                        const int o = lane - 16 + 16 * half;
+                        if (o >= S) continue;
+                        const int off[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+                        bool in = true;
+#pragma unroll
+                        for (int d = 0; d < 3; d++) { const int q = I[d] + off[d]; in = in && q >= 0 && q <= R; }
+                        if (!in) continue;
+                        const int jj = i + off[0] * s0 + off[1] * s1 + off[2];
+                        const Real a = Ag[o * NN + i], bb = Bg[o * NN + i];
+                        const Real2<Real> q = xy[jj];
+                        r[0] += a * q.x;
+                        r[1] += a * q.y;
+                        if (o == 13) r[4] = a;
+                        else { r[2] += bb * q.x; r[3] += bb * q.y; }
+                    }
+                }
+#pragma unroll
+                for (int o = 8; o > 0; o >>= 1)
+#pragma unroll
+                    for (int k = 0; k < 5; k++) r[k] += shfl_xor_any(r[k], o);
+                Real stc[5];
+#pragma unroll
+                for (int k = 0; k < 5; k++) stc[k] = shfl_any(r[k], 16);
+                if (lane == 0)
+                {
+                    const int jc = ((I[0] >> 1) * cnt1 + (I[1] >> 1)) * cnt2 + (I[2] >> 1);
+                    Real *dst = cluster.map_shared_rank(part, (unsigned)(jc % NC)) + 10 * e;
+#pragma unroll
+                    for (int k = 0; k < 5; k++)
+                    {
+                        dst[k] = r[k];
+                        dst[5 + k] = designated ? stc[k] : (Real)0;
+                    }
+                }
+            }
+            cluster.sync();  // every element's sums in its node's owner block
+            // (2) the owner block's nodes
+            {
+                const Colour<3> col(g, c);
+                for (int jc = (int)rank + NC * (int)threadIdx.x; jc < (int)col.n; jc += NC * (int)blockDim.x)
+                {
+                    int I[3];
+                    col.node(jc, I);
+                    const int i = (I[0] * N1 + I[1]) * N1 + I[2];
+                    Real h[5] = {0, 0, 0, 0, 0};
+#pragma unroll 1
+                    for (int bb = 0; bb < 8; bb++)
+                    {
+                        int E[3];
+                        bool ok = true;
+#pragma unroll
+                        for (int d = 0; d < 3; d++) { E[d] = I[d] - ((bb >> (2 - d)) & 1); ok = ok && E[d] >= 0 && E[d] < R; }
+                        if (!ok) continue;
+                        const Real *pe = part + 10 * ((E[0] * R + E[1]) * R + E[2]);
+#pragma unroll
+                        for (int k = 0; k < 5; k++) h[k] += pe[k];
+                    }
+                    const int ed = ((I[0] > 0 ? I[0] - 1 : 0) * R + (I[1] > 0 ? I[1] - 1 : 0)) * R + (I[2] > 0 ? I[2] - 1 : 0);
+                    const Real *sv = part + 10 * ed + 5;
+                    const Real sc = (Real)wedge_scale<3>(R) * wmul;
+                    Real q[5];
+                    q[0] = h[0] * sc + sv[4];
+                    q[1] = h[1] * sc + sv[4];
+                    q[2] = (Real)2 * h[2] * sc;
+                    q[3] = (Real)2 * h[3] * sc + (Real)2 * sv[0] - (Real)2 * sv[3];
+                    q[4] = (Real)2 * h[4] * sc + (Real)2 * sv[1] + (Real)2 * sv[2];
+                    Real p0, p1;
+                    if (relaxed(L, i) && node_step_tiny<Real>(q, separate, p0, p1))
+                    {
+                        Real2<Real> cur = xy[i];
+                        cur.x += p0;
+                        cur.y += p1;
+                        if (!finite_value<Real>(cur.x) || !finite_value<Real>(cur.y)) atomicOr(err, (unsigned int)ERR_NONFINITE);
+#pragma unroll 1
+                        for (int k = 0; k < NC; k++) cluster.map_shared_rank(xy, (unsigned)k)[i] = cur;
+                    }
+                }
+            }
+            cluster.sync();  // every replica updated before the next colour reads it
+        }
+        if constexpr (kDF)
+            if (kexp)
+            {
+                // the replicas hold the same values, so every block picks the same exponent
+                const int shift = df_rescale_shift(reinterpret_cast<const df *>(xy), 2 * NN);
+                if (shift)
+                {
+                    df *v = reinterpret_cast<df *>(xy);
+                    for (int k = threadIdx.x; k < 2 * NN; k += blockDim.x) v[k] = ldexp_df(v[k], shift);
+                    if (rank == 0 && threadIdx.x == 0) kexp[LEVEL] -= shift;
+                }
+                cluster.sync();  // the new exponent visible, no remote write before every rescale
+                if (shift) wmul = wedge_mult<Real>(kexp, LEVEL);
+            }
+    }
+    if (rank == 0)
+        for (int k = threadIdx.x; k < NN; k += blockDim.x) reinterpret_cast<Real2<Real> *>(L.xy)[k] = xy[k];
+    cluster.sync();  // no block leaves while another may still address its shared memory
+}
+
+template <typename Real, int LEVEL>
+__global__ void __cluster_dims__(kClusterBlocks, 1, 1) __launch_bounds__(ClusterLevel<LEVEL>::NWB * 32)
+    gs_cluster_kernel(LevelPtrs<Real> L, int iters, unsigned int *err, int separate, int *kexp)
+{
+    gs_cluster_body<Real, LEVEL>(L, iters, err, separate, kexp);
+}
+
+// one cluster per reconstruction of a lockstep batch
+template <typename Real, int LEVEL>
+__global__ void __cluster_dims__(kClusterBlocks, 1, 1) __launch_bounds__(ClusterLevel<LEVEL>::NWB * 32)
+    gs_cluster_batch_kernel(const BatchJob<Real> *jobs)
+{
+    const BatchJob<Real> &b = jobs[blockIdx.x / kClusterBlocks];
+    gs_cluster_body<Real, LEVEL>(b.L, b.iters, b.err, b.separate, b.kexp);
+}
+
 template <typename Real>
 __global__ void __launch_bounds__(128) gs_tiny0_kernel(LevelPtrs<Real> L, int iters, unsigned int *err, int separate, int *kexp)
 {
@@ -1906,6 +2136,7 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n)
 inline unsigned int blocks_for(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
 
 int g_lanes_variant = 1;  // 0: scalar float element fit in the lane kernel, 1: packed
+int g_cluster_levels = 1;  // 1: 3D level 2 in double-float by gs_cluster_kernel
 int g_tiny_levels = 1;    // 1: 3D levels 0-1 by gs_tiny0_kernel / gs_tiny1_kernel, 2: level 0 by the one-warp
                           // gs_tiny_kernel, 3: level 1 by the one-block gs_tiny_kernel, 0: by the block
                           // kernels of gs_level_kernel
@@ -2013,11 +2244,21 @@ void launch_gs_colour(const LevelPtrs<Real> &L, int colour, unsigned int *err, c
 void set_gs_variant(int v) { g_gs_variant = v; }
 void set_lanes_variant(int v) { g_lanes_variant = v; }
 void set_tiny_levels(int v) { g_tiny_levels = v; }
+void set_cluster_levels(int v) { g_cluster_levels = v; }
+bool cluster_level(int level, bool isDF) { return g_cluster_levels && isDF && level == 2; }
 
 // all sweeps of a 3D level 0 or 1 in gs_tiny_kernel (one warp per incidence of a colour)
 template <typename Real>
 bool launch_tiny_level(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s, int separate, int *kexp)
 {
+    // level 2 in double-float: one launch on a cluster (EPR_CLUSTER_LEVELS=0: a launch per colour)
+    if constexpr (std::is_same<Real, df>::value)
+        if (cluster_level(L.level, true))
+        {
+            gs_cluster_kernel<Real, 2><<<kClusterBlocks, ClusterLevel<2>::NWB * 32, ClusterLevel<2>::smem_bytes<Real>(), s>>>(
+                L, iters, err, separate, kexp);
+            return true;
+        }
     if (!g_tiny_levels || L.level > 1) return false;
     if (L.level == 0)
     {
@@ -2051,8 +2292,16 @@ static void prepare_level_kernels()
     }
 }
 
+static void prepare_cluster_kernels()
+{
+    cudaFuncSetAttribute(gs_cluster_kernel<df, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ClusterLevel<2>::smem_bytes<df>());
+    cudaFuncSetAttribute(gs_cluster_batch_kernel<df, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)ClusterLevel<2>::smem_bytes<df>());
+}
+
 void prepare_gs_kernels()
 {
+    prepare_cluster_kernels();
     prepare_level_kernels<3, float>();
     prepare_level_kernels<3, double>();
     prepare_level_kernels<3, df>();
@@ -2201,7 +2450,7 @@ int launch_gs_sweeps_df(const LevelPtrs<df> &L, int iters, unsigned int *err, cu
 {
     Grid<3> g(L.level);
     if (iters <= 0) return 0;
-    if (g.N <= persistentMaxNodes && launch_tiny_level<df>(L, iters, err, s, separate, kexp)) return 1;
+    if ((g.N <= persistentMaxNodes || cluster_level(L.level, true)) && launch_tiny_level<df>(L, iters, err, s, separate, kexp)) return 1;
     if (g.N <= persistentMaxNodes)
     {
         constexpr int MT = persistent_threads<3, df>();
@@ -2310,6 +2559,12 @@ template <typename Real>
 void launch_tiny_batch(const BatchJob<Real> *jobs, int level, int count, cudaStream_t s)
 {
     if (count <= 0) return;
+    if constexpr (std::is_same<Real, df>::value)
+        if (cluster_level(level, true))
+        {
+            gs_cluster_batch_kernel<Real, 2><<<kClusterBlocks * count, ClusterLevel<2>::NWB * 32, ClusterLevel<2>::smem_bytes<Real>(), s>>>(jobs);
+            return;
+        }
     if (level == 0)
     {
         if (g_tiny_levels == 2) gs_tiny_batch_kernel<Real, 0><<<count, 32, 0, s>>>(jobs);

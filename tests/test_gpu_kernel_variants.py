@@ -2,7 +2,9 @@
 replay) in double-float and double: the two-block cluster kernel of level 1 against the one-block
 kernel (EPR_TINY_LEVELS=1 / 3), and, with the adaptive indexer, the per-colour lists of active
 nodes against whole colours with the inactive nodes skipped (EPR_ADAPTIVE_LISTS=1 / 0).  The
-variant is chosen when the library creates its first context, so each run is its own process."""
+variant is chosen when the library creates its first context, so each run is its own process.
+The cluster kernel of double-float level 2 against a launch per colour (EPR_CLUSTER_LEVELS=1 / 0)
+sums each node's element integrals in another order, so it is compared within rounding instead."""
 import json
 import os
 import subprocess
@@ -56,3 +58,20 @@ def test_launch_variants_give_the_same_bits(env):
     for name in ("df", "fp64", "df_adaptive", "fp64_adaptive"):
         for a, b in zip(base[name], other[name]):
             assert np.array_equal(np.array(a), np.array(b)), (env, name)
+
+
+def test_cluster_level_agrees_within_rounding():
+    """Double-float level 2 on one cluster launch against a launch per colour: the same solve up to
+    the order of the element sums (double-float rounding, 2^-48 relative per operation)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    base = _run({})
+    other = _run({"EPR_CLUSTER_LEVELS": "0"})
+    for name in ("fp64", "fp64_adaptive"):  # no double-float level: the same kernels
+        for a, b in zip(base[name], other[name]):
+            assert np.array_equal(np.array(a), np.array(b)), name
+    for name in ("df", "df_adaptive"):
+        for a, b in zip(base[name], other[name]):
+            a, b = np.array(a), np.array(b)
+            assert np.linalg.norm(a - b) <= 1e-7 * np.linalg.norm(b), name
