@@ -26,7 +26,8 @@ def load_golden(name):
     return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
 
 
-VARIANT_CASES = ["knot3_d4_separate", "knot3_d4_single", "knot3_d4_seed7_min2"]
+VARIANT_CASES = ["knot3_d4_separate", "knot3_d4_single", "knot3_d4_seed7_min2", "link3_d5_a1_separate",
+                 "link3_d5_a1_single", "link3_d5_a1_seed7_min3"]
 # the adaptive indexer (--aRadius K): fixtures of its tables, system, probes and solve; and the
 # reference command line's own adaptive .tree files
 ADAPTIVE_CASES = ["knot3_d5_a1", "link3_d5_a0", "link3_d5_a3", "cliff4_d3_a1"]
@@ -36,7 +37,8 @@ ADAPTIVE_TREES = {"link3_d5_a3_tree": 3, "cliff4_d3_a1_tree": 1}
 def variant_params(flags):
     """Harness flags of a variant fixture -> parameter keywords (the reference's flag names)."""
     conv = {"--separate": ("separate", int), "--singleLevel": ("singleLevel", int), "--gsIters": ("gsIters", int),
-            "--seed": ("seed", int), "--minSolveDepth": ("minSolveDepth", int), "--iMult": ("iMult", float)}
+            "--seed": ("seed", int), "--minSolveDepth": ("minSolveDepth", int), "--iMult": ("iMult", float),
+            "--aRadius": ("aRadius", int)}
     flags = [str(f) for f in flags]
     out = {}
     for k, v in zip(flags[0::2], flags[1::2]):

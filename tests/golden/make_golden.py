@@ -51,6 +51,11 @@ VARIANTS = [
     # command line's full iteration budget) and, in 3D, the whole solve on the projected system
     ("knot3_d4_project", "knot", 4096, 0, 4, ["--project", "1"]),
     ("cliff4_d3_project", "clifford", 4000, 5, 3, ["--project", "1"]),
+    # the same schedule variants with the adaptive indexer (a narrow band, so that inactive indexed
+    # functions carry the random start, the prolongation and the hierarchical output)
+    ("link3_d5_a1_separate", "link", 6000, 3, 5, ["--aRadius", "1", "--separate", "1"]),
+    ("link3_d5_a1_single", "link", 6000, 3, 5, ["--aRadius", "1", "--singleLevel", "1", "--gsIters", "40"]),
+    ("link3_d5_a1_seed7_min3", "link", 6000, 3, 5, ["--aRadius", "1", "--seed", "7", "--minSolveDepth", "3", "--iMult", "1.5"]),
 ]
 
 # the adaptive indexer (--aRadius K >= 0, the reference command line's default is 3): name, workload,

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import exteriorpoissonrecon_gb300 as epr
-from conftest import SOLVE_CASES, load_golden
+from conftest import SOLVE_CASES, VARIANT_CASES, load_golden
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -226,9 +226,11 @@ def test_against_oracle_4d_depth5():
     r.close()
 
 
-@pytest.mark.parametrize("name", ["knot3_d4_separate", "knot3_d4_single", "knot3_d4_seed7_min2"])
+@pytest.mark.parametrize("name", VARIANT_CASES)
 def test_solver_variants(name):
-    """--separate, --singleLevel and seed/minSolveDepth/iMult schedules against the reference."""
+    """--separate, --singleLevel and seed/minSolveDepth/iMult schedules against the reference, on the
+    regular grid and with the adaptive indexer (whose narrow bands accumulate the different order of
+    the FP64 sums a little further: coefficients at 1e-8)."""
     from conftest import variant_params
     g = load_golden(name)
     depth = int(g["depth"])
@@ -237,10 +239,11 @@ def test_solver_variants(name):
     ref = g["sol_energies"]
     assert abs(st["fit_energy"] - ref[0]) < 1e-10 * ref[0]
     assert abs(st["reg_energy"] - ref[1]) < 1e-10 * ref[1]
+    tol = 1e-8 if "--aRadius" in [str(f) for f in g["flags"]] else 1e-9
     xs, ys = r.solution()
     for l in range(depth + 1):
-        assert rel(xs[l], g[f"solx_d{l}"]) < 1e-9
-        assert rel(ys[l], g[f"soly_d{l}"]) < 1e-9
+        assert rel(xs[l], g[f"solx_d{l}"]) < tol
+        assert rel(ys[l], g[f"soly_d{l}"]) < tol
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])

@@ -4,7 +4,7 @@ largest magnitude; FP64 throughout."""
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, SOLVE_CASES, load_golden
+from conftest import GOLDEN_CASES, SOLVE_CASES, VARIANT_CASES, load_golden
 from oracle import oracle as O
 
 
@@ -169,16 +169,16 @@ def test_stepped_solve(case):
 
 
 ORACLE_NAMES = {"separate": "separate", "singleLevel": "single_level", "gsIters": "gs_iters", "seed": "seed",
-                "minSolveDepth": "min_solve_depth", "iMult": "i_mult"}
+                "minSolveDepth": "min_solve_depth", "iMult": "i_mult", "aRadius": "adaptive_radius"}
 
 
-@pytest.mark.parametrize("name", ["knot3_d4_separate", "knot3_d4_single", "knot3_d4_seed7_min2"])
+@pytest.mark.parametrize("name", VARIANT_CASES)
 def test_solver_variants(name):
     from conftest import variant_params
     g = load_golden(name)
     depth = int(g["depth"])
     kw = {ORACLE_NAMES[k]: v for k, v in variant_params(g["flags"]).items()}
-    o = O.Oracle(3, depth, **kw)
+    o = O.Oracle(g["pos"].shape[1], depth, **kw)
     o.set_samples(g["pos"], g["skew"])
     o.build()
     xs, ys, e = o.solve()
