@@ -1732,29 +1732,33 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128) gs_tiny1_batch_
 // against 58.1 ms (the FP64 fits of 64 warps on 8 SMs), and level 3 (512 elements, 8 blocks of
 // 32 warps, two elements per warp, 64 registers) 81.8 against 17.7 ms in double-float.
 // ---------------------------------------------------------------------------------------------
-constexpr int kClusterBlocks = 8;
-
-template <int LEVEL>
+template <int LEVEL, int NC>
 struct ClusterLevel
 {
     static constexpr int R = 1 << LEVEL, N1 = R + 1, NN = N1 * N1 * N1, NE = R * R * R, S = 27;
-    static constexpr int NWB = NE / kClusterBlocks;  // one warp per element
+    static constexpr int NWB = NE / NC;  // one warp per element
     static constexpr bool kSmemStencil = true;
     template <typename Real>
     static constexpr size_t xy_bytes() { return (sizeof(Real2<Real>) * NN + 15) / 16 * 16; }
     template <typename Real>
     static constexpr size_t part_bytes() { return sizeof(Real) * 10 * NE; }
+    // a 16-block cluster asks for more shared memory than it uses, so that no two of its blocks
+    // share an SM (each SM sub-partition then issues for one warp)
     template <typename Real>
-    static constexpr size_t smem_bytes() { return xy_bytes<Real>() + part_bytes<Real>() + (kSmemStencil ? 2 * sizeof(Real) * S * NN : 0); }
+    static constexpr size_t smem_bytes()
+    {
+        const size_t used = xy_bytes<Real>() + part_bytes<Real>() + (kSmemStencil ? 2 * sizeof(Real) * S * NN : 0);
+        return NC == 16 && used < 116 * 1024 ? 116 * 1024 : used;
+    }
 };
 
-template <typename Real, int LEVEL>
+template <typename Real, int LEVEL, int NC>
 __device__ __forceinline__ void gs_cluster_body(const LevelPtrs<Real> &L, int iters, unsigned int *err, int separate, int *kexp)
 {
     namespace cg = cooperative_groups;
-    using CL = ClusterLevel<LEVEL>;
+    using CL = ClusterLevel<LEVEL, NC>;
     constexpr int R = CL::R, N1 = CL::N1, NN = CL::NN, NE = CL::NE, S = CL::S, s0 = N1 * N1, s1 = N1;
-    constexpr int NC = kClusterBlocks, W = NC * CL::NWB;
+    constexpr int W = NC * CL::NWB;
     constexpr bool kDF = std::is_same<Real, df>::value;
     cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ __align__(16) unsigned char cl_smem[];
@@ -1928,20 +1932,39 @@ __device__ __forceinline__ void gs_cluster_body(const LevelPtrs<Real> &L, int it
     cluster.sync();  // no block leaves while another may still address its shared memory
 }
 
-template <typename Real, int LEVEL>
-__global__ void __cluster_dims__(kClusterBlocks, 1, 1) __launch_bounds__(ClusterLevel<LEVEL>::NWB * 32)
+// launched with a cluster of NC blocks (cudaLaunchKernelEx, launch_cluster_level)
+template <typename Real, int LEVEL, int NC>
+__global__ void __launch_bounds__(ClusterLevel<LEVEL, NC>::NWB * 32)
     gs_cluster_kernel(LevelPtrs<Real> L, int iters, unsigned int *err, int separate, int *kexp)
 {
-    gs_cluster_body<Real, LEVEL>(L, iters, err, separate, kexp);
+    gs_cluster_body<Real, LEVEL, NC>(L, iters, err, separate, kexp);
 }
 
 // one cluster per reconstruction of a lockstep batch
-template <typename Real, int LEVEL>
-__global__ void __cluster_dims__(kClusterBlocks, 1, 1) __launch_bounds__(ClusterLevel<LEVEL>::NWB * 32)
-    gs_cluster_batch_kernel(const BatchJob<Real> *jobs)
+template <typename Real, int LEVEL, int NC>
+__global__ void __launch_bounds__(ClusterLevel<LEVEL, NC>::NWB * 32) gs_cluster_batch_kernel(const BatchJob<Real> *jobs)
 {
-    const BatchJob<Real> &b = jobs[blockIdx.x / kClusterBlocks];
-    gs_cluster_body<Real, LEVEL>(b.L, b.iters, b.err, b.separate, b.kexp);
+    const BatchJob<Real> &b = jobs[blockIdx.x / NC];
+    gs_cluster_body<Real, LEVEL, NC>(b.L, b.iters, b.err, b.separate, b.kexp);
+}
+
+// a launch of `count` clusters of NC blocks
+template <typename Kernel, typename... Args>
+cudaError_t launch_clusters(Kernel kernel, int nc, int count, int threads, size_t smem, cudaStream_t s, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nc * count), 1, 1);
+    cfg.blockDim = dim3((unsigned)threads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)nc;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
 template <typename Real>
@@ -2136,7 +2159,8 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n)
 inline unsigned int blocks_for(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
 
 int g_lanes_variant = 1;  // 0: scalar float element fit in the lane kernel, 1: packed
-int g_cluster_levels = 1;  // 1: 3D level 2 in double-float by gs_cluster_kernel
+int g_cluster_levels = 1;  // 1: 3D level 2 in double-float by gs_cluster_kernel (8 / 16: that cluster size)
+int g_cluster_blocks = 8;  // the cluster size chosen by prepare_cluster_kernels
 int g_tiny_levels = 1;    // 1: 3D levels 0-1 by gs_tiny0_kernel / gs_tiny1_kernel, 2: level 0 by the one-warp
                           // gs_tiny_kernel, 3: level 1 by the one-block gs_tiny_kernel, 0: by the block
                           // kernels of gs_level_kernel
@@ -2255,8 +2279,12 @@ bool launch_tiny_level(const LevelPtrs<Real> &L, int iters, unsigned int *err, c
     if constexpr (std::is_same<Real, df>::value)
         if (cluster_level(L.level, true))
         {
-            gs_cluster_kernel<Real, 2><<<kClusterBlocks, ClusterLevel<2>::NWB * 32, ClusterLevel<2>::smem_bytes<Real>(), s>>>(
-                L, iters, err, separate, kexp);
+            if (g_cluster_blocks == 16)
+                launch_clusters(gs_cluster_kernel<Real, 2, 16>, 16, 1, ClusterLevel<2, 16>::NWB * 32, ClusterLevel<2, 16>::smem_bytes<Real>(), s,
+                                L, iters, err, separate, kexp);
+            else
+                launch_clusters(gs_cluster_kernel<Real, 2, 8>, 8, 1, ClusterLevel<2, 8>::NWB * 32, ClusterLevel<2, 8>::smem_bytes<Real>(), s, L,
+                                iters, err, separate, kexp);
             return true;
         }
     if (!g_tiny_levels || L.level > 1) return false;
@@ -2292,11 +2320,39 @@ static void prepare_level_kernels()
     }
 }
 
+// the level-2 cluster's size: 16 blocks (one warp per SM sub-partition) where the device can hold
+// such a cluster with one block per SM, else 8 (EPR_CLUSTER_LEVELS=8 or 16 forces one)
 static void prepare_cluster_kernels()
 {
-    cudaFuncSetAttribute(gs_cluster_kernel<df, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ClusterLevel<2>::smem_bytes<df>());
-    cudaFuncSetAttribute(gs_cluster_batch_kernel<df, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)ClusterLevel<2>::smem_bytes<df>());
+    cudaFuncSetAttribute(gs_cluster_kernel<df, 2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ClusterLevel<2, 8>::smem_bytes<df>());
+    cudaFuncSetAttribute(gs_cluster_batch_kernel<df, 2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)ClusterLevel<2, 8>::smem_bytes<df>());
+    const int smem16 = (int)ClusterLevel<2, 16>::smem_bytes<df>();
+    bool ok16 = true;
+    for (auto k : {(const void *)gs_cluster_kernel<df, 2, 16>, (const void *)gs_cluster_batch_kernel<df, 2, 16>})
+    {
+        ok16 = ok16 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+               cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem16) == cudaSuccess;
+    }
+    int clusters = 0;
+    if (ok16)
+    {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(16, 1, 1);
+        cfg.blockDim = dim3(ClusterLevel<2, 16>::NWB * 32, 1, 1);
+        cfg.dynamicSmemBytes = (size_t)smem16;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 16;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        if (cudaOccupancyMaxActiveClusters(&clusters, (const void *)gs_cluster_kernel<df, 2, 16>, &cfg) != cudaSuccess) clusters = 0;
+    }
+    cudaGetLastError();  // an unsupported query leaves no error behind
+    if (g_cluster_levels == 8 || g_cluster_levels == 16) g_cluster_blocks = g_cluster_levels;
+    else g_cluster_blocks = clusters >= 1 ? 16 : 8;
 }
 
 void prepare_gs_kernels()
@@ -2562,7 +2618,12 @@ void launch_tiny_batch(const BatchJob<Real> *jobs, int level, int count, cudaStr
     if constexpr (std::is_same<Real, df>::value)
         if (cluster_level(level, true))
         {
-            gs_cluster_batch_kernel<Real, 2><<<kClusterBlocks * count, ClusterLevel<2>::NWB * 32, ClusterLevel<2>::smem_bytes<Real>(), s>>>(jobs);
+            if (g_cluster_blocks == 16)
+                launch_clusters(gs_cluster_batch_kernel<Real, 2, 16>, 16, count, ClusterLevel<2, 16>::NWB * 32,
+                                ClusterLevel<2, 16>::smem_bytes<Real>(), s, jobs);
+            else
+                launch_clusters(gs_cluster_batch_kernel<Real, 2, 8>, 8, count, ClusterLevel<2, 8>::NWB * 32,
+                                ClusterLevel<2, 8>::smem_bytes<Real>(), s, jobs);
             return;
         }
     if (level == 0)
