@@ -2325,11 +2325,11 @@ static void prepare_level_kernels()
 static void prepare_cluster_kernels()
 {
     cudaFuncSetAttribute(gs_cluster_kernel<df, 2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ClusterLevel<2, 8>::smem_bytes<df>());
-    cudaFuncSetAttribute(gs_cluster_batch_kernel<df, 2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)ClusterLevel<2, 8>::smem_bytes<df>());
+    cudaFuncSetAttribute(gs_cluster_batch_kernel<df, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)ClusterLevel<2, 4>::smem_bytes<df>());
     const int smem16 = (int)ClusterLevel<2, 16>::smem_bytes<df>();
     bool ok16 = true;
-    for (auto k : {(const void *)gs_cluster_kernel<df, 2, 16>, (const void *)gs_cluster_batch_kernel<df, 2, 16>})
+    for (auto k : {(const void *)gs_cluster_kernel<df, 2, 16>})
     {
         ok16 = ok16 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
                cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem16) == cudaSuccess;
@@ -2618,12 +2618,11 @@ void launch_tiny_batch(const BatchJob<Real> *jobs, int level, int count, cudaStr
     if constexpr (std::is_same<Real, df>::value)
         if (cluster_level(level, true))
         {
-            if (g_cluster_blocks == 16)
-                launch_clusters(gs_cluster_batch_kernel<Real, 2, 16>, 16, count, ClusterLevel<2, 16>::NWB * 32,
-                                ClusterLevel<2, 16>::smem_bytes<Real>(), s, jobs);
-            else
-                launch_clusters(gs_cluster_batch_kernel<Real, 2, 8>, 8, count, ClusterLevel<2, 8>::NWB * 32,
-                                ClusterLevel<2, 8>::smem_bytes<Real>(), s, jobs);
+            // clusters of 4 blocks of 16 warps: a member's phases take longer than on the solo
+            // solve's 16 blocks, but four SMs a member let 38 members relax at once (the node sums
+            // run in the same order whatever the cluster size, so the bits are the solo solve's)
+            launch_clusters(gs_cluster_batch_kernel<Real, 2, 4>, 4, count, ClusterLevel<2, 4>::NWB * 32,
+                            ClusterLevel<2, 4>::smem_bytes<Real>(), s, jobs);
             return;
         }
     if (level == 0)

@@ -1,7 +1,9 @@
 """Kernel variants that must not change any bit, through whole solves (direct launches and the graph
 replay) in double-float and double: the two-block cluster kernel of level 1 against the one-block
-kernel (EPR_TINY_LEVELS=1 / 3), and, with the adaptive indexer, the per-colour lists of active
-nodes against whole colours with the inactive nodes skipped (EPR_ADAPTIVE_LISTS=1 / 0).  The
+kernel (EPR_TINY_LEVELS=1 / 3), the level-2 cluster of 16 blocks against 8 (EPR_CLUSTER_LEVELS=8;
+the node sums run in one order whatever the cluster size), and, with the adaptive indexer, the
+per-colour lists of active nodes against whole colours with the inactive nodes skipped
+(EPR_ADAPTIVE_LISTS=1 / 0).  The
 variant is chosen when the library creates its first context, so each run is its own process.
 The cluster kernel of double-float level 2 against a launch per colour (EPR_CLUSTER_LEVELS=1 / 0)
 sums each node's element integrals in another order, so it is compared within rounding instead."""
@@ -48,7 +50,7 @@ def _run(env):
     return json.loads(r.stdout.strip().splitlines()[-1])
 
 
-@pytest.mark.parametrize("env", [{"EPR_TINY_LEVELS": "3"}, {"EPR_ADAPTIVE_LISTS": "0"}])
+@pytest.mark.parametrize("env", [{"EPR_TINY_LEVELS": "3"}, {"EPR_ADAPTIVE_LISTS": "0"}, {"EPR_CLUSTER_LEVELS": "8"}])
 def test_launch_variants_give_the_same_bits(env):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
