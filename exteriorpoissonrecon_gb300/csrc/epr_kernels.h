@@ -57,7 +57,8 @@ void set_lanes_variant(int v);
 // 1 (default): 3D levels 0-1 relax in gs_tiny_kernel (one warp per node-element incidence of a
 // colour); 0: in the block kernels
 void set_tiny_levels(int v);
-// 3D level 2 in double-float on one cluster launch (1, the default) or a launch per colour (0)
+// 3D level 2 in double-float on one cluster launch (1; 8 or 16 fix the cluster size) or a launch
+// per colour (0, the default)
 void set_cluster_levels(int v);
 bool cluster_level(int level, bool isDF);
 // double-float levels: pairs stored as x 2^-k with k = kexp[level] (epr_df.cuh)

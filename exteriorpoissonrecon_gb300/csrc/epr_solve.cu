@@ -1727,7 +1727,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128) gs_tiny1_batch_
 // cluster barrier; (2) one thread of the owner block per node adds its elements' sums in a fixed
 // order, takes the node step and writes the new pair into every replica; cluster barrier.  The
 // replicas are rescaled after every sweep as the other double-float kernels do.  One launch
-// replaces the level's 8 x 640 colour launches and their rescales at depth 8: 30.4 against 33.7 ms.
+// replaces the level's 8 x 640 colour launches and their rescales at depth 8: 28.6 ms on 16 blocks
+// (30.4 on 8) against 33.5 ms.  It is opt-in (EPR_CLUSTER_LEVELS=1): reconstructions solved
+// concurrently (threaded batches: 149 against 141 solves/s, their end-to-end runs 36 against 25)
+// lose more than the single solve gains, since a cluster holds its SMs for the whole level.
 // The same design measured slower elsewhere, so it is not used there: level 2 in double 65.2
 // against 58.1 ms (the FP64 fits of 64 warps on 8 SMs), and level 3 (512 elements, 8 blocks of
 // 32 warps, two elements per warp, 64 registers) 81.8 against 17.7 ms in double-float.
@@ -2159,7 +2162,7 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n)
 inline unsigned int blocks_for(int64_t n, int t = kThreads) { return (unsigned int)((n + t - 1) / t); }
 
 int g_lanes_variant = 1;  // 0: scalar float element fit in the lane kernel, 1: packed
-int g_cluster_levels = 1;  // 1: 3D level 2 in double-float by gs_cluster_kernel (8 / 16: that cluster size)
+int g_cluster_levels = 0;  // 1: 3D level 2 in double-float by gs_cluster_kernel (8 / 16: that cluster size)
 int g_cluster_blocks = 8;  // the cluster size chosen by prepare_cluster_kernels
 int g_tiny_levels = 1;    // 1: 3D levels 0-1 by gs_tiny0_kernel / gs_tiny1_kernel, 2: level 0 by the one-warp
                           // gs_tiny_kernel, 3: level 1 by the one-block gs_tiny_kernel, 0: by the block
@@ -2275,7 +2278,8 @@ bool cluster_level(int level, bool isDF) { return g_cluster_levels && isDF && le
 template <typename Real>
 bool launch_tiny_level(const LevelPtrs<Real> &L, int iters, unsigned int *err, cudaStream_t s, int separate, int *kexp)
 {
-    // level 2 in double-float: one launch on a cluster (EPR_CLUSTER_LEVELS=0: a launch per colour)
+    // level 2 in double-float: one launch on a cluster (EPR_CLUSTER_LEVELS=1; by default a launch
+    // per colour)
     if constexpr (std::is_same<Real, df>::value)
         if (cluster_level(L.level, true))
         {

@@ -1,12 +1,14 @@
 """Kernel variants that must not change any bit, through whole solves (direct launches and the graph
 replay) in double-float and double: the two-block cluster kernel of level 1 against the one-block
-kernel (EPR_TINY_LEVELS=1 / 3), the level-2 cluster of 16 blocks against 8 (EPR_CLUSTER_LEVELS=8;
-the node sums run in one order whatever the cluster size), and, with the adaptive indexer, the
+kernel (EPR_TINY_LEVELS=1 / 3), the optional level-2 cluster on 16 blocks against 8
+(EPR_CLUSTER_LEVELS=16 / 8: the node sums run in one order whatever the cluster size), and, with
+the adaptive indexer, the
 per-colour lists of active nodes against whole colours with the inactive nodes skipped
 (EPR_ADAPTIVE_LISTS=1 / 0).  The
 variant is chosen when the library creates its first context, so each run is its own process.
-The cluster kernel of double-float level 2 against a launch per colour (EPR_CLUSTER_LEVELS=1 / 0)
-sums each node's element integrals in another order, so it is compared within rounding instead."""
+The cluster kernel of double-float level 2 against the default launch per colour
+(EPR_CLUSTER_LEVELS=1 / unset) sums each node's element integrals in another order, so it is
+compared within rounding instead."""
 import json
 import os
 import subprocess
@@ -50,12 +52,13 @@ def _run(env):
     return json.loads(r.stdout.strip().splitlines()[-1])
 
 
-@pytest.mark.parametrize("env", [{"EPR_TINY_LEVELS": "3"}, {"EPR_ADAPTIVE_LISTS": "0"}, {"EPR_CLUSTER_LEVELS": "8"}])
-def test_launch_variants_give_the_same_bits(env):
+@pytest.mark.parametrize("base_env,env", [({}, {"EPR_TINY_LEVELS": "3"}), ({}, {"EPR_ADAPTIVE_LISTS": "0"}),
+                                           ({"EPR_CLUSTER_LEVELS": "16"}, {"EPR_CLUSTER_LEVELS": "8"})])
+def test_launch_variants_give_the_same_bits(base_env, env):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
-    base = _run({})
+    base = _run(base_env)
     other = _run(env)
     for name in ("df", "fp64", "df_adaptive", "fp64_adaptive"):
         for a, b in zip(base[name], other[name]):
@@ -68,8 +71,8 @@ def test_cluster_level_agrees_within_rounding():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
-    base = _run({})
-    other = _run({"EPR_CLUSTER_LEVELS": "0"})
+    base = _run({"EPR_CLUSTER_LEVELS": "1"})
+    other = _run({})
     for name in ("fp64", "fp64_adaptive"):  # no double-float level: the same kernels
         for a, b in zip(base[name], other[name]):
             assert np.array_equal(np.array(a), np.array(b)), name
