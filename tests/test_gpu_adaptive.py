@@ -196,3 +196,43 @@ def test_adaptive_zero_set_matches_reference(cli, flags, bound):
     ref = g["zero_vertices"][g["zero_simplices"]]
     d = Z.curve_hausdorff(segs, ref, cell / 10)
     assert d / cell <= bound, (d / cell, len(segs), len(ref))
+
+
+@pytest.mark.parametrize("dim,depth,workload,n,K,solve", [(3, 6, "link", 60000, 2, True), (4, 4, "clifford", 60000, 1, False)])
+def test_adaptive_against_oracle_larger(dim, depth, workload, n, K, solve):
+    """The adaptive indexer beyond the fixtures' sizes against the oracle's restatement: index
+    tables exactly, c and the system, two sweeps of the finest level, and (3D; the oracle's 4D
+    solve takes minutes) the whole cascadic solve."""
+    from oracle import oracle as O
+    pos, frames = epr.samples.make_workload(workload, n, seed=11)
+    pu, _ = epr.unit_cube(pos)
+    sk = epr.pack_skew(frames)
+    o = O.Oracle(dim, depth, adaptive_radius=K)
+    o.set_samples(pu, sk)
+    o.build()
+    r = epr.Reconstructor(dim, depth, pu, sk, aRadius=K)
+    for l in range(depth + 1):
+        t = r.adaptive_index(l)
+        assert t["active"] == int(o.get("nactive", l)[0])
+        assert np.array_equal(t["fnodes"], o.get("fnodes", l).astype(np.int64)), l
+        assert np.array_equal(t["enodes"], o.get("enodes", l).astype(np.int64)), l
+    assert abs(r.get("c")[0] - o.get("c")[0]) < 1e-12 * o.get("c")[0]
+    for l in (depth, depth - 1, 0):
+        assert rel(r.get("B", l), o.get("B", l)) < 1e-11
+        assert rel(r.get("R", l), o.get("R", l)) < 1e-10
+    rng = np.random.default_rng(1)
+    x = rng.uniform(-1, 1, o.nodes(depth))
+    y = rng.uniform(-1, 1, o.nodes(depth))
+    gx, gy = r.gs(depth, x, y, 2)
+    ox, oy = o.gs(depth, x, y, 2)
+    assert rel(gx, ox) < 1e-10 and rel(gy, oy) < 1e-10
+    if not solve:
+        return
+    st = r.solve()
+    xs, ys, e = o.solve()
+    assert abs(st["fit_energy"] - e[1]) < 1e-10 * e[1]
+    assert abs(st["reg_energy"] - e[2]) < 1e-10 * e[2]
+    gxs, gys = r.solution()
+    for l in range(depth + 1):
+        assert rel(gxs[l], xs[l]) < 1e-8
+        assert rel(gys[l], ys[l]) < 1e-8
