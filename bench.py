@@ -682,11 +682,12 @@ def adaptive_arm(args, pu, sk, depth, device):
                           device=device, target_energy=e64 * (1 + 1e-6), max_extra_sweeps=args.target_cap)
     for _ in range(max(args.warmup, 1)):
         r.solve()
+    build_ms = r.stats.build_ms  # device time of epr_build, the indexer's tables included
     sts = [r.solve() for _ in range(max(args.steps, 1))]
     r.close()
     ms = [s["solve_ms"] for s in sts]
     e = sts[-1]["fit_energy"] + sts[-1]["reg_energy"]
-    return {"a_radius": K, "nodes_finest": (2 ** depth + 1) ** 3, "functions_finest": int(len(t["fnodes"])),
+    return {"a_radius": K, "build_ms": build_ms, "nodes_finest": (2 ** depth + 1) ** 3, "functions_finest": int(len(t["fnodes"])),
             "active_functions_finest": t["active"], "elements_finest": int(len(t["enodes"])),
             "fp64_solve_s": st64["solve_ms"] / 1e3, "solve_s": statistics.mean(ms) / 1e3, "energy_fp64": e64,
             "energy": e, "energy_rel_diff": (e - e64) / e64,
